@@ -1,0 +1,246 @@
+/* Reference-compiled oracle: implements oracle_sweep() by calling the reference's own CPU
+ * code (cstone + sph headers) unmodified.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Compiled by oracle/ref/Makefile from the reference sources
+ * where they lie, into oracle/_ref/ (git-ignored); it exists only on a machine that holds the
+ * reference.  With -I override_fp64 first on the include path every hydro field is double
+ * (libref_fp64.so); without it the reference's default float hydro types apply
+ * (libref_f32.so).  Call sequence follows domain/test/unit/neighbors/findneighbors.cpp:61-82
+ * for the tree, sph/include/sph/find_neighbors.hpp:10-44 for the neighbours, and
+ * main/src/propagator/{std_hydro.hpp:124-168, ve_hydro.hpp:130-204} for the pair passes.
+ */
+#include "../oracle_api.h"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <span>
+#include <vector>
+
+#include "cstone/findneighbors.hpp"
+#include "cstone/focus/source_center.hpp"
+#include "cstone/primitives/gather.hpp"
+#include "cstone/sfc/sfc.hpp"
+#include "cstone/tree/csarray.hpp"
+#include "cstone/tree/octree.hpp"
+#include "cstone/traversal/groups.hpp"
+
+#include "sph/particles_data.hpp"
+#include "sph/find_neighbors.hpp"
+#include "sph/hydro_std/density.hpp"
+#include "sph/hydro_std/eos.hpp"
+#include "sph/hydro_std/iad.hpp"
+#include "sph/hydro_std/momentum_energy.hpp"
+#include "sph/hydro_ve/xmass.hpp"
+#include "sph/hydro_ve/ve_def_gradh.hpp"
+#include "sph/hydro_ve/eos.hpp"
+#include "sph/hydro_ve/iad_divv_curlv.hpp"
+#include "sph/hydro_ve/av_switches.hpp"
+#include "sph/hydro_ve/momentum_energy.hpp"
+
+using KeyType = uint64_t;
+using Dataset = sphexa::ParticlesData<cstone::CpuTag>;
+
+template<class V>
+static void fromSorted(V& dst, const double* src, const std::vector<uint32_t>& order)
+{
+    dst.resize(order.size());
+    for (size_t i = 0; i < order.size(); ++i)
+        dst[i] = src ? static_cast<typename V::value_type>(src[order[i]]) : typename V::value_type(0);
+}
+
+template<class V>
+static void toOut(double* dst, const V& src, size_t n)
+{
+    if (!dst) return;
+    if (src.size() < n) { std::fill(dst, dst + n, 0.0); return; }
+    for (size_t i = 0; i < n; ++i) dst[i] = double(src[i]);
+}
+
+extern "C" double oracle_kernel_K(double sincIndex)
+{
+    return sph::kernel_3D_k(sph::getSphKernel(sph::SphKernelType::sinc_n, sincIndex), 2.0);
+}
+
+extern "C" void oracle_tables(double sincIndex, double* wh, double* whd)
+{
+    auto a = sph::tabulateFunction<double, sph::lt::kTableSize>(sph::getSphKernel(sph::SphKernelType::sinc_n, sincIndex),
+                                                               0.0, 2.0);
+    auto b = sph::tabulateFunction<double, sph::lt::kTableSize>(
+        sph::getSphKernelDerivative(sph::SphKernelType::sinc_n, sincIndex), 0.0, 2.0);
+    std::copy(a.begin(), a.end(), wh);
+    std::copy(b.begin(), b.end(), whd);
+}
+
+extern "C" int oracle_sweep(const oracle_in* in, oracle_out* out)
+{
+    if (in->nthreads > 0) omp_set_num_threads(in->nthreads);
+    out->threads_used = omp_get_max_threads();
+    const size_t n = size_t(in->n);
+    auto bt = [](uint8_t b) { return b == 1 ? cstone::BoundaryType::periodic : cstone::BoundaryType::open; };
+
+    double lim[6];
+    std::memcpy(lim, in->box, sizeof(lim));
+    if (in->fit_box && n > 0)
+    {
+        const double* c[3] = {in->f[OF_X], in->f[OF_Y], in->f[OF_Z]};
+        for (int d = 0; d < 3; ++d)
+        {
+            if (in->bc[d] == 1) continue;
+            auto mm        = std::minmax_element(c[d], c[d] + n);
+            lim[2 * d]     = *mm.first;
+            lim[2 * d + 1] = *mm.second;
+        }
+    }
+    std::memcpy(out->box, lim, sizeof(lim));
+    cstone::Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(in->bc[0]), bt(in->bc[1]),
+                            bt(in->bc[2]));
+
+    double t0 = omp_get_wtime();
+    std::vector<KeyType> keys(n);
+    cstone::computeSfcKeys(in->f[OF_X], in->f[OF_Y], in->f[OF_Z], cstone::sfcKindPointer(keys.data()), n, box);
+    std::vector<uint32_t> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    cstone::sort_by_key(keys.begin(), keys.end(), order.begin());
+
+    Dataset d;
+    d.ng0   = in->ng0;
+    d.ngmax = in->ngmax;
+    d.gamma = in->gamma;
+    d.Kcour = in->Kcour;
+    d.minDt = in->minDt;
+    d.alphamin       = in->alphamin;
+    d.alphamax       = in->alphamax;
+    d.decay_constant = in->decay;
+    fromSorted(d.x, in->f[OF_X], order);
+    fromSorted(d.y, in->f[OF_Y], order);
+    fromSorted(d.z, in->f[OF_Z], order);
+    fromSorted(d.h, in->f[OF_H], order);
+    fromSorted(d.m, in->f[OF_M], order);
+    fromSorted(d.u, in->f[OF_U], order);
+    fromSorted(d.vx, in->f[OF_VX], order);
+    fromSorted(d.vy, in->f[OF_VY], order);
+    fromSorted(d.vz, in->f[OF_VZ], order);
+    fromSorted(d.alpha, in->f[OF_ALPHA], order);
+    double t1   = omp_get_wtime();
+    out->t_keys = t1 - t0;
+    if (out->keys) std::memcpy(out->keys, keys.data(), sizeof(KeyType) * n);
+    if (out->order) std::memcpy(out->order, order.data(), sizeof(uint32_t) * n);
+
+    auto [csTree, counts] = cstone::computeOctree<KeyType>(std::span<const KeyType>(keys), in->bucket);
+    cstone::OctreeData<KeyType, cstone::CpuTag> octree;
+    octree.resize(cstone::nNodes(csTree));
+    cstone::updateInternalTree<KeyType>(csTree, octree.data());
+    std::vector<cstone::LocalIndex> layout(cstone::nNodes(csTree) + 1, 0);
+    std::inclusive_scan(counts.begin(), counts.end(), layout.begin() + 1);
+    std::span<const KeyType> nodeKeys(octree.prefixes.data(), octree.numNodes);
+    std::vector<cstone::Vec3<double>> centers(octree.numNodes), sizes(octree.numNodes);
+    cstone::nodeFpCenters<KeyType>(nodeKeys, centers.data(), sizes.data(), box);
+    cstone::OctreeNsView<double, KeyType> view{octree.numLeafNodes,          octree.prefixes.data(),
+                                               octree.childOffsets.data(),   octree.internalToLeaf.data(),
+                                               octree.levelRange.data(),     csTree.data(),
+                                               layout.data(),                centers.data(),
+                                               sizes.data()};
+    int64_t L         = int64_t(cstone::nNodes(csTree));
+    out->num_leaves   = L;
+    out->num_nodes    = octree.numNodes;
+    out->num_internal = octree.numInternalNodes;
+    for (int l = 0; l < 23; ++l)
+        out->level_range[l] = octree.levelRange[l];
+    if (out->leaves && out->leaves_cap >= L + 1) std::memcpy(out->leaves, csTree.data(), sizeof(KeyType) * (L + 1));
+    if (out->counts && out->leaves_cap >= L) std::memcpy(out->counts, counts.data(), sizeof(unsigned) * L);
+    if (out->nodes_cap >= octree.numNodes)
+    {
+        if (out->prefixes) std::memcpy(out->prefixes, octree.prefixes.data(), sizeof(KeyType) * octree.numNodes);
+        if (out->child_offsets)
+            std::memcpy(out->child_offsets, octree.childOffsets.data(), sizeof(int32_t) * octree.numNodes);
+        if (out->internal_to_leaf)
+            std::memcpy(out->internal_to_leaf, octree.internalToLeaf.data(), sizeof(int32_t) * octree.numNodes);
+    }
+    double t2   = omp_get_wtime();
+    out->t_tree = t2 - t1;
+
+    d.treeView = view;
+    d.nc.assign(n, 1);
+    d.neighbors.assign(n * in->ngmax, 0);
+    out->h_iter_fails = -1; /* the reference prints the count but does not return it */
+    if (in->stages & (OS_NBR | OS_HYDRO))
+    {
+        sph::findNeighborsSph(d.x.data(), d.y.data(), d.z.data(), d.h.data(), 0, cstone::LocalIndex(n), box, view,
+                              d.ng0, d.ngmax, d.neighbors.data(), d.nc.data());
+        if (out->nc) std::memcpy(out->nc, d.nc.data(), sizeof(uint32_t) * n);
+        if (out->nbr) std::memcpy(out->nbr, d.neighbors.data(), sizeof(uint32_t) * n * in->ngmax);
+    }
+    double t3  = omp_get_wtime();
+    out->t_nbr = t3 - t2;
+
+    out->minDtCourant = INFINITY;
+    if (in->stages & OS_HYDRO)
+    {
+        d.sincIndex = in->sincIndex; /* tables were built with the default sinc index 6 */
+        cstone::GroupView grp{0, cstone::LocalIndex(n), 1, nullptr, nullptr};
+        auto sz = [n](auto&... v) { (v.resize(n), ...); };
+        if (in->variant == 0)
+        {
+            sz(d.rho, d.p, d.c, d.c11, d.c12, d.c13, d.c22, d.c23, d.c33, d.ax, d.ay, d.az, d.du, d.xm);
+            sph::computeDensity(grp, d, box);
+            sph::computeEOS_HydroStd(0, n, d);
+            sph::computeIAD(grp, d, box);
+            sph::computeMomentumEnergySTD(grp, d, box);
+        }
+        else
+        {
+            sz(d.xm, d.kx, d.gradh, d.prho, d.c, d.rho, d.p, d.c11, d.c12, d.c13, d.c22, d.c23, d.c33, d.divv,
+               d.curlv, d.ax, d.ay, d.az, d.du);
+            if (in->avclean) sz(d.dV11, d.dV12, d.dV13, d.dV22, d.dV23, d.dV33);
+            sph::computeXMass(grp, d, box);
+            sph::computeVeDefGradh(grp, d, box);
+            sph::computeEOS(0, n, d);
+            sph::computeIadDivvCurlv(grp, d, box);
+            sph::computeAVswitches(grp, d, box);
+            if (in->avclean) sph::computeMomentumEnergy<true>(grp, nullptr, d, box);
+            else sph::computeMomentumEnergy<false>(grp, nullptr, d, box);
+        }
+        out->minDtCourant = d.minDtCourant;
+    }
+    out->t_hydro = omp_get_wtime() - t3;
+
+    toOut(out->f[OF_X], d.x, n);
+    toOut(out->f[OF_Y], d.y, n);
+    toOut(out->f[OF_Z], d.z, n);
+    toOut(out->f[OF_H], d.h, n);
+    toOut(out->f[OF_M], d.m, n);
+    toOut(out->f[OF_U], d.u, n);
+    toOut(out->f[OF_VX], d.vx, n);
+    toOut(out->f[OF_VY], d.vy, n);
+    toOut(out->f[OF_VZ], d.vz, n);
+    toOut(out->f[OF_ALPHA], d.alpha, n);
+    toOut(out->f[OF_RHO], d.rho, n);
+    toOut(out->f[OF_P], d.p, n);
+    toOut(out->f[OF_C], d.c, n);
+    toOut(out->f[OF_C11], d.c11, n);
+    toOut(out->f[OF_C12], d.c12, n);
+    toOut(out->f[OF_C13], d.c13, n);
+    toOut(out->f[OF_C22], d.c22, n);
+    toOut(out->f[OF_C23], d.c23, n);
+    toOut(out->f[OF_C33], d.c33, n);
+    toOut(out->f[OF_AX], d.ax, n);
+    toOut(out->f[OF_AY], d.ay, n);
+    toOut(out->f[OF_AZ], d.az, n);
+    toOut(out->f[OF_DU], d.du, n);
+    toOut(out->f[OF_XM], d.xm, n);
+    toOut(out->f[OF_KX], d.kx, n);
+    toOut(out->f[OF_GRADH], d.gradh, n);
+    toOut(out->f[OF_PRHO], d.prho, n);
+    toOut(out->f[OF_DIVV], d.divv, n);
+    toOut(out->f[OF_CURLV], d.curlv, n);
+    toOut(out->f[OF_DV11], d.dV11, n);
+    toOut(out->f[OF_DV12], d.dV12, n);
+    toOut(out->f[OF_DV13], d.dV13, n);
+    toOut(out->f[OF_DV22], d.dV22, n);
+    toOut(out->f[OF_DV23], d.dV23, n);
+    toOut(out->f[OF_DV33], d.dV33, n);
+    return 0;
+}
