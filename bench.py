@@ -1,0 +1,348 @@
+"""Benchmark of the single-rank SPH hydro sweep on one GB300 (or N replicas under torchrun).
+
+Workload (the configuration the metric is quoted on): Sedov blast on a 200^3 = 8.0M particle
+lattice in [-0.5, 0.5]^3, periodic, positions jittered by U(+-0.25) lattice spacings (seed 2),
+h frozen at h0; one step = one full sweep: box, Hilbert keys, key sort and field permutation,
+cornerstone tree, neighbour lists (with the h check), and the volume-element pair passes
+(xmass, gradh, EOS, IAD + div/curl v, AV switches, momentum-energy).  FP64 form (every hydro
+field double) is the headline value; the mixed form (reference default types, FP32 pair
+arithmetic) is measured on the same workload and reported beside it with its error against
+the FP64 results of the same run.
+
+  python bench.py [--steps 20] [--warmup 3] [--impl reference]
+
+Synthetic inputs are seeded lattices (no dataset downloads); every input array (~1.6 GB) is
+larger than the 129 MB L2, so no flush is needed between steps.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SPH sweep particles/s on 1 GB300: mixed-FP32 vs FP64 at stated err; adjoint/fwd"
+UNIT = "particles/s"
+
+# Algorithmic FLOPs per neighbour pair of each VE pass (FMA = 2, div = sqrt = 1, one table
+# lookup = 7), counted from the reference j-loops' arithmetic.
+VE_FLOPS_PER_PAIR = {"xmass": 19, "gradh": 34, "iad_divv": 37 + 59, "av": 59, "me": 141}
+STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region (200 ms period)."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+                power.append(float(p[3]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def make_workload(name: str):
+    from sphexa_gb300 import workloads as W
+    if name == "sedov200_jit":
+        return W.sedov(200, jitter=0.25, seed=2)
+    if name == "sedov100_jit":
+        return W.sedov(100, jitter=0.25, seed=2)
+    if name == "fourier300":
+        return W.fourier(300)
+    if name == "sphere10M":
+        return W.sphere(10_000_000)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def cpu_baseline(side: int, threads: int = 0) -> dict:
+    """The oracle (my CPU restatement of the reference's OpenMP path) on a bounded sample of the
+    workload: the same jittered Sedov lattice at side^3 particles, one full VE sweep."""
+    from oracle import oracle as O
+    from sphexa_gb300 import workloads as W
+    O.build_port()
+    port = O.port()
+    wl = W.sedov(side, jitter=0.25, seed=2)
+    t0 = time.perf_counter()
+    r = port.sweep(wl, "ve", False, want_nbr=False, want_tree=False, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": wl.n / dt, "unit": UNIT, "cores": int(r["threads"]), "kind": "port",
+            "sample": f"one VE sweep of the same jittered Sedov lattice at {side}^3 = {wl.n} particles "
+                      f"({dt:.1f} s; stages keys {r['times']['keys']:.2f} tree {r['times']['tree']:.2f} "
+                      f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    side = args.cpu_side
+    vals = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(max(side // 2, 20))
+    t_all = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(side)
+        vals.append(last["value"])
+    wall = time.perf_counter() - t_all
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded jittered Sedov lattice", "impl": "reference",
+            "config": {"workload": args.workload, "sample_side": side, "variant": "ve", "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sedov200_jit")
+    ap.add_argument("--variant", default="ve", choices=["ve", "std"])
+    ap.add_argument("--cpu-side", type=int, default=100)
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from sphexa_gb300 import sph
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = f"cuda:{local}"
+
+    wl = make_workload(args.workload)
+    n = wl.n
+    ctx = sph.Context(local)
+    ctx.set_params(ng0=wl.params["ng0"], ngmax=wl.params["ngmax"], minDt=wl.params["minDt"])
+    peaks = measured_peaks()
+    fp64_peak = ctx.fma_peak(True)
+    fp32_peak = ctx.fma_peak(False)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed_sweeps(d, box, steps, warmup):
+        for _ in range(warmup):
+            sph.sweep(ctx, d, box, args.variant, False)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.launches()
+        stage_sum = np.zeros(8)
+        clocks = ClockSampler(local)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            sph.sweep(ctx, d, box, args.variant, False)
+            stage_sum += np.array(ctx.timings())
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        ck = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, stage_sum / steps, ctx.launches() - l0, ck
+
+    # ---------------- FP64 form (headline)
+    d64 = sph.ParticlesData.from_workload(wl, "fp64", dev)
+    box = sph.Box(wl.box.copy(), wl.bc.copy())
+    ms64, st64, launches, clocks = timed_sweeps(d64, box, args.steps, args.warmup)
+    stats = ctx.stats()
+    pairs = stats["nc_sum"]
+    value = n * args.steps * world / (ms64 * 1e-3)
+
+    # dominant kernel: largest per-stage time of the FP64 sweep
+    names = STAGES_VE if args.variant == "ve" else ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
+    dom = int(np.argmax(st64))
+    flops_pp = {"xmass": VE_FLOPS_PER_PAIR["xmass"], "gradh": VE_FLOPS_PER_PAIR["gradh"],
+                "iad_divv": VE_FLOPS_PER_PAIR["iad_divv"], "av": VE_FLOPS_PER_PAIR["av"],
+                "me": VE_FLOPS_PER_PAIR["me"]}.get(names[dom])
+    if flops_pp:
+        achieved = pairs * flops_pp / (st64[dom] * 1e-3)
+        roofline = {"bound": "fp64", "kernel": names[dom], "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
+                    "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                    "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                    "algorithmic": f"{pairs} pairs x {flops_pp} flop/pair per launch",
+                    "hbm_peak_gbs": peaks.get("hbm_gbs")}
+    else:
+        roofline = {"bound": "hbm", "kernel": names[dom], "achieved": None, "peak": peaks.get("hbm_gbs"),
+                    "unit": "GB/s", "frac": None, "traffic": None}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: seeded jittered Sedov lattice (no dataset; configs regenerated from seeds)",
+           "config": {"workload": f"{args.workload}: {n} particles, periodic [-0.5,0.5]^3, jitter +-0.25 "
+                                  f"spacing, frozen h, one full {args.variant.upper()} sweep per step",
+                      "variant": args.variant, "precision": "fp64", "n_particles": n,
+                      "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+           "roofline": roofline, "gpu_launches": launches // max(1, args.steps) * args.steps,
+           "clocks": clocks,
+           "stages_ms": {names[k]: round(float(st64[k]), 3) for k in range(len(names)) if names[k] != "-"},
+           "neighbors": {"pairs": pairs, "mean": pairs / n, "max_nc": stats["nc_max"], "capped": stats["capped"],
+                         "candidates": stats["candidates"], "fp64_rechecks": stats["fp64_rechecks"]},
+           "fp32_peak_tflops": fp32_peak / 1e12}
+
+    # ---------------- mixed form on the same workload, errors against this run's FP64 results
+    if not args.no_mixed:
+        ref64 = {k: d64.f[k].double().cpu().numpy() for k in ("xm", "kx", "rho", "ax", "ay", "az", "du", "c11",
+                                                               "divv", "alpha")}
+        del d64
+        torch.cuda.empty_cache()
+        d32 = sph.ParticlesData.from_workload(wl, "mixed", dev)
+        box32 = sph.Box(wl.box.copy(), wl.bc.copy())
+        ms32, st32, _, _ = timed_sweeps(d32, box32, args.steps, args.warmup)
+        v32 = n * args.steps * world / (ms32 * 1e-3)
+        r32 = {k: d32.f[k].double().cpu().numpy() for k in ref64}
+        a64 = np.stack([ref64["ax"], ref64["ay"], ref64["az"]], 1)
+        a32 = np.stack([r32["ax"], r32["ay"], r32["az"]], 1)
+        err = {"rho_max_rel": float(np.max(np.abs(r32["rho"] - ref64["rho"]) / np.abs(ref64["rho"]))),
+               "xm_max_rel": float(np.max(np.abs(r32["xm"] - ref64["xm"]) / np.abs(ref64["xm"]))),
+               "a_normwise": float(np.linalg.norm(a32 - a64) / max(np.linalg.norm(a64), 1e-300)),
+               "du_normwise": float(np.linalg.norm(r32["du"] - ref64["du"]) / max(np.linalg.norm(ref64["du"]),
+                                                                                   1e-300)),
+               "c11_max_rel": float(np.max(np.abs(r32["c11"] - ref64["c11"])) / np.max(np.abs(ref64["c11"])))}
+        dom32 = int(np.argmax(st32))
+        fpp32 = VE_FLOPS_PER_PAIR.get(names[dom32]) if args.variant == "ve" else None
+        out["mixed"] = {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
+                        "errors_vs_fp64": err,
+                        "stages_ms": {names[k]: round(float(st32[k]), 3) for k in range(len(names))
+                                      if names[k] != "-"},
+                        "dominant": names[dom32],
+                        "dominant_fp32_frac": (pairs * fpp32 / (st32[dom32] * 1e-3) / fp32_peak) if fpp32 else None}
+        d64 = None
+        del d32
+        torch.cuda.empty_cache()
+
+    # ---------------- end to end through the C ABI with host buffers (pinned), FP64 form
+    if not args.no_e2e:
+        d = sph.ParticlesData.from_workload(wl, "fp64", dev)
+        host_in = {k: torch.from_numpy(np.ascontiguousarray(wl.fields[k], dtype=np.float64)).pin_memory()
+                   for k in sph.INPUTS}
+        outs = ("ax", "ay", "az", "du")
+        host_out = {k: torch.empty(n, dtype=torch.float64).pin_memory() for k in outs}
+        h2d = sum(t.numel() * t.element_size() for t in host_in.values())
+        d2h = sum(t.numel() * t.element_size() for t in host_out.values())
+        boxe = sph.Box(wl.box.copy(), wl.bc.copy())
+
+        def e2e_step():
+            for k, t in host_in.items():
+                d.f[k].copy_(t, non_blocking=True)
+            sph.sweep(ctx, d, boxe, args.variant, False)
+            for k in outs:
+                host_out[k].copy_(d.f[k], non_blocking=True)
+            torch.cuda.synchronize()
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        k_e2e = max(3, args.steps // 2)
+        for _ in range(k_e2e):
+            e2e_step()
+        barrier()
+        wall = time.perf_counter() - t0
+        out["e2e"] = {"value": n * k_e2e * world / wall, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "steps": k_e2e,
+                      "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
+        del d
+
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_side)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

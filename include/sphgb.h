@@ -1,0 +1,185 @@
+/* sphgb: C ABI of the GB300-native single-rank SPH hydro sweep (sm_103a).
+ *
+ * Every entry point returns an sphgb_status (0 = success); no C++ exception crosses it.
+ * Pointers inside sphgb_particles are DEVICE pointers owned by the caller, exactly like the
+ * DeviceVector fields of the reference's DeviceParticlesData
+ * (sph/include/sph/particles_data_gpu.cuh:76-104).  The context owns everything else: sort
+ * scratch, the cornerstone tree, the octree, the neighbour lists and the kernel tables.
+ * All work is enqueued on the context's stream; a call returns once its results are ready
+ * unless noted.
+ *
+ * Two precisions share one set of entry points:
+ *   SPHGB_FP64   every field is double (the reference with HydroType=XM1Type=Tmass=double);
+ *   SPHGB_MIXED  the reference's default SphTypes (sph/include/sph/types.hpp:39-46): x,y,z,u,du
+ *                double, every other hydro field float.  Pair arithmetic runs in FP32 on
+ *                grid-local coordinate offsets; keys and neighbour tests stay exact FP64.
+ */
+#ifndef SPHGB_H
+#define SPHGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SPHGB_OK = 0,
+    SPHGB_ERR_ARG = 1,        /* invalid argument (null pointer, size, range) */
+    SPHGB_ERR_CUDA = 2,       /* a CUDA runtime call failed; sphgb_last_cuda_error() tells which */
+    SPHGB_ERR_ALLOC = 3,      /* device allocation failed */
+    SPHGB_ERR_STATE = 4,      /* call out of order (e.g. pair pass before neighbours) */
+    SPHGB_ERR_TRAVERSAL = 5,  /* octree traversal stack overflow (reference: 0xFFFFFFFF stack flag) */
+    SPHGB_ERR_NOCONV = 6,     /* h / neighbour-count iteration did not converge for some particles */
+    SPHGB_ERR_NOTFOUND = 7,   /* no CUDA device / extension not usable */
+    SPHGB_ERR_TOO_LARGE = 8   /* request exceeds a fixed capacity */
+} sphgb_status;
+
+typedef enum { SPHGB_FP64 = 0, SPHGB_MIXED = 1 } sphgb_precision;
+typedef enum { SPHGB_BC_OPEN = 0, SPHGB_BC_PERIODIC = 1 } sphgb_boundary;
+typedef enum { SPHGB_STD = 0, SPHGB_VE = 1 } sphgb_variant;
+
+typedef struct sphgb_ctx sphgb_ctx;
+
+/* cstone::Box (domain/include/cstone/sfc/box.hpp:94-174): limits and boundary types */
+typedef struct {
+    double lim[6];            /* xmin xmax ymin ymax zmin zmax */
+    uint8_t bc[3];            /* sphgb_boundary per dimension */
+} sphgb_box;
+
+/* Physics constants of sphexa::ParticlesData (sph/include/sph/particles_data.hpp:90-146) */
+typedef struct {
+    uint32_t ng0;             /* target neighbour count, default 100 */
+    uint32_t ngmax;           /* neighbour cap, default 150 */
+    uint32_t bucket;          /* leaf bucket size of the cornerstone tree, default 64 */
+    double gamma;             /* adiabatic index, default 5/3 */
+    double Kcour;             /* Courant factor, default 0.2 */
+    double sincIndex;         /* sinc kernel exponent, default 6 */
+    double alphamin, alphamax, decay_constant;  /* AV switch, defaults 0.05, 1.0, 0.2 */
+    double minDt;             /* d.minDt seen by the AV-switch decay */
+} sphgb_params;
+
+/* Field pointers of one particle set (device memory, caller-owned).  double* fields are FP64
+ * in both precisions; void* fields are double (SPHGB_FP64) or float (SPHGB_MIXED). */
+typedef struct {
+    int64_t n;
+    int32_t precision;        /* sphgb_precision */
+    uint64_t* keys;           /* optional: receives the sorted SFC keys */
+    double *x, *y, *z, *u, *du;
+    void *h, *m, *vx, *vy, *vz, *alpha;
+    void *rho, *p, *c, *xm, *kx, *gradh, *prho, *divv, *curlv;
+    void *c11, *c12, *c13, *c22, *c23, *c33;
+    void *ax, *ay, *az;
+    void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
+    uint32_t* nc;             /* neighbour count incl. self (sphexa nc field) */
+} sphgb_particles;
+
+typedef struct {
+    int64_t num_leaves, num_nodes, num_internal;
+    int32_t level_range[23];
+    int64_t nc_sum;           /* sum over targets of min(nc-1, ngmax) */
+    uint32_t nc_max;          /* max nc (incl. self) */
+    int64_t capped;           /* particles with nc - 1 > ngmax */
+    int64_t h_iterations;     /* h-iteration rounds run by the last neighbour search */
+    int64_t h_fails;          /* particles that hit the 10-iteration limit */
+    int64_t candidates;       /* candidate pairs tested by the last neighbour search */
+    int64_t fp64_rechecks;    /* candidate pairs that needed the exact FP64 test */
+} sphgb_stats;
+
+/* ---- context ---- */
+const char* sphgb_status_string(int status);
+const char* sphgb_last_cuda_error(void);
+int sphgb_version(void);
+/* create a context on `device`; stream 0 = the legacy default stream */
+int sphgb_create(sphgb_ctx** ctx, int device);
+int sphgb_destroy(sphgb_ctx* ctx);
+int sphgb_set_stream(sphgb_ctx* ctx, void* cuda_stream);
+int sphgb_set_params(sphgb_ctx* ctx, const sphgb_params* params);
+int sphgb_default_params(sphgb_params* params);
+/* kernel normalisation constant K used by the pair passes */
+int sphgb_get_kernel_K(sphgb_ctx* ctx, double* K);
+
+/* ---- domain: replaces Domain<KeyType,T,GpuTag>::sync + octreeProperties at one rank
+ *      (domain/include/cstone/domain/domain.hpp:181-234, 416-428).  Fits open box limits
+ *      (sfc/box_mpi.hpp:68-103), computes Hilbert keys (sfc/sfc.hpp:267-275), stable-sorts by
+ *      key (primitives/gather.cuh:50-76), permutes every non-null field of `p` in place, and
+ *      builds the cornerstone tree with bucket `params.bucket` (tree/csarray.hpp:429-440), the
+ *      internal octree (tree/octree.hpp:136-157) and the leaf layout.  `box` is in/out. */
+int sphgb_domain_sync(sphgb_ctx* ctx, sphgb_particles* p, sphgb_box* box);
+/* device pointers of the tree built by the last sync (valid until the next sync) */
+int sphgb_get_tree(sphgb_ctx* ctx, const uint64_t** leaves, const uint32_t** layout,
+                   const uint64_t** prefixes, const int32_t** child_offsets,
+                   const int32_t** internal_to_leaf, sphgb_stats* stats);
+/* sorted order of the last sync: order[i] = pre-sync index of sorted particle i (device) */
+int sphgb_get_order(sphgb_ctx* ctx, const uint32_t** order);
+
+/* ---- neighbours ---- */
+/* cstone::findNeighbors (domain/include/cstone/findneighbors.hpp:149-170): fixed h, no
+ * iteration.  Writes neighbors[(i-first)*ngmax + k] (reference layout, device) when non-null
+ * and nc[i-first] = neighbour count EXCLUDING self, like the reference.  Lists are sorted
+ * ascending; a particle with more than ngmax neighbours keeps its ngmax smallest indices. */
+int sphgb_find_neighbors(sphgb_ctx* ctx, const double* x, const double* y, const double* z, const void* h,
+                         int32_t h_precision, int64_t first, int64_t last, uint32_t ngmax, uint32_t* neighbors,
+                         uint32_t* nc);
+/* sph::findNeighborsSfc / findNeighborsSph (sph/include/sph/find_neighbors.hpp:10-56): builds
+ * the context's neighbour lists for [first,last) with the coupled h / nc iteration (at most 10
+ * rounds), writes p->nc (incl. self) and may update p->h.  Returns SPHGB_ERR_NOCONV (a warning:
+ * the lists are complete) when some particles did not converge, as the reference prints. */
+int sphgb_find_neighbors_sph(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* copy the context's lists out in the reference CPU layout neighbors[(i-first)*ngmax + k] */
+int sphgb_export_neighbors(sphgb_ctx* ctx, uint32_t* neighbors_device);
+
+/* ---- pair passes, each (GroupView{first,last}, Dataset&, Box) like the reference ---- */
+/* sph::computeDensity (sph/include/sph/hydro_std/density.hpp:55-60) -> rho */
+int sphgb_compute_density(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeEOS_HydroStd, ideal gas (hydro_std/eos.hpp:147-152) -> p, c */
+int sphgb_compute_eos_std(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeIAD (hydro_std/iad.hpp:74-79) -> c11..c33 */
+int sphgb_compute_iad(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeMomentumEnergySTD (hydro_std/momentum_energy.hpp:96-101) -> ax ay az du; Courant
+ * dt minimum to *minDtCourant (d.minDtCourant) when non-null */
+int sphgb_compute_momentum_energy_std(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last,
+                                      double* minDtCourant);
+/* sph::computeXMass (hydro_ve/xmass.hpp:69-74) -> xm */
+int sphgb_compute_xmass(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeVeDefGradh (hydro_ve/ve_def_gradh.hpp:80-85) -> kx, gradh */
+int sphgb_compute_ve_def_gradh(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeEOS, ideal gas (hydro_ve/eos.hpp:191-197) -> prho, c, and rho, p when non-null */
+int sphgb_compute_eos(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeIadDivvCurlv (hydro_ve/iad_divv_curlv.hpp:93-98) -> c11..c33, divv, curlv (if
+ * non-null), dV11..dV33 (if non-null) */
+int sphgb_compute_iad_divv_curlv(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeAVswitches (hydro_ve/av_switches.hpp:81-86) -> alpha (in/out), dt = params.minDt */
+int sphgb_compute_av_switches(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::computeMomentumEnergy<avClean> (hydro_ve/momentum_energy.hpp:107-115) -> ax ay az du;
+ * group_dt: optional device float per 32-particle group (reference groupDt); minDtCourant as
+ * above */
+int sphgb_compute_momentum_energy(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last,
+                                  int32_t av_clean, float* group_dt, double* minDtCourant);
+
+/* ---- whole sweep: sync + neighbours + the pair passes of one propagator step
+ *      (main/src/propagator/std_hydro.hpp:124-168, ve_hydro.hpp:130-204) ---- */
+int sphgb_sweep(sphgb_ctx* ctx, sphgb_particles* p, sphgb_box* box, int32_t variant, int32_t av_clean,
+                double* minDtCourant);
+/* same chain without the domain sync (keys, sort, tree reused): the frozen-tree sweep */
+int sphgb_sweep_passes(sphgb_ctx* ctx, sphgb_particles* p, int32_t variant, int32_t av_clean,
+                       double* minDtCourant);
+
+/* ---- statistics and timing ---- */
+int sphgb_get_stats(sphgb_ctx* ctx, sphgb_stats* stats);
+/* milliseconds of the last call of each stage, measured with CUDA events on the context
+ * stream: [0] sync [1] neighbours [2..7] pair passes in call order of the last sweep */
+int sphgb_get_timings(sphgb_ctx* ctx, float* ms, int32_t count);
+/* number of kernels this library launched since the context was created */
+int sphgb_kernel_launches(sphgb_ctx* ctx, int64_t* launches);
+/* device-wide FMA throughput (FLOP/s, FMA = 2) of the FP64 (fp64 != 0) or FP32 pipe, measured
+ * with a dependent-chain probe kernel; the roofline denominator of the pair passes (no
+ * reference counterpart: the reference records no performance figures) */
+int sphgb_measure_fma_peak(sphgb_ctx* ctx, int32_t fp64, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHGB_H */

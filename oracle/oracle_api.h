@@ -78,6 +78,35 @@ typedef struct {
 } oracle_out;
 
 int oracle_sweep(const oracle_in* in, oracle_out* out);
+
+/* One j-loop for particle 0 over an explicit neighbour list, as the reference's known-answer
+ * tests call them (sph/test/std.cpp:98-127, sph/test/ve.cpp:112-233). */
+enum oracle_jloop_kind {
+    OJ_XMASS = 0,   /* out: xm */
+    OJ_GRADH,       /* out: kx, gradh */
+    OJ_IAD_STD,     /* out: c11 c12 c13 c22 c23 c33 (volume m/rho) */
+    OJ_IAD_VE,      /* out: c11 .. c33 (volume xm/kx) */
+    OJ_DIVV,        /* out: divv curlv dV11 dV12 dV13 dV22 dV23 dV33 */
+    OJ_AV,          /* out: alpha */
+    OJ_ME_STD,      /* out: ax ay az du maxvsignal */
+    OJ_ME_VE        /* out: ax ay az du maxvsignal (avclean selects the AV cleaning) */
+};
+
+typedef struct {
+    int64_t n;
+    const double* f[OF_NFIELDS];   /* per-particle inputs by slot; NULL reads as zeros */
+    const uint32_t* neighbors;     /* neighbour list of particle 0 */
+    uint32_t count;
+    double K;                      /* kernel normalisation to use */
+    double box[6];
+    uint8_t bc[3];
+    double sincIndex;
+    double dt, alphamin, alphamax, decay;
+    int32_t loop;                  /* oracle_jloop_kind */
+    int32_t avclean;
+} oracle_jloop_in;
+
+int oracle_jloop(const oracle_jloop_in* in, double* out);
 /* kernel normalisation constant and tables for a sinc^n kernel, for table-level checks */
 double oracle_kernel_K(double sincIndex);
 void oracle_tables(double sincIndex, double* wh, double* whd); /* 20000 each */

@@ -244,3 +244,106 @@ extern "C" int oracle_sweep(const oracle_in* in, oracle_out* out)
     toOut(out->f[OF_DV33], d.dV33, n);
     return 0;
 }
+
+/* the reference j-loops themselves, as sph/test/std.cpp and sph/test/ve.cpp call them */
+extern "C" int oracle_jloop(const oracle_jloop_in* in, double* out)
+{
+    using T         = sph::SphTypes::HydroType;
+    const size_t n  = size_t(in->n);
+    std::vector<std::vector<T>> f(OF_NFIELDS, std::vector<T>(n, T(0)));
+    std::vector<double> xyz[3];
+    for (int k = 0; k < OF_NFIELDS; ++k)
+        if (in->f[k])
+            for (size_t i = 0; i < n; ++i)
+                f[k][i] = T(in->f[k][i]);
+    for (int k = 0; k < 3; ++k)
+        xyz[k].assign(in->f[k] ? in->f[k] : nullptr, in->f[k] ? in->f[k] + n : nullptr);
+    auto bt = [](uint8_t b) { return b == 1 ? cstone::BoundaryType::periodic : cstone::BoundaryType::open; };
+    cstone::Box<double> box(in->box[0], in->box[1], in->box[2], in->box[3], in->box[4], in->box[5], bt(in->bc[0]),
+                            bt(in->bc[1]), bt(in->bc[2]));
+    auto wh = sph::tabulateFunction<T, sph::lt::kTableSize>(
+        sph::getSphKernel(sph::SphKernelType::sinc_n, in->sincIndex), 0.0, 2.0);
+    auto whd = sph::tabulateFunction<T, sph::lt::kTableSize>(
+        sph::getSphKernelDerivative(sph::SphKernelType::sinc_n, in->sincIndex), 0.0, 2.0);
+    const double K  = in->K;
+    const auto* nb  = in->neighbors;
+    const unsigned c = in->count;
+    const double *x = xyz[0].data(), *y = xyz[1].data(), *z = xyz[2].data();
+    auto F          = [&](int k) { return f[k].data(); };
+    T r[8]          = {0, 0, 0, 0, 0, 0, 0, 0};
+    switch (in->loop)
+    {
+        case OJ_XMASS:
+            out[0] = sph::xmassJLoop(0, K, box, nb, c, x, y, z, F(OF_H), F(OF_M), wh.data(), whd.data());
+            break;
+        case OJ_GRADH:
+        {
+            auto [kx, gradh] = sph::veDefGradhJLoop(0, K, box, nb, c, x, y, z, F(OF_H), F(OF_M), wh.data(),
+                                                    whd.data(), F(OF_XM));
+            out[0] = kx;
+            out[1] = gradh;
+            break;
+        }
+        case OJ_IAD_STD:
+            sph::IADJLoopSTD(0, K, box, nb, c, x, y, z, F(OF_H), F(OF_M), F(OF_RHO), wh.data(), whd.data(), &r[0],
+                             &r[1], &r[2], &r[3], &r[4], &r[5]);
+            for (int q = 0; q < 6; ++q)
+                out[q] = r[q];
+            break;
+        case OJ_IAD_VE:
+            sph::IADJLoop(0, K, box, nb, c, x, y, z, F(OF_H), wh.data(), whd.data(), F(OF_XM), F(OF_KX), &r[0], &r[1],
+                          &r[2], &r[3], &r[4], &r[5]);
+            for (int q = 0; q < 6; ++q)
+                out[q] = r[q];
+            break;
+        case OJ_DIVV:
+            sph::divV_curlVJLoop(0, K, box, nb, c, x, y, z, F(OF_VX), F(OF_VY), F(OF_VZ), F(OF_H), F(OF_C11),
+                                 F(OF_C12), F(OF_C13), F(OF_C22), F(OF_C23), F(OF_C33), wh.data(), whd.data(),
+                                 F(OF_KX), F(OF_XM), &r[0], &r[1], &r[2], &r[3], &r[4], &r[5], &r[6], &r[7], true);
+            for (int q = 0; q < 8; ++q)
+                out[q] = r[q];
+            break;
+        case OJ_AV:
+            out[0] = sph::AVswitchesJLoop(0, K, box, nb, c, x, y, z, F(OF_VX), F(OF_VY), F(OF_VZ), F(OF_H), F(OF_C),
+                                          F(OF_C11), F(OF_C12), F(OF_C13), F(OF_C22), F(OF_C23), F(OF_C33), wh.data(),
+                                          whd.data(), F(OF_KX), F(OF_XM), F(OF_DIVV), in->dt, T(in->alphamin),
+                                          T(in->alphamax), T(in->decay), F(OF_ALPHA)[0]);
+            break;
+        case OJ_ME_STD:
+        {
+            T du = 0;
+            sph::momentumAndEnergyJLoop(0, K, box, nb, c, x, y, z, F(OF_VX), F(OF_VY), F(OF_VZ), F(OF_H), F(OF_M),
+                                        F(OF_RHO), F(OF_P), F(OF_C), F(OF_C11), F(OF_C12), F(OF_C13), F(OF_C22),
+                                        F(OF_C23), F(OF_C33), wh.data(), whd.data(), &r[0], &r[1], &r[2], &du, &r[4]);
+            out[0] = r[0];
+            out[1] = r[1];
+            out[2] = r[2];
+            out[3] = du;
+            out[4] = r[4];
+            break;
+        }
+        case OJ_ME_VE:
+        {
+            T du = 0;
+            const T Atmin = 0.1, Atmax = 0.2, ramp = 1.0 / (Atmax - Atmin);
+            auto call     = [&](auto avc)
+            {
+                sph::momentumAndEnergyJLoop<decltype(avc)::value>(
+                    0, K, box, nb, c, x, y, z, F(OF_VX), F(OF_VY), F(OF_VZ), F(OF_H), F(OF_M), F(OF_PRHO),
+                    (const T*)nullptr, F(OF_C), F(OF_C11), F(OF_C12), F(OF_C13), F(OF_C22), F(OF_C23), F(OF_C33),
+                    Atmin, Atmax, ramp, wh.data(), F(OF_KX), F(OF_XM), F(OF_ALPHA), F(OF_DV11), F(OF_DV12), F(OF_DV13),
+                    F(OF_DV22), F(OF_DV23), F(OF_DV33), &r[0], &r[1], &r[2], &du, &r[4]);
+            };
+            if (in->avclean) call(std::true_type{});
+            else call(std::false_type{});
+            out[0] = r[0];
+            out[1] = r[1];
+            out[2] = r[2];
+            out[3] = du;
+            out[4] = r[4];
+            break;
+        }
+        default: return 2;
+    }
+    return 0;
+}

@@ -468,7 +468,7 @@ static inline double courant(double vsig, double h, double c, float kc)
 }
 
 /* std momentumAndEnergyJLoop (hydro_std/momentum_energy_kern.hpp:12-134) */
-static double meStdJ(Data& d, const Box& b, int64_t i, float kcour)
+static double meStdJ(Data& d, const Box& b, int64_t i, float kcour, double* maxvOut = nullptr)
 {
     auto F = [&](int k) { return d.f[k].data(); };
     const double *x = F(OF_X), *y = F(OF_Y), *z = F(OF_Z), *vx = F(OF_VX), *vy = F(OF_VY), *vz = F(OF_VZ);
@@ -524,6 +524,7 @@ static double meStdJ(Data& d, const Box& b, int64_t i, float kcour)
     d.f[OF_AX][i] = d.K * mx;
     d.f[OF_AY][i] = d.K * my;
     d.f[OF_AZ][i] = d.K * mz;
+    if (maxvOut) *maxvOut = maxv;
     return courant(maxv, h[i], c[i], kcour);
 }
 
@@ -670,7 +671,7 @@ static double avRv(const double R[3], double eta, double etaCrit, const double g
 }
 
 /* VE momentumAndEnergyJLoop<avClean> (hydro_ve/momentum_energy_kern.hpp:65-222) */
-static double meVeJ(Data& d, const Box& b, int64_t i, bool avClean, float kcour)
+static double meVeJ(Data& d, const Box& b, int64_t i, bool avClean, float kcour, double* maxvOut = nullptr)
 {
     auto F = [&](int k) { return d.f[k].data(); };
     const double *x = F(OF_X), *y = F(OF_Y), *z = F(OF_Z), *vx = F(OF_VX), *vy = F(OF_VY), *vz = F(OF_VZ);
@@ -746,6 +747,7 @@ static double meVeJ(Data& d, const Box& b, int64_t i, bool avClean, float kcour)
     d.f[OF_AX][i] = -d.K * mx;
     d.f[OF_AY][i] = -d.K * my;
     d.f[OF_AZ][i] = -d.K * mz;
+    if (maxvOut) *maxvOut = maxv;
     return courant(maxv, h[i], c[i], kcour);
 }
 
@@ -928,5 +930,62 @@ extern "C" int oracle_sweep(const oracle_in* in, oracle_out* out)
 
     for (int k = 0; k < OF_NFIELDS; ++k)
         if (out->f[k]) std::memcpy(out->f[k], d.f[k].data(), sizeof(double) * n);
+    return 0;
+}
+
+/* One j-loop of particle 0 over an explicit list, for the reference's known-answer tests. */
+extern "C" int oracle_jloop(const oracle_jloop_in* in, double* out)
+{
+    if (!in || !out || in->n <= 0 || !in->neighbors) return 1;
+    const int64_t n = in->n;
+    Data d;
+    d.n = n;
+    d.ngmax = in->count;
+    for (int k = 0; k < OF_NFIELDS; ++k) {
+        d.f[k].assign(n, 0.0);
+        if (in->f[k]) std::memcpy(d.f[k].data(), in->f[k], sizeof(double) * n);
+    }
+    d.nc.assign(n, 1);
+    d.nc[0] = in->count + 1;
+    d.nbr.assign(size_t(n) * in->count, 0);
+    std::memcpy(d.nbr.data(), in->neighbors, sizeof(uint32_t) * in->count);
+    d.K = in->K;
+    tables(in->sincIndex, d.wh, d.whd);
+    Box box = makeBox(in->box, in->bc);
+    double maxv = 0;
+    switch (in->loop) {
+    case OJ_XMASS: out[0] = xmassJ(d, box, 0); break;
+    case OJ_GRADH:
+        gradhJ(d, box, 0);
+        out[0] = d.f[OF_KX][0];
+        out[1] = d.f[OF_GRADH][0];
+        break;
+    case OJ_IAD_STD:
+    case OJ_IAD_VE:
+        if (in->loop == OJ_IAD_STD) iadJ(d, box, 0, d.f[OF_M].data(), d.f[OF_RHO].data());
+        else iadJ(d, box, 0, d.f[OF_XM].data(), d.f[OF_KX].data());
+        for (int q = 0; q < 6; ++q) out[q] = d.f[OF_C11 + q][0];
+        break;
+    case OJ_DIVV:
+        divvJ(d, box, 0, true);
+        out[0] = d.f[OF_DIVV][0];
+        out[1] = d.f[OF_CURLV][0];
+        for (int q = 0; q < 6; ++q) out[2 + q] = d.f[OF_DV11 + q][0];
+        break;
+    case OJ_AV:
+        out[0] = avJ(d, box, 0, in->dt, in->alphamin, in->alphamax, in->decay, d.f[OF_ALPHA][0]);
+        break;
+    case OJ_ME_STD:
+    case OJ_ME_VE:
+        if (in->loop == OJ_ME_STD) meStdJ(d, box, 0, 0.2f, &maxv);
+        else meVeJ(d, box, 0, in->avclean != 0, 0.2f, &maxv);
+        out[0] = d.f[OF_AX][0];
+        out[1] = d.f[OF_AY][0];
+        out[2] = d.f[OF_AZ][0];
+        out[3] = d.f[OF_DU][0];
+        out[4] = maxv;
+        break;
+    default: return 2;
+    }
     return 0;
 }

@@ -1,0 +1,350 @@
+// C ABI of the sphgb sweep (include/sphgb.h).  Every entry point validates its arguments,
+// selects the context's device, runs on the context's stream and returns an sphgb_status;
+// no C++ exception crosses the boundary.
+#include <cstdio>
+#include <mutex>
+#include <new>
+
+#include "pairs.cuh"
+
+namespace sphgb {
+
+namespace {
+thread_local char gCudaError[256] = "";
+}
+
+void setCudaError(cudaError_t e, const char* what)
+{
+    std::snprintf(gCudaError, sizeof(gCudaError), "%s: %s (%d)", what, cudaGetErrorString(e), int(e));
+}
+
+namespace {
+
+int useDevice(sphgb_ctx* c)
+{
+    if (!c) return SPHGB_ERR_ARG;
+    SPHGB_CUDA(cudaSetDevice(c->device));
+    return SPHGB_OK;
+}
+
+// CUDA-event bracket of one stage on the context stream
+struct StageTimer {
+    sphgb_ctx* c;
+    int stage;
+    StageTimer(sphgb_ctx* ctx, int s) : c(ctx), stage(s) { cudaEventRecord(c->ev[2 * s], c->stream); }
+    void stop()
+    {
+        cudaEventRecord(c->ev[2 * stage + 1], c->stream);
+    }
+};
+
+void collectTimings(sphgb_ctx* c, int upto)
+{
+    for (int s = 0; s < upto; ++s) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev[2 * s], c->ev[2 * s + 1]) == cudaSuccess) c->stageMs[s] = ms;
+    }
+}
+
+int checkRange(const sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p || first < 0 || last > p->n || first >= last) return SPHGB_ERR_ARG;
+    return SPHGB_OK;
+}
+
+}  // namespace
+}  // namespace sphgb
+
+using namespace sphgb;
+
+extern "C" {
+
+const char* sphgb_status_string(int s)
+{
+    switch (s) {
+    case SPHGB_OK: return "ok";
+    case SPHGB_ERR_ARG: return "invalid argument";
+    case SPHGB_ERR_CUDA: return "CUDA runtime error";
+    case SPHGB_ERR_ALLOC: return "device allocation failed";
+    case SPHGB_ERR_STATE: return "call out of order";
+    case SPHGB_ERR_TRAVERSAL: return "octree traversal stack overflow";
+    case SPHGB_ERR_NOCONV: return "h / neighbour-count iteration did not converge for some particles";
+    case SPHGB_ERR_NOTFOUND: return "no usable CUDA device";
+    case SPHGB_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+    default: return "unknown status";
+    }
+}
+
+const char* sphgb_last_cuda_error(void) { return sphgb::gCudaError; }
+
+int sphgb_version(void) { return 100; }
+
+int sphgb_default_params(sphgb_params* p)
+{
+    if (!p) return SPHGB_ERR_ARG;
+    p->ng0 = 100;
+    p->ngmax = 150;
+    p->bucket = 64;
+    p->gamma = 5.0 / 3.0;
+    p->Kcour = 0.2;
+    p->sincIndex = 6.0;
+    p->alphamin = 0.05;
+    p->alphamax = 1.0;
+    p->decay_constant = 0.2;
+    p->minDt = 1e-6;
+    return SPHGB_OK;
+}
+
+int sphgb_create(sphgb_ctx** out, int device)
+{
+    if (!out) return SPHGB_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return SPHGB_ERR_NOTFOUND;
+    if (device < 0 || device >= count) return SPHGB_ERR_ARG;
+    SPHGB_CUDA(cudaSetDevice(device));
+    sphgb_ctx* c = new (std::nothrow) sphgb_ctx();
+    if (!c) return SPHGB_ERR_ALLOC;
+    c->device = device;
+    sphgb_default_params(&c->prm);
+    cudaError_t e = cudaMalloc(&c->dFlags, sizeof(int));
+    if (e != cudaSuccess) {
+        setCudaError(e, "cudaMalloc");
+        delete c;
+        return SPHGB_ERR_ALLOC;
+    }
+    cudaMemset(c->dFlags, 0, sizeof(int));
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    int s = buildTables(c);
+    if (s != SPHGB_OK) {
+        sphgb_destroy(c);
+        return s;
+    }
+    *out = c;
+    return SPHGB_OK;
+}
+
+int sphgb_destroy(sphgb_ctx* c)
+{
+    if (!c) return SPHGB_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    DBuf* bufs[] = {&c->keys,     &c->keysAlt,      &c->order,         &c->orderAlt,      &c->sortTemp,
+                    &c->gatherScratch, &c->minmax,  &c->splitCount,    &c->splitOffset,   &c->leafKeysTmp,
+                    &c->internalTmp,   &c->internalCodes, &c->leaves,  &c->layout,        &c->prefixes,
+                    &c->childOffsets,  &c->internalToLeaf, &c->nodeCenter, &c->nodeSize,  &c->nodeBoxF,
+                    &c->levelRangeDev, &c->nbr,     &c->ncount,        &c->active,        &c->counters,
+                    &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
+                    &c->gridLoc,  &c->hInv64,       &c->reduceScratch};
+    for (DBuf* b : bufs) b->release();
+    if (c->dFlags) cudaFree(c->dFlags);
+    for (auto& ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    delete c;
+    return SPHGB_OK;
+}
+
+int sphgb_set_stream(sphgb_ctx* c, void* stream)
+{
+    SPHGB_TRY(useDevice(c));
+    c->stream = static_cast<cudaStream_t>(stream);
+    return SPHGB_OK;
+}
+
+int sphgb_set_params(sphgb_ctx* c, const sphgb_params* p)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || p->ngmax == 0 || p->bucket == 0 || p->ng0 == 0 || !(p->sincIndex > 0)) return SPHGB_ERR_ARG;
+    bool tables = p->sincIndex != c->prm.sincIndex || !c->tablesReady;
+    c->prm = *p;
+    if (tables) SPHGB_TRY(buildTables(c));
+    return SPHGB_OK;
+}
+
+int sphgb_get_kernel_K(sphgb_ctx* c, double* K)
+{
+    if (!c || !K) return SPHGB_ERR_ARG;
+    *K = c->K;
+    return SPHGB_OK;
+}
+
+int sphgb_domain_sync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || !box) return SPHGB_ERR_ARG;
+    if (p->precision != SPHGB_FP64 && p->precision != SPHGB_MIXED) return SPHGB_ERR_ARG;
+    StageTimer t(c, kStageSync);
+    int s = domainSync(c, p, box);
+    t.stop();
+    if (s == SPHGB_OK) {
+        SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+        collectTimings(c, 1);
+    }
+    return s;
+}
+
+int sphgb_get_tree(sphgb_ctx* c, const uint64_t** leaves, const uint32_t** layout, const uint64_t** prefixes,
+                   const int32_t** childOffsets, const int32_t** internalToLeaf, sphgb_stats* stats)
+{
+    if (!c) return SPHGB_ERR_ARG;
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    if (leaves) *leaves = reinterpret_cast<const uint64_t*>(c->leaves.p);
+    if (layout) *layout = c->layout.as<uint32_t>();
+    if (prefixes) *prefixes = reinterpret_cast<const uint64_t*>(c->prefixes.p);
+    if (childOffsets) *childOffsets = c->childOffsets.as<int32_t>();
+    if (internalToLeaf) *internalToLeaf = c->internalToLeaf.as<int32_t>();
+    if (stats) *stats = c->stats;
+    return SPHGB_OK;
+}
+
+int sphgb_get_order(sphgb_ctx* c, const uint32_t** order)
+{
+    if (!c || !order) return SPHGB_ERR_ARG;
+    if (!c->haveSync) return SPHGB_ERR_STATE;
+    *order = c->order.as<uint32_t>();
+    return SPHGB_OK;
+}
+
+int sphgb_find_neighbors(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,
+                         int32_t hPrec, int64_t first, int64_t last, uint32_t ngmax, uint32_t* neighbors, uint32_t* nc)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    if (first < 0 || last > c->n || first >= last) return SPHGB_ERR_ARG;
+    StageTimer t(c, kStageNbr);
+    int s = findNeighborsFixed(c, x, y, z, h, hPrec, first, last, ngmax, neighbors, nc);
+    t.stop();
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return s;
+}
+
+int sphgb_find_neighbors_sph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    SPHGB_TRY(checkRange(p, first, last));
+    if (last > c->n) return SPHGB_ERR_ARG;
+    StageTimer t(c, kStageNbr);
+    int s = findNeighborsSph(c, p, first, last);
+    t.stop();
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    collectTimings(c, 2);
+    return s;
+}
+
+int sphgb_export_neighbors(sphgb_ctx* c, uint32_t* out)
+{
+    SPHGB_TRY(useDevice(c));
+    return exportNeighbors(c, out);
+}
+
+#define SPHGB_PASS(name, call)                                  \
+    int name                                                    \
+    {                                                           \
+        SPHGB_TRY(useDevice(c));                                \
+        SPHGB_TRY(checkRange(p, first, last));                  \
+        int s_ = (call);                                        \
+        if (s_ != SPHGB_OK) return s_;                          \
+        SPHGB_CUDA(cudaStreamSynchronize(c->stream));           \
+        return SPHGB_OK;                                        \
+    }
+
+SPHGB_PASS(sphgb_compute_density(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passDensity(c, p, first, last))
+SPHGB_PASS(sphgb_compute_eos_std(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passEosStd(c, p, first, last))
+SPHGB_PASS(sphgb_compute_iad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passIadStd(c, p, first, last))
+SPHGB_PASS(sphgb_compute_momentum_energy_std(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last,
+                                             double* minDtCourant),
+           passMomentumEnergyStd(c, p, first, last, minDtCourant))
+SPHGB_PASS(sphgb_compute_xmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passXMass(c, p, first, last))
+SPHGB_PASS(sphgb_compute_ve_def_gradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passGradh(c, p, first, last))
+SPHGB_PASS(sphgb_compute_eos(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passEosVe(c, p, first, last))
+SPHGB_PASS(sphgb_compute_iad_divv_curlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passIadDivvCurlv(c, p, first, last))
+SPHGB_PASS(sphgb_compute_av_switches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last),
+           passAVswitches(c, p, first, last))
+SPHGB_PASS(sphgb_compute_momentum_energy(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last,
+                                         int32_t avClean, float* groupDt, double* minDtCourant),
+           passMomentumEnergyVe(c, p, first, last, avClean, groupDt, minDtCourant))
+
+int sphgb_sweep_passes(sphgb_ctx* c, sphgb_particles* p, int32_t variant, int32_t avClean, double* minDtCourant)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || !c->haveTree) return SPHGB_ERR_STATE;
+    const int64_t first = 0, last = p->n;
+    int s;
+    {
+        StageTimer t(c, kStageNbr);
+        s = findNeighborsSph(c, p, first, last);
+        t.stop();
+        if (s != SPHGB_OK && s != SPHGB_ERR_NOCONV) return s;
+    }
+    int st = s;
+    auto stage = [&](int k, auto&& fn) {
+        StageTimer t(c, kStagePass0 + k);
+        int r = fn();
+        t.stop();
+        return r;
+    };
+    if (variant == SPHGB_STD) {
+        SPHGB_TRY(stage(0, [&] { return passDensity(c, p, first, last); }));
+        SPHGB_TRY(stage(1, [&] { return passEosStd(c, p, first, last); }));
+        SPHGB_TRY(stage(2, [&] { return passIadStd(c, p, first, last); }));
+        SPHGB_TRY(stage(3, [&] { return passMomentumEnergyStd(c, p, first, last, minDtCourant); }));
+    } else if (variant == SPHGB_VE) {
+        SPHGB_TRY(stage(0, [&] { return passXMass(c, p, first, last); }));
+        SPHGB_TRY(stage(1, [&] { return passGradh(c, p, first, last); }));
+        SPHGB_TRY(stage(2, [&] { return passEosVe(c, p, first, last); }));
+        SPHGB_TRY(stage(3, [&] { return passIadDivvCurlv(c, p, first, last); }));
+        SPHGB_TRY(stage(4, [&] { return passAVswitches(c, p, first, last); }));
+        SPHGB_TRY(stage(5, [&] { return passMomentumEnergyVe(c, p, first, last, avClean, nullptr, minDtCourant); }));
+    } else {
+        return SPHGB_ERR_ARG;
+    }
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    collectTimings(c, variant == SPHGB_STD ? kStagePass0 + 4 : kStagePass0 + 6);
+    return st;
+}
+
+int sphgb_sweep(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box, int32_t variant, int32_t avClean,
+                double* minDtCourant)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || !box) return SPHGB_ERR_ARG;
+    if (variant != SPHGB_STD && variant != SPHGB_VE) return SPHGB_ERR_ARG;
+    {
+        StageTimer t(c, kStageSync);
+        int s = domainSync(c, p, box);
+        t.stop();
+        if (s != SPHGB_OK) return s;
+    }
+    return sphgb_sweep_passes(c, p, variant, avClean, minDtCourant);
+}
+
+int sphgb_get_stats(sphgb_ctx* c, sphgb_stats* s)
+{
+    if (!c || !s) return SPHGB_ERR_ARG;
+    *s = c->stats;
+    return SPHGB_OK;
+}
+
+int sphgb_get_timings(sphgb_ctx* c, float* ms, int32_t count)
+{
+    if (!c || !ms || count < 0) return SPHGB_ERR_ARG;
+    for (int k = 0; k < count && k < kNumStages; ++k) ms[k] = c->stageMs[k];
+    return SPHGB_OK;
+}
+
+int sphgb_kernel_launches(sphgb_ctx* c, int64_t* n)
+{
+    if (!c || !n) return SPHGB_ERR_ARG;
+    *n = c->launches;
+    return SPHGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// Internal state of an sphgb context and the helpers every translation unit uses.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sphgb {
+
+// last CUDA error text, readable through sphgb_last_cuda_error()
+void setCudaError(cudaError_t e, const char* what);
+
+#define SPHGB_CUDA(call)                                   \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) {                           \
+            ::sphgb::setCudaError(e_, #call);              \
+            return SPHGB_ERR_CUDA;                         \
+        }                                                  \
+    } while (0)
+
+#define SPHGB_TRY(call)                      \
+    do {                                     \
+        int s_ = (call);                     \
+        if (s_ != SPHGB_OK) return s_;       \
+    } while (0)
+
+// growable device buffer
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need)
+    {
+        if (need <= bytes && p) return SPHGB_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t alloc = need < 256 ? 256 : need;
+        cudaError_t e = cudaMalloc(&p, alloc);
+        if (e != cudaSuccess) {
+            setCudaError(e, "cudaMalloc");
+            p = nullptr;
+            return SPHGB_ERR_ALLOC;
+        }
+        bytes = alloc;
+        return SPHGB_OK;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template<class T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+};
+
+enum Stage { kStageSync = 0, kStageNbr = 1, kStagePass0 = 2, kNumStages = 8 };
+
+}  // namespace sphgb
+
+struct sphgb_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    sphgb_params prm{};
+    double K = 0.0;
+    bool tablesReady = false;
+
+    sphgb::DevBox box{};
+    sphgb_box hbox{};
+    bool haveBox = false;
+    int64_t n = 0;
+
+    // domain sync
+    sphgb::DBuf keys, keysAlt, order, orderAlt, sortTemp, gatherScratch, minmax;
+    bool haveSync = false;
+
+    // cornerstone tree and octree
+    int64_t numLeaves = 0, numInternal = 0, numNodes = 0;
+    int32_t levelRange[sphgb::kMaxLevel + 2] = {};
+    sphgb::DBuf splitCount, splitOffset, leafKeysTmp, internalTmp, internalCodes;
+    sphgb::DBuf leaves, layout, prefixes, childOffsets, internalToLeaf;
+    sphgb::DBuf nodeCenter, nodeSize;   // double3-packed, 3 doubles per node (reference nodeFpCenters)
+    sphgb::DBuf nodeBoxF;               // float4 {cx, cy, cz, pad} + float4 {sx, sy, sz, -}: traversal
+    sphgb::DBuf levelRangeDev;
+    bool haveTree = false;
+
+    // neighbour lists: nbr[k * stride + (i - first)], transposed for coalesced pair-loop reads
+    int64_t nbrFirst = 0, nbrLast = 0, nbrStride = 0;
+    uint32_t nbrNgmax = 0;
+    sphgb::DBuf nbr, ncount, active, counters;
+    bool haveNbr = false;
+    int precisionBuilt = -1;
+    const double* xBuilt = nullptr;
+
+    // kernel tables (FP64 and FP32)
+    sphgb::DBuf wh64, whd64, wh32, whd32;
+
+    // mixed precision grid-local coordinates: packed cell (21 bits per axis) + float4 {dx,dy,dz,1/h}
+    sphgb::DBuf gridKey, gridLoc;
+    // per-particle reciprocals reused by the FP64 passes (same IEEE results as in-loop division)
+    sphgb::DBuf hInv64;
+    // validity of the precomputes: the lists' epoch and the field pointers they were made from
+    int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;
+    const void* prepMixedFor = nullptr;
+    const void* prepMixedH = nullptr;
+    const void* prepFp64H = nullptr;
+    sphgb::DBuf reduceScratch;
+
+    // device status word and small counters
+    int* dFlags = nullptr;
+
+    // statistics and timing
+    sphgb_stats stats{};
+    cudaEvent_t ev[2 * sphgb::kNumStages] = {};
+    float stageMs[sphgb::kNumStages] = {};
+    int64_t launches = 0;
+};
+
+namespace sphgb {
+
+// per-translation-unit entry points used by capi.cu
+int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box);
+int buildTree(sphgb_ctx* c);
+int buildTables(sphgb_ctx* c);
+int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,
+                       int32_t hPrec, int64_t first, int64_t last, uint32_t ngmax, uint32_t* nbrOut, uint32_t* ncOut);
+int exportNeighbors(sphgb_ctx* c, uint32_t* out);
+int prepareMixed(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int prepareFp64(sphgb_ctx* c, sphgb_particles* p);
+
+int passDensity(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passEosStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passIadStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passMomentumEnergyStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, double* minDt);
+int passXMass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passEosVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, int avClean, float* groupDt,
+                         double* minDt);
+
+// min-reduction of per-block Courant dt partials into one double on the host
+int reduceMinDt(sphgb_ctx* c, const double* partials, int count, double* out);
+
+inline unsigned gridFor(int64_t work, int block) { return unsigned((work + block - 1) / block); }
+
+// launch bookkeeping: count one kernel launch and check the launch error
+inline int launched(sphgb_ctx* c, const char* what)
+{
+    c->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        setCudaError(e, what);
+        return SPHGB_ERR_CUDA;
+    }
+    return SPHGB_OK;
+}
+
+}  // namespace sphgb

@@ -1,0 +1,384 @@
+// Standard-SPH pair passes: density, ideal-gas EOS, IAD, momentum and energy.
+//
+// FP64 form: the arithmetic of the reference j-loops in the same order
+//   density  -> xmassJLoop with rho<->xm swapped, then rho = m / xm
+//               (sph/include/sph/hydro_std/density.hpp:41-60, hydro_ve/xmass_kern.hpp:50-79)
+//   EOS      -> idealGasEOS_u (hydro_std/eos.hpp:54-80, sph/eos.hpp:34-44)
+//   IAD      -> IADJLoopSTD (hydro_std/iad_kern.hpp:12-77)
+//   ME       -> momentumAndEnergyJLoop + tsKCourant (hydro_std/momentum_energy_kern.hpp:12-134,
+//               momentum_energy.hpp:41-101)
+// with per-particle reciprocals (1/h) hoisted out of the pair loop; they are the same IEEE
+// divisions, so the results are unchanged.
+// Mixed form: FP32 pair arithmetic on grid-local offsets, Kahan sums, per-particle epilogues
+// (normalisation, 3x3 inverse factor) in FP64.
+#include "pairs.cuh"
+
+namespace sphgb {
+
+namespace {
+
+// ---------------------------------------------------------------- density / xmass
+template<class P, bool StoreRho>
+__global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
+                                                          const void* m, const void* wh, double K, void* out)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = lv.capped(ii);
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        const double* tab = static_cast<const double*>(wh);
+        auto t = cf.target(i);
+        double hi = ld<double>(h, i), mi = ld<double>(m, i);
+        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        double rho0 = mi;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            double rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            double dist = sqrt(rx * rx + ry * ry + rz * rz);
+            rho0 += tableLookup(tab, dist * hInv) * ld<double>(m, j);
+        }
+        double xm = mi / (rho0 * K * h3Inv);
+        st<double>(out, i, StoreRho ? mi / xm : xm);
+    } else {
+        const float* tab = static_cast<const float*>(wh);
+        auto t = cm.target(i);
+        float mi = ld<float>(m, i);
+        KSum rho0;
+        rho0.add(mi);
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            float rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+            rho0.add(tableLookup(tab, dist * t.hInv) * ld<float>(m, j));
+        }
+        double hi = double(ld<float>(h, i));
+        double rho = rho0.value64() * K / (hi * hi * hi);
+        st<float>(out, i, StoreRho ? float(rho) : float(double(mi) / rho));
+    }
+}
+
+// ---------------------------------------------------------------- EOS
+template<class P>
+__global__ void eosStdKernel(int64_t first, int64_t last, const double* u, const void* rho, double gamma, void* p,
+                             void* c)
+{
+    using T = typename P::T;
+    int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    double tmp = u[i] * (gamma - 1.0);
+    double pi = double(ld<T>(rho, i)) * tmp;
+    st<T>(p, i, T(pi));
+    st<T>(c, i, T(sqrt(gamma * tmp)));
+}
+
+// ---------------------------------------------------------------- IAD
+struct IadOut {
+    void *c11, *c12, *c13, *c22, *c23, *c33;
+};
+
+// volume of j: num[j] / den[j] (std: m / rho, ve: xm / kx)
+template<class P>
+__global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
+                                                        const void* num, const void* den, const void* wh, double K,
+                                                        IadOut o)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = lv.capped(ii);
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        const double* tab = static_cast<const double*>(wh);
+        auto t = cf.target(i);
+        double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
+        double t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            double rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            double dist = sqrt(rx * rx + ry * ry + rz * rz);
+            double w = tableLookup(tab, dist * hiInv);
+            double vw = ld<double>(num, j) / ld<double>(den, j) * w;
+            t11 += rx * rx * vw;
+            t12 += rx * ry * vw;
+            t13 += rx * rz * vw;
+            t22 += ry * ry * vw;
+            t23 += ry * rz * vw;
+            t33 += rz * rz * vw;
+        }
+        double cc[6];
+        iadInvert<double>(t11, t12, t13, t22, t23, t33, hi, K, cc);
+        st<double>(o.c11, i, cc[0]);
+        st<double>(o.c12, i, cc[1]);
+        st<double>(o.c13, i, cc[2]);
+        st<double>(o.c22, i, cc[3]);
+        st<double>(o.c23, i, cc[4]);
+        st<double>(o.c33, i, cc[5]);
+    } else {
+        const float* tab = static_cast<const float*>(wh);
+        auto t = cm.target(i);
+        KSum t11, t12, t13, t22, t23, t33;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            float rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+            float w = tableLookup(tab, dist * t.hInv);
+            float vw = __fdividef(ld<float>(num, j), ld<float>(den, j)) * w;
+            t11.add(rx * rx * vw);
+            t12.add(rx * ry * vw);
+            t13.add(rx * rz * vw);
+            t22.add(ry * ry * vw);
+            t23.add(ry * rz * vw);
+            t33.add(rz * rz * vw);
+        }
+        float cc[6];
+        iadInvert<float>(t11.value(), t12.value(), t13.value(), t22.value(), t23.value(), t33.value(),
+                         double(ld<float>(h, i)), K, cc);
+        st<float>(o.c11, i, cc[0]);
+        st<float>(o.c12, i, cc[1]);
+        st<float>(o.c13, i, cc[2]);
+        st<float>(o.c22, i, cc[3]);
+        st<float>(o.c23, i, cc[4]);
+        st<float>(o.c33, i, cc[5]);
+    }
+}
+
+// ---------------------------------------------------------------- momentum and energy (std)
+struct MeStdArgs {
+    const void *vx, *vy, *vz, *h, *m, *rho, *p, *c;
+    const void *c11, *c12, *c13, *c22, *c23, *c33;
+    const void* wh;
+    const double* hInv64;
+    double K;
+    float Kcour;
+    void *ax, *ay, *az;
+    double* du;
+    unsigned long long* minDt;
+};
+
+template<class P>
+__global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64 cf, CoordMixed cm, MeStdArgs a)
+{
+    const int64_t i0 = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const bool valid = i0 < lv.last;
+    const int64_t i = valid ? i0 : lv.first;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = valid ? lv.capped(ii) : 0u;
+    double dt = INFINITY;
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        using T = double;
+        const double* tab = static_cast<const double*>(a.wh);
+        auto t = cf.target(i);
+        T hi = ld<T>(a.h, i), roi = ld<T>(a.rho, i), pri = ld<T>(a.p, i), ci = ld<T>(a.c, i);
+        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        T mi_roi = ld<T>(a.m, i) / roi;
+        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
+        T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
+        T maxv = 0, mx = 0, my = 0, mz = 0, en = 0;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T hjInv = __ldg(a.hInv64 + j);
+            T v1 = dist * hiInv, v2 = dist * hjInv;
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            T hjInv3 = hjInv * hjInv * hjInv;
+            T Wi = hiInv3 * tableLookup(tab, v1);
+            T Wj = hjInv3 * tableLookup(tab, v2);
+            T a1i = c11i * rx + c12i * ry + c13i * rz;
+            T a2i = c12i * rx + c22i * ry + c23i * rz;
+            T a3i = c13i * rx + c23i * ry + c33i * rz;
+            T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
+            T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
+            T a1j = c11j * rx + c12j * ry + c13j * rz;
+            T a2j = c12j * rx + c22j * ry + c23j * rz;
+            T a3j = c13j * rx + c23j * ry + c33j * rz;
+            T roj = ld<T>(a.rho, j), cj = ld<T>(a.c, j);
+            T wij = rv / dist;
+            T visc = T(0.5) * artificialViscosity<T>(1.0, 1.0, ci, cj, wij);
+            T vsig = ci + cj - T(3) * wij;
+            maxv = (vsig > maxv) ? vsig : maxv;
+            T mj = ld<T>(a.m, j);
+            T mjrojWj = mj / roj * Wj;
+            T mjproi = mj * pri / (T(1) * roi * roi);
+            {
+                T aa = Wi * (mjproi + visc * mi_roi);
+                T bb = mjrojWj * (ld<T>(a.p, j) / (roj * T(1)) + visc);
+                mx += aa * a1i + bb * a1j;
+                my += aa * a2i + bb * a2j;
+                mz += aa * a3i + bb * a3j;
+            }
+            {
+                T aa = Wi * (T(2) * mjproi + visc * mi_roi);
+                T bb = visc * mjrojWj;
+                en += vxij * (aa * a1i + bb * a1j) + vyij * (aa * a2i + bb * a2j) + vzij * (aa * a3i + bb * a3j);
+            }
+        }
+        if (valid) {
+            a.du[i] = -a.K * 0.5 * en;
+            st<T>(a.ax, i, a.K * mx);
+            st<T>(a.ay, i, a.K * my);
+            st<T>(a.az, i, a.K * mz);
+            dt = courantDt(maxv, hi, ci, a.Kcour);
+        }
+    } else {
+        using T = float;
+        const float* tab = static_cast<const float*>(a.wh);
+        auto t = cm.target(i);
+        T hi = ld<T>(a.h, i), roi = ld<T>(a.rho, i), pri = ld<T>(a.p, i), ci = ld<T>(a.c, i);
+        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        T mi_roi = ld<T>(a.m, i) / roi;
+        T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
+        T proi2 = pri / (roi * roi);
+        T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
+        T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
+        T maxv = 0;
+        KSum mx, my, mz, en;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            T rinv = rsqrtf(r2);
+            T dist = r2 * rinv;
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T v1 = dist * hiInv, v2 = dist * hjInv;
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            T Wi = hiInv3 * tableLookup(tab, v1);
+            T Wj = (hjInv * hjInv * hjInv) * tableLookup(tab, v2);
+            T a1i = c11i * rx + c12i * ry + c13i * rz;
+            T a2i = c12i * rx + c22i * ry + c23i * rz;
+            T a3i = c13i * rx + c23i * ry + c33i * rz;
+            T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
+            T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
+            T a1j = c11j * rx + c12j * ry + c13j * rz;
+            T a2j = c12j * rx + c22j * ry + c23j * rz;
+            T a3j = c13j * rx + c23j * ry + c33j * rz;
+            T roj = ld<T>(a.rho, j), cj = ld<T>(a.c, j);
+            T rojInv = __frcp_rn(roj);
+            T wij = rv * rinv;
+            T visc = T(0.5) * artificialViscosity<T>(1.f, 1.f, ci, cj, wij);
+            T vsig = ci + cj - T(3) * wij;
+            maxv = (vsig > maxv) ? vsig : maxv;
+            T mj = ld<T>(a.m, j);
+            T mjrojWj = mj * rojInv * Wj;
+            T mjproi = mj * proi2;
+            T aa = Wi * (mjproi + visc * mi_roi);
+            T bb = mjrojWj * (ld<T>(a.p, j) * rojInv + visc);
+            mx.add(aa * a1i + bb * a1j);
+            my.add(aa * a2i + bb * a2j);
+            mz.add(aa * a3i + bb * a3j);
+            T ae = Wi * (T(2) * mjproi + visc * mi_roi);
+            T be = visc * mjrojWj;
+            en.add(vxij * (ae * a1i + be * a1j) + vyij * (ae * a2i + be * a2j) + vzij * (ae * a3i + be * a3j));
+        }
+        if (valid) {
+            a.du[i] = -a.K * 0.5 * en.value64();
+            st<T>(a.ax, i, float(a.K * mx.value64()));
+            st<T>(a.ay, i, float(a.K * my.value64()));
+            st<T>(a.az, i, float(a.K * mz.value64()));
+            dt = courantDt(double(maxv), double(hi), double(ci), a.Kcour);
+        }
+    }
+    if (a.minDt) blockMinDt(dt, a.minDt);
+}
+
+template<class P>
+int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, void* out, bool storeRho)
+{
+    SPHGB_TRY(checkPass(c, p, first, last));
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    CoordFp64 cf = coordFp64(c, p);
+    CoordMixed cm = coordMixed(c);
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    unsigned blocks = gridFor(last - first, kPairBlock);
+    if (storeRho)
+        xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
+    else
+        xmassKernel<P, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
+    return launched(c, "xmassKernel");
+}
+
+template<class P>
+int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, const void* num, const void* den)
+{
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
+        lv, coordFp64(c, p), coordMixed(c), p->h, num, den, wh, c->K, IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
+    return launched(c, "iadKernel");
+}
+
+template<class P>
+int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, double* minDt)
+{
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    MeStdArgs a{p->vx,  p->vy,  p->vz,  p->h,  p->m,  p->rho, p->p, p->c, p->c11, p->c12, p->c13, p->c22, p->c23,
+                p->c33, nullptr, c->hInv64.as<double>(), c->K, float(c->prm.Kcour), p->ax, p->ay, p->az, p->du,
+                nullptr};
+    a.wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    SPHGB_TRY(beginDtReduction(c, &a.minDt));
+    meStdKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p),
+                                                                                     coordMixed(c), a);
+    SPHGB_TRY(launched(c, "meStdKernel"));
+    return endDtReduction(c, a.minDt, minDt);
+}
+
+}  // namespace
+
+int passDensity(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->rho || !p->m || !p->h) return SPHGB_ERR_ARG;
+    if (p->precision == SPHGB_MIXED) return launchXmass<MixedTag>(c, p, first, last, p->rho, true);
+    return launchXmass<Fp64Tag>(c, p, first, last, p->rho, true);
+}
+
+int passXMass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->xm || !p->m || !p->h) return SPHGB_ERR_ARG;
+    if (p->precision == SPHGB_MIXED) return launchXmass<MixedTag>(c, p, first, last, p->xm, false);
+    return launchXmass<Fp64Tag>(c, p, first, last, p->xm, false);
+}
+
+int passEosStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->u || !p->rho || !p->p || !p->c || first < 0 || last > p->n || first >= last) return SPHGB_ERR_ARG;
+    unsigned blocks = gridFor(last - first, 256);
+    if (p->precision == SPHGB_MIXED)
+        eosStdKernel<MixedTag><<<blocks, 256, 0, c->stream>>>(first, last, p->u, p->rho, c->prm.gamma, p->p, p->c);
+    else
+        eosStdKernel<Fp64Tag><<<blocks, 256, 0, c->stream>>>(first, last, p->u, p->rho, c->prm.gamma, p->p, p->c);
+    return launched(c, "eosStdKernel");
+}
+
+int passIadStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->m || !p->rho || !p->c11 || !p->c12 || !p->c13 || !p->c22 || !p->c23 || !p->c33) return SPHGB_ERR_ARG;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    if (p->precision == SPHGB_MIXED) return launchIad<MixedTag>(c, p, first, last, p->m, p->rho);
+    return launchIad<Fp64Tag>(c, p, first, last, p->m, p->rho);
+}
+
+int passMomentumEnergyStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, double* minDt)
+{
+    if (!p->vx || !p->vy || !p->vz || !p->rho || !p->p || !p->c || !p->ax || !p->ay || !p->az || !p->du ||
+        !p->c11)
+        return SPHGB_ERR_ARG;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    if (p->precision == SPHGB_MIXED) return launchMeStd<MixedTag>(c, p, first, last, minDt);
+    return launchMeStd<Fp64Tag>(c, p, first, last, minDt);
+}
+
+}  // namespace sphgb

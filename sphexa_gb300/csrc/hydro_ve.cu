@@ -1,0 +1,684 @@
+// Volume-element SPH pair passes with the artificial-viscosity switch.
+//
+// FP64 form follows the reference j-loops operation by operation:
+//   gradh     -> veDefGradhJLoop (sph/include/sph/hydro_ve/ve_def_gradh_kern.hpp:43-90)
+//   EOS       -> computeIdealGasEOS_Impl (hydro_ve/eos.hpp:52-94)
+//   IAD+divv  -> IADJLoop then divV_curlVJLoop over the same list in one kernel
+//                (hydro_ve/iad_kern.hpp:43-109, divv_curlv_kern.hpp:43-123)
+//   AV switch -> AVswitchesJLoop (hydro_ve/av_switches_kern.hpp:43-137)
+//   ME        -> momentumAndEnergyJLoop<avClean> + avRvCorrection (hydro_ve/momentum_energy_kern.hpp)
+// The mixed form runs the same loops in FP32 on grid-local offsets with Kahan sums.
+#include "pairs.cuh"
+
+namespace sphgb {
+
+namespace {
+
+// ---------------------------------------------------------------- gradh (kx, gradh)
+template<class P>
+__global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
+                                                          const void* m, const void* xm, const void* wh,
+                                                          const void* whd, double K, void* kxOut, void* gradhOut)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = lv.capped(ii);
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        const double *tw = static_cast<const double*>(wh), *tdw = static_cast<const double*>(whd);
+        auto t = cf.target(i);
+        double hi = ld<double>(h, i), mi = ld<double>(m, i), xmi = ld<double>(xm, i);
+        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        double kxi = xmi, whomega = -3.0 * xmi, wrho0 = -3.0 * mi;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            double rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            double dist = sqrt(rx * rx + ry * ry + rz * rz);
+            double v = dist * hInv;
+            double w = tableLookup(tw, v), dw = tableLookup(tdw, v);
+            double dterh = -(3.0 * w + v * dw);
+            double xmj = ld<double>(xm, j);
+            kxi += w * xmj;
+            whomega += dterh * xmj;
+            wrho0 += dterh * ld<double>(m, j);
+        }
+        kxi *= K * h3Inv;
+        whomega *= K * h3Inv * hInv;
+        wrho0 *= K * h3Inv * hInv;
+        whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
+        double rhoi = kxi * mi / xmi;
+        double dhdrho = -hi / (rhoi * 3.0);
+        st<double>(kxOut, i, kxi);
+        st<double>(gradhOut, i, 1.0 - dhdrho * whomega);
+    } else {
+        const float *tw = static_cast<const float*>(wh), *tdw = static_cast<const float*>(whd);
+        auto t = cm.target(i);
+        float mi = ld<float>(m, i), xmi = ld<float>(xm, i);
+        KSum kx, whom, wr0;
+        kx.add(xmi);
+        whom.add(-3.f * xmi);
+        wr0.add(-3.f * mi);
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            float rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+            float v = dist * t.hInv;
+            float w = tableLookup(tw, v), dw = tableLookup(tdw, v);
+            float dterh = -(3.f * w + v * dw);
+            float xmj = ld<float>(xm, j);
+            kx.add(w * xmj);
+            whom.add(dterh * xmj);
+            wr0.add(dterh * ld<float>(m, j));
+        }
+        double hi = double(ld<float>(h, i)), hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
+        double kxi = kx.value64() * (K * h3Inv);
+        double wo = whom.value64() * (K * h3Inv * hInv);
+        double wr = wr0.value64() * (K * h3Inv * hInv);
+        wo = wo * double(mi) / double(xmi) + (kxi - K * double(xmi) * h3Inv) * wr;
+        double rhoi = kxi * double(mi) / double(xmi);
+        double dhdrho = -hi / (rhoi * 3.0);
+        st<float>(kxOut, i, float(kxi));
+        st<float>(gradhOut, i, float(1.0 - dhdrho * wo));
+    }
+}
+
+// ---------------------------------------------------------------- EOS (ideal gas, VE)
+template<class P>
+__global__ void eosVeKernel(int64_t first, int64_t last, const double* u, const void* m, const void* kx,
+                            const void* xm, const void* gradh, double gamma, void* prho, void* c, void* rho, void* p)
+{
+    using T = typename P::T;
+    int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    T kxi = ld<T>(kx, i), mi = ld<T>(m, i), xmi = ld<T>(xm, i);
+    T rhoi = kxi * mi / xmi;
+    double tmp = u[i] * (gamma - 1.0);
+    double pi = double(rhoi) * tmp;
+    st<T>(prho, i, T(pi / double(kxi * mi * mi * ld<T>(gradh, i))));
+    st<T>(c, i, T(sqrt(gamma * tmp)));
+    if (rho) st<T>(rho, i, rhoi);
+    if (p) st<T>(p, i, T(pi));
+}
+
+// ---------------------------------------------------------------- IAD + divv/curlv
+struct IadDivvArgs {
+    const void *h, *vx, *vy, *vz, *xm, *kx, *wh;
+    double K;
+    void *c11, *c12, *c13, *c22, *c23, *c33, *divv, *curlv;
+    void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
+};
+
+template<class P>
+__global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = lv.capped(ii);
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        using T = double;
+        const double* tab = static_cast<const double*>(a.wh);
+        auto t = cf.target(i);
+        T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        T t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            T w = tableLookup(tab, dist * hiInv);
+            T vw = ld<T>(a.xm, j) / ld<T>(a.kx, j) * w;
+            t11 += rx * rx * vw;
+            t12 += rx * ry * vw;
+            t13 += rx * rz * vw;
+            t22 += ry * ry * vw;
+            t23 += ry * rz * vw;
+            t33 += rz * rz * vw;
+        }
+        T cc[6];
+        iadInvert<T>(t11, t12, t13, t22, t23, t33, hi, a.K, cc);
+        st<T>(a.c11, i, cc[0]);
+        st<T>(a.c12, i, cc[1]);
+        st<T>(a.c13, i, cc[2]);
+        st<T>(a.c22, i, cc[3]);
+        st<T>(a.c23, i, cc[4]);
+        st<T>(a.c33, i, cc[5]);
+
+        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        T dVx[3] = {0, 0, 0}, dVy[3] = {0, 0, 0}, dVz[3] = {0, 0, 0};
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            T vxji = ld<T>(a.vx, j) - vxi, vyji = ld<T>(a.vy, j) - vyi, vzji = ld<T>(a.vz, j) - vzi;
+            T Wi = tableLookup(tab, dist * hiInv);
+            T tA0 = -(cc[0] * rx + cc[1] * ry + cc[2] * rz) * Wi;
+            T tA1 = -(cc[1] * rx + cc[3] * ry + cc[4] * rz) * Wi;
+            T tA2 = -(cc[2] * rx + cc[4] * ry + cc[5] * rz) * Wi;
+            T xmj = ld<T>(a.xm, j);
+            T sx = vxji * xmj, sy = vyji * xmj, sz = vzji * xmj;
+            dVx[0] += sx * tA0;
+            dVx[1] += sx * tA1;
+            dVx[2] += sx * tA2;
+            dVy[0] += sy * tA0;
+            dVy[1] += sy * tA1;
+            dVy[2] += sy * tA2;
+            dVz[0] += sz * tA0;
+            dVz[1] += sz * tA1;
+            dVz[2] += sz * tA2;
+        }
+        T nk = a.K * hiInv3 / ld<T>(a.kx, i);
+        st<T>(a.divv, i, nk * (dVx[0] + dVy[1] + dVz[2]));
+        if (a.curlv) {
+            T cv0 = dVz[1] - dVy[2], cv1 = dVx[2] - dVz[0], cv2 = dVy[0] - dVx[1];
+            st<T>(a.curlv, i, nk * sqrt(cv0 * cv0 + (cv1 * cv1 + cv2 * cv2)));
+        }
+        if (a.dV11) {
+            st<T>(a.dV11, i, nk * dVx[0]);
+            st<T>(a.dV12, i, nk * (dVx[1] + dVy[0]));
+            st<T>(a.dV13, i, nk * (dVx[2] + dVz[0]));
+            st<T>(a.dV22, i, nk * dVy[1]);
+            st<T>(a.dV23, i, nk * (dVy[2] + dVz[1]));
+            st<T>(a.dV33, i, nk * dVz[2]);
+        }
+    } else {
+        using T = float;
+        const float* tab = static_cast<const float*>(a.wh);
+        auto t = cm.target(i);
+        KSum t11, t12, t13, t22, t23, t33;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+            T w = tableLookup(tab, dist * t.hInv);
+            T vw = __fdividef(ld<T>(a.xm, j), ld<T>(a.kx, j)) * w;
+            t11.add(rx * rx * vw);
+            t12.add(rx * ry * vw);
+            t13.add(rx * rz * vw);
+            t22.add(ry * ry * vw);
+            t23.add(ry * rz * vw);
+            t33.add(rz * rz * vw);
+        }
+        double hi = double(ld<T>(a.h, i));
+        T cc[6];
+        iadInvert<T>(t11.value(), t12.value(), t13.value(), t22.value(), t23.value(), t33.value(), hi, a.K, cc);
+        st<T>(a.c11, i, cc[0]);
+        st<T>(a.c12, i, cc[1]);
+        st<T>(a.c13, i, cc[2]);
+        st<T>(a.c22, i, cc[3]);
+        st<T>(a.c23, i, cc[4]);
+        st<T>(a.c33, i, cc[5]);
+
+        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        KSum dVx[3], dVy[3], dVz[3];
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+            T vxji = ld<T>(a.vx, j) - vxi, vyji = ld<T>(a.vy, j) - vyi, vzji = ld<T>(a.vz, j) - vzi;
+            T Wi = tableLookup(tab, dist * t.hInv);
+            T tA0 = -(cc[0] * rx + cc[1] * ry + cc[2] * rz) * Wi;
+            T tA1 = -(cc[1] * rx + cc[3] * ry + cc[4] * rz) * Wi;
+            T tA2 = -(cc[2] * rx + cc[4] * ry + cc[5] * rz) * Wi;
+            T xmj = ld<T>(a.xm, j);
+            T sx = vxji * xmj, sy = vyji * xmj, sz = vzji * xmj;
+            dVx[0].add(sx * tA0);
+            dVx[1].add(sx * tA1);
+            dVx[2].add(sx * tA2);
+            dVy[0].add(sy * tA0);
+            dVy[1].add(sy * tA1);
+            dVy[2].add(sy * tA2);
+            dVz[0].add(sz * tA0);
+            dVz[1].add(sz * tA1);
+            dVz[2].add(sz * tA2);
+        }
+        double hInv = 1.0 / hi;
+        double nk = a.K * (hInv * hInv * hInv) / double(ld<T>(a.kx, i));
+        double gx[3], gy[3], gz[3];
+        for (int q = 0; q < 3; ++q) {
+            gx[q] = dVx[q].value64();
+            gy[q] = dVy[q].value64();
+            gz[q] = dVz[q].value64();
+        }
+        st<T>(a.divv, i, T(nk * (gx[0] + gy[1] + gz[2])));
+        if (a.curlv) {
+            double cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
+            st<T>(a.curlv, i, T(nk * sqrt(cv0 * cv0 + cv1 * cv1 + cv2 * cv2)));
+        }
+        if (a.dV11) {
+            st<T>(a.dV11, i, T(nk * gx[0]));
+            st<T>(a.dV12, i, T(nk * (gx[1] + gy[0])));
+            st<T>(a.dV13, i, T(nk * (gx[2] + gz[0])));
+            st<T>(a.dV22, i, T(nk * gy[1]));
+            st<T>(a.dV23, i, T(nk * (gy[2] + gz[1])));
+            st<T>(a.dV33, i, T(nk * gz[2]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- AV switches
+struct AvArgs {
+    const void *h, *vx, *vy, *vz, *c, *c11, *c12, *c13, *c22, *c23, *c33, *kx, *xm, *divv, *wh;
+    double K, dt, alphamin, alphamax, decay;
+    void* alpha;
+};
+
+template<class P>
+__global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf, CoordMixed cm, AvArgs a)
+{
+    using T = typename P::T;
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = lv.capped(ii);
+    const T* tab = static_cast<const T*>(a.wh);
+    T hi = ld<T>(a.h, i), ci = ld<T>(a.c, i);
+    T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+    T c11 = ld<T>(a.c11, i), c12 = ld<T>(a.c12, i), c13 = ld<T>(a.c13, i);
+    T c22 = ld<T>(a.c22, i), c23 = ld<T>(a.c23, i), c33 = ld<T>(a.c33, i);
+    T vsig_i = T(1.e-40) * ci;
+    T divvi = ld<T>(a.divv, i);
+    T gx, gy, gz;
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        auto t = cf.target(i);
+        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        gx = gy = gz = 0;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            T vsig = 0.0;
+            if (rv < 0.0) vsig = ci + ld<T>(a.c, j) - 3.0 * rv / dist;
+            vsig_i = fmax(vsig_i, vsig);
+            T Wi = a.K * hiInv3 * tableLookup(tab, dist * hiInv);
+            T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
+            T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
+            T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
+            T fac = ld<T>(a.xm, j) / ld<T>(a.kx, j) * (divvi - ld<T>(a.divv, j));
+            gx += fac * t1;
+            gy += fac * t2;
+            gz += fac * t3;
+        }
+    } else {
+        auto t = cm.target(i);
+        const float kh3 = float(a.K) * t.hInv * t.hInv * t.hInv;
+        KSum sx, sy, sz;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            T rinv = rsqrtf(r2);
+            T dist = r2 * rinv;
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            T vsig = 0.f;
+            if (rv < 0.f) vsig = ci + ld<T>(a.c, j) - 3.f * rv * rinv;
+            vsig_i = fmaxf(vsig_i, vsig);
+            T Wi = kh3 * tableLookup(tab, dist * t.hInv);
+            T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
+            T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
+            T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
+            T fac = __fdividef(ld<T>(a.xm, j), ld<T>(a.kx, j)) * (divvi - ld<T>(a.divv, j));
+            sx.add(fac * t1);
+            sy.add(fac * t2);
+            sz.add(fac * t3);
+        }
+        gx = sx.value();
+        gy = sy.value();
+        gz = sz.value();
+    }
+    // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
+    T alpha_i = ld<T>(a.alpha, i);
+    T gdv = sqrt(gx * gx + gy * gy + gz * gz);
+    T aloc = 0.0;
+    if (divvi < T(0)) {
+        T ac = hi * hi * gdv;
+        aloc = T(a.alphamax) * ac / (ac + hi * fabs(divvi) + T(0.05) * ci);
+    }
+    if (aloc >= alpha_i) alpha_i = aloc;
+    else {
+        T decay = hi / (T(a.decay) * vsig_i);
+        T adot = (aloc >= T(a.alphamin)) ? (aloc - alpha_i) / decay : (T(a.alphamin) - alpha_i) / decay;
+        alpha_i += adot * T(a.dt);
+    }
+    st<T>(a.alpha, i, alpha_i);
+}
+
+// ---------------------------------------------------------------- momentum and energy (VE)
+struct MeVeArgs {
+    const void *vx, *vy, *vz, *h, *m, *prho, *c, *kx, *xm, *alpha;
+    const void *c11, *c12, *c13, *c22, *c23, *c33;
+    const void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
+    const void* wh;
+    const double* hInv64;
+    double K;
+    float Kcour;
+    void *ax, *ay, *az;
+    double* du;
+    float* groupDt;
+    unsigned long long* minDt;
+};
+
+template<class T>
+__device__ __forceinline__ T quadForm(T rx, T ry, T rz, const T g[6])
+{
+    T s0 = g[0] * rx + g[1] * ry + g[2] * rz;
+    T s1 = g[3] * ry + g[4] * rz;
+    T s2 = g[5] * rz;
+    return rx * s0 + (ry * s1 + rz * s2);  // dot is a right fold (util/array.hpp:237-240)
+}
+
+// avRvCorrection (hydro_ve/momentum_energy_kern.hpp:43-63)
+template<class T>
+__device__ __forceinline__ T avRv(T rx, T ry, T rz, T eta, T etaCrit, const T gi[6], const T gj[6])
+{
+    T d1 = quadForm(rx, ry, rz, gi), d2 = quadForm(rx, ry, rz, gj), d3 = T(1);
+    if (eta < etaCrit) {
+        T e = T(5) * (eta - etaCrit);
+        d3 = exp(-e * e);
+    }
+    T A = (d2 != T(0)) ? d1 / d2 : T(0);
+    T Ap1 = T(1) + A;
+    T phi = T(0.5) * d3 * fmax(T(0), fmin(T(1), T(4) * A / (Ap1 * Ap1)));
+    return -phi * (d1 + d2);
+}
+
+template<class P, bool AvClean>
+__global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 cf, CoordMixed cm, MeVeArgs a)
+{
+    using T = typename P::T;
+    const int64_t i0 = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const bool valid = i0 < lv.last;
+    const int64_t i = valid ? i0 : lv.first;
+    const int64_t ii = i - lv.first;
+    const unsigned nc = valid ? lv.capped(ii) : 0u;
+    const T* tab = static_cast<const T*>(a.wh);
+    constexpr T Atmin = T(0.1), Atmax = T(0.2), ramp = T(1) / (Atmax - Atmin);
+
+    T hi = ld<T>(a.h, i), mi = ld<T>(a.m, i), ci = ld<T>(a.c, i), kxi = ld<T>(a.kx, i), ai = ld<T>(a.alpha, i);
+    T xmi = ld<T>(a.xm, i), prhoi = ld<T>(a.prho, i);
+    T rhoi = kxi * mi / xmi;
+    T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+    T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
+    T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
+    T gi[6] = {0, 0, 0, 0, 0, 0};
+    if constexpr (AvClean) {
+        gi[0] = ld<T>(a.dV11, i);
+        gi[1] = ld<T>(a.dV12, i);
+        gi[2] = ld<T>(a.dV13, i);
+        gi[3] = ld<T>(a.dV22, i);
+        gi[4] = ld<T>(a.dV23, i);
+        gi[5] = ld<T>(a.dV33, i);
+    }
+    const T etaCrit = T(cbrt(32.0 * M_PI / 3.0 / double(nc + 1)));
+    T maxv = 0;
+    double dt = INFINITY;
+
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        auto t = cf.target(i);
+        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        T mx = 0, my = 0, mz = 0, en = 0, avE = 0;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz;
+            cf.diff(t, j, twoH, rx, ry, rz);
+            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T hjInv = __ldg(a.hInv64 + j);
+            T v1 = dist * hiInv, v2 = dist * hjInv;
+            T hjInv3 = hjInv * hjInv * hjInv;
+            T Wi = hiInv3 * tableLookup(tab, v1);
+            T Wj = hjInv3 * tableLookup(tab, v2);
+            T a1i = -(c11i * rx + c12i * ry + c13i * rz) * Wi;
+            T a2i = -(c12i * rx + c22i * ry + c23i * rz) * Wi;
+            T a3i = -(c13i * rx + c23i * ry + c33i * rz) * Wi;
+            T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
+            T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
+            T a1j = -(c11j * rx + c12j * ry + c13j * rz) * Wj;
+            T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
+            T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
+            T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
+            T rhoj = ld<T>(a.kx, j) * mj / xmj;
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            if constexpr (AvClean) {
+                T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
+                           ld<T>(a.dV22, j), ld<T>(a.dV23, j), ld<T>(a.dV33, j)};
+                rv += avRv<T>(rx, ry, rz, fmin(v1, v2), etaCrit, gi, gj);
+            }
+            T wij = rv / dist;
+            T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
+            T vsig = T(0.5) * (ci + cj) - T(2) * wij;
+            maxv = (vsig > maxv) ? vsig : maxv;
+            T am, bm;
+            T At = fabs(rhoi - rhoj) / (rhoi + rhoj);
+            if (At < Atmin) {
+                am = xmi * xmi;
+                bm = xmj * xmj;
+            } else if (At > Atmax) {
+                am = xmi * xmj;
+                bm = am;
+            } else {
+                T s = ramp * (At - Atmin);
+                am = pow(xmi, T(2) - s) * pow(xmj, s);
+                bm = pow(xmj, T(2) - s) * pow(xmi, s);
+            }
+            T av = mj / rhoi * visc, bv = mj / rhoj * visc;
+            T avx = T(0.5) * (av * a1i + bv * a1j);
+            T avy = T(0.5) * (av * a2i + bv * a2j);
+            T avz = T(0.5) * (av * a3i + bv * a3j);
+            avE += avx * vxij + avy * vyij + avz * vzij;
+            en += mj * am * (vxij * a1i + vyij * a2i + vzij * a3i);
+            T momi = mj * prhoi * am, momj = mj * ld<T>(a.prho, j) * bm;
+            mx += momi * a1i + momj * a1j + avx;
+            my += momi * a2i + momj * a2j + avy;
+            mz += momi * a3i + momj * a3j + avz;
+        }
+        if (valid) {
+            avE = fmax(T(0), avE);
+            a.du[i] = a.K * (prhoi * en + T(0.5) * avE);
+            st<T>(a.ax, i, -a.K * mx);
+            st<T>(a.ay, i, -a.K * my);
+            st<T>(a.az, i, -a.K * mz);
+            dt = courantDt(maxv, hi, ci, a.Kcour);
+        }
+    } else {
+        auto t = cm.target(i);
+        T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
+        T rhoiInv = __frcp_rn(rhoi);
+        KSum mx, my, mz, en, avE;
+        for (unsigned k = 0; k < nc; ++k) {
+            uint32_t j = lv.at(ii, k);
+            T rx, ry, rz, hjInv;
+            cm.diff(t, j, rx, ry, rz, hjInv);
+            T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            T rinv = rsqrtf(r2);
+            T dist = r2 * rinv;
+            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T v1 = dist * hiInv, v2 = dist * hjInv;
+            T Wi = hiInv3 * tableLookup(tab, v1);
+            T Wj = (hjInv * hjInv * hjInv) * tableLookup(tab, v2);
+            T a1i = -(c11i * rx + c12i * ry + c13i * rz) * Wi;
+            T a2i = -(c12i * rx + c22i * ry + c23i * rz) * Wi;
+            T a3i = -(c13i * rx + c23i * ry + c33i * rz) * Wi;
+            T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
+            T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
+            T a1j = -(c11j * rx + c12j * ry + c13j * rz) * Wj;
+            T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
+            T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
+            T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
+            T rhoj = ld<T>(a.kx, j) * mj * __frcp_rn(xmj);
+            T rv = rx * vxij + ry * vyij + rz * vzij;
+            if constexpr (AvClean) {
+                T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
+                           ld<T>(a.dV22, j), ld<T>(a.dV23, j), ld<T>(a.dV33, j)};
+                rv += avRv<T>(rx, ry, rz, fminf(v1, v2), etaCrit, gi, gj);
+            }
+            T wij = rv * rinv;
+            T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
+            T vsig = T(0.5) * (ci + cj) - T(2) * wij;
+            maxv = (vsig > maxv) ? vsig : maxv;
+            T am, bm;
+            T At = fabsf(rhoi - rhoj) / (rhoi + rhoj);
+            if (At < Atmin) {
+                am = xmi * xmi;
+                bm = xmj * xmj;
+            } else if (At > Atmax) {
+                am = xmi * xmj;
+                bm = am;
+            } else {
+                T s = ramp * (At - Atmin);
+                am = powf(xmi, T(2) - s) * powf(xmj, s);
+                bm = powf(xmj, T(2) - s) * powf(xmi, s);
+            }
+            T av = mj * rhoiInv * visc, bv = mj * __frcp_rn(rhoj) * visc;
+            T avx = T(0.5) * (av * a1i + bv * a1j);
+            T avy = T(0.5) * (av * a2i + bv * a2j);
+            T avz = T(0.5) * (av * a3i + bv * a3j);
+            avE.add(avx * vxij + avy * vyij + avz * vzij);
+            en.add(mj * am * (vxij * a1i + vyij * a2i + vzij * a3i));
+            T momi = mj * prhoi * am, momj = mj * ld<T>(a.prho, j) * bm;
+            mx.add(momi * a1i + momj * a1j + avx);
+            my.add(momi * a2i + momj * a2j + avy);
+            mz.add(momi * a3i + momj * a3j + avz);
+        }
+        if (valid) {
+            double ave = fmax(0.0, avE.value64());
+            a.du[i] = a.K * (double(prhoi) * en.value64() + 0.5 * ave);
+            st<T>(a.ax, i, T(-a.K * mx.value64()));
+            st<T>(a.ay, i, T(-a.K * my.value64()));
+            st<T>(a.az, i, T(-a.K * mz.value64()));
+            dt = courantDt(double(maxv), double(hi), double(ci), a.Kcour);
+        }
+    }
+    if (a.groupDt) {
+        double g = dt;
+        for (int o = 16; o > 0; o >>= 1) g = fmin(g, __shfl_xor_sync(0xffffffffu, g, o));
+        if ((threadIdx.x & 31) == 0 && i0 < lv.last) a.groupDt[(i0 - lv.first) / 32] = float(g);
+    }
+    if (a.minDt) blockMinDt(dt, a.minDt);
+}
+
+}  // namespace
+
+int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->h || !p->m || !p->xm || !p->kx || !p->gradh) return SPHGB_ERR_ARG;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    unsigned blocks = gridFor(last - first, kPairBlock);
+    if (p->precision == SPHGB_MIXED)
+        gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
+                                                                    p->xm, c->wh32.p, c->whd32.p, c->K, p->kx,
+                                                                    p->gradh);
+    else
+        gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
+                                                                   p->xm, c->wh64.p, c->whd64.p, c->K, p->kx,
+                                                                   p->gradh);
+    return launched(c, "gradhKernel");
+}
+
+int passEosVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->u || !p->m || !p->kx || !p->xm || !p->gradh || !p->prho || !p->c || first < 0 || last > p->n ||
+        first >= last)
+        return SPHGB_ERR_ARG;
+    unsigned blocks = gridFor(last - first, 256);
+    if (p->precision == SPHGB_MIXED)
+        eosVeKernel<MixedTag><<<blocks, 256, 0, c->stream>>>(first, last, p->u, p->m, p->kx, p->xm, p->gradh,
+                                                            c->prm.gamma, p->prho, p->c, p->rho, p->p);
+    else
+        eosVeKernel<Fp64Tag><<<blocks, 256, 0, c->stream>>>(first, last, p->u, p->m, p->kx, p->xm, p->gradh,
+                                                           c->prm.gamma, p->prho, p->c, p->rho, p->p);
+    return launched(c, "eosVeKernel");
+}
+
+int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->h || !p->vx || !p->vy || !p->vz || !p->xm || !p->kx || !p->c11 || !p->c12 || !p->c13 || !p->c22 ||
+        !p->c23 || !p->c33 || !p->divv)
+        return SPHGB_ERR_ARG;
+    const bool gradV = p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    IadDivvArgs a{p->h,   p->vx,  p->vy,  p->vz,   p->xm,    nullptr, nullptr, c->K,   p->c11, p->c12,
+                  p->c13, p->c22, p->c23, p->c33,  p->divv,  p->curlv, gradV ? p->dV11 : nullptr,
+                  p->dV12, p->dV13, p->dV22, p->dV23, p->dV33};
+    a.kx = p->kx;
+    unsigned blocks = gridFor(last - first, kPairBlock);
+    if (p->precision == SPHGB_MIXED) {
+        a.wh = c->wh32.p;
+        iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+    } else {
+        a.wh = c->wh64.p;
+        iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+    }
+    return launched(c, "iadDivvKernel");
+}
+
+int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->h || !p->vx || !p->c || !p->c11 || !p->kx || !p->xm || !p->divv || !p->alpha) return SPHGB_ERR_ARG;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    AvArgs a{p->h,   p->vx,  p->vy,  p->vz, p->c,  p->c11,         p->c12,          p->c13,
+             p->c22, p->c23, p->c33, p->kx, p->xm, p->divv,        nullptr,         c->K,
+             c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant, p->alpha};
+    unsigned blocks = gridFor(last - first, kPairBlock);
+    if (p->precision == SPHGB_MIXED) {
+        a.wh = c->wh32.p;
+        avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+    } else {
+        a.wh = c->wh64.p;
+        avKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+    }
+    return launched(c, "avKernel");
+}
+
+int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, int avClean, float* groupDt,
+                         double* minDt)
+{
+    if (!p->vx || !p->vy || !p->vz || !p->prho || !p->c || !p->kx || !p->xm || !p->alpha || !p->ax || !p->ay ||
+        !p->az || !p->du || !p->c11)
+        return SPHGB_ERR_ARG;
+    if (avClean && !(p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33)) return SPHGB_ERR_ARG;
+    SPHGB_TRY(checkPass(c, p, first, last));
+    ListView lv = listView(c);
+    lv.first = first;
+    lv.last = last;
+    MeVeArgs a{p->vx,   p->vy,   p->vz,   p->h,    p->m,    p->prho, p->c,    p->kx,   p->xm,   p->alpha,
+               p->c11,  p->c12,  p->c13,  p->c22,  p->c23,  p->c33,  p->dV11, p->dV12, p->dV13, p->dV22,
+               p->dV23, p->dV33, nullptr, c->hInv64.as<double>(), c->K, float(c->prm.Kcour), p->ax, p->ay,
+               p->az,   p->du,   groupDt, nullptr};
+    SPHGB_TRY(beginDtReduction(c, &a.minDt));
+    unsigned blocks = gridFor(last - first, kPairBlock);
+    auto cf = coordFp64(c, p);
+    auto cm = coordMixed(c);
+    if (p->precision == SPHGB_MIXED) {
+        a.wh = c->wh32.p;
+        if (avClean) meVeKernel<MixedTag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+        else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+    } else {
+        a.wh = c->wh64.p;
+        if (avClean) meVeKernel<Fp64Tag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+        else meVeKernel<Fp64Tag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+    }
+    SPHGB_TRY(launched(c, "meVeKernel"));
+    return endDtReduction(c, a.minDt, minDt);
+}
+
+}  // namespace sphgb

@@ -1,0 +1,476 @@
+// Neighbour lists per warp-group of 32 SFC-consecutive target particles.
+//
+// Replaces cstone::findNeighbors / sph::findNeighborsSph (domain/include/cstone/findneighbors.hpp:
+// 77-170, sph/include/sph/find_neighbors.hpp:10-56) and the reference GPU's per-pass warp
+// traversal (domain/include/cstone/traversal/find_neighbors.cuh:182-489).  The set of neighbours
+// of i is exactly the reference CPU set {j != i : d2(i,j) < 4 h_i^2}, with d2 rounded as in
+// distanceSq (minimum image by rint when the 2h box of i leaves a periodic box).
+//
+// Per warp: one depth-first walk of the octree in SFC order against the group's search box, so
+// candidate leaves arrive in ascending particle order and every list comes out sorted.
+// Contiguous leaf ranges are merged and staged 32 candidates at a time in shared memory.  Each
+// target first tests a candidate in FP32 on coordinates relative to the group origin; only
+// pairs whose FP32 distance lies within a rounding margin of the radius are re-tested exactly
+// in FP64.  Lists are stored transposed, nbr[k * stride + (i - first)], so that the pair
+// passes read them coalesced.
+#include <cub/cub.cuh>
+
+#include "context.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kNbrBlock = 128;
+constexpr int kWarpsPerBlock = kNbrBlock / kWarp;
+constexpr int kStack = 192;  // 8 children x (21 levels + 3)
+
+struct NbrArgs {
+    const double *x, *y, *z;
+    const void* h;
+    int hIsFloat;
+    int64_t first, last;
+    const uint32_t* active;  // optional: only targets with active[i - first] != 0 are searched
+    const int32_t* childOffsets;
+    const int32_t* internalToLeaf;
+    const uint32_t* layout;
+    const float4* nodeBox;
+    int64_t numNodes;
+    DevBox box;
+    uint32_t ngmax;
+    int64_t stride;
+    uint32_t* nbr;
+    uint32_t* count;           // [last-first] neighbours excluding self (uncapped)
+    int* flags;
+    unsigned long long* stats; // [0] candidates [1] fp64 rechecks
+};
+
+__device__ __forceinline__ double loadH(const void* h, int isFloat, int64_t i)
+{
+    return isFloat ? double(static_cast<const float*>(h)[i]) : static_cast<const double*>(h)[i];
+}
+
+__device__ __forceinline__ double foldRint(double d, const DevBox& b, int k)
+{
+    // minimum image of the reference's distanceSq<true> / applyPbc: d - L * rint(d / L)
+    return __dsub_rn(d, __dmul_rn(b.L[k], rint(__dmul_rn(d, b.iL[k]))));
+}
+
+struct WarpSmem {
+    int32_t stack[kStack];
+    double xs[kWarp], ys[kWarp], zs[kWarp];
+    float fx[kWarp], fy[kWarp], fz[kWarp];
+};
+
+__global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
+{
+    __shared__ WarpSmem smem[kWarpsPerBlock];
+    const int lane = threadIdx.x & (kWarp - 1);
+    WarpSmem& sm = smem[threadIdx.x / kWarp];
+    const int64_t g0 = a.first + (int64_t(blockIdx.x) * kWarpsPerBlock + threadIdx.x / kWarp) * kWarp;
+    if (g0 >= a.last) return;
+    const int64_t i = g0 + lane;
+    bool valid = i < a.last && (a.active == nullptr || a.active[i - a.first] != 0);
+    const unsigned validMask = __ballot_sync(0xffffffffu, valid);
+    if (validMask == 0) return;
+    const int leader = __ffs(validMask) - 1;
+
+    double xi = 0, yi = 0, zi = 0, hi = 0;
+    if (valid) {
+        xi = a.x[i];
+        yi = a.y[i];
+        zi = a.z[i];
+        hi = loadH(a.h, a.hIsFloat, i);
+    }
+    const double r2 = __dmul_rn(__dmul_rn(4.0, hi), hi);  // reference radiusSq = 4 h h
+    const DevBox& b = a.box;
+    const bool anyPbc = b.pbc[0] | b.pbc[1] | b.pbc[2];
+    const double twoH = __dmul_rn(2.0, hi);
+    const bool inside = __dsub_rn(xi, twoH) >= b.lo[0] && __dsub_rn(yi, twoH) >= b.lo[1] &&
+                        __dsub_rn(zi, twoH) >= b.lo[2] && __dadd_rn(xi, twoH) <= b.hi[0] &&
+                        __dadd_rn(yi, twoH) <= b.hi[1] && __dadd_rn(zi, twoH) <= b.hi[2];
+    const bool usePbc = anyPbc && !inside;
+
+    // group origin and target offsets relative to it (minimum image in periodic dims)
+    const double ox = __shfl_sync(0xffffffffu, xi, leader);
+    const double oy = __shfl_sync(0xffffffffu, yi, leader);
+    const double oz = __shfl_sync(0xffffffffu, zi, leader);
+    double rel[3] = {xi - ox, yi - oy, zi - oz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (b.pbc[k]) rel[k] -= b.L[k] * rint(rel[k] * b.iL[k]);
+    const float dxi = float(rel[0]), dyi = float(rel[1]), dzi = float(rel[2]);
+    const float rf = valid ? __double2float_ru(twoH) : 0.f;
+
+    // group search box in relative coordinates
+    float gmin[3] = {valid ? dxi - rf : INFINITY, valid ? dyi - rf : INFINITY, valid ? dzi - rf : INFINITY};
+    float gmax[3] = {valid ? dxi + rf : -INFINITY, valid ? dyi + rf : -INFINITY, valid ? dzi + rf : -INFINITY};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            gmin[k] = fminf(gmin[k], __shfl_xor_sync(0xffffffffu, gmin[k], o));
+            gmax[k] = fmaxf(gmax[k], __shfl_xor_sync(0xffffffffu, gmax[k], o));
+        }
+    bool exactOnly = false;
+    float gc[3], gs[3], Rg = 0.f;
+    const double oc[3] = {ox, oy, oz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (b.pbc[k] && (gmax[k] - gmin[k]) > 0.25f * b.Lf[k]) exactOnly = true;
+        double cAbs = oc[k] + 0.5 * (double(gmin[k]) + double(gmax[k]));
+        if (b.pbc[k]) cAbs -= b.L[k] * floor((cAbs - b.lo[k]) * b.iL[k]);  // into [lo, hi)
+        gc[k] = float(cAbs);
+        double pad = (fabs(b.lo[k]) + fabs(b.hi[k])) * 0x1p-21;
+        gs[k] = __double2float_ru(0.5 * (double(gmax[k]) - double(gmin[k])) + pad);
+        Rg = fmaxf(Rg, fmaxf(fabsf(gmin[k]), fabsf(gmax[k])));
+    }
+    // FP32 decision margin on d2: covers the rounding of the offsets (<= 3 ulp of Rg each) and
+    // of the squared sum; pairs inside the margin get the exact FP64 test
+    const float r2f = float(r2);
+    const float margin = 64.f * 0x1p-24f * (Rg + rf) * (Rg + rf);
+
+    unsigned cnt = 0;
+    unsigned long long tested = 0, rechecked = 0;
+    const int64_t ii = i - a.first;
+
+    auto flush = [&](int64_t ja, int m) {
+        // stage candidates [ja, ja+m) in shared memory
+        if (lane < m) {
+            int64_t j = ja + lane;
+            double xj = a.x[j], yj = a.y[j], zj = a.z[j];
+            sm.xs[lane] = xj;
+            sm.ys[lane] = yj;
+            sm.zs[lane] = zj;
+            double d[3] = {xj - ox, yj - oy, zj - oz};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (b.pbc[k]) d[k] -= b.L[k] * rint(d[k] * b.iL[k]);
+            sm.fx[lane] = float(d[0]);
+            sm.fy[lane] = float(d[1]);
+            sm.fz[lane] = float(d[2]);
+        }
+        __syncwarp();
+        if (valid) {
+            tested += m;
+            for (int t = 0; t < m; ++t) {
+                float ex = dxi - sm.fx[t], ey = dyi - sm.fy[t], ez = dzi - sm.fz[t];
+                float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                bool in;
+                if (!exactOnly && d2f < r2f - margin) in = true;
+                else if (!exactOnly && d2f > r2f + margin) in = false;
+                else {
+                    ++rechecked;
+                    double dx = __dsub_rn(sm.xs[t], xi), dy = __dsub_rn(sm.ys[t], yi), dz = __dsub_rn(sm.zs[t], zi);
+                    if (usePbc) {
+                        if (b.pbc[0]) dx = foldRint(dx, b, 0);
+                        if (b.pbc[1]) dy = foldRint(dy, b, 1);
+                        if (b.pbc[2]) dz = foldRint(dz, b, 2);
+                    }
+                    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                    in = d2 < r2;
+                }
+                int64_t j = ja + t;
+                if (in && j != i) {
+                    if (cnt < a.ngmax) a.nbr[int64_t(cnt) * a.stride + ii] = uint32_t(j);
+                    ++cnt;
+                }
+            }
+        }
+        __syncwarp();
+    };
+
+    int64_t pa = 0, pb = 0;  // pending contiguous candidate range
+    auto addLeaf = [&](int32_t leaf) {
+        int64_t la = a.layout[leaf], lb = a.layout[leaf + 1];
+        if (la == lb) return;
+        if (la != pb) {
+            while (pb > pa) {
+                int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
+                flush(pa, m);
+                pa += m;
+            }
+            pa = la;
+        }
+        pb = lb;
+        while (pb - pa >= kWarp) {
+            flush(pa, kWarp);
+            pa += kWarp;
+        }
+    };
+
+    // depth-first walk in SFC order: children pushed in reverse so child 0 is popped first
+    if (lane == 0) sm.stack[0] = 0;
+    int sp = 1;
+    __syncwarp();
+    bool overflow = false;
+    while (sp > 0) {
+        int32_t node = sm.stack[--sp];
+        int32_t co = a.childOffsets[node];
+        if (co == 0) {
+            addLeaf(a.internalToLeaf[node]);
+            continue;
+        }
+        bool ov = false;
+        int32_t child = co + (lane & 7);
+        if (lane < 8) {
+            float4 c4 = a.nodeBox[2 * child], s4 = a.nodeBox[2 * child + 1];
+            float cc[3] = {c4.x, c4.y, c4.z}, ss[3] = {s4.x, s4.y, s4.z};
+            ov = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float dd = fabsf(cc[k] - gc[k]);
+                if (b.pbc[k]) dd = fminf(dd, b.Lf[k] - dd);
+                ov = ov && (dd <= ss[k] + gs[k]);
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, ov);
+        int k = __popc(m);
+        if (sp + k > kStack) {
+            overflow = true;
+            break;
+        }
+        __syncwarp();
+        if (ov) sm.stack[sp + __popc(m >> (lane + 1))] = child;
+        sp += k;
+        __syncwarp();
+    }
+    if (overflow) {
+        if (lane == 0) atomicOr(a.flags, kFlagStackOverflow);
+        return;
+    }
+    while (pb > pa) {
+        int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
+        flush(pa, m);
+        pa += m;
+    }
+
+    if (valid) a.count[ii] = cnt;
+    // warp-aggregated statistics
+    for (int o = 16; o > 0; o >>= 1) {
+        tested += __shfl_xor_sync(0xffffffffu, tested, o);
+        rechecked += __shfl_xor_sync(0xffffffffu, rechecked, o);
+    }
+    if (lane == 0 && a.stats) {
+        atomicAdd(&a.stats[0], tested);
+        atomicAdd(&a.stats[1], rechecked);
+    }
+}
+
+// h / nc iteration step (sph/include/sph/find_neighbors.hpp:26-37, updateH kernels.hpp:26-32):
+// marks targets that leave [ng0/4, ngmax+1] and updates their h; counts active and failed.
+template<class Th>
+__global__ void hIterKernel(const uint32_t* __restrict__ count, Th* __restrict__ h, uint32_t* __restrict__ active,
+                            uint8_t* __restrict__ iters, int64_t first, int64_t nWork, unsigned ng0, unsigned ngmax,
+                            unsigned long long* __restrict__ counters)
+{
+    int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= nWork) return;
+    unsigned nc = count[k] + 1;
+    unsigned ngmin = ng0 / 4;
+    bool bad = (ngmin > nc) || (nc - 1 > ngmax);
+    bool go = bad && iters[k] < 10 && (active[k] != 0);
+    if (go) {
+        Th hv = h[first + k];
+        const Th c0 = Th(1023.0);
+        const Th ex = Th(1.0) / Th(10.0);
+        h[first + k] = hv * Th(0.5) * pow(Th(1) + c0 * ng0 / Th(nc), ex);
+        iters[k]++;
+        atomicAdd(&counters[2], 1ull);
+    }
+    active[k] = go ? 1u : 0u;
+}
+
+__global__ void ncOutKernel(const uint32_t* __restrict__ count, const uint8_t* __restrict__ iters, int64_t nWork,
+                            uint32_t ngmax, uint32_t* __restrict__ nc, int addSelf,
+                            unsigned long long* __restrict__ counters)
+{
+    int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    unsigned long long capped = 0, sum = 0, fails = 0;
+    unsigned mx = 0;
+    if (k < nWork) {
+        uint32_t cnt = count[k];
+        if (nc) nc[k] = cnt + (addSelf ? 1u : 0u);
+        capped = cnt > ngmax;
+        sum = min(cnt, ngmax);
+        mx = cnt + 1;
+        fails = (iters && iters[k] >= 10) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        capped += __shfl_xor_sync(0xffffffffu, capped, o);
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        fails += __shfl_xor_sync(0xffffffffu, fails, o);
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&counters[3], sum);
+        atomicAdd(&counters[4], capped);
+        atomicMax(&counters[5], (unsigned long long)mx);
+        atomicAdd(&counters[6], fails);
+    }
+}
+
+__global__ void exportKernel(const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ count, int64_t nWork,
+                             int64_t stride, uint32_t ngmax, uint32_t* __restrict__ out)
+{
+    int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= nWork) return;
+    uint32_t c = min(count[k], ngmax);
+    for (uint32_t q = 0; q < c; ++q) out[k * ngmax + q] = nbr[int64_t(q) * stride + k];
+}
+
+__global__ void fillOnes(uint32_t* p, int64_t n)
+{
+    int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k < n) p[k] = 1u;
+}
+
+int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int hIsFloat,
+              int64_t first, int64_t last, uint32_t ngmax, const uint32_t* active)
+{
+    NbrArgs a;
+    a.x = x;
+    a.y = y;
+    a.z = z;
+    a.h = h;
+    a.hIsFloat = hIsFloat;
+    a.first = first;
+    a.last = last;
+    a.active = active;
+    a.childOffsets = c->childOffsets.as<int32_t>();
+    a.internalToLeaf = c->internalToLeaf.as<int32_t>();
+    a.layout = c->layout.as<uint32_t>();
+    a.nodeBox = c->nodeBoxF.as<float4>();
+    a.numNodes = c->numNodes;
+    a.box = c->box;
+    a.ngmax = ngmax;
+    a.stride = c->nbrStride;
+    a.nbr = c->nbr.as<uint32_t>();
+    a.count = c->ncount.as<uint32_t>();
+    a.flags = c->dFlags;
+    a.stats = c->counters.as<unsigned long long>();
+    int64_t groups = (last - first + kWarp - 1) / kWarp;
+    unsigned blocks = unsigned((groups + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    nbrGroupKernel<<<blocks, kNbrBlock, 0, c->stream>>>(a);
+    return launched(c, "nbrGroupKernel");
+}
+
+int prepareLists(sphgb_ctx* c, int64_t first, int64_t last, uint32_t ngmax)
+{
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    if (first < 0 || last > c->n || first >= last) return SPHGB_ERR_ARG;
+    const int64_t nWork = last - first;
+    c->nbrStride = (nWork + 31) / 32 * 32;
+    SPHGB_TRY(c->nbr.ensure(sizeof(uint32_t) * size_t(ngmax) * c->nbrStride));
+    SPHGB_TRY(c->ncount.ensure(sizeof(uint32_t) * c->nbrStride));
+    SPHGB_TRY(c->active.ensure(sizeof(uint32_t) * c->nbrStride + c->nbrStride));
+    SPHGB_TRY(c->counters.ensure(sizeof(unsigned long long) * 8));
+    SPHGB_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * 8, c->stream));
+    SPHGB_CUDA(cudaMemsetAsync(c->dFlags, 0, sizeof(int), c->stream));
+    c->nbrFirst = first;
+    c->nbrLast = last;
+    c->nbrNgmax = ngmax;
+    return SPHGB_OK;
+}
+
+int finishStats(sphgb_ctx* c, int64_t hIters)
+{
+    unsigned long long h[8];
+    int flags = 0;
+    SPHGB_CUDA(cudaMemcpyAsync(h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaMemcpyAsync(&flags, c->dFlags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    c->stats.candidates = int64_t(h[0]);
+    c->stats.fp64_rechecks = int64_t(h[1]);
+    c->stats.nc_sum = int64_t(h[3]);
+    c->stats.capped = int64_t(h[4]);
+    c->stats.nc_max = uint32_t(h[5]);
+    c->stats.h_fails = int64_t(h[6]);
+    c->stats.h_iterations = hIters;
+    if (flags & kFlagStackOverflow) return SPHGB_ERR_TRAVERSAL;
+    return SPHGB_OK;
+}
+
+}  // namespace
+
+int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!p->x || !p->y || !p->z || !p->h) return SPHGB_ERR_ARG;
+    const uint32_t ngmax = c->prm.ngmax;
+    if (c->prm.ng0 > ngmax) return SPHGB_ERR_ARG;  // reference: "ng0 should be smaller than ngmax"
+    SPHGB_TRY(prepareLists(c, first, last, ngmax));
+    const int64_t nWork = last - first;
+    const int hf = p->precision == SPHGB_MIXED;
+    uint32_t* active = c->active.as<uint32_t>();
+    uint8_t* iters = reinterpret_cast<uint8_t*>(active + c->nbrStride);
+    SPHGB_CUDA(cudaMemsetAsync(iters, 0, c->nbrStride, c->stream));
+    SPHGB_TRY(runSearch(c, p->x, p->y, p->z, p->h, hf, first, last, ngmax, nullptr));
+
+    unsigned long long* ctr = c->counters.as<unsigned long long>();
+    fillOnes<<<gridFor(nWork, 256), 256, 0, c->stream>>>(active, nWork);
+    SPHGB_TRY(launched(c, "fillOnes"));
+    int64_t rounds = 0;
+    for (int it = 0; it < 10; ++it) {
+        SPHGB_CUDA(cudaMemsetAsync(ctr + 2, 0, sizeof(unsigned long long), c->stream));
+        if (hf)
+            hIterKernel<float><<<gridFor(nWork, 256), 256, 0, c->stream>>>(
+                c->ncount.as<uint32_t>(), static_cast<float*>(p->h), active, iters, first, nWork, c->prm.ng0, ngmax,
+                ctr);
+        else
+            hIterKernel<double><<<gridFor(nWork, 256), 256, 0, c->stream>>>(
+                c->ncount.as<uint32_t>(), static_cast<double*>(p->h), active, iters, first, nWork, c->prm.ng0, ngmax,
+                ctr);
+        SPHGB_TRY(launched(c, "hIterKernel"));
+        unsigned long long nact = 0;
+        SPHGB_CUDA(cudaMemcpyAsync(&nact, ctr + 2, sizeof(nact), cudaMemcpyDeviceToHost, c->stream));
+        SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+        if (nact == 0) break;
+        ++rounds;
+        SPHGB_TRY(runSearch(c, p->x, p->y, p->z, p->h, hf, first, last, ngmax, active));
+    }
+    ncOutKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->ncount.as<uint32_t>(), iters, nWork, ngmax,
+                                                             p->nc ? p->nc + first : nullptr, 1, ctr);
+    SPHGB_TRY(launched(c, "ncOutKernel"));
+    SPHGB_TRY(finishStats(c, rounds));
+    c->nbrEpoch++;
+    c->haveNbr = true;
+    c->precisionBuilt = p->precision;
+    c->xBuilt = p->x;
+    return c->stats.h_fails > 0 ? SPHGB_ERR_NOCONV : SPHGB_OK;
+}
+
+int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int32_t hPrec,
+                       int64_t first, int64_t last, uint32_t ngmax, uint32_t* nbrOut, uint32_t* ncOut)
+{
+    if (!x || !y || !z || !h || ngmax == 0) return SPHGB_ERR_ARG;
+    SPHGB_TRY(prepareLists(c, first, last, ngmax));
+    const int64_t nWork = last - first;
+    SPHGB_TRY(runSearch(c, x, y, z, h, hPrec == SPHGB_MIXED, first, last, ngmax, nullptr));
+    ncOutKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->ncount.as<uint32_t>(), nullptr, nWork, ngmax, ncOut, 0,
+                                                             c->counters.as<unsigned long long>());
+    SPHGB_TRY(launched(c, "ncOutKernel"));
+    if (nbrOut) {
+        exportKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->nbr.as<uint32_t>(), c->ncount.as<uint32_t>(),
+                                                                  nWork, c->nbrStride, ngmax, nbrOut);
+        SPHGB_TRY(launched(c, "exportKernel"));
+    }
+    SPHGB_TRY(finishStats(c, 0));
+    c->nbrEpoch++;
+    c->haveNbr = true;
+    c->precisionBuilt = hPrec;
+    c->xBuilt = x;
+    return SPHGB_OK;
+}
+
+int exportNeighbors(sphgb_ctx* c, uint32_t* out)
+{
+    if (!c->haveNbr) return SPHGB_ERR_STATE;
+    if (!out) return SPHGB_ERR_ARG;
+    const int64_t nWork = c->nbrLast - c->nbrFirst;
+    exportKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->nbr.as<uint32_t>(), c->ncount.as<uint32_t>(), nWork,
+                                                              c->nbrStride, c->nbrNgmax, out);
+    SPHGB_TRY(launched(c, "exportKernel"));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
+
+}  // namespace sphgb

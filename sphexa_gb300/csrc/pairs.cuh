@@ -1,0 +1,232 @@
+// Pair-loop building blocks shared by the std and VE passes.
+//
+// One thread per target particle i walks its own neighbour list nbr[k * stride + (i - first)];
+// a warp holds 32 SFC-consecutive targets, so each list row is one coalesced 128-byte read and
+// the neighbours of a warp overlap heavily in L1.
+//
+// Two arithmetic forms:
+//   Fp64  : every operation in double, in the reference's order (the plain drop-in);
+//   Mixed : FP32 pair arithmetic.  A coordinate difference is formed from the 21-bit grid cells
+//           of both particles (exact integer difference, periodic wrap in integers) plus the
+//           difference of their FP32 offsets inside the cell: rx = di * u + (xl_i - xl_j), one
+//           rounding.  Sums that the error budget needs are Kahan-compensated.
+#pragma once
+
+#include "context.cuh"
+
+namespace sphgb {
+
+struct Fp64Tag {
+    using T = double;
+};
+struct MixedTag {
+    using T = float;
+};
+
+constexpr int kPairBlock = 128;
+
+// ---- neighbour list access ----
+struct ListView {
+    const uint32_t* nbr;
+    const uint32_t* count;
+    int64_t stride, first, last;
+    uint32_t ngmax;
+    __device__ __forceinline__ unsigned capped(int64_t ii) const { return min(count[ii], ngmax); }
+    __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k) const
+    {
+        return __ldg(nbr + int64_t(k) * stride + ii);
+    }
+};
+
+inline ListView listView(const sphgb_ctx* c)
+{
+    return ListView{c->nbr.as<uint32_t>(), c->ncount.as<uint32_t>(), c->nbrStride, c->nbrFirst, c->nbrLast,
+                    c->nbrNgmax};
+}
+
+// ---- FP64 coordinates: reference distancePBC / legacy applyPBC (box.hpp:216-254) ----
+struct CoordFp64 {
+    const double *x, *y, *z;
+    double L[3];
+    int pbc[3];
+    struct Target {
+        double x, y, z;
+    };
+    __device__ __forceinline__ Target target(int64_t i) const { return {x[i], y[i], z[i]}; }
+    __device__ __forceinline__ void diff(const Target& t, int64_t j, double twoH, double& rx, double& ry,
+                                         double& rz) const
+    {
+        rx = t.x - x[j];
+        ry = t.y - y[j];
+        rz = t.z - z[j];
+        if (pbc[0] && rx > twoH) rx -= L[0];
+        else if (pbc[0] && rx < -twoH) rx += L[0];
+        if (pbc[1] && ry > twoH) ry -= L[1];
+        else if (pbc[1] && ry < -twoH) ry += L[1];
+        if (pbc[2] && rz > twoH) rz -= L[2];
+        else if (pbc[2] && rz < -twoH) rz += L[2];
+    }
+};
+
+inline CoordFp64 coordFp64(const sphgb_ctx* c, const sphgb_particles* p)
+{
+    CoordFp64 r;
+    r.x = p->x;
+    r.y = p->y;
+    r.z = p->z;
+    for (int k = 0; k < 3; ++k) {
+        r.L[k] = c->box.L[k];
+        r.pbc[k] = c->box.pbc[k];
+    }
+    return r;
+}
+
+// ---- Mixed coordinates: 21-bit grid cell per axis packed in 64 bits + FP32 in-cell offset ----
+constexpr int kGridBits = 21;
+constexpr int kGridMask = (1 << kGridBits) - 1;
+
+struct CoordMixed {
+    const u64* cell;     // ix | iy << 21 | iz << 42
+    const float4* loc;   // {xl, yl, zl, 1/h}
+    float u[3];          // cell edge per axis (box length / 2^21)
+    int pbc[3];
+    struct Target {
+        int ix, iy, iz;
+        float xl, yl, zl, hInv;
+    };
+    __device__ __forceinline__ Target target(int64_t i) const
+    {
+        u64 k = cell[i];
+        float4 l = loc[i];
+        return {int(k & kGridMask), int((k >> kGridBits) & kGridMask), int(k >> (2 * kGridBits)), l.x, l.y, l.z, l.w};
+    }
+    __device__ __forceinline__ static int wrap(int d, int on)
+    {
+        constexpr int R = 1 << kGridBits;
+        if (on) {
+            d = d > R / 2 ? d - R : d;
+            d = d < -R / 2 ? d + R : d;
+        }
+        return d;
+    }
+    // returns 1/h_j through hjInv
+    __device__ __forceinline__ void diff(const Target& t, int64_t j, float& rx, float& ry, float& rz,
+                                         float& hjInv) const
+    {
+        u64 k = __ldg(cell + j);
+        float4 l = __ldg(loc + j);
+        int dx = wrap(t.ix - int(k & kGridMask), pbc[0]);
+        int dy = wrap(t.iy - int((k >> kGridBits) & kGridMask), pbc[1]);
+        int dz = wrap(t.iz - int(k >> (2 * kGridBits)), pbc[2]);
+        rx = fmaf(float(dx), u[0], t.xl - l.x);
+        ry = fmaf(float(dy), u[1], t.yl - l.y);
+        rz = fmaf(float(dz), u[2], t.zl - l.z);
+        hjInv = l.w;
+    }
+};
+
+inline CoordMixed coordMixed(const sphgb_ctx* c)
+{
+    CoordMixed r;
+    r.cell = c->gridKey.as<u64>();
+    r.loc = c->gridLoc.as<float4>();
+    for (int k = 0; k < 3; ++k) {
+        r.u[k] = float(c->box.L[k] / double(1 << kGridBits));
+        r.pbc[k] = c->box.pbc[k];
+    }
+    return r;
+}
+
+// ---- Kahan-compensated FP32 accumulator ----
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v)
+    {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s - c; }
+    __device__ __forceinline__ double value64() const { return double(s) - double(c); }
+};
+
+// ---- helpers ----
+template<class T>
+__device__ __forceinline__ T ld(const void* p, int64_t i)
+{
+    return __ldg(static_cast<const T*>(p) + i);
+}
+
+template<class T>
+__device__ __forceinline__ void st(void* p, int64_t i, T v)
+{
+    static_cast<T*>(p)[i] = v;
+}
+
+// reference artificial_viscosity (sph/include/sph/kernels.hpp:70-84)
+template<class T>
+__device__ __forceinline__ T artificialViscosity(T ai, T aj, T ci, T cj, T w)
+{
+    T v = T(0);
+    if (w < T(0)) {
+        T sig = (ai + aj) / T(4.0) * (ci + cj) - T(2.0) * w;
+        v = -sig * w;
+    }
+    return v;
+}
+
+// reference tsKCourant (kernels.hpp:10-16); Kcour travels as float
+__device__ __forceinline__ double courantDt(double vsig, double h, double c, float kc)
+{
+    double v = vsig > 0.0 ? vsig : c;
+    return double(kc) * h / v;
+}
+
+// block-wide min of positive doubles into one device word (bit patterns of positive doubles are
+// ordered like their values)
+__device__ __forceinline__ void blockMinDt(double v, unsigned long long* out)
+{
+    __shared__ unsigned long long s[kPairBlock / kWarp];
+    unsigned long long b = __double_as_longlong(v);
+    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x / 32] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = s[0];
+        for (int q = 1; q < kPairBlock / kWarp; ++q) m = min(m, s[q]);
+        atomicMin(out, m);
+    }
+}
+
+// normalise tau by 2^-(mean exponent), invert, scale by h^3 / K (hydro_std/iad_kern.hpp:52-76)
+template<class T>
+__device__ __forceinline__ void iadInvert(T t11, T t12, T t13, T t22, T t23, T t33, double hi, double K, T* cOut)
+{
+    auto ex = [](T v) { return v == T(0) ? 0 : ilogb(v); };
+    int es = ex(t11) + ex(t12) + ex(t13) + ex(t22) + ex(t23) + ex(t33);
+    T nrm = ldexp(T(1), -es / 6);
+    t11 *= nrm;
+    t12 *= nrm;
+    t13 *= nrm;
+    t22 *= nrm;
+    t23 *= nrm;
+    t33 *= nrm;
+    T det = t11 * t22 * t33 + T(2) * t12 * t23 * t13 - t11 * t23 * t23 - t22 * t13 * t13 - t33 * t12 * t12;
+    // factor = normalization * h^3 / (det * K); the reference forms it with K in FP64
+    double fac = double(nrm) * (hi * hi * hi) / (double(det) * K);
+    T f = T(fac);
+    cOut[0] = (t22 * t33 - t23 * t23) * f;
+    cOut[1] = (t13 * t23 - t33 * t12) * f;
+    cOut[2] = (t12 * t23 - t22 * t13) * f;
+    cOut[3] = (t11 * t33 - t13 * t13) * f;
+    cOut[4] = (t13 * t12 - t11 * t23) * f;
+    cOut[5] = (t11 * t22 - t12 * t12) * f;
+}
+
+// per-pass launch helpers implemented in prep.cu
+int beginDtReduction(sphgb_ctx* c, unsigned long long** dst);
+int endDtReduction(sphgb_ctx* c, unsigned long long* dst, double* out);
+int checkPass(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last);
+
+}  // namespace sphgb

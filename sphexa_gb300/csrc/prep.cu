@@ -1,0 +1,170 @@
+// Per-sweep preparation shared by the pair passes: kernel tables and normalisation K, the
+// mixed form's grid-local coordinates, FP64 reciprocals, and the Courant-dt reduction word.
+#include <cmath>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+
+#include "pairs.cuh"
+
+namespace sphgb {
+
+namespace {
+
+// sinc(pi/2 v) and its derivative (sph/include/sph/kernels.hpp:35-61)
+double sincStd(double v)
+{
+    if (v == 0.0) return 1.0;
+    const double pv = M_PI_2 * v;
+    return std::sin(pv) / pv;
+}
+double sincStdDeriv(double v)
+{
+    if (v == 0.0) return 0.0;
+    const double pv = M_PI_2 * v;
+    const double s = std::sin(pv) / pv;
+    return s * M_PI_2 * ((std::cos(pv) / std::sin(pv)) - 1.0 / pv);
+}
+
+// 3D normalisation of sinc^n on [0, 2] by composite Simpson with 2000 intervals, odd and even
+// samples summed in ascending order (sph/include/sph/sph_kernel_tables.hpp:30-77)
+double kernelNormalisation(double n)
+{
+    auto f = [n](double x) { return 4.0 * M_PI * x * x * std::pow(sincStd(x), n); };
+    const int intervals = 2000;
+    const double a = 0.0, b = 2.0, hs = (b - a) / double(intervals);
+    std::vector<double> odd(intervals / 2), even(intervals / 2 - 1);
+    for (size_t i = 0; i < odd.size(); ++i) odd[i] = f(a + double(2 * (i + 1) - 1) * hs);
+    for (size_t i = 0; i < even.size(); ++i) even[i] = f(a + double(2 * (i + 1)) * hs);
+    std::sort(odd.begin(), odd.end());
+    std::sort(even.begin(), even.end());
+    double s = hs / 3.0 *
+               (f(a) + f(b) + 4.0 * std::accumulate(odd.begin(), odd.end(), 0.0) +
+                2.0 * std::accumulate(even.begin(), even.end(), 0.0));
+    return 1.0 / s;
+}
+
+__global__ void mixedCoordsKernel(const double* __restrict__ x, const double* __restrict__ y,
+                                  const double* __restrict__ z, const void* __restrict__ h, int hIsFloat, int64_t n,
+                                  DevBox box, u64* __restrict__ cell, float4* __restrict__ loc)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const double c[3] = {x[i], y[i], z[i]};
+    unsigned ic[3];
+    float l[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double u = box.L[k] / double(1 << kGridBits);
+        double g = floor((c[k] - box.lo[k]) / u);
+        g = fmin(fmax(g, 0.0), double(kGridMask));
+        ic[k] = unsigned(g);
+        l[k] = float(c[k] - (box.lo[k] + g * u));
+    }
+    double hi = hIsFloat ? double(static_cast<const float*>(h)[i]) : static_cast<const double*>(h)[i];
+    cell[i] = u64(ic[0]) | (u64(ic[1]) << kGridBits) | (u64(ic[2]) << (2 * kGridBits));
+    loc[i] = make_float4(l[0], l[1], l[2], float(1.0 / hi));
+}
+
+__global__ void recipKernel(const double* __restrict__ h, int64_t n, double* __restrict__ out)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) out[i] = 1.0 / h[i];
+}
+
+__global__ void initDtWord(unsigned long long* p) { *p = 0x7ff0000000000000ull; /* +inf */ }
+
+}  // namespace
+
+int buildTables(sphgb_ctx* c)
+{
+    const double n = c->prm.sincIndex;
+    std::vector<double> wh(kTableSize), whd(kTableSize);
+    std::vector<float> wf(kTableSize), wdf(kTableSize);
+    // tabulateFunction on [0, 2] (sph/include/sph/sph_kernel_tables.hpp:81-95)
+    const double dx = (2.0 - 0.0) / (kTableSize - 1);
+    for (int i = 0; i < kTableSize; ++i) {
+        double v = 0.0 + i * dx;
+        wh[i] = std::pow(sincStd(v), n);
+        whd[i] = n * std::pow(sincStd(v), n - 1) * sincStdDeriv(v);
+        wf[i] = float(wh[i]);
+        wdf[i] = float(whd[i]);
+    }
+    c->K = kernelNormalisation(n);
+    SPHGB_TRY(c->wh64.ensure(sizeof(double) * kTableSize));
+    SPHGB_TRY(c->whd64.ensure(sizeof(double) * kTableSize));
+    SPHGB_TRY(c->wh32.ensure(sizeof(float) * kTableSize));
+    SPHGB_TRY(c->whd32.ensure(sizeof(float) * kTableSize));
+    SPHGB_CUDA(cudaMemcpy(c->wh64.p, wh.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->whd64.p, whd.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->wh32.p, wf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->whd32.p, wdf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
+    c->tablesReady = true;
+    return SPHGB_OK;
+}
+
+int prepareMixed(sphgb_ctx* c, sphgb_particles* p, int64_t, int64_t)
+{
+    const int64_t n = p->n;
+    SPHGB_TRY(c->gridKey.ensure(sizeof(u64) * n));
+    SPHGB_TRY(c->gridLoc.ensure(sizeof(float4) * n));
+    mixedCoordsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(p->x, p->y, p->z, p->h, p->precision == SPHGB_MIXED, n,
+                                                             c->box, c->gridKey.as<u64>(), c->gridLoc.as<float4>());
+    return launched(c, "mixedCoordsKernel");
+}
+
+int prepareFp64(sphgb_ctx* c, sphgb_particles* p)
+{
+    const int64_t n = p->n;
+    SPHGB_TRY(c->hInv64.ensure(sizeof(double) * n));
+    recipKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(static_cast<const double*>(p->h), n, c->hInv64.as<double>());
+    return launched(c, "recipKernel");
+}
+
+// preconditions of every pair pass; refreshes the per-particle precomputes when h or the lists
+// changed since they were made
+int checkPass(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last)
+{
+    if (!c->haveNbr || !c->tablesReady) return SPHGB_ERR_STATE;
+    if (!p || !p->x || !p->y || !p->z || !p->h) return SPHGB_ERR_ARG;
+    if (first < c->nbrFirst || last > c->nbrLast || first >= last || p->n < last) return SPHGB_ERR_ARG;
+    if (p->precision != SPHGB_FP64 && p->precision != SPHGB_MIXED) return SPHGB_ERR_ARG;
+    sphgb_particles* q = const_cast<sphgb_particles*>(p);
+    if (p->precision == SPHGB_MIXED) {
+        if (c->prepMixedFor != p->x || c->prepMixedH != p->h || c->prepEpoch != c->nbrEpoch) {
+            SPHGB_TRY(prepareMixed(c, q, first, last));
+            c->prepMixedFor = p->x;
+            c->prepMixedH = p->h;
+            c->prepEpoch = c->nbrEpoch;
+        }
+    } else {
+        if (c->prepFp64H != p->h || c->prepEpoch64 != c->nbrEpoch) {
+            SPHGB_TRY(prepareFp64(c, q));
+            c->prepFp64H = p->h;
+            c->prepEpoch64 = c->nbrEpoch;
+        }
+    }
+    return SPHGB_OK;
+}
+
+int beginDtReduction(sphgb_ctx* c, unsigned long long** dst)
+{
+    SPHGB_TRY(c->reduceScratch.ensure(sizeof(unsigned long long) * 4));
+    *dst = c->reduceScratch.as<unsigned long long>();
+    initDtWord<<<1, 1, 0, c->stream>>>(*dst);
+    return launched(c, "initDtWord");
+}
+
+int endDtReduction(sphgb_ctx* c, unsigned long long* dst, double* out)
+{
+    if (!out) return SPHGB_OK;
+    unsigned long long bits = 0;
+    SPHGB_CUDA(cudaMemcpyAsync(&bits, dst, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    *out = v;
+    return SPHGB_OK;
+}
+
+}  // namespace sphgb
