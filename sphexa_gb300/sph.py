@@ -221,15 +221,22 @@ class Domain:
                     level_range=np.array(st.level_range[:], dtype=np.int32))
 
 
+class _DeviceView:
+    """borrowed view of library-owned device memory for torch.as_tensor"""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, True), "version": 2,
+                                         "strides": None}
+
+
 def _device_array(ptr: int, n: int, dtype) -> np.ndarray:
-    out = np.empty(n, dtype=dtype)
-    if n:
-        torch.cuda.synchronize()
-        cudart = torch.cuda.cudart()
-        res = cudart.cudaMemcpy(out.ctypes.data, ptr, out.nbytes, 2)  # device -> host
-        if int(res) != 0:
-            raise RuntimeError(f"cudaMemcpy failed ({int(res)})")
-    return out
+    dtype = np.dtype(dtype)
+    if n == 0:
+        return np.empty(0, dtype=dtype)
+    signed = {8: "<i8", 4: "<i4"}[dtype.itemsize]
+    torch.cuda.synchronize()
+    t = torch.as_tensor(_DeviceView(ptr, n, signed), device="cuda")
+    return t.cpu().numpy().view(dtype).copy()
 
 
 def _device_u32(ptr: int, n: int) -> np.ndarray:
