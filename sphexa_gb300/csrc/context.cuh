@@ -106,8 +106,12 @@ struct sphgb_ctx {
 
     // mixed precision grid-local coordinates: packed cell (21 bits per axis) + float4 {dx,dy,dz,1/h}
     sphgb::DBuf gridKey, gridLoc;
-    // per-particle reciprocals reused by the FP64 passes (same IEEE results as in-loop division)
+    // per-particle reciprocals reused by the FP64 passes: [0,n) 1/h, [n,2n) 1/h^3 (same IEEE
+    // results as the in-loop divisions of the reference)
     sphgb::DBuf hInv64;
+    // per-particle quotients of pass inputs, rebuilt at the start of every pass that reads them
+    // (VE: rho, m/rho, xm/kx, m*prho, ln xm; std: m/rho, p/rho, p/rho^2)
+    sphgb::DBuf aux;
     // validity of the precomputes: the lists' epoch and the field pointers they were made from
     int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;
     const void* prepMixedFor = nullptr;

@@ -1,16 +1,16 @@
 // Standard-SPH pair passes: density, ideal-gas EOS, IAD, momentum and energy.
 //
-// FP64 form: the arithmetic of the reference j-loops in the same order
+// Reference j-loops restated:
 //   density  -> xmassJLoop with rho<->xm swapped, then rho = m / xm
 //               (sph/include/sph/hydro_std/density.hpp:41-60, hydro_ve/xmass_kern.hpp:50-79)
 //   EOS      -> idealGasEOS_u (hydro_std/eos.hpp:54-80, sph/eos.hpp:34-44)
 //   IAD      -> IADJLoopSTD (hydro_std/iad_kern.hpp:12-77)
 //   ME       -> momentumAndEnergyJLoop + tsKCourant (hydro_std/momentum_energy_kern.hpp:12-134,
 //               momentum_energy.hpp:41-101)
-// with per-particle reciprocals (1/h) hoisted out of the pair loop; they are the same IEEE
-// divisions, so the results are unchanged.
-// Mixed form: FP32 pair arithmetic on grid-local offsets, Kahan sums, per-particle epilogues
-// (normalisation, 3x3 inverse factor) in FP64.
+// FP64 form: per-particle quotients (m/rho, p/rho, p/rho^2, 1/h, 1/h^3) are formed once per
+// particle, 1/|r| comes from rsqrt, periodic wrap tests run only where they can fire; results
+// agree with the reference to rounding.  Mixed form: FP32 pair arithmetic on grid-local
+// offsets, Kahan sums, per-particle epilogues (normalisation, 3x3 inverse factor) in FP64.
 #include "pairs.cuh"
 
 namespace sphgb {
@@ -31,13 +31,14 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
         double rho0 = mi;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            double dist = sqrt(rx * rx + ry * ry + rz * rz);
-            rho0 += tableLookup(tab, dist * hInv) * ld<double>(m, j);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            double r2 = rx * rx + ry * ry + rz * rz;
+            rho0 += tableLookup(tab, r2 * invDist(r2) * hInv) * ld<double>(m, j);
         }
         double xm = mi / (rho0 * K * h3Inv);
         st<double>(out, i, StoreRho ? mi / xm : xm);
@@ -74,16 +75,42 @@ __global__ void eosStdKernel(int64_t first, int64_t last, const double* u, const
     st<T>(c, i, T(sqrt(gamma * tmp)));
 }
 
+// ---------------------------------------------------------------- per-particle quotients
+// aux[0,n) m/rho, [n,2n) p/rho, [2n,3n) p/rho^2
+template<class T>
+__global__ void stdAuxKernel(int64_t n, const void* m, const void* rho, const void* p, T* aux)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    T ri = ld<T>(rho, i);
+    aux[i] = ld<T>(m, i) / ri;
+    if (p) {
+        T pi = ld<T>(p, i);
+        aux[n + i] = pi / (ri * T(1));
+        aux[2 * n + i] = pi / (T(1) * ri * ri);
+    }
+}
+
+template<class P>
+int launchStdAux(sphgb_ctx* c, const sphgb_particles* p, bool withPressure)
+{
+    using T = typename P::T;
+    const int64_t n = p->n;
+    SPHGB_TRY(c->aux.ensure(sizeof(T) * 3 * n));
+    stdAuxKernel<T><<<gridFor(n, 256), 256, 0, c->stream>>>(n, p->m, p->rho, withPressure ? p->p : nullptr,
+                                                            c->aux.as<T>());
+    return launched(c, "stdAuxKernel");
+}
+
 // ---------------------------------------------------------------- IAD
 struct IadOut {
     void *c11, *c12, *c13, *c22, *c23, *c33;
 };
 
-// volume of j: num[j] / den[j] (std: m / rho, ve: xm / kx)
+// vol[j] = m[j] / rho[j], formed once per particle (the reference divides per pair)
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
-                                                        const void* num, const void* den, const void* wh, double K,
-                                                        IadOut o)
+                                                        const void* vol, const void* wh, double K, IadOut o)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -93,14 +120,15 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
         const double* tab = static_cast<const double*>(wh);
         auto t = cf.target(i);
         double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
         double t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            double dist = sqrt(rx * rx + ry * ry + rz * rz);
-            double w = tableLookup(tab, dist * hiInv);
-            double vw = ld<double>(num, j) / ld<double>(den, j) * w;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            double r2 = rx * rx + ry * ry + rz * rz;
+            double w = tableLookup(tab, r2 * invDist(r2) * hiInv);
+            double vw = ld<double>(vol, j) * w;
             t11 += rx * rx * vw;
             t12 += rx * ry * vw;
             t13 += rx * rz * vw;
@@ -126,7 +154,7 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
             cm.diff(t, j, rx, ry, rz, hjInv);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             float w = tableLookup(tab, dist * t.hInv);
-            float vw = __fdividef(ld<float>(num, j), ld<float>(den, j)) * w;
+            float vw = ld<float>(vol, j) * w;
             t11.add(rx * rx * vw);
             t12.add(rx * ry * vw);
             t13.add(rx * rz * vw);
@@ -151,7 +179,9 @@ struct MeStdArgs {
     const void *vx, *vy, *vz, *h, *m, *rho, *p, *c;
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void* wh;
-    const double* hInv64;
+    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3
+    const void* aux;       // m/rho, p/rho, p/rho^2
+    int64_t n;
     double K;
     float Kcour;
     void *ax, *ay, *az;
@@ -162,35 +192,43 @@ struct MeStdArgs {
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64 cf, CoordMixed cm, MeStdArgs a)
 {
+    using T = typename P::T;
     const int64_t i0 = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     const bool valid = i0 < lv.last;
     const int64_t i = valid ? i0 : lv.first;
     const int64_t ii = i - lv.first;
     const unsigned nc = valid ? lv.capped(ii) : 0u;
+    const T* tab = static_cast<const T*>(a.wh);
+    const T* aux = static_cast<const T*>(a.aux);
+    const T *auxMoR = aux, *auxPoR = aux + a.n, *auxPoR2 = aux + 2 * a.n;
     double dt = INFINITY;
+
+    T hi = ld<T>(a.h, i), ci = ld<T>(a.c, i);
+    T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+    T mi_roi = auxMoR[i], proi2 = auxPoR2[i];
+    T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
+    T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
+    T maxv = 0;
+
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        using T = double;
-        const double* tab = static_cast<const double*>(a.wh);
         auto t = cf.target(i);
-        T hi = ld<T>(a.h, i), roi = ld<T>(a.rho, i), pri = ld<T>(a.p, i), ci = ld<T>(a.c, i);
-        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
-        T mi_roi = ld<T>(a.m, i) / roi;
-        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
-        T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
-        T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
-        T maxv = 0, mx = 0, my = 0, mz = 0, en = 0;
+        const double* hInv = a.hInv64;
+        const double* hInv3 = a.hInv64 + a.n;
+        T hiInv = hInv[i], hiInv3 = hInv3[i], twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
+        T mx = 0, my = 0, mz = 0, en = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            T r2 = rx * rx + ry * ry + rz * rz;
+            T rinv = invDist(r2);
+            T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
-            T hjInv = __ldg(a.hInv64 + j);
-            T v1 = dist * hiInv, v2 = dist * hjInv;
+            T v1 = dist * hiInv, v2 = dist * __ldg(hInv + j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            T hjInv3 = hjInv * hjInv * hjInv;
             T Wi = hiInv3 * tableLookup(tab, v1);
-            T Wj = hjInv3 * tableLookup(tab, v2);
+            T Wj = __ldg(hInv3 + j) * tableLookup(tab, v2);
             T a1i = c11i * rx + c12i * ry + c13i * rz;
             T a2i = c12i * rx + c22i * ry + c23i * rz;
             T a3i = c13i * rx + c23i * ry + c33i * rz;
@@ -199,17 +237,17 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             T a1j = c11j * rx + c12j * ry + c13j * rz;
             T a2j = c12j * rx + c22j * ry + c23j * rz;
             T a3j = c13j * rx + c23j * ry + c33j * rz;
-            T roj = ld<T>(a.rho, j), cj = ld<T>(a.c, j);
-            T wij = rv / dist;
+            T cj = ld<T>(a.c, j);
+            T wij = rv * rinv;
             T visc = T(0.5) * artificialViscosity<T>(1.0, 1.0, ci, cj, wij);
             T vsig = ci + cj - T(3) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
             T mj = ld<T>(a.m, j);
-            T mjrojWj = mj / roj * Wj;
-            T mjproi = mj * pri / (T(1) * roi * roi);
+            T mjrojWj = __ldg(auxMoR + j) * Wj;
+            T mjproi = mj * proi2;
             {
                 T aa = Wi * (mjproi + visc * mi_roi);
-                T bb = mjrojWj * (ld<T>(a.p, j) / (roj * T(1)) + visc);
+                T bb = mjrojWj * (__ldg(auxPoR + j) + visc);
                 mx += aa * a1i + bb * a1j;
                 my += aa * a2i + bb * a2j;
                 mz += aa * a3i + bb * a3j;
@@ -228,17 +266,8 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             dt = courantDt(maxv, hi, ci, a.Kcour);
         }
     } else {
-        using T = float;
-        const float* tab = static_cast<const float*>(a.wh);
         auto t = cm.target(i);
-        T hi = ld<T>(a.h, i), roi = ld<T>(a.rho, i), pri = ld<T>(a.p, i), ci = ld<T>(a.c, i);
-        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
-        T mi_roi = ld<T>(a.m, i) / roi;
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
-        T proi2 = pri / (roi * roi);
-        T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
-        T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
-        T maxv = 0;
         KSum mx, my, mz, en;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
@@ -260,17 +289,16 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             T a1j = c11j * rx + c12j * ry + c13j * rz;
             T a2j = c12j * rx + c22j * ry + c23j * rz;
             T a3j = c13j * rx + c23j * ry + c33j * rz;
-            T roj = ld<T>(a.rho, j), cj = ld<T>(a.c, j);
-            T rojInv = __frcp_rn(roj);
+            T cj = ld<T>(a.c, j);
             T wij = rv * rinv;
             T visc = T(0.5) * artificialViscosity<T>(1.f, 1.f, ci, cj, wij);
             T vsig = ci + cj - T(3) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
             T mj = ld<T>(a.m, j);
-            T mjrojWj = mj * rojInv * Wj;
+            T mjrojWj = __ldg(auxMoR + j) * Wj;
             T mjproi = mj * proi2;
             T aa = Wi * (mjproi + visc * mi_roi);
-            T bb = mjrojWj * (ld<T>(a.p, j) * rojInv + visc);
+            T bb = mjrojWj * (__ldg(auxPoR + j) + visc);
             mx.add(aa * a1i + bb * a1j);
             my.add(aa * a2i + bb * a2j);
             mz.add(aa * a3i + bb * a3j);
@@ -308,27 +336,51 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
 }
 
 template<class P>
-int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, const void* num, const void* den)
+int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 {
+    SPHGB_TRY(launchStdAux<P>(c, p, false));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
     const void* wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
     iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
-        lv, coordFp64(c, p), coordMixed(c), p->h, num, den, wh, c->K, IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
+        lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, c->K,
+        IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
     return launched(c, "iadKernel");
 }
 
 template<class P>
 int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, double* minDt)
 {
+    SPHGB_TRY(launchStdAux<P>(c, p, true));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    MeStdArgs a{p->vx,  p->vy,  p->vz,  p->h,  p->m,  p->rho, p->p, p->c, p->c11, p->c12, p->c13, p->c22, p->c23,
-                p->c33, nullptr, c->hInv64.as<double>(), c->K, float(c->prm.Kcour), p->ax, p->ay, p->az, p->du,
-                nullptr};
+    MeStdArgs a{};
+    a.vx = p->vx;
+    a.vy = p->vy;
+    a.vz = p->vz;
+    a.h = p->h;
+    a.m = p->m;
+    a.rho = p->rho;
+    a.p = p->p;
+    a.c = p->c;
+    a.c11 = p->c11;
+    a.c12 = p->c12;
+    a.c13 = p->c13;
+    a.c22 = p->c22;
+    a.c23 = p->c23;
+    a.c33 = p->c33;
     a.wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    a.hInv64 = c->hInv64.as<double>();
+    a.aux = c->aux.p;
+    a.n = p->n;
+    a.K = c->K;
+    a.Kcour = float(c->prm.Kcour);
+    a.ax = p->ax;
+    a.ay = p->ay;
+    a.az = p->az;
+    a.du = p->du;
     SPHGB_TRY(beginDtReduction(c, &a.minDt));
     meStdKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p),
                                                                                      coordMixed(c), a);
@@ -367,14 +419,14 @@ int passIadStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 {
     if (!p->m || !p->rho || !p->c11 || !p->c12 || !p->c13 || !p->c22 || !p->c23 || !p->c33) return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
-    if (p->precision == SPHGB_MIXED) return launchIad<MixedTag>(c, p, first, last, p->m, p->rho);
-    return launchIad<Fp64Tag>(c, p, first, last, p->m, p->rho);
+    if (p->precision == SPHGB_MIXED) return launchIad<MixedTag>(c, p, first, last);
+    return launchIad<Fp64Tag>(c, p, first, last);
 }
 
 int passMomentumEnergyStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, double* minDt)
 {
     if (!p->vx || !p->vy || !p->vz || !p->rho || !p->p || !p->c || !p->ax || !p->ay || !p->az || !p->du ||
-        !p->c11)
+        !p->c11 || !p->m)
         return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
     if (p->precision == SPHGB_MIXED) return launchMeStd<MixedTag>(c, p, first, last, minDt);

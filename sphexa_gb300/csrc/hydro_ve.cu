@@ -1,18 +1,52 @@
 // Volume-element SPH pair passes with the artificial-viscosity switch.
 //
-// FP64 form follows the reference j-loops operation by operation:
+// Reference j-loops restated:
 //   gradh     -> veDefGradhJLoop (sph/include/sph/hydro_ve/ve_def_gradh_kern.hpp:43-90)
 //   EOS       -> computeIdealGasEOS_Impl (hydro_ve/eos.hpp:52-94)
 //   IAD+divv  -> IADJLoop then divV_curlVJLoop over the same list in one kernel
 //                (hydro_ve/iad_kern.hpp:43-109, divv_curlv_kern.hpp:43-123)
 //   AV switch -> AVswitchesJLoop (hydro_ve/av_switches_kern.hpp:43-137)
 //   ME        -> momentumAndEnergyJLoop<avClean> + avRvCorrection (hydro_ve/momentum_energy_kern.hpp)
-// The mixed form runs the same loops in FP32 on grid-local offsets with Kahan sums.
+//
+// The passes are FP64-pipe bound in the FP64 form, so the pair loops spend as few FP64
+// instructions as the result allows: quotients of per-particle fields (rho_j, m_j/rho_j,
+// xm_j/kx_j, m_j*prho_j) are formed once per particle; 1/|r| comes from rsqrt and serves both
+// |r| and rv/|r|; the Atwood-number branches are decided by comparison, and the ramp's four
+// pow() calls become one exp() of the precomputed ln xm difference; the periodic wrap tests run
+// only for targets whose 2h box touches a periodic face.  Results agree with the reference to
+// rounding (<= 1e-12 relative).  The mixed form runs the same loops in FP32 on grid-local
+// offsets with Kahan sums.
 #include "pairs.cuh"
 
 namespace sphgb {
 
 namespace {
+
+// ---------------------------------------------------------------- per-particle quotients
+template<class T>
+__global__ void veAuxKernel(int64_t n, const void* m, const void* kx, const void* xm, const void* prho, T* aux)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    T mi = ld<T>(m, i), kxi = ld<T>(kx, i), xmi = ld<T>(xm, i);
+    T rho = kxi * mi / xmi;
+    aux[i] = rho;
+    aux[n + i] = mi / rho;
+    aux[2 * n + i] = xmi / kxi;
+    if (prho) aux[3 * n + i] = mi * ld<T>(prho, i);
+    if constexpr (std::is_same_v<T, double>) aux[4 * n + i] = log(xmi);
+    else aux[4 * n + i] = log2f(xmi);
+}
+
+template<class P>
+int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
+{
+    using T = typename P::T;
+    const int64_t n = p->n;
+    SPHGB_TRY(c->aux.ensure(sizeof(T) * 5 * n));
+    veAuxKernel<T><<<gridFor(n, 256), 256, 0, c->stream>>>(n, p->m, p->kx, p->xm, p->prho, c->aux.as<T>());
+    return launched(c, "veAuxKernel");
+}
 
 // ---------------------------------------------------------------- gradh (kx, gradh)
 template<class P>
@@ -29,13 +63,14 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i), xmi = ld<double>(xm, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
         double kxi = xmi, whomega = -3.0 * xmi, wrho0 = -3.0 * mi;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            double dist = sqrt(rx * rx + ry * ry + rz * rz);
-            double v = dist * hInv;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            double r2 = rx * rx + ry * ry + rz * rz;
+            double v = r2 * invDist(r2) * hInv;
             double w = tableLookup(tw, v), dw = tableLookup(tdw, v);
             double dterh = -(3.0 * w + v * dw);
             double xmj = ld<double>(xm, j);
@@ -105,6 +140,7 @@ __global__ void eosVeKernel(int64_t first, int64_t last, const double* u, const 
 // ---------------------------------------------------------------- IAD + divv/curlv
 struct IadDivvArgs {
     const void *h, *vx, *vy, *vz, *xm, *kx, *wh;
+    const void* vol;  // aux: xm/kx per particle
     double K;
     void *c11, *c12, *c13, *c22, *c23, *c33, *divv, *curlv;
     void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
@@ -122,14 +158,15 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         const double* tab = static_cast<const double*>(a.wh);
         auto t = cf.target(i);
         T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
         T t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            T dist = sqrt(rx * rx + ry * ry + rz * rz);
-            T w = tableLookup(tab, dist * hiInv);
-            T vw = ld<T>(a.xm, j) / ld<T>(a.kx, j) * w;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            T r2 = rx * rx + ry * ry + rz * rz;
+            T w = tableLookup(tab, r2 * invDist(r2) * hiInv);
+            T vw = ld<T>(a.vol, j) * w;
             t11 += rx * rx * vw;
             t12 += rx * ry * vw;
             t13 += rx * rz * vw;
@@ -151,10 +188,10 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            T r2 = rx * rx + ry * ry + rz * rz;
             T vxji = ld<T>(a.vx, j) - vxi, vyji = ld<T>(a.vy, j) - vyi, vzji = ld<T>(a.vz, j) - vzi;
-            T Wi = tableLookup(tab, dist * hiInv);
+            T Wi = tableLookup(tab, r2 * invDist(r2) * hiInv);
             T tA0 = -(cc[0] * rx + cc[1] * ry + cc[2] * rz) * Wi;
             T tA1 = -(cc[1] * rx + cc[3] * ry + cc[4] * rz) * Wi;
             T tA2 = -(cc[2] * rx + cc[4] * ry + cc[5] * rz) * Wi;
@@ -195,7 +232,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             cm.diff(t, j, rx, ry, rz, hjInv);
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             T w = tableLookup(tab, dist * t.hInv);
-            T vw = __fdividef(ld<T>(a.xm, j), ld<T>(a.kx, j)) * w;
+            T vw = ld<T>(a.vol, j) * w;
             t11.add(rx * rx * vw);
             t12.add(rx * ry * vw);
             t13.add(rx * rz * vw);
@@ -263,7 +300,8 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
 
 // ---------------------------------------------------------------- AV switches
 struct AvArgs {
-    const void *h, *vx, *vy, *vz, *c, *c11, *c12, *c13, *c22, *c23, *c33, *kx, *xm, *divv, *wh;
+    const void *h, *vx, *vy, *vz, *c, *c11, *c12, *c13, *c22, *c23, *c33, *divv, *wh;
+    const void* vol;  // aux: xm/kx
     double K, dt, alphamin, alphamax, decay;
     void* alpha;
 };
@@ -287,22 +325,24 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
         T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
+        const T kh3 = a.K * hiInv3;
         gx = gy = gz = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            T r2 = rx * rx + ry * ry + rz * rz;
+            T rinv = invDist(r2);
+            T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            T vsig = 0.0;
-            if (rv < 0.0) vsig = ci + ld<T>(a.c, j) - 3.0 * rv / dist;
-            vsig_i = fmax(vsig_i, vsig);
-            T Wi = a.K * hiInv3 * tableLookup(tab, dist * hiInv);
+            if (rv < 0.0) vsig_i = fmax(vsig_i, ci + ld<T>(a.c, j) - 3.0 * rv * rinv);
+            T Wi = kh3 * tableLookup(tab, dist * hiInv);
             T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
             T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
             T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
-            T fac = ld<T>(a.xm, j) / ld<T>(a.kx, j) * (divvi - ld<T>(a.divv, j));
+            T fac = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j));
             gx += fac * t1;
             gy += fac * t2;
             gz += fac * t3;
@@ -320,14 +360,12 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            T vsig = 0.f;
-            if (rv < 0.f) vsig = ci + ld<T>(a.c, j) - 3.f * rv * rinv;
-            vsig_i = fmaxf(vsig_i, vsig);
+            if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + ld<T>(a.c, j) - 3.f * rv * rinv);
             T Wi = kh3 * tableLookup(tab, dist * t.hInv);
             T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
             T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
             T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
-            T fac = __fdividef(ld<T>(a.xm, j), ld<T>(a.kx, j)) * (divvi - ld<T>(a.divv, j));
+            T fac = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j));
             sx.add(fac * t1);
             sy.add(fac * t2);
             sz.add(fac * t3);
@@ -359,7 +397,9 @@ struct MeVeArgs {
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
     const void* wh;
-    const double* hInv64;
+    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3
+    const void* aux;       // rho, m/rho, xm/kx, m*prho, ln xm (5 x n)
+    int64_t n;
     double K;
     float Kcour;
     void *ax, *ay, *az;
@@ -402,11 +442,13 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
     const int64_t ii = i - lv.first;
     const unsigned nc = valid ? lv.capped(ii) : 0u;
     const T* tab = static_cast<const T*>(a.wh);
+    const T* aux = static_cast<const T*>(a.aux);
+    const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n;
     constexpr T Atmin = T(0.1), Atmax = T(0.2), ramp = T(1) / (Atmax - Atmin);
 
-    T hi = ld<T>(a.h, i), mi = ld<T>(a.m, i), ci = ld<T>(a.c, i), kxi = ld<T>(a.kx, i), ai = ld<T>(a.alpha, i);
+    T hi = ld<T>(a.h, i), mi = ld<T>(a.m, i), ci = ld<T>(a.c, i), ai = ld<T>(a.alpha, i);
     T xmi = ld<T>(a.xm, i), prhoi = ld<T>(a.prho, i);
-    T rhoi = kxi * mi / xmi;
+    T rhoi = auxRho[i], lnxmi = auxLnXm[i];
     T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
     T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
     T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
@@ -420,24 +462,30 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
         gi[5] = ld<T>(a.dV33, i);
     }
     const T etaCrit = T(cbrt(32.0 * M_PI / 3.0 / double(nc + 1)));
+    const T xmi2 = xmi * xmi;
+    (void)mi;
     T maxv = 0;
     double dt = INFINITY;
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        const double* hInv = a.hInv64;
+        const double* hInv3 = a.hInv64 + a.n;
+        T hiInv = hInv[i], hiInv3 = hInv3[i], twoH = 2.0 * hi;
+        const bool wrap = cf.needsWrap(t, twoH);
+        const T rhoiInv = 1.0 / rhoi;
         T mx = 0, my = 0, mz = 0, en = 0, avE = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
-            cf.diff(t, j, twoH, rx, ry, rz);
-            T dist = sqrt(rx * rx + ry * ry + rz * rz);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            T r2 = rx * rx + ry * ry + rz * rz;
+            T rinv = invDist(r2);
+            T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
-            T hjInv = __ldg(a.hInv64 + j);
-            T v1 = dist * hiInv, v2 = dist * hjInv;
-            T hjInv3 = hjInv * hjInv * hjInv;
+            T v1 = dist * hiInv, v2 = dist * __ldg(hInv + j);
             T Wi = hiInv3 * tableLookup(tab, v1);
-            T Wj = hjInv3 * tableLookup(tab, v2);
+            T Wj = __ldg(hInv3 + j) * tableLookup(tab, v2);
             T a1i = -(c11i * rx + c12i * ry + c13i * rz) * Wi;
             T a2i = -(c12i * rx + c22i * ry + c23i * rz) * Wi;
             T a3i = -(c13i * rx + c23i * ry + c33i * rz) * Wi;
@@ -447,37 +495,40 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
             T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
             T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
-            T rhoj = ld<T>(a.kx, j) * mj / xmj;
+            T rhoj = __ldg(auxRho + j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
                            ld<T>(a.dV22, j), ld<T>(a.dV23, j), ld<T>(a.dV33, j)};
                 rv += avRv<T>(rx, ry, rz, fmin(v1, v2), etaCrit, gi, gj);
             }
-            T wij = rv / dist;
+            T wij = rv * rinv;
             T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
             T vsig = T(0.5) * (ci + cj) - T(2) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
+            // Atwood number |rhoi - rhoj| / (rhoi + rhoj) against Atmin / Atmax, without dividing
+            T dr = fabs(rhoi - rhoj), sr = rhoi + rhoj;
             T am, bm;
-            T At = fabs(rhoi - rhoj) / (rhoi + rhoj);
-            if (At < Atmin) {
-                am = xmi * xmi;
+            if (dr < Atmin * sr) {
+                am = xmi2;
                 bm = xmj * xmj;
-            } else if (At > Atmax) {
+            } else if (dr > Atmax * sr) {
                 am = xmi * xmj;
                 bm = am;
             } else {
-                T s = ramp * (At - Atmin);
-                am = pow(xmi, T(2) - s) * pow(xmj, s);
-                bm = pow(xmj, T(2) - s) * pow(xmi, s);
+                // xmi^(2-s) xmj^s = xmi^2 q and xmj^(2-s) xmi^s = xmj^2 / q, q = (xmj/xmi)^s
+                T s = ramp * (dr / sr - Atmin);
+                T q = exp(s * (__ldg(auxLnXm + j) - lnxmi));
+                am = xmi2 * q;
+                bm = xmj * xmj / q;
             }
-            T av = mj / rhoi * visc, bv = mj / rhoj * visc;
+            T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
             T avx = T(0.5) * (av * a1i + bv * a1j);
             T avy = T(0.5) * (av * a2i + bv * a2j);
             T avz = T(0.5) * (av * a3i + bv * a3j);
             avE += avx * vxij + avy * vyij + avz * vzij;
             en += mj * am * (vxij * a1i + vyij * a2i + vzij * a3i);
-            T momi = mj * prhoi * am, momj = mj * ld<T>(a.prho, j) * bm;
+            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
             mx += momi * a1i + momj * a1j + avx;
             my += momi * a2i + momj * a2j + avy;
             mz += momi * a3i + momj * a3j + avz;
@@ -515,7 +566,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
             T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
             T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
-            T rhoj = ld<T>(a.kx, j) * mj * __frcp_rn(xmj);
+            T rhoj = __ldg(auxRho + j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
@@ -526,26 +577,27 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
             T vsig = T(0.5) * (ci + cj) - T(2) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
+            T dr = fabsf(rhoi - rhoj), sr = rhoi + rhoj;
             T am, bm;
-            T At = fabsf(rhoi - rhoj) / (rhoi + rhoj);
-            if (At < Atmin) {
-                am = xmi * xmi;
+            if (dr < Atmin * sr) {
+                am = xmi2;
                 bm = xmj * xmj;
-            } else if (At > Atmax) {
+            } else if (dr > Atmax * sr) {
                 am = xmi * xmj;
                 bm = am;
             } else {
-                T s = ramp * (At - Atmin);
-                am = powf(xmi, T(2) - s) * powf(xmj, s);
-                bm = powf(xmj, T(2) - s) * powf(xmi, s);
+                T s = ramp * (__fdividef(dr, sr) - Atmin);
+                T q = exp2f(s * (__ldg(auxLnXm + j) - lnxmi));
+                am = xmi2 * q;
+                bm = xmj * xmj * __frcp_rn(q);
             }
-            T av = mj * rhoiInv * visc, bv = mj * __frcp_rn(rhoj) * visc;
+            T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
             T avx = T(0.5) * (av * a1i + bv * a1j);
             T avy = T(0.5) * (av * a2i + bv * a2j);
             T avz = T(0.5) * (av * a3i + bv * a3j);
             avE.add(avx * vxij + avy * vyij + avz * vzij);
             en.add(mj * am * (vxij * a1i + vyij * a2i + vzij * a3i));
-            T momi = mj * prhoi * am, momj = mj * ld<T>(a.prho, j) * bm;
+            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
             mx.add(momi * a1i + momj * a1j + avx);
             my.add(momi * a2i + momj * a2j + avy);
             mz.add(momi * a3i + momj * a3j + avz);
@@ -606,19 +658,43 @@ int passEosVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 {
     if (!p->h || !p->vx || !p->vy || !p->vz || !p->xm || !p->kx || !p->c11 || !p->c12 || !p->c13 || !p->c22 ||
-        !p->c23 || !p->c33 || !p->divv)
+        !p->c23 || !p->c33 || !p->divv || !p->m)
         return SPHGB_ERR_ARG;
     const bool gradV = p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33;
     SPHGB_TRY(checkPass(c, p, first, last));
+    const bool mixed = p->precision == SPHGB_MIXED;
+    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    IadDivvArgs a{p->h,   p->vx,  p->vy,  p->vz,   p->xm,    nullptr, nullptr, c->K,   p->c11, p->c12,
-                  p->c13, p->c22, p->c23, p->c33,  p->divv,  p->curlv, gradV ? p->dV11 : nullptr,
-                  p->dV12, p->dV13, p->dV22, p->dV23, p->dV33};
+    const size_t es = mixed ? 4 : 8;
+    IadDivvArgs a{};
+    a.h = p->h;
+    a.vx = p->vx;
+    a.vy = p->vy;
+    a.vz = p->vz;
+    a.xm = p->xm;
     a.kx = p->kx;
+    a.vol = c->aux.as<char>() + 2 * es * p->n;
+    a.K = c->K;
+    a.c11 = p->c11;
+    a.c12 = p->c12;
+    a.c13 = p->c13;
+    a.c22 = p->c22;
+    a.c23 = p->c23;
+    a.c33 = p->c33;
+    a.divv = p->divv;
+    a.curlv = p->curlv;
+    if (gradV) {
+        a.dV11 = p->dV11;
+        a.dV12 = p->dV12;
+        a.dV13 = p->dV13;
+        a.dV22 = p->dV22;
+        a.dV23 = p->dV23;
+        a.dV33 = p->dV33;
+    }
     unsigned blocks = gridFor(last - first, kPairBlock);
-    if (p->precision == SPHGB_MIXED) {
+    if (mixed) {
         a.wh = c->wh32.p;
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else {
@@ -630,16 +706,20 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
 
 int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 {
-    if (!p->h || !p->vx || !p->c || !p->c11 || !p->kx || !p->xm || !p->divv || !p->alpha) return SPHGB_ERR_ARG;
+    if (!p->h || !p->vx || !p->c || !p->c11 || !p->kx || !p->xm || !p->divv || !p->alpha || !p->m)
+        return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
+    const bool mixed = p->precision == SPHGB_MIXED;
+    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    AvArgs a{p->h,   p->vx,  p->vy,  p->vz, p->c,  p->c11,         p->c12,          p->c13,
-             p->c22, p->c23, p->c33, p->kx, p->xm, p->divv,        nullptr,         c->K,
-             c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant, p->alpha};
+    const size_t es = mixed ? 4 : 8;
+    AvArgs a{p->h,   p->vx,  p->vy,  p->vz,   p->c,    p->c11, p->c12,
+             p->c13, p->c22, p->c23, p->c33,  p->divv, nullptr, c->aux.as<char>() + 2 * es * p->n,
+             c->K,   c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant, p->alpha};
     unsigned blocks = gridFor(last - first, kPairBlock);
-    if (p->precision == SPHGB_MIXED) {
+    if (mixed) {
         a.wh = c->wh32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else {
@@ -653,22 +733,53 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
                          double* minDt)
 {
     if (!p->vx || !p->vy || !p->vz || !p->prho || !p->c || !p->kx || !p->xm || !p->alpha || !p->ax || !p->ay ||
-        !p->az || !p->du || !p->c11)
+        !p->az || !p->du || !p->c11 || !p->m)
         return SPHGB_ERR_ARG;
     if (avClean && !(p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33)) return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
+    const bool mixed = p->precision == SPHGB_MIXED;
+    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    MeVeArgs a{p->vx,   p->vy,   p->vz,   p->h,    p->m,    p->prho, p->c,    p->kx,   p->xm,   p->alpha,
-               p->c11,  p->c12,  p->c13,  p->c22,  p->c23,  p->c33,  p->dV11, p->dV12, p->dV13, p->dV22,
-               p->dV23, p->dV33, nullptr, c->hInv64.as<double>(), c->K, float(c->prm.Kcour), p->ax, p->ay,
-               p->az,   p->du,   groupDt, nullptr};
+    MeVeArgs a{};
+    a.vx = p->vx;
+    a.vy = p->vy;
+    a.vz = p->vz;
+    a.h = p->h;
+    a.m = p->m;
+    a.prho = p->prho;
+    a.c = p->c;
+    a.kx = p->kx;
+    a.xm = p->xm;
+    a.alpha = p->alpha;
+    a.c11 = p->c11;
+    a.c12 = p->c12;
+    a.c13 = p->c13;
+    a.c22 = p->c22;
+    a.c23 = p->c23;
+    a.c33 = p->c33;
+    a.dV11 = p->dV11;
+    a.dV12 = p->dV12;
+    a.dV13 = p->dV13;
+    a.dV22 = p->dV22;
+    a.dV23 = p->dV23;
+    a.dV33 = p->dV33;
+    a.hInv64 = c->hInv64.as<double>();
+    a.aux = c->aux.p;
+    a.n = p->n;
+    a.K = c->K;
+    a.Kcour = float(c->prm.Kcour);
+    a.ax = p->ax;
+    a.ay = p->ay;
+    a.az = p->az;
+    a.du = p->du;
+    a.groupDt = groupDt;
     SPHGB_TRY(beginDtReduction(c, &a.minDt));
     unsigned blocks = gridFor(last - first, kPairBlock);
     auto cf = coordFp64(c, p);
     auto cm = coordMixed(c);
-    if (p->precision == SPHGB_MIXED) {
+    if (mixed) {
         a.wh = c->wh32.p;
         if (avClean) meVeKernel<MixedTag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);

@@ -47,12 +47,20 @@ inline ListView listView(const sphgb_ctx* c)
 // ---- FP64 coordinates: reference distancePBC / legacy applyPBC (box.hpp:216-254) ----
 struct CoordFp64 {
     const double *x, *y, *z;
-    double L[3];
+    double L[3], lo[3], hi[3];
     int pbc[3];
     struct Target {
         double x, y, z;
     };
     __device__ __forceinline__ Target target(int64_t i) const { return {x[i], y[i], z[i]}; }
+    // true when the 2h box of the target crosses a periodic face; otherwise no neighbour can be a
+    // periodic image (|rx| < 2h < L/2) and the wrap tests of applyPBC never fire
+    __device__ __forceinline__ bool needsWrap(const Target& t, double twoH) const
+    {
+        return (pbc[0] && (t.x - twoH < lo[0] || t.x + twoH > hi[0])) ||
+               (pbc[1] && (t.y - twoH < lo[1] || t.y + twoH > hi[1])) ||
+               (pbc[2] && (t.z - twoH < lo[2] || t.z + twoH > hi[2]));
+    }
     __device__ __forceinline__ void diff(const Target& t, int64_t j, double twoH, double& rx, double& ry,
                                          double& rz) const
     {
@@ -66,6 +74,17 @@ struct CoordFp64 {
         if (pbc[2] && rz > twoH) rz -= L[2];
         else if (pbc[2] && rz < -twoH) rz += L[2];
     }
+    // legacy applyPBC only where it can change the result
+    __device__ __forceinline__ void diffFast(const Target& t, int64_t j, double twoH, bool wrap, double& rx,
+                                             double& ry, double& rz) const
+    {
+        if (wrap) diff(t, j, twoH, rx, ry, rz);
+        else {
+            rx = t.x - x[j];
+            ry = t.y - y[j];
+            rz = t.z - z[j];
+        }
+    }
 };
 
 inline CoordFp64 coordFp64(const sphgb_ctx* c, const sphgb_particles* p)
@@ -76,10 +95,16 @@ inline CoordFp64 coordFp64(const sphgb_ctx* c, const sphgb_particles* p)
     r.z = p->z;
     for (int k = 0; k < 3; ++k) {
         r.L[k] = c->box.L[k];
+        r.lo[k] = c->box.lo[k];
+        r.hi[k] = c->box.hi[k];
         r.pbc[k] = c->box.pbc[k];
     }
     return r;
 }
+
+// 1/sqrt(r2) and sqrt(r2) in FP64 through the reciprocal square root: one special-function
+// seed plus FMA refinement instead of an IEEE sqrt and an IEEE divide
+__device__ __forceinline__ double invDist(double r2) { return rsqrt(r2); }
 
 // ---- Mixed coordinates: 21-bit grid cell per axis packed in 64 bits + FP32 in-cell offset ----
 constexpr int kGridBits = 21;

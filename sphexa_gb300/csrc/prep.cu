@@ -69,7 +69,10 @@ __global__ void mixedCoordsKernel(const double* __restrict__ x, const double* __
 __global__ void recipKernel(const double* __restrict__ h, int64_t n, double* __restrict__ out)
 {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-    if (i < n) out[i] = 1.0 / h[i];
+    if (i >= n) return;
+    double hi = 1.0 / h[i];
+    out[i] = hi;
+    out[n + i] = hi * hi * hi;
 }
 
 __global__ void initDtWord(unsigned long long* p) { *p = 0x7ff0000000000000ull; /* +inf */ }
@@ -116,7 +119,7 @@ int prepareMixed(sphgb_ctx* c, sphgb_particles* p, int64_t, int64_t)
 int prepareFp64(sphgb_ctx* c, sphgb_particles* p)
 {
     const int64_t n = p->n;
-    SPHGB_TRY(c->hInv64.ensure(sizeof(double) * n));
+    SPHGB_TRY(c->hInv64.ensure(sizeof(double) * 2 * n));
     recipKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(static_cast<const double*>(p->h), n, c->hInv64.as<double>());
     return launched(c, "recipKernel");
 }

@@ -225,7 +225,7 @@ class _DeviceView:
     """borrowed view of library-owned device memory for torch.as_tensor"""
 
     def __init__(self, ptr: int, n: int, typestr: str):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, True), "version": 2,
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2,
                                          "strides": None}
 
 
