@@ -22,6 +22,20 @@ GOLDEN_SWEEPS = ["sweep_sedov10_std.npz", "sweep_random2000_ve_clean.npz", "swee
 FP64_RTOL = 1e-12
 
 
+# components are compared against the magnitude of their whole tensor / vector: an off-diagonal
+# IAD entry or an acceleration component can vanish by symmetry (perfect lattices) and then only
+# carries rounding noise of the size of its siblings
+GROUPS = {"c11": "C", "c12": "C", "c13": "C", "c22": "C", "c23": "C", "c33": "C",
+          "ax": "A", "ay": "A", "az": "A",
+          "dV11": "D", "dV12": "D", "dV13": "D", "dV22": "D", "dV23": "D", "dV33": "D"}
+
+
+def field_scale(ref: dict, name: str) -> float:
+    g = GROUPS.get(name)
+    members = [k for k, v in GROUPS.items() if v == g and k in ref] if g else [name]
+    return max(float(np.max(np.abs(ref[k]))) for k in members) + 1e-300
+
+
 def run_gpu(ctx, wl, variant, avclean, precision="fp64"):
     import torch
     from sphexa_gb300 import sph
@@ -82,8 +96,8 @@ def test_fp64_sweep_matches_reference(gpu_ctx, name):
         if name_f in ("x", "y", "z", "h", "m", "u", "vx", "vy", "vz"):
             np.testing.assert_array_equal(r[name_f], g[k])
             continue
-        scale = np.max(np.abs(g[k])) + 1e-300
-        err = np.max(np.abs(r[name_f] - g[k])) / scale
+        ref = {q[4:]: g[q] for q in g if q.startswith("out_")}
+        err = np.max(np.abs(r[name_f] - g[k])) / field_scale(ref, name_f)
         assert err <= FP64_RTOL, f"{name_f}: {err:.3e}"
     assert r["minDt"] == pytest.approx(float(g["minDtCourant"]), rel=1e-12)
 
@@ -101,7 +115,7 @@ def mixed_errors(r32: dict, ref: dict) -> dict:
         e["a"] = float(np.linalg.norm(a32 - a64) / np.linalg.norm(a64))
     for f in ("du", "c11", "c22", "c12", "divv", "curlv", "alpha", "gradh", "prho", "p", "c"):
         if f in r32 and np.any(ref[f] != 0):
-            e[f] = float(np.max(np.abs(r32[f] - ref[f])) / np.max(np.abs(ref[f])))
+            e[f] = float(np.max(np.abs(r32[f] - ref[f])) / field_scale(ref, f))
     return e
 
 
@@ -138,8 +152,7 @@ def test_fp64_against_live_oracle_midsize(gpu_ctx, port, case):
         np.testing.assert_array_equal(flat_sets(r["nbr"], r["nc"], ng), flat_sets(ref["nbr"], ref["nc"], ng))
         for f in ("rho", "c11", "c23", "ax", "ay", "az", "du") + (("xm", "kx", "gradh", "divv", "curlv", "alpha")
                                                                   if variant == "ve" else ()):
-            scale = np.max(np.abs(ref[f])) + 1e-300
-            err = np.max(np.abs(r[f] - ref[f])) / scale
+            err = np.max(np.abs(r[f] - ref[f])) / field_scale(ref, f)
             assert err <= FP64_RTOL, f"{case} {variant} {f}: {err:.3e}"
 
 
