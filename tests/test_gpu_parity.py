@@ -107,14 +107,14 @@ def mixed_errors(r32: dict, ref: dict) -> dict:
     normwise; other fields max |d| / max |ref|."""
     e = {}
     for f in ("rho", "xm", "kx"):
-        if f in r32 and np.any(ref[f] != 0):
+        if f in r32 and f in ref and np.all(ref[f] != 0):
             e[f] = float(np.max(np.abs(r32[f] - ref[f]) / np.abs(ref[f])))
     a32 = np.stack([r32["ax"], r32["ay"], r32["az"]], 1)
     a64 = np.stack([ref["ax"], ref["ay"], ref["az"]], 1)
     if np.any(a64 != 0):
         e["a"] = float(np.linalg.norm(a32 - a64) / np.linalg.norm(a64))
     for f in ("du", "c11", "c22", "c12", "divv", "curlv", "alpha", "gradh", "prho", "p", "c"):
-        if f in r32 and np.any(ref[f] != 0):
+        if f in r32 and f in ref and np.any(ref[f] != 0):
             e[f] = float(np.max(np.abs(r32[f] - ref[f])) / field_scale(ref, f))
     return e
 
