@@ -113,6 +113,11 @@ int sphgb_get_tree(sphgb_ctx* ctx, const uint64_t** leaves, const uint32_t** lay
                    const int32_t** internal_to_leaf, sphgb_stats* stats);
 /* sorted order of the last sync: order[i] = pre-sync index of sorted particle i (device) */
 int sphgb_get_order(sphgb_ctx* ctx, const uint32_t** order);
+/* permute one more per-particle field (device, n elements of elem_bytes = 1, 2, 4 or 8) into the
+ * order of the last sync, in place: the reference's sync reorders every property it is handed
+ * (domain/include/cstone/domain/domain.hpp:533-595); sphgb_domain_sync reorders the fields of
+ * sphgb_particles, this call the rest (x_m1, du_m1, temp, ...) */
+int sphgb_apply_order(sphgb_ctx* ctx, void* field, int32_t elem_bytes);
 
 /* ---- neighbours ---- */
 /* cstone::findNeighbors (domain/include/cstone/findneighbors.hpp:149-170): fixed h, no
@@ -177,6 +182,7 @@ int sphgb_kernel_launches(sphgb_ctx* ctx, int64_t* launches);
  * with a dependent-chain probe kernel; the roofline denominator of the pair passes (no
  * reference counterpart: the reference records no performance figures) */
 int sphgb_measure_fma_peak(sphgb_ctx* ctx, int32_t fp64, double* flops_per_s);
+
 
 #ifdef __cplusplus
 }

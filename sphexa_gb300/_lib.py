@@ -72,6 +72,7 @@ SIGNATURES = {
     "sphgb_get_tree": [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                        C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(SphgbStats)],
     "sphgb_get_order": [_P, C.POINTER(C.c_void_p)],
+    "sphgb_apply_order": [_P, _P, C.c_int32],
     "sphgb_find_neighbors": [_P, _P, _P, _P, _P, C.c_int32, _I64, _I64, C.c_uint32, _P, _P],
     "sphgb_find_neighbors_sph": [_P, C.POINTER(SphgbParticles), _I64, _I64],
     "sphgb_export_neighbors": [_P, _P],

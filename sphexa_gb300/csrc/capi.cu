@@ -205,6 +205,12 @@ int sphgb_get_order(sphgb_ctx* c, const uint32_t** order)
     return SPHGB_OK;
 }
 
+int sphgb_apply_order(sphgb_ctx* c, void* field, int32_t elemBytes)
+{
+    SPHGB_TRY(useDevice(c));
+    return applyOrder(c, field, elemBytes);
+}
+
 int sphgb_find_neighbors(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,
                          int32_t hPrec, int64_t first, int64_t last, uint32_t ngmax, uint32_t* neighbors, uint32_t* nc)
 {

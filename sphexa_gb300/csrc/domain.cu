@@ -244,7 +244,35 @@ __global__ void layoutKernel(const u64* __restrict__ keys, int64_t n, const u64*
 
 __global__ void setKey(u64* p, u64 v) { *p = v; }
 
+template<class T>
+__global__ void permuteKernel(const T* __restrict__ src, T* __restrict__ dst, const uint32_t* __restrict__ order,
+                              int64_t n)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) dst[i] = src[order[i]];
+}
+
 }  // namespace
+
+int applyOrder(sphgb_ctx* c, void* field, int esz)
+{
+    if (!c->haveSync) return SPHGB_ERR_STATE;
+    if (!field || (esz != 1 && esz != 2 && esz != 4 && esz != 8)) return SPHGB_ERR_ARG;
+    const int64_t n = c->n;
+    SPHGB_TRY(c->gatherScratch.ensure(size_t(esz) * n));
+    const uint32_t* ord = c->order.as<uint32_t>();
+    unsigned blocks = gridFor(n, kBlock);
+    switch (esz) {
+    case 1: permuteKernel<uint8_t><<<blocks, kBlock, 0, c->stream>>>((const uint8_t*)field, c->gatherScratch.as<uint8_t>(), ord, n); break;
+    case 2: permuteKernel<uint16_t><<<blocks, kBlock, 0, c->stream>>>((const uint16_t*)field, c->gatherScratch.as<uint16_t>(), ord, n); break;
+    case 4: permuteKernel<uint32_t><<<blocks, kBlock, 0, c->stream>>>((const uint32_t*)field, c->gatherScratch.as<uint32_t>(), ord, n); break;
+    default: permuteKernel<u64><<<blocks, kBlock, 0, c->stream>>>((const u64*)field, c->gatherScratch.as<u64>(), ord, n); break;
+    }
+    SPHGB_TRY(launched(c, "permuteKernel"));
+    SPHGB_CUDA(cudaMemcpyAsync(field, c->gatherScratch.p, size_t(esz) * n, cudaMemcpyDeviceToDevice, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
 
 int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
 {

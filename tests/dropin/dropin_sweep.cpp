@@ -1,0 +1,108 @@
+// A VE and a std sweep written the way the reference's propagators call them
+// (main/src/propagator/ve_hydro.hpp:130-204, std_hydro.hpp:124-168), through the drop-in adapter.
+// Reads binary particle fields (x y z h m u vx vy vz alpha as FP64) from argv[1], writes the
+// outputs in SFC order to argv[2].  Precision: "fp64" or "mixed" in argv[3], variant "ve"/"std" in argv[4].
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mock_reference.hpp"
+#include "sphgb/dropin.hpp"
+
+using namespace mockref;
+namespace dr = sphgb::dropin;
+
+template<class V, class T>
+void upload(V& dv, const std::vector<T>& host)
+{
+    dv.resize(host.size());
+    cudaMemcpy(rawPtr(dv), host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+template<class V>
+void download(V& dv, std::FILE* f)
+{
+    using T = std::remove_pointer_t<decltype(rawPtr(dv))>;
+    std::vector<T> h(dv.size());
+    cudaMemcpy(h.data(), rawPtr(dv), h.size() * sizeof(T), cudaMemcpyDeviceToHost);
+    std::vector<double> o(h.begin(), h.end());
+    std::fwrite(o.data(), sizeof(double), o.size(), f);
+}
+
+template<class Th>
+int run(const char* in, const char* out, bool ve, double lim[6], int bc[3])
+{
+    std::FILE* f = std::fopen(in, "rb");
+    if (!f) return 2;
+    long long n = 0;
+    if (std::fread(&n, sizeof(n), 1, f) != 1) return 2;
+    std::vector<double> a(10 * n);
+    if (std::fread(a.data(), sizeof(double), a.size(), f) != a.size()) return 2;
+    std::fclose(f);
+    auto col = [&](int k) { return std::vector<double>(a.begin() + k * n, a.begin() + (k + 1) * n); };
+    auto colT = [&](int k) { auto c = col(k); return std::vector<Th>(c.begin(), c.end()); };
+
+    ParticlesData<Th, Th> d;
+    auto& dv = d.devData;
+    upload(dv.x, col(0));
+    upload(dv.y, col(1));
+    upload(dv.z, col(2));
+    upload(dv.h, colT(3));
+    upload(dv.m, colT(4));
+    upload(dv.u, col(5));
+    upload(dv.vx, colT(6));
+    upload(dv.vy, colT(7));
+    upload(dv.vz, colT(8));
+    upload(dv.alpha, colT(9));
+    for (auto* v : {&dv.rho, &dv.p, &dv.c, &dv.xm, &dv.kx, &dv.gradh, &dv.prho, &dv.divv, &dv.curlv, &dv.c11, &dv.c12,
+                    &dv.c13, &dv.c22, &dv.c23, &dv.c33, &dv.ax, &dv.ay, &dv.az})
+        v->resize(n);
+    dv.du.resize(n);
+    dv.keys.resize(n);
+    dv.nc.resize(n);
+
+    auto bt = [](int b) { return b == 1 ? BoundaryType::periodic : BoundaryType::open; };
+    Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
+    dr::SingleRankDomain<uint64_t, double, Box<double>> domain(0, 1, 64, 64, 0.5f, box);
+    domain.sync(d);
+    GroupView grp{0, uint32_t(n), 1, nullptr, nullptr};
+    dr::findNeighborsSfc(0, n, d, domain.box());
+    if (ve) {
+        dr::computeXMass(grp, d, domain.box());
+        dr::computeVeDefGradh(grp, d, domain.box());
+        dr::computeEOS(0, n, d);
+        dr::computeIadDivvCurlv(grp, d, domain.box());
+        dr::computeAVswitches(grp, d, domain.box());
+        dr::computeMomentumEnergy<false>(grp, nullptr, d, domain.box());
+    } else {
+        dr::computeDensity(grp, d, domain.box());
+        dr::computeEOS_HydroStd(0, n, d);
+        dr::computeIAD(grp, d, domain.box());
+        dr::computeMomentumEnergySTD(grp, d, domain.box());
+    }
+    std::FILE* o = std::fopen(out, "wb");
+    for (auto* v : {&dv.rho, &dv.c11, &dv.c12, &dv.ax, &dv.ay, &dv.az, &dv.xm, &dv.kx, &dv.divv, &dv.alpha})
+        download(*v, o);
+    download(dv.du, o);
+    std::fwrite(&d.minDtCourant, sizeof(double), 1, o);
+    std::fclose(o);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 5) return 1;
+    double lim[6];
+    int bc[3];
+    for (int k = 0; k < 6; ++k) lim[k] = std::atof(argv[5 + k]);
+    for (int k = 0; k < 3; ++k) bc[k] = std::atoi(argv[11 + k]);
+    bool ve = std::string(argv[4]) == "ve";
+    try {
+        if (std::string(argv[3]) == "mixed") return run<float>(argv[1], argv[2], ve, lim, bc);
+        return run<double>(argv[1], argv[2], ve, lim, bc);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "%s\n", e.what());
+        return 3;
+    }
+}
