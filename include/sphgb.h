@@ -183,6 +183,21 @@ int sphgb_kernel_launches(sphgb_ctx* ctx, int64_t* launches);
  * reference counterpart: the reference records no performance figures) */
 int sphgb_measure_fma_peak(sphgb_ctx* ctx, int32_t fp64, double* flops_per_s);
 
+/* ---- allocation-free entry point ----
+ * No counterpart in the reference.  For callers that must not let a library call cudaMalloc or
+ * cudaFree (their device memory is owned by their own pool allocator, or they cannot afford the
+ * implicit device synchronisation of allocation inside a time-step loop): fits the open box
+ * dimensions to the particle extrema like sphgb_domain_sync and writes the Hilbert key of every
+ * particle, in input order, into `keys` (device, n entries).  x, y, z are device pointers;
+ * `box` is a host struct, updated in place.  Needs no context and allocates nothing: its
+ * reduction scratch is a fixed 3 MiB device array inside the library (held by every GPU that
+ * loads it until the process exits), which caps n at 268,435,456; larger n returns
+ * SPHGB_ERR_TOO_LARGE.  The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  Every call shares the array: calls that overlap on the GPU, on
+ * one device, race.  Runs on `stream` (0 = legacy default) and returns after synchronising it. */
+int sphgb_sfc_keys_noalloc(const double* x, const double* y, const double* z, int64_t n, sphgb_box* box,
+                           uint64_t* keys, void* stream);
+
 
 #ifdef __cplusplus
 }

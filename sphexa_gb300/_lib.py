@@ -94,6 +94,7 @@ SIGNATURES = {
     "sphgb_get_timings": [_P, C.POINTER(C.c_float), C.c_int32],
     "sphgb_kernel_launches": [_P, C.POINTER(C.c_int64)],
     "sphgb_measure_fma_peak": [_P, C.c_int32, C.POINTER(C.c_double)],
+    "sphgb_sfc_keys_noalloc": [_P, _P, _P, _I64, C.POINTER(SphgbBox), _P, _P],
 }
 RESTYPES = {"sphgb_status_string": C.c_char_p, "sphgb_last_cuda_error": C.c_char_p}
 
