@@ -171,6 +171,25 @@ int sphgb_sweep(sphgb_ctx* ctx, sphgb_particles* p, sphgb_box* box, int32_t vari
 int sphgb_sweep_passes(sphgb_ctx* ctx, sphgb_particles* p, int32_t variant, int32_t av_clean,
                        double* minDtCourant);
 
+/* ---- adjoint ----
+ * No reference counterpart (the reference has no gradients).  Reverse mode of the std chain
+ * density -> EOS -> IAD -> momentum-energy, for the state left by the last forward passes on the
+ * frozen neighbour lists of the last search (over all particles, first = 0, last = n), FP64 form.
+ * Seeds are dL/d(output) per particle (device, double; NULL = zero); outputs are dL/d(input)
+ * (device, double).  The Courant time step is not differentiated. */
+typedef struct {
+    const void *rho, *ax, *ay, *az;   /* dL/drho, dL/da */
+    const double* du;                 /* dL/ddu */
+} sphgb_seeds;
+
+typedef struct {
+    double *x, *y, *z;                /* dL/dx */
+    double *vx, *vy, *vz;             /* dL/dv */
+    double *h, *u;                    /* dL/dh, dL/du */
+} sphgb_grads;
+
+int sphgb_adjoint_std(sphgb_ctx* ctx, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads);
+
 /* ---- statistics and timing ---- */
 int sphgb_get_stats(sphgb_ctx* ctx, sphgb_stats* stats);
 /* milliseconds of the last call of each stage, measured with CUDA events on the context

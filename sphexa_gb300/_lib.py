@@ -55,6 +55,14 @@ class SphgbStats(C.Structure):
                 ("candidates", C.c_int64), ("fp64_rechecks", C.c_int64)]
 
 
+class SphgbSeeds(C.Structure):
+    _fields_ = [("rho", C.c_void_p), ("ax", C.c_void_p), ("ay", C.c_void_p), ("az", C.c_void_p), ("du", C.c_void_p)]
+
+
+class SphgbGrads(C.Structure):
+    _fields_ = [(f, C.c_void_p) for f in ("x", "y", "z", "vx", "vy", "vz", "h", "u")]
+
+
 # name -> (argtypes); every function returns int status unless listed in RESTYPES
 _P = C.c_void_p
 _I64 = C.c_int64
@@ -90,6 +98,7 @@ SIGNATURES = {
     "sphgb_sweep": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox), C.c_int32, C.c_int32,
                     C.POINTER(C.c_double)],
     "sphgb_sweep_passes": [_P, C.POINTER(SphgbParticles), C.c_int32, C.c_int32, C.POINTER(C.c_double)],
+    "sphgb_adjoint_std": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbSeeds), C.POINTER(SphgbGrads)],
     "sphgb_get_stats": [_P, C.POINTER(SphgbStats)],
     "sphgb_get_timings": [_P, C.POINTER(C.c_float), C.c_int32],
     "sphgb_kernel_launches": [_P, C.POINTER(C.c_int64)],

@@ -1,0 +1,586 @@
+// Adjoint (reverse mode) of the standard SPH chain  density -> EOS -> IAD -> momentum-energy
+// over the frozen neighbour lists of the last search, in FP64.
+//
+// Forward functions differentiated (reference j-loops):
+//   rho_i = K h_i^-3 (m_i + sum_j m_j w(r_ij / h_i))                 hydro_std/density.hpp:41-60
+//   p_i = (gamma-1) rho_i u_i,  c_i = sqrt(gamma (gamma-1) u_i)      hydro_std/eos.hpp:54-80
+//   C_i = tau_i^-1 h_i^3 / K,  tau_i = sum_j (m_j/rho_j) w r r^T       hydro_std/iad_kern.hpp:12-77
+//   a_i = K sum_j (alpha A_i + beta A_j),  du_i = -K/2 sum_j v_ij.(alpha' A_i + beta' A_j)
+//                                                                    hydro_std/momentum_energy_kern.hpp:12-134
+// w is the table interpolant (sph/include/sph/table_lookup.hpp:10-26) and its derivative is the
+// slope of the interval, so forward and adjoint describe the same piecewise function.  The
+// Courant time step is not differentiated.
+//
+// Scatter without atomics: every pair (i owns the list, j is the neighbour) is evaluated twice,
+// once by thread i over its list for the partials of i's quantities and once by thread j over the
+// transposed list for the partials of j's quantities.  Each thread writes only its own particle,
+// so the sums are deterministic.  No per-pair value is stored.
+#include <cub/cub.cuh>
+
+#include "pairs.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kAdjBlock = 128;
+
+// interpolant value and slope (dw/dv) of the interval holding v
+__device__ __forceinline__ double lookupSlope(const double* __restrict__ tab, double v, double& slope)
+{
+    constexpr int nInt = kTableSize - 1;
+    constexpr double dx = 2.0 / double(nInt);
+    constexpr double invDx = 1.0 / dx;
+    int idx = int(v * invDx);
+    if (idx >= nInt) {
+        slope = 0.0;
+        return 0.0;
+    }
+    double a = __ldg(tab + idx), b = __ldg(tab + idx + 1);
+    slope = (b - a) * invDx;
+    return a + slope * (v - double(idx) * dx);
+}
+
+struct AdjArgs {
+    // forward state
+    const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *rho, *p, *c;
+    const double *c11, *c12, *c13, *c22, *c23, *c33;
+    const double* wh;
+    double K, gamma;
+    DevBox box;
+    // lists: own (transposed layout) and incoming (CSR by neighbour)
+    ListView lv;
+    const uint32_t* tOff;
+    const uint32_t* tIdx;
+    int64_t n;
+    // seeds
+    const double *sRho, *sAx, *sAy, *sAz, *sDu;
+    // per-particle adjoint state
+    double *bx, *by, *bz, *bvx, *bvy, *bvz, *bh, *bu;  // outputs
+    double *bRho, *bP, *bC, *bCij;                      // bCij: 6 x n
+    double* tauBar;                                     // 6 x n
+};
+
+struct Side {
+    double x, y, z, vx, vy, vz, h, hInv, m, rho, p, c, C[6];
+};
+
+__device__ __forceinline__ Side loadSide(const AdjArgs& a, int64_t i)
+{
+    Side s;
+    s.x = a.x[i];
+    s.y = a.y[i];
+    s.z = a.z[i];
+    s.vx = a.vx[i];
+    s.vy = a.vy[i];
+    s.vz = a.vz[i];
+    s.h = a.h[i];
+    s.hInv = 1.0 / s.h;
+    s.m = a.m[i];
+    s.rho = a.rho[i];
+    s.p = a.p[i];
+    s.c = a.c[i];
+    s.C[0] = a.c11[i];
+    s.C[1] = a.c12[i];
+    s.C[2] = a.c13[i];
+    s.C[3] = a.c22[i];
+    s.C[4] = a.c23[i];
+    s.C[5] = a.c33[i];
+    return s;
+}
+
+// r = x_i - x_j with the legacy periodic fold at 2 h_i (box.hpp:216-238)
+__device__ __forceinline__ void pairR(const DevBox& b, const Side& I, const Side& J, double r[3])
+{
+    const double twoH = 2.0 * I.h;
+    const double d[3] = {I.x - J.x, I.y - J.y, I.z - J.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = d[k];
+        if (b.pbc[k] && v > twoH) v -= b.L[k];
+        else if (b.pbc[k] && v < -twoH) v += b.L[k];
+        r[k] = v;
+    }
+}
+
+__device__ __forceinline__ void symv(const double C[6], const double r[3], double out[3])
+{
+    out[0] = C[0] * r[0] + C[1] * r[1] + C[2] * r[2];
+    out[1] = C[1] * r[0] + C[3] * r[1] + C[4] * r[2];
+    out[2] = C[2] * r[0] + C[4] * r[1] + C[5] * r[2];
+}
+
+// gradient of the stored components of a symmetric C from A = C r and Abar
+__device__ __forceinline__ void symvAdj(const double Ab[3], const double r[3], double Cb[6])
+{
+    Cb[0] += Ab[0] * r[0];
+    Cb[1] += Ab[0] * r[1] + Ab[1] * r[0];
+    Cb[2] += Ab[0] * r[2] + Ab[2] * r[0];
+    Cb[3] += Ab[1] * r[1];
+    Cb[4] += Ab[1] * r[2] + Ab[2] * r[1];
+    Cb[5] += Ab[2] * r[2];
+}
+
+// partials of one momentum-energy pair term of i (list owner) with neighbour j, given the seeds
+// gA = K abar_i and gE = -K/2 dubar_i.  Output for the side selected by ForI.
+struct PairGrad {
+    double r[3], v[3], h, rho, p, c, C[6];
+};
+
+template<bool ForI>
+__device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, const Side& I, const Side& J,
+                                          const double gA[3], double gE, PairGrad& g)
+{
+    double r[3];
+    pairR(b, I, J, r);
+    const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const double rinv = rsqrt(r2), d = r2 * rinv;
+    const double v[3] = {I.vx - J.vx, I.vy - J.vy, I.vz - J.vz};
+    const double v1 = d * I.hInv, v2 = d * J.hInv;
+    double dwi, dwj;
+    const double wi = lookupSlope(tab, v1, dwi), wj = lookupSlope(tab, v2, dwj);
+    const double hi3 = I.hInv * I.hInv * I.hInv, hj3 = J.hInv * J.hInv * J.hInv;
+    const double Wi = hi3 * wi, Wj = hj3 * wj;
+    double Ai[3], Aj[3];
+    symv(I.C, r, Ai);
+    symv(J.C, r, Aj);
+    const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    const double W = rv * rinv;
+    const double cs = I.c + J.c;
+    const double visc = W < 0.0 ? 0.5 * (-(0.5 * cs - 2.0 * W) * W) : 0.0;
+    const double qi = J.m * I.p / (I.rho * I.rho), si = I.m / I.rho, tj = J.m / J.rho, uj = J.p / J.rho;
+    const double alpha = Wi * (qi + visc * si), beta = tj * Wj * (uj + visc);
+    const double alphaP = Wi * (2.0 * qi + visc * si), betaP = visc * tj * Wj;
+
+    const double vAi = v[0] * Ai[0] + v[1] * Ai[1] + v[2] * Ai[2];
+    const double vAj = v[0] * Aj[0] + v[1] * Aj[1] + v[2] * Aj[2];
+    const double bAlpha = gA[0] * Ai[0] + gA[1] * Ai[1] + gA[2] * Ai[2];
+    const double bBeta = gA[0] * Aj[0] + gA[1] * Aj[1] + gA[2] * Aj[2];
+    const double bAlphaP = gE * vAi, bBetaP = gE * vAj;
+
+    double Abi[3], Abj[3], vb[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        Abi[k] = gA[k] * alpha + gE * alphaP * v[k];
+        Abj[k] = gA[k] * beta + gE * betaP * v[k];
+        vb[k] = gE * (alphaP * Ai[k] + betaP * Aj[k]);
+    }
+    const double bWi = bAlpha * (qi + visc * si) + bAlphaP * (2.0 * qi + visc * si);
+    const double bqi = (bAlpha + 2.0 * bAlphaP) * Wi;
+    const double bsi = (bAlpha + bAlphaP) * Wi * visc;
+    const double bVisc = (bAlpha + bAlphaP) * Wi * si + (bBeta + bBetaP) * tj * Wj;
+    const double btj = bBeta * Wj * (uj + visc) + bBetaP * visc * Wj;
+    const double bWj = bBeta * tj * (uj + visc) + bBetaP * visc * tj;
+    const double buj = bBeta * tj * Wj;
+
+    double bW = 0.0, bcs = 0.0;
+    if (W < 0.0) {
+        bW = bVisc * 0.5 * (-0.5 * cs + 4.0 * W);
+        bcs = bVisc * 0.5 * (-0.5 * W);
+    }
+    double rb[3];
+    const double bd = bWi * hi3 * dwi * I.hInv + bWj * hj3 * dwj * J.hInv;
+    double CAi[3], CAj[3];
+    symv(I.C, Abi, CAi);
+    symv(J.C, Abj, CAj);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        rb[k] = bW * rinv * (v[k] - W * r[k] * rinv) + CAi[k] + CAj[k] + bd * r[k] * rinv;
+        vb[k] += bW * r[k] * rinv;
+    }
+    for (int k = 0; k < 3; ++k) {
+        g.r[k] = rb[k];
+        g.v[k] = vb[k];
+    }
+    for (int q = 0; q < 6; ++q) g.C[q] = 0.0;
+    g.c = bcs;
+    if constexpr (ForI) {
+        g.h = bWi * (-I.hInv * hi3 * (3.0 * wi + v1 * dwi));
+        g.p = bqi * J.m / (I.rho * I.rho);
+        g.rho = bqi * (-2.0 * qi / I.rho) + bsi * (-si / I.rho);
+        symvAdj(Abi, r, g.C);
+    } else {
+        g.h = bWj * (-J.hInv * hj3 * (3.0 * wj + v2 * dwj));
+        g.p = buj / J.rho;
+        g.rho = btj * (-tj / J.rho) + buj * (-uj / J.rho);
+        symvAdj(Abj, r, g.C);
+    }
+}
+
+__global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const Side S = loadSide(a, k);
+    double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
+    auto seedsOf = [&](int64_t i, double gA[3], double& gE) {
+        gA[0] = a.sAx ? a.K * a.sAx[i] : 0.0;
+        gA[1] = a.sAy ? a.K * a.sAy[i] : 0.0;
+        gA[2] = a.sAz ? a.K * a.sAz[i] : 0.0;
+        gE = a.sDu ? -0.5 * a.K * a.sDu[i] : 0.0;
+    };
+    // k as list owner
+    {
+        double gA[3], gE;
+        seedsOf(k, gA, gE);
+        if (gA[0] != 0.0 || gA[1] != 0.0 || gA[2] != 0.0 || gE != 0.0) {
+            const unsigned nc = a.lv.capped(k);
+            for (unsigned q = 0; q < nc; ++q) {
+                const Side J = loadSide(a, a.lv.at(k, q));
+                PairGrad g;
+                mePairAdj<true>(a.box, a.wh, S, J, gA, gE, g);
+                for (int t = 0; t < 3; ++t) {
+                    bx[t] += g.r[t];
+                    bv[t] += g.v[t];
+                }
+                bh += g.h;
+                brho += g.rho;
+                bp += g.p;
+                bc += g.c;
+                for (int t = 0; t < 6; ++t) bC[t] += g.C[t];
+            }
+        }
+    }
+    // k as neighbour of i
+    for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
+        const int64_t i = a.tIdx[e];
+        double gA[3], gE;
+        seedsOf(i, gA, gE);
+        if (gA[0] == 0.0 && gA[1] == 0.0 && gA[2] == 0.0 && gE == 0.0) continue;
+        const Side I = loadSide(a, i);
+        PairGrad g;
+        mePairAdj<false>(a.box, a.wh, I, S, gA, gE, g);
+        for (int t = 0; t < 3; ++t) {
+            bx[t] -= g.r[t];
+            bv[t] -= g.v[t];
+        }
+        bh += g.h;
+        brho += g.rho;
+        bp += g.p;
+        bc += g.c;
+        for (int t = 0; t < 6; ++t) bC[t] += g.C[t];
+    }
+    a.bx[k] = bx[0];
+    a.by[k] = bx[1];
+    a.bz[k] = bx[2];
+    a.bvx[k] = bv[0];
+    a.bvy[k] = bv[1];
+    a.bvz[k] = bv[2];
+    a.bh[k] = bh;
+    a.bRho[k] = brho + (a.sRho ? a.sRho[k] : 0.0);
+    a.bP[k] = bp;
+    a.bC[k] = bc;
+    for (int t = 0; t < 6; ++t) a.bCij[t * a.n + k] = bC[t];
+}
+
+// tau_bar = -s M G M with M = C / s, s = h^3 / K, G the symmetric gradient of C;
+// s_bar = G : M  -> h_bar += s_bar 3 h^2 / K
+__global__ void iadPrepKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const double h = a.h[k], s = h * h * h / a.K;
+    const double C[6] = {a.c11[k], a.c12[k], a.c13[k], a.c22[k], a.c23[k], a.c33[k]};
+    double Mf[3][3], G[3][3];
+    const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) {
+            int t = idx[r][q];
+            Mf[r][q] = C[t] / s;
+            double cb = a.bCij[t * a.n + k];
+            G[r][q] = (r == q) ? cb : 0.5 * cb;
+        }
+    double MG[3][3], T[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) {
+            MG[r][q] = Mf[r][0] * G[0][q] + Mf[r][1] * G[1][q] + Mf[r][2] * G[2][q];
+        }
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) T[r][q] = -s * (MG[r][0] * Mf[0][q] + MG[r][1] * Mf[1][q] + MG[r][2] * Mf[2][q]);
+    double sb = 0.0;
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) sb += G[r][q] * Mf[r][q];
+    a.bh[k] += sb * 3.0 * h * h / a.K;
+    a.tauBar[0 * a.n + k] = T[0][0];
+    a.tauBar[1 * a.n + k] = 0.5 * (T[0][1] + T[1][0]);
+    a.tauBar[2 * a.n + k] = 0.5 * (T[0][2] + T[2][0]);
+    a.tauBar[3 * a.n + k] = T[1][1];
+    a.tauBar[4 * a.n + k] = 0.5 * (T[1][2] + T[2][1]);
+    a.tauBar[5 * a.n + k] = T[2][2];
+}
+
+__device__ __forceinline__ double quadTau(const AdjArgs& a, int64_t i, const double r[3], double Tr[3])
+{
+    const double t11 = a.tauBar[i], t12 = a.tauBar[a.n + i], t13 = a.tauBar[2 * a.n + i];
+    const double t22 = a.tauBar[3 * a.n + i], t23 = a.tauBar[4 * a.n + i], t33 = a.tauBar[5 * a.n + i];
+    Tr[0] = t11 * r[0] + t12 * r[1] + t13 * r[2];
+    Tr[1] = t12 * r[0] + t22 * r[1] + t23 * r[2];
+    Tr[2] = t13 * r[0] + t23 * r[1] + t33 * r[2];
+    return r[0] * Tr[0] + r[1] * Tr[1] + r[2] * Tr[2];
+}
+
+// tau_i += V_j w(d/h_i) r r^T, V_j = m_j / rho_j
+__global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const Side S = loadSide(a, k);
+    double bx[3] = {0, 0, 0}, bh = 0, brho = 0;
+    {
+        const unsigned nc = a.lv.capped(k);
+        for (unsigned q = 0; q < nc; ++q) {
+            const int64_t j = a.lv.at(k, q);
+            const Side J = loadSide(a, j);
+            double r[3], Tr[3];
+            pairR(a.box, S, J, r);
+            const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            const double rinv = rsqrt(r2), d = r2 * rinv;
+            double dw;
+            const double w = lookupSlope(a.wh, d * S.hInv, dw);
+            const double Q = quadTau(a, k, r, Tr);
+            const double V = J.m / J.rho;
+            for (int t = 0; t < 3; ++t) bx[t] += V * (2.0 * w * Tr[t] + Q * dw * S.hInv * r[t] * rinv);
+            bh += -V * Q * dw * d * S.hInv * S.hInv;
+        }
+    }
+    for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
+        const int64_t i = a.tIdx[e];
+        const Side I = loadSide(a, i);
+        double r[3], Tr[3];
+        pairR(a.box, I, S, r);
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        const double rinv = rsqrt(r2), d = r2 * rinv;
+        double dw;
+        const double w = lookupSlope(a.wh, d * I.hInv, dw);
+        const double Q = quadTau(a, i, r, Tr);
+        const double V = S.m / S.rho;
+        for (int t = 0; t < 3; ++t) bx[t] -= V * (2.0 * w * Tr[t] + Q * dw * I.hInv * r[t] * rinv);
+        brho += -(V / S.rho) * w * Q;
+    }
+    a.bx[k] += bx[0];
+    a.by[k] += bx[1];
+    a.bz[k] += bx[2];
+    a.bh[k] += bh;
+    a.bRho[k] += brho;
+}
+
+// p = (gamma-1) rho u, c = sqrt(gamma (gamma-1) u)
+__global__ void eosAdjKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const double g1 = a.gamma - 1.0;
+    const double u = a.u[k], rho = a.rho[k], c = a.c[k];
+    a.bRho[k] += a.bP[k] * g1 * u;
+    a.bu[k] = a.bP[k] * g1 * rho + (c > 0.0 ? a.bC[k] * a.gamma * g1 / (2.0 * c) : 0.0);
+}
+
+// rho_i = K h_i^-3 (m_i + sum_j m_j w(d/h_i))
+__global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const Side S = loadSide(a, k);
+    double bx[3] = {0, 0, 0};
+    const double brk = a.bRho[k];
+    const double hi3 = S.hInv * S.hInv * S.hInv;
+    double bh = brk * (-3.0 * S.rho * S.hInv);
+    {
+        const unsigned nc = a.lv.capped(k);
+        double sdw = 0.0;
+        for (unsigned q = 0; q < nc; ++q) {
+            const int64_t j = a.lv.at(k, q);
+            double r[3];
+            const Side J = loadSide(a, j);
+            pairR(a.box, S, J, r);
+            const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            const double rinv = rsqrt(r2), d = r2 * rinv;
+            double dw;
+            lookupSlope(a.wh, d * S.hInv, dw);
+            const double f = brk * a.K * hi3 * J.m * dw * S.hInv * rinv;
+            for (int t = 0; t < 3; ++t) bx[t] += f * r[t];
+            sdw += J.m * dw * d;
+        }
+        bh += brk * a.K * hi3 * sdw * (-S.hInv * S.hInv);
+    }
+    for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
+        const int64_t i = a.tIdx[e];
+        const Side I = loadSide(a, i);
+        double r[3];
+        pairR(a.box, I, S, r);
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        const double rinv = rsqrt(r2), d = r2 * rinv;
+        double dw;
+        lookupSlope(a.wh, d * I.hInv, dw);
+        const double hI3 = I.hInv * I.hInv * I.hInv;
+        const double f = a.bRho[i] * a.K * hI3 * S.m * dw * I.hInv * rinv;
+        (void)d;
+        for (int t = 0; t < 3; ++t) bx[t] -= f * r[t];
+    }
+    a.bx[k] += bx[0];
+    a.by[k] += bx[1];
+    a.bz[k] += bx[2];
+    a.bh[k] += bh;
+}
+
+// ---- transposed lists: (j << 32 | i) keys sorted, CSR offsets by j ----
+__global__ void pairKeysKernel(ListView lv, const uint32_t* __restrict__ off, u64* __restrict__ keys)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last - lv.first) return;
+    unsigned nc = lv.capped(i);
+    uint64_t base = off[i];
+    for (unsigned q = 0; q < nc; ++q) keys[base + q] = (u64(lv.at(i, q)) << 32) | u64(i);
+}
+
+__global__ void cappedCountKernel(ListView lv, uint32_t* __restrict__ cnt)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < lv.last - lv.first) cnt[i] = lv.capped(i);
+    else if (i == lv.last - lv.first) cnt[i] = 0;
+}
+
+__global__ void csrFromKeysKernel(const u64* __restrict__ keys, int64_t pairs, int64_t n, uint32_t* __restrict__ tOff,
+                                  uint32_t* __restrict__ tIdx)
+{
+    int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (e < pairs) {
+        u64 kk = keys[e];
+        tIdx[e] = uint32_t(kk & 0xffffffffu);
+        uint32_t j = uint32_t(kk >> 32);
+        uint32_t jPrev = e == 0 ? 0xffffffffu : uint32_t(keys[e - 1] >> 32);
+        if (j != jPrev) {
+            // first entry of column j: also fill empty columns between jPrev and j
+            uint32_t from = (e == 0) ? 0u : jPrev + 1;
+            for (uint32_t q = from; q <= j; ++q) tOff[q] = uint32_t(e);
+        }
+        if (e == pairs - 1)
+            for (int64_t q = int64_t(j) + 1; q <= n; ++q) tOff[q] = uint32_t(pairs);
+    }
+    if (pairs == 0 && e <= n) tOff[e] = 0;
+}
+
+}  // namespace
+
+int buildTranspose(sphgb_ctx* c)
+{
+    if (c->transEpoch == c->nbrEpoch) return SPHGB_OK;
+    ListView lv = listView(c);
+    const int64_t nWork = lv.last - lv.first;
+    SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (nWork + 1)));
+    SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (nWork + 1)));
+    cappedCountKernel<<<gridFor(nWork + 1, 256), 256, 0, c->stream>>>(lv, c->splitCount.as<uint32_t>());
+    SPHGB_TRY(launched(c, "cappedCountKernel"));
+    size_t tmp = 0;
+    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(),
+                                             int(nWork + 1), c->stream));
+    SPHGB_TRY(c->sortTemp.ensure(tmp));
+    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(c->sortTemp.p, tmp, c->splitCount.as<uint32_t>(),
+                                             c->splitOffset.as<uint32_t>(), int(nWork + 1), c->stream));
+    uint32_t pairs32 = 0;
+    SPHGB_CUDA(cudaMemcpyAsync(&pairs32, c->splitOffset.as<uint32_t>() + nWork, sizeof(uint32_t),
+                               cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    const int64_t pairs = pairs32;
+    SPHGB_TRY(c->adjKeys.ensure(sizeof(u64) * (pairs + 1)));
+    SPHGB_TRY(c->adjKeysAlt.ensure(sizeof(u64) * (pairs + 1)));
+    SPHGB_TRY(c->tOff.ensure(sizeof(uint32_t) * (nWork + 1)));
+    SPHGB_TRY(c->tIdx.ensure(sizeof(uint32_t) * (pairs + 1)));
+    pairKeysKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(lv, c->splitOffset.as<uint32_t>(),
+                                                              c->adjKeysAlt.as<u64>());
+    SPHGB_TRY(launched(c, "pairKeysKernel"));
+    if (pairs > 0) {
+        tmp = 0;
+        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->adjKeysAlt.as<u64>(), c->adjKeys.as<u64>(),
+                                                  int(pairs), 0, 64, c->stream));
+        SPHGB_TRY(c->sortTemp.ensure(tmp));
+        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->adjKeysAlt.as<u64>(), c->adjKeys.as<u64>(),
+                                                  int(pairs), 0, 64, c->stream));
+    }
+    int64_t work = pairs > 0 ? pairs : nWork + 1;
+    csrFromKeysKernel<<<gridFor(work, 256), 256, 0, c->stream>>>(c->adjKeys.as<u64>(), pairs, nWork,
+                                                                c->tOff.as<uint32_t>(), c->tIdx.as<uint32_t>());
+    SPHGB_TRY(launched(c, "csrFromKeysKernel"));
+    c->transEpoch = c->nbrEpoch;
+    c->transPairs = pairs;
+    return SPHGB_OK;
+}
+
+int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g)
+{
+    if (!c->haveNbr) return SPHGB_ERR_STATE;
+    if (p->precision != SPHGB_FP64) return SPHGB_ERR_ARG;
+    if (c->nbrFirst != 0 || c->nbrLast != p->n) return SPHGB_ERR_ARG;
+    if (!p->x || !p->y || !p->z || !p->vx || !p->vy || !p->vz || !p->h || !p->m || !p->u || !p->rho || !p->p ||
+        !p->c || !p->c11 || !p->c12 || !p->c13 || !p->c22 || !p->c23 || !p->c33)
+        return SPHGB_ERR_ARG;
+    if (!g || !g->x || !g->y || !g->z || !g->vx || !g->vy || !g->vz || !g->h || !g->u) return SPHGB_ERR_ARG;
+    const int64_t n = p->n;
+    SPHGB_TRY(buildTranspose(c));
+    SPHGB_TRY(c->adjState.ensure(sizeof(double) * 15 * n));
+    double* st = c->adjState.as<double>();
+
+    AdjArgs a{};
+    a.x = p->x;
+    a.y = p->y;
+    a.z = p->z;
+    a.vx = static_cast<const double*>(p->vx);
+    a.vy = static_cast<const double*>(p->vy);
+    a.vz = static_cast<const double*>(p->vz);
+    a.h = static_cast<const double*>(p->h);
+    a.m = static_cast<const double*>(p->m);
+    a.u = p->u;
+    a.rho = static_cast<const double*>(p->rho);
+    a.p = static_cast<const double*>(p->p);
+    a.c = static_cast<const double*>(p->c);
+    a.c11 = static_cast<const double*>(p->c11);
+    a.c12 = static_cast<const double*>(p->c12);
+    a.c13 = static_cast<const double*>(p->c13);
+    a.c22 = static_cast<const double*>(p->c22);
+    a.c23 = static_cast<const double*>(p->c23);
+    a.c33 = static_cast<const double*>(p->c33);
+    a.wh = c->wh64.as<double>();
+    a.K = c->K;
+    a.gamma = c->prm.gamma;
+    a.box = c->box;
+    a.lv = listView(c);
+    a.tOff = c->tOff.as<uint32_t>();
+    a.tIdx = c->tIdx.as<uint32_t>();
+    a.n = n;
+    if (s) {
+        a.sRho = static_cast<const double*>(s->rho);
+        a.sAx = static_cast<const double*>(s->ax);
+        a.sAy = static_cast<const double*>(s->ay);
+        a.sAz = static_cast<const double*>(s->az);
+        a.sDu = s->du;
+    }
+    a.bx = g->x;
+    a.by = g->y;
+    a.bz = g->z;
+    a.bvx = g->vx;
+    a.bvy = g->vy;
+    a.bvz = g->vz;
+    a.bh = g->h;
+    a.bu = g->u;
+    a.bRho = st;
+    a.bP = st + n;
+    a.bC = st + 2 * n;
+    a.bCij = st + 3 * n;
+    a.tauBar = st + 9 * n;
+
+    const unsigned blocks = gridFor(n, kAdjBlock);
+    meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "meAdjKernel"));
+    iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "iadPrepKernel"));
+    iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "iadAdjKernel"));
+    eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "eosAdjKernel"));
+    densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "densityAdjKernel"));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
+
+}  // namespace sphgb

@@ -135,7 +135,8 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->childOffsets,  &c->internalToLeaf, &c->nodeCenter, &c->nodeSize,  &c->nodeBoxF,
                     &c->levelRangeDev, &c->nbr,     &c->ncount,        &c->active,        &c->counters,
                     &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
-                    &c->gridLoc,  &c->hInv64,       &c->reduceScratch};
+                    &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
+                    &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -330,6 +331,13 @@ int sphgb_sweep(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box, int32_t varian
         if (s != SPHGB_OK) return s;
     }
     return sphgb_sweep_passes(c, p, variant, avClean, minDtCourant);
+}
+
+int sphgb_adjoint_std(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || !grads) return SPHGB_ERR_ARG;
+    return adjointStd(c, p, seeds, grads);
 }
 
 int sphgb_get_stats(sphgb_ctx* c, sphgb_stats* s)

@@ -112,6 +112,10 @@ struct sphgb_ctx {
     // per-particle quotients of pass inputs, rebuilt at the start of every pass that reads them
     // (VE: rho, m/rho, xm/kx, m*prho, ln xm; std: m/rho, p/rho, p/rho^2)
     sphgb::DBuf aux;
+    // adjoint: incoming lists as CSR (tOff, tIdx) built from sorted (j<<32|i) keys, and the
+    // per-particle adjoint state of the intermediate fields
+    sphgb::DBuf adjKeys, adjKeysAlt, tOff, tIdx, adjState;
+    int64_t transEpoch = -1, transPairs = 0;
     // validity of the precomputes: the lists' epoch and the field pointers they were made from
     int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;
     const void* prepMixedFor = nullptr;
@@ -154,6 +158,9 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
 int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
 int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, int avClean, float* groupDt,
                          double* minDt);
+
+int buildTranspose(sphgb_ctx* c);
+int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g);
 
 // min-reduction of per-block Courant dt partials into one double on the host
 int reduceMinDt(sphgb_ctx* c, const double* partials, int count, double* out);

@@ -124,8 +124,9 @@ int prepareFp64(sphgb_ctx* c, sphgb_particles* p)
     return launched(c, "recipKernel");
 }
 
-// preconditions of every pair pass; refreshes the per-particle precomputes when h or the lists
-// changed since they were made
+// preconditions of every pair pass; rebuilds the per-particle precomputes from the current x y z
+// h on every call (one elementwise kernel): a caller may change positions or smoothing lengths
+// between passes while the neighbour lists stay frozen, as gradient checks do
 int checkPass(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last)
 {
     if (!c->haveNbr || !c->tablesReady) return SPHGB_ERR_STATE;
@@ -133,21 +134,8 @@ int checkPass(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t las
     if (first < c->nbrFirst || last > c->nbrLast || first >= last || p->n < last) return SPHGB_ERR_ARG;
     if (p->precision != SPHGB_FP64 && p->precision != SPHGB_MIXED) return SPHGB_ERR_ARG;
     sphgb_particles* q = const_cast<sphgb_particles*>(p);
-    if (p->precision == SPHGB_MIXED) {
-        if (c->prepMixedFor != p->x || c->prepMixedH != p->h || c->prepEpoch != c->nbrEpoch) {
-            SPHGB_TRY(prepareMixed(c, q, first, last));
-            c->prepMixedFor = p->x;
-            c->prepMixedH = p->h;
-            c->prepEpoch = c->nbrEpoch;
-        }
-    } else {
-        if (c->prepFp64H != p->h || c->prepEpoch64 != c->nbrEpoch) {
-            SPHGB_TRY(prepareFp64(c, q));
-            c->prepFp64H = p->h;
-            c->prepEpoch64 = c->nbrEpoch;
-        }
-    }
-    return SPHGB_OK;
+    if (p->precision == SPHGB_MIXED) return prepareMixed(c, q, first, last);
+    return prepareFp64(c, q);
 }
 
 int beginDtReduction(sphgb_ctx* c, unsigned long long** dst)
