@@ -37,6 +37,46 @@ def loss_of(sw, rho_t, vals):
     return float(AG.loss_rho_a(rho, ax, ay, az, rho_t).item())
 
 
+def test_adjoint_matches_fp64_reference_gradient(port):
+    """Every gradient component of every particle against torch autograd through the FP64 torch
+    restatement of the same chain on the same frozen edges (tests/torch_reference.py)."""
+    import torch
+    from sphexa_gb300 import autograd as AG, sph
+    from torch_reference import std_chain
+    wl, ctx, sw, rho_t = setup(side=10, seed=7)
+    n = wl.n
+    ng = int(ctx.params.ngmax)
+    nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
+    cnt = np.minimum(sw.d.nc.cpu().numpy().astype(np.int64) - 1, ng)
+    ei = np.repeat(np.arange(n), cnt)
+    ej = np.concatenate([nb[k, :cnt[k]] for k in range(n)])
+    dev = "cuda:0"
+    ei_t, ej_t = torch.tensor(ei, device=dev), torch.tensor(ej, device=dev)
+    wh, _ = port.tables(6.0)
+    tab = torch.tensor(wh, dtype=torch.float64, device=dev)
+    inp = [t.clone().requires_grad_(True) for t in sw.inputs()]
+    m = sw.d.m.clone()
+    out_ref = std_chain(*inp, m, ei_t, ej_t, tab, ctx.K, float(ctx.params.gamma),
+                        torch.tensor(wl.box[1::2] - wl.box[0::2], dtype=torch.float64), [True, True, True])
+    L_ref = AG.loss_rho_a(*out_ref[:4], rho_t)
+    L_ref.backward()
+    g_ref = {f: inp[k].grad.detach().cpu().numpy() for k, f in enumerate(FIELDS)}
+
+    base = [t.detach().clone().requires_grad_(True) for t in sw.inputs()]
+    out = AG.StdSweepFunction.apply(sw, *base)
+    for a, b in zip(out, out_ref):
+        ref = b.detach().cpu().numpy()
+        assert np.max(np.abs(a.detach().cpu().numpy() - ref)) <= 1e-10 * (np.max(np.abs(ref)) + 1e-300)
+    L = AG.loss_rho_a(*out[:4], rho_t)
+    L.backward()
+    for k, f in enumerate(FIELDS):
+        g = base[k].grad.detach().cpu().numpy()
+        err = np.linalg.norm(g - g_ref[f]) / (np.linalg.norm(g_ref[f]) + 1e-300)
+        print(f"reference gradient {f:3s}: normwise rel {err:.3e}")
+        assert err <= 1e-9, f
+    ctx.close()
+
+
 def test_adjoint_matches_central_differences():
     import torch
     from sphexa_gb300 import autograd as AG
