@@ -139,6 +139,48 @@ def cpu_baseline(side: int, threads: int = 0) -> dict:
                       f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
 
 
+def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int) -> dict:
+    """Forward std chain (density, EOS, IAD, momentum-energy on frozen lists) against its adjoint
+    for the loss sum (rho - rho_target)^2 + sum |a|^2, FP64, CUDA events on the default stream."""
+    import torch
+    from sphexa_gb300 import autograd as AG, sph, workloads as W
+    wl = W.fourier(side, seed=5, rho_seed=55, v_seed=555, target_seed=5555)
+    d = sph.ParticlesData.from_workload(wl, "fp64", dev)
+    box = sph.Box(wl.box.copy(), wl.bc.copy())
+    sw = AG.FrozenStdSweep(ctx, d, box)
+    sw.freeze()
+    order = sph.Domain(ctx, box).order(wl.n)
+    rho_t = torch.tensor(wl.fields["rho_target"][order], dtype=torch.float64, device=dev)
+    vals = sw.inputs()
+
+    def timed(fn, k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    outs = sw.forward(*vals)
+    rho, ax, ay, az, du = outs
+    seeds = (2.0 * (rho - rho_t), 2.0 * ax, 2.0 * ay, 2.0 * az, None)
+    t0 = time.perf_counter()
+    sw.backward(*seeds)  # first call also builds the incoming (transposed) lists
+    torch.cuda.synchronize()
+    first_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(max(1, warmup)):
+        sw.forward(*vals)
+        sw.backward(*seeds)
+    k = max(3, steps // 2)
+    fwd = timed(lambda: sw.forward(*vals), k)
+    adj = timed(lambda: sw.backward(*seeds), k)
+    return {"workload": f"adjoint config: jittered Fourier lattice {side}^3 = {wl.n} particles, frozen lists",
+            "form": "fp64 std chain", "forward_ms": fwd, "adjoint_ms": adj, "ratio": adj / fwd,
+            "first_adjoint_ms_incl_transpose": first_ms, "steps": k}
+
+
 def run_reference(args) -> None:
     rank, world, _ = env_rank()
     if rank != 0:
@@ -177,6 +219,8 @@ def main() -> None:
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-side", type=int, default=100)
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -334,6 +378,10 @@ def main() -> None:
                       "d2h_bytes_per_step": d2h, "steps": k_e2e,
                       "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
         del d
+
+    # ---------------- adjoint / forward on the adjoint configuration (1M particles, FP64 std chain)
+    if not args.no_adjoint:
+        out["adjoint"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup)
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.cpu_side)
