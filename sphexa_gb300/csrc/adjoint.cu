@@ -59,10 +59,12 @@ struct AdjArgs {
     double *bx, *by, *bz, *bvx, *bvy, *bvz, *bh, *bu;  // outputs
     double *bRho, *bP, *bC, *bCij;                      // bCij: 6 x n
     double* tauBar;                                     // 6 x n
+    // per-particle quotients formed once: 1/h, m/rho, p/rho, 1/rho, p/rho^2
+    const double *hInv, *mOverRho, *pOverRho, *rhoInv, *pOverRho2;
 };
 
 struct Side {
-    double x, y, z, vx, vy, vz, h, hInv, m, rho, p, c, C[6];
+    double x, y, z, vx, vy, vz, h, hInv, m, moR, poR, rInv, poR2, c, C[6];
 };
 
 __device__ __forceinline__ Side loadSide(const AdjArgs& a, int64_t i)
@@ -75,10 +77,12 @@ __device__ __forceinline__ Side loadSide(const AdjArgs& a, int64_t i)
     s.vy = a.vy[i];
     s.vz = a.vz[i];
     s.h = a.h[i];
-    s.hInv = 1.0 / s.h;
+    s.hInv = a.hInv[i];
     s.m = a.m[i];
-    s.rho = a.rho[i];
-    s.p = a.p[i];
+    s.moR = a.mOverRho[i];
+    s.poR = a.pOverRho[i];
+    s.rInv = a.rhoInv[i];
+    s.poR2 = a.pOverRho2[i];
     s.c = a.c[i];
     s.C[0] = a.c11[i];
     s.C[1] = a.c12[i];
@@ -86,6 +90,21 @@ __device__ __forceinline__ Side loadSide(const AdjArgs& a, int64_t i)
     s.C[3] = a.c22[i];
     s.C[4] = a.c23[i];
     s.C[5] = a.c33[i];
+    return s;
+}
+
+// the fields the IAD and density reverse passes read of a particle
+__device__ __forceinline__ Side loadPos(const AdjArgs& a, int64_t i)
+{
+    Side s;
+    s.x = a.x[i];
+    s.y = a.y[i];
+    s.z = a.z[i];
+    s.h = a.h[i];
+    s.hInv = a.hInv[i];
+    s.m = a.m[i];
+    s.moR = a.mOverRho[i];
+    s.rInv = a.rhoInv[i];
     return s;
 }
 
@@ -148,7 +167,7 @@ __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, co
     const double W = rv * rinv;
     const double cs = I.c + J.c;
     const double visc = W < 0.0 ? 0.5 * (-(0.5 * cs - 2.0 * W) * W) : 0.0;
-    const double qi = J.m * I.p / (I.rho * I.rho), si = I.m / I.rho, tj = J.m / J.rho, uj = J.p / J.rho;
+    const double qi = J.m * I.poR2, si = I.moR, tj = J.moR, uj = J.poR;
     const double alpha = Wi * (qi + visc * si), beta = tj * Wj * (uj + visc);
     const double alphaP = Wi * (2.0 * qi + visc * si), betaP = visc * tj * Wj;
 
@@ -196,13 +215,13 @@ __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, co
     g.c = bcs;
     if constexpr (ForI) {
         g.h = bWi * (-I.hInv * hi3 * (3.0 * wi + v1 * dwi));
-        g.p = bqi * J.m / (I.rho * I.rho);
-        g.rho = bqi * (-2.0 * qi / I.rho) + bsi * (-si / I.rho);
+        g.p = bqi * J.m * I.rInv * I.rInv;
+        g.rho = (bqi * (-2.0 * qi) + bsi * (-si)) * I.rInv;
         symvAdj(Abi, r, g.C);
     } else {
         g.h = bWj * (-J.hInv * hj3 * (3.0 * wj + v2 * dwj));
-        g.p = buj / J.rho;
-        g.rho = btj * (-tj / J.rho) + buj * (-uj / J.rho);
+        g.p = buj * J.rInv;
+        g.rho = (btj * (-tj) + buj * (-uj)) * J.rInv;
         symvAdj(Abj, r, g.C);
     }
 }
@@ -324,13 +343,13 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
-    const Side S = loadSide(a, k);
+    const Side S = loadPos(a, k);
     double bx[3] = {0, 0, 0}, bh = 0, brho = 0;
     {
         const unsigned nc = a.lv.capped(k);
         for (unsigned q = 0; q < nc; ++q) {
             const int64_t j = a.lv.at(k, q);
-            const Side J = loadSide(a, j);
+            const Side J = loadPos(a, j);
             double r[3], Tr[3];
             pairR(a.box, S, J, r);
             const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
@@ -338,14 +357,14 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
             double dw;
             const double w = lookupSlope(a.wh, d * S.hInv, dw);
             const double Q = quadTau(a, k, r, Tr);
-            const double V = J.m / J.rho;
+            const double V = J.moR;
             for (int t = 0; t < 3; ++t) bx[t] += V * (2.0 * w * Tr[t] + Q * dw * S.hInv * r[t] * rinv);
             bh += -V * Q * dw * d * S.hInv * S.hInv;
         }
     }
     for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
         const int64_t i = a.tIdx[e];
-        const Side I = loadSide(a, i);
+        const Side I = loadPos(a, i);
         double r[3], Tr[3];
         pairR(a.box, I, S, r);
         const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
@@ -353,9 +372,9 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
         double dw;
         const double w = lookupSlope(a.wh, d * I.hInv, dw);
         const double Q = quadTau(a, i, r, Tr);
-        const double V = S.m / S.rho;
+        const double V = S.moR;
         for (int t = 0; t < 3; ++t) bx[t] -= V * (2.0 * w * Tr[t] + Q * dw * I.hInv * r[t] * rinv);
-        brho += -(V / S.rho) * w * Q;
+        brho += -(V * S.rInv) * w * Q;
     }
     a.bx[k] += bx[0];
     a.by[k] += bx[1];
@@ -380,18 +399,18 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
-    const Side S = loadSide(a, k);
+    const Side S = loadPos(a, k);
     double bx[3] = {0, 0, 0};
     const double brk = a.bRho[k];
     const double hi3 = S.hInv * S.hInv * S.hInv;
-    double bh = brk * (-3.0 * S.rho * S.hInv);
+    double bh = brk * (-3.0 * a.rho[k] * S.hInv);
     {
         const unsigned nc = a.lv.capped(k);
         double sdw = 0.0;
         for (unsigned q = 0; q < nc; ++q) {
             const int64_t j = a.lv.at(k, q);
             double r[3];
-            const Side J = loadSide(a, j);
+            const Side J = loadPos(a, j);
             pairR(a.box, S, J, r);
             const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
             const double rinv = rsqrt(r2), d = r2 * rinv;
@@ -405,7 +424,7 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
     }
     for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
         const int64_t i = a.tIdx[e];
-        const Side I = loadSide(a, i);
+        const Side I = loadPos(a, i);
         double r[3];
         pairR(a.box, I, S, r);
         const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
@@ -421,6 +440,18 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
     a.by[k] += bx[1];
     a.bz[k] += bx[2];
     a.bh[k] += bh;
+}
+
+__global__ void adjQuotientsKernel(AdjArgs a, double* q)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const double rho = a.rho[k], rInv = 1.0 / rho;
+    q[k] = 1.0 / a.h[k];
+    q[a.n + k] = a.m[k] / rho;
+    q[2 * a.n + k] = a.p[k] / rho;
+    q[3 * a.n + k] = rInv;
+    q[4 * a.n + k] = a.p[k] / (rho * rho);
 }
 
 // ---- transposed lists: (j << 32 | i) keys sorted, CSR offsets by j ----
@@ -517,7 +548,7 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     if (!g || !g->x || !g->y || !g->z || !g->vx || !g->vy || !g->vz || !g->h || !g->u) return SPHGB_ERR_ARG;
     const int64_t n = p->n;
     SPHGB_TRY(buildTranspose(c));
-    SPHGB_TRY(c->adjState.ensure(sizeof(double) * 15 * n));
+    SPHGB_TRY(c->adjState.ensure(sizeof(double) * 20 * n));
     double* st = c->adjState.as<double>();
 
     AdjArgs a{};
@@ -567,8 +598,16 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     a.bC = st + 2 * n;
     a.bCij = st + 3 * n;
     a.tauBar = st + 9 * n;
+    double* quot = st + 15 * n;
+    a.hInv = quot;
+    a.mOverRho = quot + n;
+    a.pOverRho = quot + 2 * n;
+    a.rhoInv = quot + 3 * n;
+    a.pOverRho2 = quot + 4 * n;
 
     const unsigned blocks = gridFor(n, kAdjBlock);
+    adjQuotientsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a, quot);
+    SPHGB_TRY(launched(c, "adjQuotientsKernel"));
     meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "meAdjKernel"));
     iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
