@@ -98,7 +98,8 @@ SIGNATURES = {
     "sphgb_sweep": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox), C.c_int32, C.c_int32,
                     C.POINTER(C.c_double)],
     "sphgb_sweep_passes": [_P, C.POINTER(SphgbParticles), C.c_int32, C.c_int32, C.POINTER(C.c_double)],
-    "sphgb_adjoint_std": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbSeeds), C.POINTER(SphgbGrads)],
+    "sphgb_adjoint_std": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbSeeds), C.POINTER(SphgbGrads),
+                          C.c_int32],
     "sphgb_get_stats": [_P, C.POINTER(SphgbStats)],
     "sphgb_get_timings": [_P, C.POINTER(C.c_float), C.c_int32],
     "sphgb_kernel_launches": [_P, C.POINTER(C.c_int64)],

@@ -19,10 +19,11 @@ from ._lib import check
 class FrozenStdSweep:
     """Context + particle set whose SFC order, tree and neighbour lists are fixed at freeze()."""
 
-    def __init__(self, ctx: sph.Context, d: sph.ParticlesData, box: sph.Box):
+    def __init__(self, ctx: sph.Context, d: sph.ParticlesData, box: sph.Box, deterministic: bool = False):
         if d.precision != "fp64":
             raise ValueError("the adjoint runs in the FP64 form")
         self.ctx, self.d, self.box = ctx, d, box
+        self.deterministic = deterministic
 
     def freeze(self) -> None:
         """domain sync + neighbour search; afterwards the order and the lists stay as they are."""
@@ -58,7 +59,8 @@ class FrozenStdSweep:
         for k, t in out.items():
             setattr(grads, k, t.data_ptr())
         s = self.d.c_struct()
-        check(self.ctx.lib.sphgb_adjoint_std(self.ctx.h, C.byref(s), C.byref(seeds), C.byref(grads)),
+        check(self.ctx.lib.sphgb_adjoint_std(self.ctx.h, C.byref(s), C.byref(seeds), C.byref(grads),
+                                            int(self.deterministic)),
               "sphgb_adjoint_std")
         return tuple(out[k] for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u"))
 

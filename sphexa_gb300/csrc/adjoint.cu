@@ -143,10 +143,12 @@ __device__ __forceinline__ void symvAdj(const double Ab[3], const double r[3], d
 // partials of one momentum-energy pair term of i (list owner) with neighbour j, given the seeds
 // gA = K abar_i and gE = -K/2 dubar_i.  Output for the side selected by ForI.
 struct PairGrad {
-    double r[3], v[3], h, rho, p, c, C[6];
+    double r[3], v[3], c;                 // dS/dr (r = x_i - x_j), dS/dv_ij, dS/dc_i = dS/dc_j
+    double hI, rhoI, pI, CI[6];           // partials of i's fields (WantI)
+    double hJ, rhoJ, pJ, CJ[6];           // partials of j's fields (WantJ)
 };
 
-template<bool ForI>
+template<bool WantI, bool WantJ>
 __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, const Side& I, const Side& J,
                                           const double gA[3], double gE, PairGrad& g)
 {
@@ -211,19 +213,81 @@ __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, co
         g.r[k] = rb[k];
         g.v[k] = vb[k];
     }
-    for (int q = 0; q < 6; ++q) g.C[q] = 0.0;
     g.c = bcs;
-    if constexpr (ForI) {
-        g.h = bWi * (-I.hInv * hi3 * (3.0 * wi + v1 * dwi));
-        g.p = bqi * J.m * I.rInv * I.rInv;
-        g.rho = (bqi * (-2.0 * qi) + bsi * (-si)) * I.rInv;
-        symvAdj(Abi, r, g.C);
-    } else {
-        g.h = bWj * (-J.hInv * hj3 * (3.0 * wj + v2 * dwj));
-        g.p = buj * J.rInv;
-        g.rho = (btj * (-tj) + buj * (-uj)) * J.rInv;
-        symvAdj(Abj, r, g.C);
+    if constexpr (WantI) {
+        for (int q = 0; q < 6; ++q) g.CI[q] = 0.0;
+        g.hI = bWi * (-I.hInv * hi3 * (3.0 * wi + v1 * dwi));
+        g.pI = bqi * J.m * I.rInv * I.rInv;
+        g.rhoI = (bqi * (-2.0 * qi) + bsi * (-si)) * I.rInv;
+        symvAdj(Abi, r, g.CI);
     }
+    if constexpr (WantJ) {
+        for (int q = 0; q < 6; ++q) g.CJ[q] = 0.0;
+        g.hJ = bWj * (-J.hInv * hj3 * (3.0 * wj + v2 * dwj));
+        g.pJ = buj * J.rInv;
+        g.rhoJ = (btj * (-tj) + buj * (-uj)) * J.rInv;
+        symvAdj(Abj, r, g.CJ);
+    }
+}
+
+// seeds of the pair terms of list owner i: gA = K abar_i, gE = -K/2 dubar_i
+__device__ __forceinline__ bool seedsOf(const AdjArgs& a, int64_t i, double gA[3], double& gE)
+{
+    gA[0] = a.sAx ? a.K * a.sAx[i] : 0.0;
+    gA[1] = a.sAy ? a.K * a.sAy[i] : 0.0;
+    gA[2] = a.sAz ? a.K * a.sAz[i] : 0.0;
+    gE = a.sDu ? -0.5 * a.K * a.sDu[i] : 0.0;
+    return gA[0] != 0.0 || gA[1] != 0.0 || gA[2] != 0.0 || gE != 0.0;
+}
+
+// one evaluation per pair: i's partials summed in registers, j's scattered with atomics
+__global__ void __launch_bounds__(kAdjBlock) meAdjScatterKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double gA[3], gE;
+    double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
+    if (seedsOf(a, k, gA, gE)) {
+        const Side S = loadSide(a, k);
+        const unsigned nc = a.lv.capped(k);
+        for (unsigned q = 0; q < nc; ++q) {
+            const int64_t j = a.lv.at(k, q);
+            const Side J = loadSide(a, j);
+            PairGrad g;
+            mePairAdj<true, true>(a.box, a.wh, S, J, gA, gE, g);
+            for (int t = 0; t < 3; ++t) {
+                bx[t] += g.r[t];
+                bv[t] += g.v[t];
+            }
+            bh += g.hI;
+            brho += g.rhoI;
+            bp += g.pI;
+            bc += g.c;
+            for (int t = 0; t < 6; ++t) bC[t] += g.CI[t];
+            atomicAdd(a.bx + j, -g.r[0]);
+            atomicAdd(a.by + j, -g.r[1]);
+            atomicAdd(a.bz + j, -g.r[2]);
+            atomicAdd(a.bvx + j, -g.v[0]);
+            atomicAdd(a.bvy + j, -g.v[1]);
+            atomicAdd(a.bvz + j, -g.v[2]);
+            atomicAdd(a.bh + j, g.hJ);
+            atomicAdd(a.bRho + j, g.rhoJ);
+            atomicAdd(a.bP + j, g.pJ);
+            atomicAdd(a.bC + j, g.c);
+            for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + j, g.CJ[t]);
+        }
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bvx + k, bv[0]);
+    atomicAdd(a.bvy + k, bv[1]);
+    atomicAdd(a.bvz + k, bv[2]);
+    atomicAdd(a.bh + k, bh);
+    atomicAdd(a.bRho + k, brho + (a.sRho ? a.sRho[k] : 0.0));
+    atomicAdd(a.bP + k, bp);
+    atomicAdd(a.bC + k, bc);
+    for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + k, bC[t]);
 }
 
 __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
@@ -232,31 +296,24 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
     if (k >= a.n) return;
     const Side S = loadSide(a, k);
     double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
-    auto seedsOf = [&](int64_t i, double gA[3], double& gE) {
-        gA[0] = a.sAx ? a.K * a.sAx[i] : 0.0;
-        gA[1] = a.sAy ? a.K * a.sAy[i] : 0.0;
-        gA[2] = a.sAz ? a.K * a.sAz[i] : 0.0;
-        gE = a.sDu ? -0.5 * a.K * a.sDu[i] : 0.0;
-    };
     // k as list owner
     {
         double gA[3], gE;
-        seedsOf(k, gA, gE);
-        if (gA[0] != 0.0 || gA[1] != 0.0 || gA[2] != 0.0 || gE != 0.0) {
+        if (seedsOf(a, k, gA, gE)) {
             const unsigned nc = a.lv.capped(k);
             for (unsigned q = 0; q < nc; ++q) {
                 const Side J = loadSide(a, a.lv.at(k, q));
                 PairGrad g;
-                mePairAdj<true>(a.box, a.wh, S, J, gA, gE, g);
+                mePairAdj<true, false>(a.box, a.wh, S, J, gA, gE, g);
                 for (int t = 0; t < 3; ++t) {
                     bx[t] += g.r[t];
                     bv[t] += g.v[t];
                 }
-                bh += g.h;
-                brho += g.rho;
-                bp += g.p;
+                bh += g.hI;
+                brho += g.rhoI;
+                bp += g.pI;
                 bc += g.c;
-                for (int t = 0; t < 6; ++t) bC[t] += g.C[t];
+                for (int t = 0; t < 6; ++t) bC[t] += g.CI[t];
             }
         }
     }
@@ -264,20 +321,19 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
     for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
         const int64_t i = a.tIdx[e];
         double gA[3], gE;
-        seedsOf(i, gA, gE);
-        if (gA[0] == 0.0 && gA[1] == 0.0 && gA[2] == 0.0 && gE == 0.0) continue;
+        if (!seedsOf(a, i, gA, gE)) continue;
         const Side I = loadSide(a, i);
         PairGrad g;
-        mePairAdj<false>(a.box, a.wh, I, S, gA, gE, g);
+        mePairAdj<false, true>(a.box, a.wh, I, S, gA, gE, g);
         for (int t = 0; t < 3; ++t) {
             bx[t] -= g.r[t];
             bv[t] -= g.v[t];
         }
-        bh += g.h;
-        brho += g.rho;
-        bp += g.p;
+        bh += g.hJ;
+        brho += g.rhoJ;
+        bp += g.pJ;
         bc += g.c;
-        for (int t = 0; t < 6; ++t) bC[t] += g.C[t];
+        for (int t = 0; t < 6; ++t) bC[t] += g.CJ[t];
     }
     a.bx[k] = bx[0];
     a.by[k] = bx[1];
@@ -442,6 +498,77 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
     a.bh[k] += bh;
 }
 
+// one evaluation per pair with atomic scatter to the neighbour (IAD)
+__global__ void __launch_bounds__(kAdjBlock) iadAdjScatterKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const Side S = loadPos(a, k);
+    double bx[3] = {0, 0, 0}, bh = 0;
+    const unsigned nc = a.lv.capped(k);
+    for (unsigned q = 0; q < nc; ++q) {
+        const int64_t j = a.lv.at(k, q);
+        const Side J = loadPos(a, j);
+        double r[3], Tr[3];
+        pairR(a.box, S, J, r);
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        const double rinv = rsqrt(r2), d = r2 * rinv;
+        double dw;
+        const double w = lookupSlope(a.wh, d * S.hInv, dw);
+        const double Q = quadTau(a, k, r, Tr);
+        const double V = J.moR;
+        double rb[3];
+        for (int t = 0; t < 3; ++t) {
+            rb[t] = V * (2.0 * w * Tr[t] + Q * dw * S.hInv * r[t] * rinv);
+            bx[t] += rb[t];
+        }
+        bh += -V * Q * dw * d * S.hInv * S.hInv;
+        atomicAdd(a.bx + j, -rb[0]);
+        atomicAdd(a.by + j, -rb[1]);
+        atomicAdd(a.bz + j, -rb[2]);
+        atomicAdd(a.bRho + j, -(V * J.rInv) * w * Q);
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bh + k, bh);
+}
+
+// one evaluation per pair with atomic scatter to the neighbour (density)
+__global__ void __launch_bounds__(kAdjBlock) densityAdjScatterKernel(AdjArgs a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const Side S = loadPos(a, k);
+    double bx[3] = {0, 0, 0};
+    const double brk = a.bRho[k];
+    const double hi3 = S.hInv * S.hInv * S.hInv;
+    double bh = brk * (-3.0 * a.rho[k] * S.hInv);
+    const unsigned nc = a.lv.capped(k);
+    double sdw = 0.0;
+    for (unsigned q = 0; q < nc; ++q) {
+        const int64_t j = a.lv.at(k, q);
+        double r[3];
+        const Side J = loadPos(a, j);
+        pairR(a.box, S, J, r);
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        const double rinv = rsqrt(r2), d = r2 * rinv;
+        double dw;
+        lookupSlope(a.wh, d * S.hInv, dw);
+        const double f = brk * a.K * hi3 * J.m * dw * S.hInv * rinv;
+        for (int t = 0; t < 3; ++t) bx[t] += f * r[t];
+        sdw += J.m * dw * d;
+        atomicAdd(a.bx + j, -f * r[0]);
+        atomicAdd(a.by + j, -f * r[1]);
+        atomicAdd(a.bz + j, -f * r[2]);
+    }
+    bh += brk * a.K * hi3 * sdw * (-S.hInv * S.hInv);
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bh + k, bh);
+}
+
 __global__ void adjQuotientsKernel(AdjArgs a, double* q)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -537,7 +664,7 @@ int buildTranspose(sphgb_ctx* c)
     return SPHGB_OK;
 }
 
-int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g)
+int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic)
 {
     if (!c->haveNbr) return SPHGB_ERR_STATE;
     if (p->precision != SPHGB_FP64) return SPHGB_ERR_ARG;
@@ -547,7 +674,7 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
         return SPHGB_ERR_ARG;
     if (!g || !g->x || !g->y || !g->z || !g->vx || !g->vy || !g->vz || !g->h || !g->u) return SPHGB_ERR_ARG;
     const int64_t n = p->n;
-    SPHGB_TRY(buildTranspose(c));
+    if (deterministic) SPHGB_TRY(buildTranspose(c));
     SPHGB_TRY(c->adjState.ensure(sizeof(double) * 20 * n));
     double* st = c->adjState.as<double>();
 
@@ -608,15 +735,26 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     const unsigned blocks = gridFor(n, kAdjBlock);
     adjQuotientsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a, quot);
     SPHGB_TRY(launched(c, "adjQuotientsKernel"));
-    meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "meAdjKernel"));
+    if (deterministic) {
+        meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "meAdjKernel"));
+    } else {
+        // accumulators start at zero; every contribution arrives by atomic add
+        for (double* q : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h})
+            SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
+        SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(double) * 9 * n, c->stream));
+        meAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "meAdjScatterKernel"));
+    }
     iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "iadPrepKernel"));
-    iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    if (deterministic) iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else iadAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "iadAdjKernel"));
     eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "eosAdjKernel"));
-    densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    if (deterministic) densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else densityAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "densityAdjKernel"));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;

@@ -333,11 +333,12 @@ int sphgb_sweep(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box, int32_t varian
     return sphgb_sweep_passes(c, p, variant, avClean, minDtCourant);
 }
 
-int sphgb_adjoint_std(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads)
+int sphgb_adjoint_std(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads,
+                      int32_t deterministic)
 {
     SPHGB_TRY(useDevice(c));
     if (!p || !grads) return SPHGB_ERR_ARG;
-    return adjointStd(c, p, seeds, grads);
+    return adjointStd(c, p, seeds, grads, deterministic);
 }
 
 int sphgb_get_stats(sphgb_ctx* c, sphgb_stats* s)

@@ -160,7 +160,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
                          double* minDt);
 
 int buildTranspose(sphgb_ctx* c);
-int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g);
+int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic);
 
 // min-reduction of per-block Courant dt partials into one double on the host
 int reduceMinDt(sphgb_ctx* c, const double* partials, int count, double* out);

@@ -17,14 +17,14 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
 
 
-def setup(side=12, seed=5):
+def setup(side=12, seed=5, deterministic=False):
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
     ctx = sph.Context(0)
     d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
     box = sph.Box(wl.box.copy(), wl.bc.copy())
-    sw = AG.FrozenStdSweep(ctx, d, box)
+    sw = AG.FrozenStdSweep(ctx, d, box, deterministic=deterministic)
     sw.freeze()
     order = sph.Domain(ctx, box).order(wl.n)
     rho_t = torch.tensor(wl.fields["rho_target"][order], dtype=torch.float64, device="cuda:0")
@@ -37,13 +37,14 @@ def loss_of(sw, rho_t, vals):
     return float(AG.loss_rho_a(rho, ax, ay, az, rho_t).item())
 
 
-def test_adjoint_matches_fp64_reference_gradient(port):
+@pytest.mark.parametrize("deterministic", [False, True])
+def test_adjoint_matches_fp64_reference_gradient(port, deterministic):
     """Every gradient component of every particle against torch autograd through the FP64 torch
     restatement of the same chain on the same frozen edges (tests/torch_reference.py)."""
     import torch
     from sphexa_gb300 import autograd as AG, sph
     from torch_reference import std_chain
-    wl, ctx, sw, rho_t = setup(side=10, seed=7)
+    wl, ctx, sw, rho_t = setup(side=10, seed=7, deterministic=deterministic)
     n = wl.n
     ng = int(ctx.params.ngmax)
     nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
@@ -74,6 +75,19 @@ def test_adjoint_matches_fp64_reference_gradient(port):
         err = np.linalg.norm(g - g_ref[f]) / (np.linalg.norm(g_ref[f]) + 1e-300)
         print(f"reference gradient {f:3s}: normwise rel {err:.3e}")
         assert err <= 1e-9, f
+    ctx.close()
+
+
+def test_deterministic_adjoint_is_bit_reproducible():
+    import torch
+    wl, ctx, sw, rho_t = setup(side=10, seed=9, deterministic=True)
+    vals = sw.inputs()
+    rho, ax, ay, az, du = sw.forward(*vals)
+    seeds = (2.0 * (rho - rho_t), 2.0 * ax, 2.0 * ay, 2.0 * az, None)
+    g1 = [t.cpu().numpy() for t in sw.backward(*seeds)]
+    g2 = [t.cpu().numpy() for t in sw.backward(*seeds)]
+    for a, b in zip(g1, g2):
+        np.testing.assert_array_equal(a, b)
     ctx.close()
 
 
