@@ -38,6 +38,9 @@ UNIT = "particles/s"
 # Algorithmic FLOPs per neighbour pair of each VE pass (FMA = 2, div = sqrt = 1, one table
 # lookup = 7), counted from the reference j-loops' arithmetic.
 VE_FLOPS_PER_PAIR = {"xmass": 19, "gradh": 34, "iad_divv": 37 + 59, "av": 59, "me": 141}
+# DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
+# dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count
+NCU_DRAM_BYTES_PER_PARTICLE = {"me": 692.8, "iad_divv": 585.8}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
 
 
@@ -291,8 +294,11 @@ def main() -> None:
                 "me": VE_FLOPS_PER_PAIR["me"]}.get(names[dom])
     if flops_pp:
         achieved = pairs * flops_pp / (st64[dom] * 1e-3)
+        traffic = NCU_DRAM_BYTES_PER_PARTICLE.get(names[dom])
         roofline = {"bound": "fp64", "kernel": names[dom], "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
-                    "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                    "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                    "traffic": traffic * n if traffic else None,
+                    "traffic_source": "ncu dram bytes of the same kernel at 1M particles, scaled by particles",
                     "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
                     "algorithmic": f"{pairs} pairs x {flops_pp} flop/pair per launch",
                     "hbm_peak_gbs": peaks.get("hbm_gbs")}
