@@ -8,14 +8,16 @@
 //
 // Per warp: one depth-first walk of the octree in SFC order against the group's search box, so
 // candidate leaves arrive in ascending particle order and every list comes out sorted.
-// Contiguous leaf ranges are merged and staged 32 candidates at a time in shared memory.  Each
-// target first tests a candidate in FP32 on coordinates relative to the group origin; only
-// pairs whose FP32 distance lies within a rounding margin of the radius are re-tested exactly
-// in FP64.  Lists are stored transposed, nbr[k * stride + (i - first)], so that the pair
-// passes read them coalesced.
+// Contiguous leaf ranges are merged and staged 32 candidates at a time in shared memory.
+// Positions are read in the grid form of the mixed passes: a 21-bit cell per axis plus an FP32
+// offset inside the cell.  Offsets from the group origin are (cell difference, wrapped exactly
+// in integers) x cell edge + (offset difference), so neither staging nor the distance filter
+// runs an FP64 instruction.  Only pairs whose FP32 distance lies within a rounding margin of the
+// radius are re-tested in FP64 from the original coordinates.  Lists are stored transposed,
+// nbr[k * stride + (i - first)], so that the pair passes read them coalesced.
 #include <cub/cub.cuh>
 
-#include "context.cuh"
+#include "pairs.cuh"
 
 namespace sphgb {
 
@@ -29,6 +31,9 @@ struct NbrArgs {
     const double *x, *y, *z;
     const void* h;
     int hIsFloat;
+    const u64* cell;      // packed grid cell per particle
+    const float4* loc;    // FP32 offset inside the cell (w unused here)
+    float u[3];           // cell edge per axis
     int64_t first, last;
     const uint32_t* active;  // optional: only targets with active[i - first] != 0 are searched
     const int32_t* childOffsets;
@@ -56,9 +61,24 @@ __device__ __forceinline__ double foldRint(double d, const DevBox& b, int k)
     return __dsub_rn(d, __dmul_rn(b.L[k], rint(__dmul_rn(d, b.iL[k]))));
 }
 
+__device__ __forceinline__ void unpackCell(u64 c, int ic[3])
+{
+    ic[0] = int(c & kGridMask);
+    ic[1] = int((c >> kGridBits) & kGridMask);
+    ic[2] = int(c >> (2 * kGridBits));
+}
+
+// offset of a particle (cell cj, offset lj) from the origin (cell co, offset lo), FP32
+__device__ __forceinline__ void gridOffset(const NbrArgs& a, const int cj[3], float4 lj, const int co[3], float4 lo,
+                                           float r[3])
+{
+    const float lv[3] = {lj.x - lo.x, lj.y - lo.y, lj.z - lo.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = fmaf(float(CoordMixed::wrap(cj[k] - co[k], a.box.pbc[k])), a.u[k], lv[k]);
+}
+
 struct WarpSmem {
     int32_t stack[kStack];
-    double xs[kWarp], ys[kWarp], zs[kWarp];
     float fx[kWarp], fy[kWarp], fz[kWarp];
 };
 
@@ -74,35 +94,39 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     const unsigned validMask = __ballot_sync(0xffffffffu, valid);
     if (validMask == 0) return;
     const int leader = __ffs(validMask) - 1;
-
-    double xi = 0, yi = 0, zi = 0, hi = 0;
-    if (valid) {
-        xi = a.x[i];
-        yi = a.y[i];
-        zi = a.z[i];
-        hi = loadH(a.h, a.hIsFloat, i);
-    }
-    const double r2 = __dmul_rn(__dmul_rn(4.0, hi), hi);  // reference radiusSq = 4 h h
     const DevBox& b = a.box;
-    const bool anyPbc = b.pbc[0] | b.pbc[1] | b.pbc[2];
-    const double twoH = __dmul_rn(2.0, hi);
-    const bool inside = __dsub_rn(xi, twoH) >= b.lo[0] && __dsub_rn(yi, twoH) >= b.lo[1] &&
-                        __dsub_rn(zi, twoH) >= b.lo[2] && __dadd_rn(xi, twoH) <= b.hi[0] &&
-                        __dadd_rn(yi, twoH) <= b.hi[1] && __dadd_rn(zi, twoH) <= b.hi[2];
-    const bool usePbc = anyPbc && !inside;
 
-    // group origin and target offsets relative to it (minimum image in periodic dims)
-    const double ox = __shfl_sync(0xffffffffu, xi, leader);
-    const double oy = __shfl_sync(0xffffffffu, yi, leader);
-    const double oz = __shfl_sync(0xffffffffu, zi, leader);
-    double rel[3] = {xi - ox, yi - oy, zi - oz};
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        if (b.pbc[k]) rel[k] -= b.L[k] * rint(rel[k] * b.iL[k]);
-    const float dxi = float(rel[0]), dyi = float(rel[1]), dzi = float(rel[2]);
+    // targets: grid form for the filter, exact FP64 radius and periodic decision
+    const int64_t iv = valid ? i : g0 + leader;
+    const u64 cellI = a.cell[iv];
+    const float4 locI = a.loc[iv];
+    const double hi = valid ? loadH(a.h, a.hIsFloat, i) : 0.0;
+    const double r2 = __dmul_rn(__dmul_rn(4.0, hi), hi);  // reference radiusSq = 4 h h
+    const double twoH = __dmul_rn(2.0, hi);
+    bool usePbc = false;
+    if (valid && (b.pbc[0] | b.pbc[1] | b.pbc[2])) {
+        const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+        const bool inside = __dsub_rn(xi, twoH) >= b.lo[0] && __dsub_rn(yi, twoH) >= b.lo[1] &&
+                            __dsub_rn(zi, twoH) >= b.lo[2] && __dadd_rn(xi, twoH) <= b.hi[0] &&
+                            __dadd_rn(yi, twoH) <= b.hi[1] && __dadd_rn(zi, twoH) <= b.hi[2];
+        usePbc = !inside;
+    }
+
+    // group origin = the leader's cell and offset
+    int co[3], ci[3];
+    unpackCell(__shfl_sync(0xffffffffu, cellI, leader), co);
+    unpackCell(cellI, ci);
+    float4 lo;
+    lo.x = __shfl_sync(0xffffffffu, locI.x, leader);
+    lo.y = __shfl_sync(0xffffffffu, locI.y, leader);
+    lo.z = __shfl_sync(0xffffffffu, locI.z, leader);
+    lo.w = 0.f;
+    float reli[3];
+    gridOffset(a, ci, locI, co, lo, reli);
+    const float dxi = reli[0], dyi = reli[1], dzi = reli[2];
     const float rf = valid ? __double2float_ru(twoH) : 0.f;
 
-    // group search box in relative coordinates
+    // group search box relative to the origin
     float gmin[3] = {valid ? dxi - rf : INFINITY, valid ? dyi - rf : INFINITY, valid ? dzi - rf : INFINITY};
     float gmax[3] = {valid ? dxi + rf : -INFINITY, valid ? dyi + rf : -INFINITY, valid ? dzi + rf : -INFINITY};
 #pragma unroll
@@ -111,21 +135,25 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
             gmin[k] = fminf(gmin[k], __shfl_xor_sync(0xffffffffu, gmin[k], o));
             gmax[k] = fmaxf(gmax[k], __shfl_xor_sync(0xffffffffu, gmax[k], o));
         }
+    // absolute position of the origin from its cell (FP32 suffices for pruning, see the pad)
     bool exactOnly = false;
     float gc[3], gs[3], Rg = 0.f;
-    const double oc[3] = {ox, oy, oz};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         if (b.pbc[k] && (gmax[k] - gmin[k]) > 0.25f * b.Lf[k]) exactOnly = true;
-        double cAbs = oc[k] + 0.5 * (double(gmin[k]) + double(gmax[k]));
-        if (b.pbc[k]) cAbs -= b.L[k] * floor((cAbs - b.lo[k]) * b.iL[k]);  // into [lo, hi)
-        gc[k] = float(cAbs);
-        double pad = (fabs(b.lo[k]) + fabs(b.hi[k])) * 0x1p-21;
-        gs[k] = __double2float_ru(0.5 * (double(gmax[k]) - double(gmin[k])) + pad);
+        const float lok = (k == 0) ? lo.x : (k == 1 ? lo.y : lo.z);
+        float cAbs = float(b.lo[k]) + fmaf(float(co[k]), a.u[k], lok) + 0.5f * (gmin[k] + gmax[k]);
+        if (b.pbc[k]) {
+            if (cAbs >= float(b.hi[k])) cAbs -= b.Lf[k];
+            else if (cAbs < float(b.lo[k])) cAbs += b.Lf[k];
+        }
+        gc[k] = cAbs;
+        const float pad = float((fabs(b.lo[k]) + fabs(b.hi[k])) * 0x1p-19);
+        gs[k] = 0.5f * (gmax[k] - gmin[k]) + pad;
         Rg = fmaxf(Rg, fmaxf(fabsf(gmin[k]), fabsf(gmax[k])));
     }
-    // FP32 decision margin on d2: covers the rounding of the offsets (<= 3 ulp of Rg each) and
-    // of the squared sum; pairs inside the margin get the exact FP64 test
+    // FP32 decision margin on d2: covers the rounding of cell edge, offsets and the squared sum;
+    // pairs inside the margin get the exact FP64 test
     const float r2f = float(r2);
     const float margin = 64.f * 0x1p-24f * (Rg + rf) * (Rg + rf);
 
@@ -134,42 +162,39 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     const int64_t ii = i - a.first;
 
     auto flush = [&](int64_t ja, int m) {
-        // stage candidates [ja, ja+m) in shared memory
         if (lane < m) {
-            int64_t j = ja + lane;
-            double xj = a.x[j], yj = a.y[j], zj = a.z[j];
-            sm.xs[lane] = xj;
-            sm.ys[lane] = yj;
-            sm.zs[lane] = zj;
-            double d[3] = {xj - ox, yj - oy, zj - oz};
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                if (b.pbc[k]) d[k] -= b.L[k] * rint(d[k] * b.iL[k]);
-            sm.fx[lane] = float(d[0]);
-            sm.fy[lane] = float(d[1]);
-            sm.fz[lane] = float(d[2]);
+            const int64_t j = ja + lane;
+            int cj[3];
+            unpackCell(a.cell[j], cj);
+            float rj[3];
+            gridOffset(a, cj, a.loc[j], co, lo, rj);
+            sm.fx[lane] = rj[0];
+            sm.fy[lane] = rj[1];
+            sm.fz[lane] = rj[2];
         }
         __syncwarp();
         if (valid) {
             tested += m;
             for (int t = 0; t < m; ++t) {
-                float ex = dxi - sm.fx[t], ey = dyi - sm.fy[t], ez = dzi - sm.fz[t];
-                float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                const float ex = dxi - sm.fx[t], ey = dyi - sm.fy[t], ez = dzi - sm.fz[t];
+                const float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
                 bool in;
                 if (!exactOnly && d2f < r2f - margin) in = true;
                 else if (!exactOnly && d2f > r2f + margin) in = false;
                 else {
                     ++rechecked;
-                    double dx = __dsub_rn(sm.xs[t], xi), dy = __dsub_rn(sm.ys[t], yi), dz = __dsub_rn(sm.zs[t], zi);
+                    const int64_t j = ja + t;
+                    double dx = __dsub_rn(a.x[j], a.x[i]), dy = __dsub_rn(a.y[j], a.y[i]),
+                           dz = __dsub_rn(a.z[j], a.z[i]);
                     if (usePbc) {
                         if (b.pbc[0]) dx = foldRint(dx, b, 0);
                         if (b.pbc[1]) dy = foldRint(dy, b, 1);
                         if (b.pbc[2]) dz = foldRint(dz, b, 2);
                     }
-                    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+                    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
                     in = d2 < r2;
                 }
-                int64_t j = ja + t;
+                const int64_t j = ja + t;
                 if (in && j != i) {
                     if (cnt < a.ngmax) a.nbr[int64_t(cnt) * a.stride + ii] = uint32_t(j);
                     ++cnt;
@@ -181,11 +206,11 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
 
     int64_t pa = 0, pb = 0;  // pending contiguous candidate range
     auto addLeaf = [&](int32_t leaf) {
-        int64_t la = a.layout[leaf], lb = a.layout[leaf + 1];
+        const int64_t la = a.layout[leaf], lb = a.layout[leaf + 1];
         if (la == lb) return;
         if (la != pb) {
             while (pb > pa) {
-                int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
+                const int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
                 flush(pa, m);
                 pa += m;
             }
@@ -204,17 +229,17 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     __syncwarp();
     bool overflow = false;
     while (sp > 0) {
-        int32_t node = sm.stack[--sp];
-        int32_t co = a.childOffsets[node];
-        if (co == 0) {
+        const int32_t node = sm.stack[--sp];
+        const int32_t co8 = a.childOffsets[node];
+        if (co8 == 0) {
             addLeaf(a.internalToLeaf[node]);
             continue;
         }
         bool ov = false;
-        int32_t child = co + (lane & 7);
+        const int32_t child = co8 + (lane & 7);
         if (lane < 8) {
-            float4 c4 = a.nodeBox[2 * child], s4 = a.nodeBox[2 * child + 1];
-            float cc[3] = {c4.x, c4.y, c4.z}, ss[3] = {s4.x, s4.y, s4.z};
+            const float4 c4 = a.nodeBox[2 * child], s4 = a.nodeBox[2 * child + 1];
+            const float cc[3] = {c4.x, c4.y, c4.z}, ss[3] = {s4.x, s4.y, s4.z};
             ov = true;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -223,8 +248,8 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
                 ov = ov && (dd <= ss[k] + gs[k]);
             }
         }
-        unsigned m = __ballot_sync(0xffffffffu, ov);
-        int k = __popc(m);
+        const unsigned m = __ballot_sync(0xffffffffu, ov);
+        const int k = __popc(m);
         if (sp + k > kStack) {
             overflow = true;
             break;
@@ -239,7 +264,7 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         return;
     }
     while (pb > pa) {
-        int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
+        const int m = int(pb - pa < kWarp ? pb - pa : int64_t(kWarp));
         flush(pa, m);
         pa += m;
     }
@@ -324,6 +349,28 @@ __global__ void fillOnes(uint32_t* p, int64_t n)
     if (k < n) p[k] = 1u;
 }
 
+// grid form of all particles' positions (cells + FP32 offsets), shared with the mixed passes
+__global__ void gridFormKernel(const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ z, int64_t n, DevBox box, u64* __restrict__ cell,
+                               float4* __restrict__ loc)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const double c[3] = {x[i], y[i], z[i]};
+    unsigned ic[3];
+    float l[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double u = box.L[k] / double(1 << kGridBits);
+        double g = floor((c[k] - box.lo[k]) / u);
+        g = fmin(fmax(g, 0.0), double(kGridMask));
+        ic[k] = unsigned(g);
+        l[k] = float(c[k] - (box.lo[k] + g * u));
+    }
+    cell[i] = u64(ic[0]) | (u64(ic[1]) << kGridBits) | (u64(ic[2]) << (2 * kGridBits));
+    loc[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
 int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int hIsFloat,
               int64_t first, int64_t last, uint32_t ngmax, const uint32_t* active)
 {
@@ -333,6 +380,9 @@ int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, c
     a.z = z;
     a.h = h;
     a.hIsFloat = hIsFloat;
+    a.cell = c->gridKey.as<u64>();
+    a.loc = c->gridLoc.as<float4>();
+    for (int k = 0; k < 3; ++k) a.u[k] = float(c->box.L[k] / double(1 << kGridBits));
     a.first = first;
     a.last = last;
     a.active = active;
@@ -354,7 +404,8 @@ int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, c
     return launched(c, "nbrGroupKernel");
 }
 
-int prepareLists(sphgb_ctx* c, int64_t first, int64_t last, uint32_t ngmax)
+int prepareLists(sphgb_ctx* c, const double* x, const double* y, const double* z, int64_t first, int64_t last,
+                 uint32_t ngmax)
 {
     if (!c->haveTree) return SPHGB_ERR_STATE;
     if (first < 0 || last > c->n || first >= last) return SPHGB_ERR_ARG;
@@ -366,6 +417,12 @@ int prepareLists(sphgb_ctx* c, int64_t first, int64_t last, uint32_t ngmax)
     SPHGB_TRY(c->counters.ensure(sizeof(unsigned long long) * 8));
     SPHGB_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(unsigned long long) * 8, c->stream));
     SPHGB_CUDA(cudaMemsetAsync(c->dFlags, 0, sizeof(int), c->stream));
+    // grid form of every particle (neighbours may be anywhere in [0, n))
+    SPHGB_TRY(c->gridKey.ensure(sizeof(u64) * c->n));
+    SPHGB_TRY(c->gridLoc.ensure(sizeof(float4) * c->n));
+    gridFormKernel<<<gridFor(c->n, 256), 256, 0, c->stream>>>(x, y, z, c->n, c->box, c->gridKey.as<u64>(),
+                                                             c->gridLoc.as<float4>());
+    SPHGB_TRY(launched(c, "gridFormKernel"));
     c->nbrFirst = first;
     c->nbrLast = last;
     c->nbrNgmax = ngmax;
@@ -397,7 +454,7 @@ int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     if (!p->x || !p->y || !p->z || !p->h) return SPHGB_ERR_ARG;
     const uint32_t ngmax = c->prm.ngmax;
     if (c->prm.ng0 > ngmax) return SPHGB_ERR_ARG;  // reference: "ng0 should be smaller than ngmax"
-    SPHGB_TRY(prepareLists(c, first, last, ngmax));
+    SPHGB_TRY(prepareLists(c, p->x, p->y, p->z, first, last, ngmax));
     const int64_t nWork = last - first;
     const int hf = p->precision == SPHGB_MIXED;
     uint32_t* active = c->active.as<uint32_t>();
@@ -442,7 +499,7 @@ int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const dou
                        int64_t first, int64_t last, uint32_t ngmax, uint32_t* nbrOut, uint32_t* ncOut)
 {
     if (!x || !y || !z || !h || ngmax == 0) return SPHGB_ERR_ARG;
-    SPHGB_TRY(prepareLists(c, first, last, ngmax));
+    SPHGB_TRY(prepareLists(c, x, y, z, first, last, ngmax));
     const int64_t nWork = last - first;
     SPHGB_TRY(runSearch(c, x, y, z, h, hPrec == SPHGB_MIXED, first, last, ngmax, nullptr));
     ncOutKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->ncount.as<uint32_t>(), nullptr, nWork, ngmax, ncOut, 0,
