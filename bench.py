@@ -35,9 +35,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "SPH sweep particles/s on 1 GB300: mixed-FP32 vs FP64 at stated err; adjoint/fwd"
 UNIT = "particles/s"
 
-# Algorithmic FLOPs per neighbour pair of each VE pass (FMA = 2, div = sqrt = 1, one table
-# lookup = 7), counted from the reference j-loops' arithmetic.
-VE_FLOPS_PER_PAIR = {"xmass": 19, "gradh": 34, "iad_divv": 37 + 59, "av": 59, "me": 141}
+# Algorithmic FLOPs per neighbour pair of each pass on the jittered Sedov lattice: the reference
+# j-loops instantiated on a counting scalar (+ - * / sqrt and each transcendental call 1 flop,
+# an FMA 2), workload mean sum(flops) / sum(pairs); oracle/flop_table.json, workload sedov_jit_20.
+VE_FLOPS_PER_PAIR = {"xmass": 20.2, "gradh": 34.4, "iad_divv": 37.6 + 59.3, "av": 55.3, "me": 136.2}
+STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
 # dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count
 NCU_DRAM_BYTES_PER_PARTICLE = {"me": 692.8, "iad_divv": 585.8}
@@ -289,9 +291,7 @@ def main() -> None:
     # dominant kernel: largest per-stage time of the FP64 sweep
     names = STAGES_VE if args.variant == "ve" else ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
     dom = int(np.argmax(st64))
-    flops_pp = {"xmass": VE_FLOPS_PER_PAIR["xmass"], "gradh": VE_FLOPS_PER_PAIR["gradh"],
-                "iad_divv": VE_FLOPS_PER_PAIR["iad_divv"], "av": VE_FLOPS_PER_PAIR["av"],
-                "me": VE_FLOPS_PER_PAIR["me"]}.get(names[dom])
+    flops_pp = (VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR).get(names[dom])
     if flops_pp:
         achieved = pairs * flops_pp / (st64[dom] * 1e-3)
         traffic = NCU_DRAM_BYTES_PER_PARTICLE.get(names[dom])
@@ -341,7 +341,7 @@ def main() -> None:
                                                                                    1e-300)),
                "c11_max_rel": float(np.max(np.abs(r32["c11"] - ref64["c11"])) / np.max(np.abs(ref64["c11"])))}
         dom32 = int(np.argmax(st32))
-        fpp32 = VE_FLOPS_PER_PAIR.get(names[dom32]) if args.variant == "ve" else None
+        fpp32 = (VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR).get(names[dom32])
         out["mixed"] = {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
                         "errors_vs_fp64": err,
                         "stages_ms": {names[k]: round(float(st32[k]), 3) for k in range(len(names))
