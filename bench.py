@@ -114,32 +114,75 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
 
 
+# name -> (description used verbatim as config.workload by both arms, constructor)
+WORKLOADS = {
+    "sedov200_jit": ("sedov200_jit: 8000000 particles, periodic [-0.5,0.5]^3, jitter +-0.25 spacing (seed 2), "
+                     "Sedov u, v = 0, frozen h",
+                     lambda W: W.sedov(200, jitter=0.25, seed=2)),
+    "sedov100_jit": ("sedov100_jit: 1000000 particles, periodic [-0.5,0.5]^3, jitter +-0.25 spacing (seed 2), "
+                     "Sedov u, v = 0, frozen h",
+                     lambda W: W.sedov(100, jitter=0.25, seed=2)),
+    "fourier300": ("fourier300: 27000000 particles, periodic unit box, jitter +-0.3 spacing (seed 3), Fourier "
+                   "density field in the masses (seed 33), v ~ N(0, 0.1^2) (seed 333), u = 1",
+                   lambda W: W.fourier(300)),
+    "sphere10M": ("sphere10M: 10000000 particles in the unit sphere, open boundaries, r = sqrt(U) (seed 4), "
+                  "u = 0.05, v = 0, h from the local number density",
+                  lambda W: W.sphere(10_000_000)),
+}
+
+
 def make_workload(name: str):
     from sphexa_gb300 import workloads as W
-    if name == "sedov200_jit":
-        return W.sedov(200, jitter=0.25, seed=2)
-    if name == "sedov100_jit":
-        return W.sedov(100, jitter=0.25, seed=2)
-    if name == "fourier300":
-        return W.fourier(300)
-    if name == "sphere10M":
-        return W.sphere(10_000_000)
-    raise SystemExit(f"unknown workload {name}")
+    if name not in WORKLOADS:
+        raise SystemExit(f"unknown workload {name}")
+    return WORKLOADS[name][1](W)
 
 
-def cpu_baseline(side: int, threads: int = 0) -> dict:
+def bench_config(args, world: int) -> dict:
+    """config object shared by the GPU arm and the reference arm (same workload string)."""
+    return {"workload": WORKLOADS[args.workload][0] + f"; one full {args.variant.upper()} sweep per step",
+            "variant": args.variant, "precision": "fp64",
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
+
+
+def structure_report(ctx, d, stats: dict, ngmax: int) -> dict:
+    """Octree depth, neighbour-count histogram, capped count and per-group (32 SFC-consecutive
+    targets) pair load of the last sweep."""
+    lr = [int(v) for v in stats["level_range"]]
+    depth = max(k for k in range(len(lr) - 1) if lr[k + 1] > lr[k]) if any(lr) else 0
+    nc = d.nc.cpu().numpy().astype(np.int64)
+    pairs = np.minimum(nc - 1, ngmax)
+    edges = [0, 25, 50, 75, 100, 125, 150, 151, 10 ** 9]
+    hist = np.histogram(nc, bins=edges)[0]
+    g = pairs[: (len(pairs) // 32) * 32].reshape(-1, 32).sum(1)
+    return {"octree_depth": depth, "num_leaves": stats["num_leaves"], "num_nodes": stats["num_nodes"],
+            "nc_hist": {f"[{edges[k]},{edges[k + 1]})": int(hist[k]) for k in range(len(hist))},
+            "nc_min": int(nc.min()), "nc_max": int(nc.max()), "capped": stats["capped"],
+            "h_iterations": stats["h_iterations"],
+            "group_pairs": {"mean": float(g.mean()), "p99": float(np.percentile(g, 99)), "max": int(g.max()),
+                            "max_over_mean": float(g.max() / g.mean())}}
+
+
+# bounded CPU sample of each workload: the same generator at side^3 particles
+SAMPLES = {"sedov200_jit": lambda W, s: W.sedov(s, jitter=0.25, seed=2),
+           "sedov100_jit": lambda W, s: W.sedov(s, jitter=0.25, seed=2),
+           "fourier300": lambda W, s: W.fourier(s),
+           "sphere10M": lambda W, s: W.sphere(s ** 3)}
+
+
+def cpu_baseline(side: int, threads: int = 0, workload: str = "sedov200_jit", variant: str = "ve") -> dict:
     """The oracle (my CPU restatement of the reference's OpenMP path) on a bounded sample of the
-    workload: the same jittered Sedov lattice at side^3 particles, one full VE sweep."""
+    workload: the same generator at side^3 particles, one full sweep."""
     from oracle import oracle as O
     from sphexa_gb300 import workloads as W
     O.build_port()
     port = O.port()
-    wl = W.sedov(side, jitter=0.25, seed=2)
+    wl = SAMPLES[workload](W, side)
     t0 = time.perf_counter()
-    r = port.sweep(wl, "ve", False, want_nbr=False, want_tree=False, nthreads=threads)
+    r = port.sweep(wl, variant, False, want_nbr=False, want_tree=False, nthreads=threads)
     dt = time.perf_counter() - t0
     return {"value": wl.n / dt, "unit": UNIT, "cores": int(r["threads"]), "kind": "port",
-            "sample": f"one VE sweep of the same jittered Sedov lattice at {side}^3 = {wl.n} particles "
+            "sample": f"one {variant.upper()} sweep of the same generator ({workload}) at {wl.n} particles "
                       f"({dt:.1f} s; stages keys {r['times']['keys']:.2f} tree {r['times']['tree']:.2f} "
                       f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
 
@@ -193,19 +236,19 @@ def run_reference(args) -> None:
     side = args.cpu_side
     vals = []
     for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(max(side // 2, 20))
+        cpu_baseline(max(side // 2, 20), workload=args.workload, variant=args.variant)
     t_all = time.perf_counter()
     last = None
     for _ in range(args.steps):
-        last = cpu_baseline(side)
+        last = cpu_baseline(side, workload=args.workload, variant=args.variant)
         vals.append(last["value"])
     wall = time.perf_counter() - t_all
     v = statistics.median(vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: seeded jittered Sedov lattice", "impl": "reference",
-            "config": {"workload": args.workload, "sample_side": side, "variant": "ve", "precision": "fp64"},
+            "data": "synthetic: seeded generator of the named configuration (no dataset)", "impl": "reference",
+            "config": bench_config(args, world),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
                              "sample": last["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -309,22 +352,22 @@ def main() -> None:
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic: seeded jittered Sedov lattice (no dataset; configs regenerated from seeds)",
-           "config": {"workload": f"{args.workload}: {n} particles, periodic [-0.5,0.5]^3, jitter +-0.25 "
-                                  f"spacing, frozen h, one full {args.variant.upper()} sweep per step",
-                      "variant": args.variant, "precision": "fp64", "n_particles": n,
-                      "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+           "data": "synthetic: seeded generator of the named configuration (no dataset)",
+           "config": bench_config(args, world), "n_particles": n,
            "roofline": roofline, "gpu_launches": launches // max(1, args.steps) * args.steps,
            "clocks": clocks,
            "stages_ms": {names[k]: round(float(st64[k]), 3) for k in range(len(names)) if names[k] != "-"},
            "neighbors": {"pairs": pairs, "mean": pairs / n, "max_nc": stats["nc_max"], "capped": stats["capped"],
                          "candidates": stats["candidates"], "fp64_rechecks": stats["fp64_rechecks"]},
            "fp32_peak_tflops": fp32_peak / 1e12}
+    if args.workload in ("fourier300", "sphere10M"):
+        out["structure"] = structure_report(ctx, d64, stats, int(wl.params["ngmax"]))
 
     # ---------------- mixed form on the same workload, errors against this run's FP64 results
     if not args.no_mixed:
-        ref64 = {k: d64.f[k].double().cpu().numpy() for k in ("xm", "kx", "rho", "ax", "ay", "az", "du", "c11",
-                                                               "divv", "alpha")}
+        ref64 = {k: d64.f[k].double().cpu().numpy()
+                 for k in ("xm", "kx", "rho", "ax", "ay", "az", "du", "c11", "c12", "c13", "c22", "c23", "c33",
+                           "divv", "curlv", "alpha")}
         del d64
         torch.cuda.empty_cache()
         d32 = sph.ParticlesData.from_workload(wl, "mixed", dev)
@@ -340,6 +383,13 @@ def main() -> None:
                "du_normwise": float(np.linalg.norm(r32["du"] - ref64["du"]) / max(np.linalg.norm(ref64["du"]),
                                                                                    1e-300)),
                "c11_max_rel": float(np.max(np.abs(r32["c11"] - ref64["c11"])) / np.max(np.abs(ref64["c11"])))}
+        cij = [f"c{a}{b}" for a, b in ("11", "12", "13", "22", "23", "33")]
+        cmag = max(float(np.max(np.abs(ref64[k]))) for k in cij)
+        err["cij_max_over_tensor_max"] = max(float(np.max(np.abs(r32[k] - ref64[k]))) for k in cij) / cmag
+        for k in ("divv", "curlv", "alpha"):
+            scale = float(np.max(np.abs(ref64[k])))
+            err[f"{k}_max_over_field_max"] = (float(np.max(np.abs(r32[k] - ref64[k]))) / scale) if scale > 0 else \
+                float(np.max(np.abs(r32[k] - ref64[k])))
         dom32 = int(np.argmax(st32))
         fpp32 = (VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR).get(names[dom32])
         out["mixed"] = {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
@@ -390,7 +440,7 @@ def main() -> None:
         out["adjoint"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup)
 
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_side)
+        out["cpu_baseline"] = cpu_baseline(args.cpu_side, workload=args.workload, variant=args.variant)
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
