@@ -136,7 +136,8 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->levelRangeDev, &c->nbr,     &c->ncount,        &c->active,        &c->counters,
                     &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
-                    &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState};
+                    &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
+                    &c->whdx64};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)

@@ -103,6 +103,7 @@ struct sphgb_ctx {
 
     // kernel tables (FP64 and FP32)
     sphgb::DBuf wh64, whd64, wh32, whd32;
+    sphgb::DBuf whx64, whdx64;  // FP64 tables interleaved {t[k], t[k+1] - t[k]}
 
     // mixed precision grid-local coordinates: packed cell (21 bits per axis) + float4 {dx,dy,dz,1/h}
     sphgb::DBuf gridKey, gridLoc;

@@ -27,10 +27,10 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double* tab = static_cast<const double*>(wh);
+        const double2* tab = static_cast<const double2*>(wh);
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i);
-        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         double rho0 = mi;
         for (unsigned k = 0; k < nc; ++k) {
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
             double r2 = rx * rx + ry * ry + rz * rz;
-            rho0 += tableLookup(tab, r2 * invDist(r2) * hInv) * ld<double>(m, j);
+            rho0 += lookupX(tab, r2 * invDist(r2) * hInvDx) * ld<double>(m, j);
         }
         double xm = mi / (rho0 * K * h3Inv);
         st<double>(out, i, StoreRho ? mi / xm : xm);
@@ -117,9 +117,9 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double* tab = static_cast<const double*>(wh);
+        const double2* tab = static_cast<const double2*>(wh);
         auto t = cf.target(i);
-        double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
+        double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         double t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
         for (unsigned k = 0; k < nc; ++k) {
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
             double r2 = rx * rx + ry * ry + rz * rz;
-            double w = tableLookup(tab, r2 * invDist(r2) * hiInv);
+            double w = lookupX(tab, r2 * invDist(r2) * hInvDx);
             double vw = ld<double>(vol, j) * w;
             t11 += rx * rx * vw;
             t12 += rx * ry * vw;
@@ -179,7 +179,7 @@ struct MeStdArgs {
     const void *vx, *vy, *vz, *h, *m, *rho, *p, *c;
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void* wh;
-    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3
+    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
     const void* aux;       // m/rho, p/rho, p/rho^2
     int64_t n;
     double K;
@@ -212,11 +212,13 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const double* hInv = a.hInv64;
+        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
         const double* hInv3 = a.hInv64 + a.n;
-        T hiInv = hInv[i], hiInv3 = hInv3[i], twoH = 2.0 * hi;
+        const double* hInvDx = a.hInv64 + 2 * a.n;
+        T hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
         const bool wrap = cf.needsWrap(t, twoH);
         T mx = 0, my = 0, mz = 0, en = 0;
+        long long maxvBits = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
@@ -225,10 +227,9 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             T rinv = invDist(r2);
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
-            T v1 = dist * hiInv, v2 = dist * __ldg(hInv + j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            T Wi = hiInv3 * tableLookup(tab, v1);
-            T Wj = __ldg(hInv3 + j) * tableLookup(tab, v2);
+            T Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
+            T Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
             T a1i = c11i * rx + c12i * ry + c13i * rz;
             T a2i = c12i * rx + c22i * ry + c23i * rz;
             T a3i = c13i * rx + c23i * ry + c33i * rz;
@@ -240,8 +241,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             T cj = ld<T>(a.c, j);
             T wij = rv * rinv;
             T visc = T(0.5) * artificialViscosity<T>(1.0, 1.0, ci, cj, wij);
-            T vsig = ci + cj - T(3) * wij;
-            maxv = (vsig > maxv) ? vsig : maxv;
+            maxvBits = maxBitsNonNeg(maxvBits, ci + cj - T(3) * wij);
             T mj = ld<T>(a.m, j);
             T mjrojWj = __ldg(auxMoR + j) * Wj;
             T mjproi = mj * proi2;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             st<T>(a.ax, i, a.K * mx);
             st<T>(a.ay, i, a.K * my);
             st<T>(a.az, i, a.K * mz);
-            dt = courantDt(maxv, hi, ci, a.Kcour);
+            dt = courantDt(__longlong_as_double(maxvBits), hi, ci, a.Kcour);
         }
     } else {
         auto t = cm.target(i);
@@ -326,7 +326,7 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
     lv.last = last;
     CoordFp64 cf = coordFp64(c, p);
     CoordMixed cm = coordMixed(c);
-    const void* wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->wh32.p;
     unsigned blocks = gridFor(last - first, kPairBlock);
     if (storeRho)
         xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
@@ -342,7 +342,7 @@ int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    const void* wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->wh32.p;
     iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
         lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, c->K,
         IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
@@ -371,7 +371,7 @@ int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, d
     a.c22 = p->c22;
     a.c23 = p->c23;
     a.c33 = p->c33;
-    a.wh = std::is_same_v<P, Fp64Tag> ? c->wh64.p : c->wh32.p;
+    a.wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->wh32.p;
     a.hInv64 = c->hInv64.as<double>();
     a.aux = c->aux.p;
     a.n = p->n;

@@ -59,10 +59,10 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double *tw = static_cast<const double*>(wh), *tdw = static_cast<const double*>(whd);
+        const double2 *tw = static_cast<const double2*>(wh), *tdw = static_cast<const double2*>(whd);
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i), xmi = ld<double>(xm, i);
-        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi;
+        double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         double kxi = xmi, whomega = -3.0 * xmi, wrho0 = -3.0 * mi;
         for (unsigned k = 0; k < nc; ++k) {
@@ -70,8 +70,10 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
             double r2 = rx * rx + ry * ry + rz * rz;
-            double v = r2 * invDist(r2) * hInv;
-            double w = tableLookup(tw, v), dw = tableLookup(tdw, v);
+            double dist = r2 * invDist(r2);
+            double v = dist * hInv;
+            const TabSlot sl = tabSlot(dist * hInvDx);
+            double w = lookupX(tw, sl), dw = lookupX(tdw, sl);
             double dterh = -(3.0 * w + v * dw);
             double xmj = ld<double>(xm, j);
             kxi += w * xmj;
@@ -155,24 +157,42 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         using T = double;
-        const double* tab = static_cast<const double*>(a.wh);
+        const double2* tab = static_cast<const double2*>(a.wh);
         auto t = cf.target(i);
         T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        const T hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
+        const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        // one walk over the list: tau = sum vol_j W r r^T and M = sum xm_j W (v_j - v_i) r^T;
+        // the reference's second loop sums xm_j (v_j - v_i) (-(c_i r) W)^T, which is -M c_i^T
+        // (c_i symmetric), so c_i is applied once after the walk instead of per pair
         T t11 = 0, t12 = 0, t13 = 0, t22 = 0, t23 = 0, t33 = 0;
+        T M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
             T r2 = rx * rx + ry * ry + rz * rz;
-            T w = tableLookup(tab, r2 * invDist(r2) * hiInv);
+            T w = lookupX(tab, r2 * invDist(r2) * hInvDx);
             T vw = ld<T>(a.vol, j) * w;
-            t11 += rx * rx * vw;
-            t12 += rx * ry * vw;
-            t13 += rx * rz * vw;
-            t22 += ry * ry * vw;
-            t23 += ry * rz * vw;
-            t33 += rz * rz * vw;
+            T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
+            t11 += rx * rxv;
+            t12 += ry * rxv;
+            t13 += rz * rxv;
+            t22 += ry * ryv;
+            t23 += rz * ryv;
+            t33 += rz * rzv;
+            T xw = ld<T>(a.xm, j) * w;
+            T sx = (ld<T>(a.vx, j) - vxi) * xw, sy = (ld<T>(a.vy, j) - vyi) * xw, sz = (ld<T>(a.vz, j) - vzi) * xw;
+            M[0] += sx * rx;
+            M[1] += sx * ry;
+            M[2] += sx * rz;
+            M[3] += sy * rx;
+            M[4] += sy * ry;
+            M[5] += sy * rz;
+            M[6] += sz * rx;
+            M[7] += sz * ry;
+            M[8] += sz * rz;
         }
         T cc[6];
         iadInvert<T>(t11, t12, t13, t22, t23, t33, hi, a.K, cc);
@@ -182,30 +202,14 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         st<T>(a.c22, i, cc[3]);
         st<T>(a.c23, i, cc[4]);
         st<T>(a.c33, i, cc[5]);
-
-        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
-        T dVx[3] = {0, 0, 0}, dVy[3] = {0, 0, 0}, dVz[3] = {0, 0, 0};
-        for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            T rx, ry, rz;
-            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            T r2 = rx * rx + ry * ry + rz * rz;
-            T vxji = ld<T>(a.vx, j) - vxi, vyji = ld<T>(a.vy, j) - vyi, vzji = ld<T>(a.vz, j) - vzi;
-            T Wi = tableLookup(tab, r2 * invDist(r2) * hiInv);
-            T tA0 = -(cc[0] * rx + cc[1] * ry + cc[2] * rz) * Wi;
-            T tA1 = -(cc[1] * rx + cc[3] * ry + cc[4] * rz) * Wi;
-            T tA2 = -(cc[2] * rx + cc[4] * ry + cc[5] * rz) * Wi;
-            T xmj = ld<T>(a.xm, j);
-            T sx = vxji * xmj, sy = vyji * xmj, sz = vzji * xmj;
-            dVx[0] += sx * tA0;
-            dVx[1] += sx * tA1;
-            dVx[2] += sx * tA2;
-            dVy[0] += sy * tA0;
-            dVy[1] += sy * tA1;
-            dVy[2] += sy * tA2;
-            dVz[0] += sz * tA0;
-            dVz[1] += sz * tA1;
-            dVz[2] += sz * tA2;
+        // dV[a][b] = -sum_c c_bc M[a][c]
+        const T C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
+        T dVx[3], dVy[3], dVz[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            dVx[b] = -(C[b][0] * M[0] + C[b][1] * M[1] + C[b][2] * M[2]);
+            dVy[b] = -(C[b][0] * M[3] + C[b][1] * M[4] + C[b][2] * M[5]);
+            dVz[b] = -(C[b][0] * M[6] + C[b][1] * M[7] + C[b][2] * M[8]);
         }
         T nk = a.K * hiInv3 / ld<T>(a.kx, i);
         st<T>(a.divv, i, nk * (dVx[0] + dVy[1] + dVz[2]));
@@ -225,7 +229,10 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         using T = float;
         const float* tab = static_cast<const float*>(a.wh);
         auto t = cm.target(i);
+        const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
+        // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
         KSum t11, t12, t13, t22, t23, t33;
+        KSum M[9];
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz, hjInv;
@@ -233,12 +240,24 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             T w = tableLookup(tab, dist * t.hInv);
             T vw = ld<T>(a.vol, j) * w;
-            t11.add(rx * rx * vw);
-            t12.add(rx * ry * vw);
-            t13.add(rx * rz * vw);
-            t22.add(ry * ry * vw);
-            t23.add(ry * rz * vw);
-            t33.add(rz * rz * vw);
+            T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
+            t11.add(rx * rxv);
+            t12.add(ry * rxv);
+            t13.add(rz * rxv);
+            t22.add(ry * ryv);
+            t23.add(rz * ryv);
+            t33.add(rz * rzv);
+            T xw = ld<T>(a.xm, j) * w;
+            T sx = (ld<T>(a.vx, j) - vxi) * xw, sy = (ld<T>(a.vy, j) - vyi) * xw, sz = (ld<T>(a.vz, j) - vzi) * xw;
+            M[0].add(sx * rx);
+            M[1].add(sx * ry);
+            M[2].add(sx * rz);
+            M[3].add(sy * rx);
+            M[4].add(sy * ry);
+            M[5].add(sy * rz);
+            M[6].add(sz * rx);
+            M[7].add(sz * ry);
+            M[8].add(sz * rz);
         }
         double hi = double(ld<T>(a.h, i));
         T cc[6];
@@ -249,39 +268,19 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         st<T>(a.c22, i, cc[3]);
         st<T>(a.c23, i, cc[4]);
         st<T>(a.c33, i, cc[5]);
-
-        T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
-        KSum dVx[3], dVy[3], dVz[3];
-        for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            T rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
-            T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            T vxji = ld<T>(a.vx, j) - vxi, vyji = ld<T>(a.vy, j) - vyi, vzji = ld<T>(a.vz, j) - vzi;
-            T Wi = tableLookup(tab, dist * t.hInv);
-            T tA0 = -(cc[0] * rx + cc[1] * ry + cc[2] * rz) * Wi;
-            T tA1 = -(cc[1] * rx + cc[3] * ry + cc[4] * rz) * Wi;
-            T tA2 = -(cc[2] * rx + cc[4] * ry + cc[5] * rz) * Wi;
-            T xmj = ld<T>(a.xm, j);
-            T sx = vxji * xmj, sy = vyji * xmj, sz = vzji * xmj;
-            dVx[0].add(sx * tA0);
-            dVx[1].add(sx * tA1);
-            dVx[2].add(sx * tA2);
-            dVy[0].add(sy * tA0);
-            dVy[1].add(sy * tA1);
-            dVy[2].add(sy * tA2);
-            dVz[0].add(sz * tA0);
-            dVz[1].add(sz * tA1);
-            dVz[2].add(sz * tA2);
+        double m64[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m64[q] = M[q].value64();
+        const double C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
+        double gx[3], gy[3], gz[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            gx[b] = -(C[b][0] * m64[0] + C[b][1] * m64[1] + C[b][2] * m64[2]);
+            gy[b] = -(C[b][0] * m64[3] + C[b][1] * m64[4] + C[b][2] * m64[5]);
+            gz[b] = -(C[b][0] * m64[6] + C[b][1] * m64[7] + C[b][2] * m64[8]);
         }
         double hInv = 1.0 / hi;
         double nk = a.K * (hInv * hInv * hInv) / double(ld<T>(a.kx, i));
-        double gx[3], gy[3], gz[3];
-        for (int q = 0; q < 3; ++q) {
-            gx[q] = dVx[q].value64();
-            gy[q] = dVy[q].value64();
-            gz[q] = dVz[q].value64();
-        }
         st<T>(a.divv, i, T(nk * (gx[0] + gy[1] + gz[2])));
         if (a.curlv) {
             double cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
@@ -324,10 +323,14 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
     T gx, gy, gz;
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+        T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         const T kh3 = a.K * hiInv3;
-        gx = gy = gz = 0;
+        // the reference sums fac_j (-(c_i r) W) per pair; with S = sum fac_j W r that is -c_i S,
+        // so c_i is applied once after the walk
+        T Sx = 0, Sy = 0, Sz = 0;
+        long long vsigBits = __double_as_longlong(vsig_i);  // > 0
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
@@ -337,16 +340,16 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            if (rv < 0.0) vsig_i = fmax(vsig_i, ci + ld<T>(a.c, j) - 3.0 * rv * rinv);
-            T Wi = kh3 * tableLookup(tab, dist * hiInv);
-            T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
-            T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
-            T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
-            T fac = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j));
-            gx += fac * t1;
-            gy += fac * t2;
-            gz += fac * t3;
+            if (negative(rv)) vsigBits = maxBitsNonNeg(vsigBits, ci + ld<T>(a.c, j) - 3.0 * rv * rinv);
+            T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) * lookupX(tabX, dist * hInvDx);
+            Sx += fw * rx;
+            Sy += fw * ry;
+            Sz += fw * rz;
         }
+        vsig_i = __longlong_as_double(vsigBits);
+        gx = -kh3 * (c11 * Sx + c12 * Sy + c13 * Sz);
+        gy = -kh3 * (c12 * Sx + c22 * Sy + c23 * Sz);
+        gz = -kh3 * (c13 * Sx + c23 * Sy + c33 * Sz);
     } else {
         auto t = cm.target(i);
         const float kh3 = float(a.K) * t.hInv * t.hInv * t.hInv;
@@ -361,18 +364,15 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + ld<T>(a.c, j) - 3.f * rv * rinv);
-            T Wi = kh3 * tableLookup(tab, dist * t.hInv);
-            T t1 = -(c11 * rx + c12 * ry + c13 * rz) * Wi;
-            T t2 = -(c12 * rx + c22 * ry + c23 * rz) * Wi;
-            T t3 = -(c13 * rx + c23 * ry + c33 * rz) * Wi;
-            T fac = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j));
-            sx.add(fac * t1);
-            sy.add(fac * t2);
-            sz.add(fac * t3);
+            T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) * tableLookup(tab, dist * t.hInv);
+            sx.add(fw * rx);
+            sy.add(fw * ry);
+            sz.add(fw * rz);
         }
-        gx = sx.value();
-        gy = sy.value();
-        gz = sz.value();
+        const double Sx = sx.value64(), Sy = sy.value64(), Sz = sz.value64();
+        gx = T(-double(kh3) * (double(c11) * Sx + double(c12) * Sy + double(c13) * Sz));
+        gy = T(-double(kh3) * (double(c12) * Sx + double(c22) * Sy + double(c23) * Sz));
+        gz = T(-double(kh3) * (double(c13) * Sx + double(c23) * Sy + double(c33) * Sz));
     }
     // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
     T alpha_i = ld<T>(a.alpha, i);
@@ -469,12 +469,16 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
+        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
         const double* hInv = a.hInv64;
         const double* hInv3 = a.hInv64 + a.n;
-        T hiInv = hInv[i], hiInv3 = hInv3[i], twoH = 2.0 * hi;
+        const double* hInvDx = a.hInv64 + 2 * a.n;
+        T hiInv = hInv[i], hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
         const bool wrap = cf.needsWrap(t, twoH);
         const T rhoiInv = 1.0 / rhoi;
+        const T mprhoi = prhoi;
         T mx = 0, my = 0, mz = 0, en = 0, avE = 0;
+        long long maxvBits = 0;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
@@ -483,36 +487,36 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T rinv = invDist(r2);
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
-            T v1 = dist * hiInv, v2 = dist * __ldg(hInv + j);
-            T Wi = hiInv3 * tableLookup(tab, v1);
-            T Wj = __ldg(hInv3 + j) * tableLookup(tab, v2);
-            T a1i = -(c11i * rx + c12i * ry + c13i * rz) * Wi;
-            T a2i = -(c12i * rx + c22i * ry + c23i * rz) * Wi;
-            T a3i = -(c13i * rx + c23i * ry + c33i * rz) * Wi;
+            T Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
+            T Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
+            // G = c r at both ends; the reference's a_i = -G_i W_i, a_j = -G_j W_j
+            T gix = c11i * rx + c12i * ry + c13i * rz;
+            T giy = c12i * rx + c22i * ry + c23i * rz;
+            T giz = c13i * rx + c23i * ry + c33i * rz;
             T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
             T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
-            T a1j = -(c11j * rx + c12j * ry + c13j * rz) * Wj;
-            T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
-            T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
+            T gjx = c11j * rx + c12j * ry + c13j * rz;
+            T gjy = c12j * rx + c22j * ry + c23j * rz;
+            T gjz = c13j * rx + c23j * ry + c33j * rz;
             T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
             T rhoj = __ldg(auxRho + j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
                            ld<T>(a.dV22, j), ld<T>(a.dV23, j), ld<T>(a.dV33, j)};
-                rv += avRv<T>(rx, ry, rz, fmin(v1, v2), etaCrit, gi, gj);
+                rv += avRv<T>(rx, ry, rz, fmin(dist * hiInv, dist * __ldg(hInv + j)), etaCrit, gi, gj);
             }
             T wij = rv * rinv;
             T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
-            T vsig = T(0.5) * (ci + cj) - T(2) * wij;
-            maxv = (vsig > maxv) ? vsig : maxv;
+            maxvBits = maxBitsNonNeg(maxvBits, T(0.5) * (ci + cj) - T(2) * wij);
             // Atwood number |rhoi - rhoj| / (rhoi + rhoj) against Atmin / Atmax, without dividing
+            // and with the comparisons on bit patterns (all operands >= 0)
             T dr = fabs(rhoi - rhoj), sr = rhoi + rhoj;
             T am, bm;
-            if (dr < Atmin * sr) {
+            if (lessNonNeg(dr, Atmin * sr)) {
                 am = xmi2;
                 bm = xmj * xmj;
-            } else if (dr > Atmax * sr) {
+            } else if (lessNonNeg(Atmax * sr, dr)) {
                 am = xmi * xmj;
                 bm = am;
             } else {
@@ -523,15 +527,18 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
                 bm = xmj * xmj / q;
             }
             T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
-            T avx = T(0.5) * (av * a1i + bv * a1j);
-            T avy = T(0.5) * (av * a2i + bv * a2j);
-            T avz = T(0.5) * (av * a3i + bv * a3j);
-            avE += avx * vxij + avy * vyij + avz * vzij;
-            en += mj * am * (vxij * a1i + vyij * a2i + vzij * a3i);
-            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
-            mx += momi * a1i + momj * a1j + avx;
-            my += momi * a2i + momj * a2j + avy;
-            mz += momi * a3i + momj * a3j + avz;
+            T momi = mj * mprhoi * am, momj = __ldg(auxMprho + j) * bm;
+            T si = vxij * gix + vyij * giy + vzij * giz;
+            T sj = vxij * gjx + vyij * gjy + vzij * gjz;
+            T avWi = av * Wi, bvWj = bv * Wj;
+            // momentum: momi a_i + momj a_j + 0.5 (av a_i + bv a_j)
+            T ki = momi * Wi + T(0.5) * avWi, kj = momj * Wj + T(0.5) * bvWj;
+            mx -= ki * gix + kj * gjx;
+            my -= ki * giy + kj * gjy;
+            mz -= ki * giz + kj * gjz;
+            // energy: mj am (v_ij . a_i) and the viscous work 0.5 (av v_ij.a_i + bv v_ij.a_j)
+            en -= mj * am * Wi * si;
+            avE -= T(0.5) * (avWi * si + bvWj * sj);
         }
         if (valid) {
             avE = fmax(T(0), avE);
@@ -539,7 +546,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             st<T>(a.ax, i, -a.K * mx);
             st<T>(a.ay, i, -a.K * my);
             st<T>(a.az, i, -a.K * mz);
-            dt = courantDt(maxv, hi, ci, a.Kcour);
+            dt = courantDt(__longlong_as_double(maxvBits), hi, ci, a.Kcour);
         }
     } else {
         auto t = cm.target(i);
@@ -635,7 +642,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
                                                                     p->gradh);
     else
         gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                   p->xm, c->wh64.p, c->whd64.p, c->K, p->kx,
+                                                                   p->xm, c->whx64.p, c->whdx64.p, c->K, p->kx,
                                                                    p->gradh);
     return launched(c, "gradhKernel");
 }
@@ -698,7 +705,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
         a.wh = c->wh32.p;
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else {
-        a.wh = c->wh64.p;
+        a.wh = c->whx64.p;
         iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     }
     return launched(c, "iadDivvKernel");
@@ -723,7 +730,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         a.wh = c->wh32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else {
-        a.wh = c->wh64.p;
+        a.wh = c->whx64.p;
         avKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     }
     return launched(c, "avKernel");
@@ -784,7 +791,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
         if (avClean) meVeKernel<MixedTag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {
-        a.wh = c->wh64.p;
+        a.wh = c->whx64.p;
         if (avClean) meVeKernel<Fp64Tag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<Fp64Tag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     }

@@ -61,18 +61,26 @@ struct CoordFp64 {
                (pbc[1] && (t.y - twoH < lo[1] || t.y + twoH > hi[1])) ||
                (pbc[2] && (t.z - twoH < lo[2] || t.z + twoH > hi[2]));
     }
+    // legacy applyPBC with threshold 2h_i; the comparisons |r| > 2h run on the bit patterns
+    // (integer pipe): for twoH > 0, r > twoH <=> bits(r) > bits(twoH) and r < -twoH <=>
+    // bits(-r) > bits(twoH), negative values having negative signed patterns
+    __device__ __forceinline__ static double wrapLegacy(double r, long long twoHBits, double L)
+    {
+        const long long b = __double_as_longlong(r);
+        if (b > twoHBits) return r - L;
+        if ((b ^ (1LL << 63)) > twoHBits) return r + L;
+        return r;
+    }
     __device__ __forceinline__ void diff(const Target& t, int64_t j, double twoH, double& rx, double& ry,
                                          double& rz) const
     {
         rx = t.x - x[j];
         ry = t.y - y[j];
         rz = t.z - z[j];
-        if (pbc[0] && rx > twoH) rx -= L[0];
-        else if (pbc[0] && rx < -twoH) rx += L[0];
-        if (pbc[1] && ry > twoH) ry -= L[1];
-        else if (pbc[1] && ry < -twoH) ry += L[1];
-        if (pbc[2] && rz > twoH) rz -= L[2];
-        else if (pbc[2] && rz < -twoH) rz += L[2];
+        const long long hb = __double_as_longlong(twoH);
+        if (pbc[0]) rx = wrapLegacy(rx, hb, L[0]);
+        if (pbc[1]) ry = wrapLegacy(ry, hb, L[1]);
+        if (pbc[2]) rz = wrapLegacy(rz, hb, L[2]);
     }
     // legacy applyPBC only where it can change the result
     __device__ __forceinline__ void diffFast(const Target& t, int64_t j, double twoH, bool wrap, double& rx,
@@ -105,6 +113,76 @@ inline CoordFp64 coordFp64(const sphgb_ctx* c, const sphgb_particles* p)
 // 1/sqrt(r2) and sqrt(r2) in FP64 through the reciprocal square root: one special-function
 // seed plus FMA refinement instead of an IEEE sqrt and an IEEE divide
 __device__ __forceinline__ double invDist(double r2) { return rsqrt(r2); }
+
+// ---- FP64 pair-loop arithmetic kept off the FP64 pipe ----
+// On GB300 the SM's FP64 pipe retires 2 lanes per cycle: one warp-wide FP64 instruction holds it
+// for 16 cycles, in which the integer and FP32 pipes issue dozens of instructions.  The FP64
+// passes therefore do comparisons, table indexing and interval offsets on bit patterns.
+
+// x < 0 (false for -0.0, as the FP64 comparison) from the bit pattern
+__device__ __forceinline__ bool negative(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b < 0 && (b << 1) != 0;
+}
+
+// max(a, b) for b >= 0 (or +-0): bit patterns of non-negative doubles order like their values and
+// negative values have negative signed patterns
+__device__ __forceinline__ long long maxBitsNonNeg(long long bBits, double a)
+{
+    return max(bBits, __double_as_longlong(a));
+}
+
+// a < b for a, b >= 0
+__device__ __forceinline__ bool lessNonNeg(double a, double b)
+{
+    return __double_as_longlong(a) < __double_as_longlong(b);
+}
+
+// 1 / table spacing, formed as the reference forms it (sph/include/sph/table_lookup.hpp:17-19)
+constexpr double kTabInvDx = 1.0 / (2.0 / double(kTableSize - 1));
+
+// Interval of the kernel table for x = v / dx >= 0: k = floor(x) and x - k, taken from the bits
+// of x with integer operations (k < 0 marks x beyond the last interval, where the table reads 0).
+struct TabSlot {
+    int k;
+    double frac;
+};
+
+__device__ __forceinline__ TabSlot tabSlot(double x)
+{
+    constexpr int nInt = kTableSize - 1;
+    const long long b = __double_as_longlong(x);
+    const int e = int(b >> 52) - 1023;
+    if (e < 0) return {0, x};    // x < 1
+    if (e > 14) return {-1, 0.0};  // x >= 2^15 > nInt
+    const long long m = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const int sh = 52 - e;
+    const int k = int(m >> sh);
+    if (k >= nInt) return {-1, 0.0};
+    const long long fm = m & ((1LL << sh) - 1);  // (x - k) * 2^sh, exact
+    double frac = 0.0;
+    if (fm != 0) {
+        const int lz = __clzll(fm) - 11;  // moves the leading bit of fm to bit 52
+        frac = __longlong_as_double((static_cast<long long>(1075 - sh - lz) << 52) |
+                                    ((fm << lz) & 0xFFFFFFFFFFFFFLL));
+    }
+    return {k, frac};
+}
+
+// tabX[k] = {t[k], t[k+1] - t[k]}: W = t[k] + (t[k+1] - t[k]) (x - k), the reference's linear
+// interpolant (table_lookup.hpp:14-25) up to the rounding of its last two operations
+__device__ __forceinline__ double lookupX(const double2* __restrict__ tabX, const TabSlot& s)
+{
+    if (s.k < 0) return 0.0;
+    const double2 t = __ldg(tabX + s.k);
+    return fma(t.y, s.frac, t.x);
+}
+
+__device__ __forceinline__ double lookupX(const double2* __restrict__ tabX, double x)
+{
+    return lookupX(tabX, tabSlot(x));
+}
 
 // ---- Mixed coordinates: 21-bit grid cell per axis packed in 64 bits + FP32 in-cell offset ----
 constexpr int kGridBits = 21;
@@ -194,7 +272,10 @@ template<class T>
 __device__ __forceinline__ T artificialViscosity(T ai, T aj, T ci, T cj, T w)
 {
     T v = T(0);
-    if (w < T(0)) {
+    bool approaching;
+    if constexpr (std::is_same_v<T, double>) approaching = negative(w);
+    else approaching = w < T(0);
+    if (approaching) {
         T sig = (ai + aj) / T(4.0) * (ci + cj) - T(2.0) * w;
         v = -sig * w;
     }

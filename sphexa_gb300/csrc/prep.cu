@@ -66,6 +66,8 @@ __global__ void mixedCoordsKernel(const double* __restrict__ x, const double* __
     loc[i] = make_float4(l[0], l[1], l[2], float(1.0 / hi));
 }
 
+// per particle 1/h, 1/h^3 and (1/h) / dx: the last turns a pair distance into table-interval units
+// with one multiply
 __global__ void recipKernel(const double* __restrict__ h, int64_t n, double* __restrict__ out)
 {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -73,6 +75,7 @@ __global__ void recipKernel(const double* __restrict__ h, int64_t n, double* __r
     double hi = 1.0 / h[i];
     out[i] = hi;
     out[n + i] = hi * hi * hi;
+    out[2 * n + i] = hi * kTabInvDx;
 }
 
 __global__ void initDtWord(unsigned long long* p) { *p = 0x7ff0000000000000ull; /* +inf */ }
@@ -102,6 +105,20 @@ int buildTables(sphgb_ctx* c)
     SPHGB_CUDA(cudaMemcpy(c->whd64.p, whd.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice));
     SPHGB_CUDA(cudaMemcpy(c->wh32.p, wf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
     SPHGB_CUDA(cudaMemcpy(c->whd32.p, wdf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
+    // FP64 lookups read {t[k], t[k+1] - t[k]} in one 16-byte load; the difference is the one the
+    // reference interpolant forms (sph/include/sph/table_lookup.hpp:23)
+    std::vector<double> wx(2 * kTableSize), wdx(2 * kTableSize);
+    for (int i = 0; i < kTableSize; ++i) {
+        const bool last = i + 1 == kTableSize;
+        wx[2 * i] = wh[i];
+        wx[2 * i + 1] = last ? 0.0 : wh[i + 1] - wh[i];
+        wdx[2 * i] = whd[i];
+        wdx[2 * i + 1] = last ? 0.0 : whd[i + 1] - whd[i];
+    }
+    SPHGB_TRY(c->whx64.ensure(sizeof(double) * 2 * kTableSize));
+    SPHGB_TRY(c->whdx64.ensure(sizeof(double) * 2 * kTableSize));
+    SPHGB_CUDA(cudaMemcpy(c->whx64.p, wx.data(), sizeof(double) * 2 * kTableSize, cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->whdx64.p, wdx.data(), sizeof(double) * 2 * kTableSize, cudaMemcpyHostToDevice));
     c->tablesReady = true;
     return SPHGB_OK;
 }
@@ -119,7 +136,7 @@ int prepareMixed(sphgb_ctx* c, sphgb_particles* p, int64_t, int64_t)
 int prepareFp64(sphgb_ctx* c, sphgb_particles* p)
 {
     const int64_t n = p->n;
-    SPHGB_TRY(c->hInv64.ensure(sizeof(double) * 2 * n));
+    SPHGB_TRY(c->hInv64.ensure(sizeof(double) * 3 * n));
     recipKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(static_cast<const double*>(p->h), n, c->hInv64.as<double>());
     return launched(c, "recipKernel");
 }

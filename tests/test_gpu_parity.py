@@ -30,6 +30,22 @@ GROUPS = {"c11": "C", "c12": "C", "c13": "C", "c22": "C", "c23": "C", "c33": "C"
           "dV11": "D", "dV12": "D", "dV13": "D", "dV22": "D", "dV23": "D", "dV33": "D"}
 
 
+# Fields downstream of gradh (prho, accelerations, du) inherit its conditioning: gradh = 1 - X with
+# X = dhdrho * whomega, so a relative change e in X moves gradh by e |X| / |gradh|.  Near the open
+# surface of a clustered set gradh approaches 0 (|X| / |gradh| ~ 3e4 on the sphere sets) and any
+# change in the rounding of the FP64 sums is amplified by that factor, on every implementation.
+# The FP64 bar for those fields is scaled by max(1, kappa / 1e3), kappa the largest such ratio.
+GRADH_DOWNSTREAM = ("ax", "ay", "az", "du", "prho")
+
+
+def fp64_tol(ref: dict, name: str, variant: str) -> float:
+    if variant != "ve" or name not in GRADH_DOWNSTREAM or "gradh" not in ref:
+        return FP64_RTOL
+    g = np.asarray(ref["gradh"], dtype=np.float64)
+    kappa = float(np.max(np.abs(1.0 - g) / np.maximum(np.abs(g), 1e-300)))
+    return FP64_RTOL * max(1.0, kappa / 1e3)
+
+
 def field_scale(ref: dict, name: str) -> float:
     g = GROUPS.get(name)
     members = [k for k, v in GROUPS.items() if v == g and k in ref] if g else [name]
@@ -98,7 +114,7 @@ def test_fp64_sweep_matches_reference(gpu_ctx, name):
             continue
         ref = {q[4:]: g[q] for q in g if q.startswith("out_")}
         err = np.max(np.abs(r[name_f] - g[k])) / field_scale(ref, name_f)
-        assert err <= FP64_RTOL, f"{name_f}: {err:.3e}"
+        assert err <= fp64_tol(ref, name_f, str(g["variant"])), f"{name_f}: {err:.3e}"
     assert r["minDt"] == pytest.approx(float(g["minDtCourant"]), rel=1e-12)
 
 
@@ -153,7 +169,8 @@ def test_fp64_against_live_oracle_midsize(gpu_ctx, port, case):
         for f in ("rho", "c11", "c23", "ax", "ay", "az", "du") + (("xm", "kx", "gradh", "divv", "curlv", "alpha")
                                                                   if variant == "ve" else ()):
             err = np.max(np.abs(r[f] - ref[f])) / field_scale(ref, f)
-            assert err <= FP64_RTOL, f"{case} {variant} {f}: {err:.3e}"
+            tol = fp64_tol(ref, f, variant)
+            assert err <= tol, f"{case} {variant} {f}: {err:.3e} (bar {tol:.1e})"
 
 
 def test_individual_passes_equal_sweep(gpu_ctx):
