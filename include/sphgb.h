@@ -96,6 +96,12 @@ int sphgb_create(sphgb_ctx** ctx, int device);
 int sphgb_destroy(sphgb_ctx* ctx);
 int sphgb_set_stream(sphgb_ctx* ctx, void* cuda_stream);
 int sphgb_set_params(sphgb_ctx* ctx, const sphgb_params* params);
+/* Summation order of the FP64 VE momentum-energy pass (no reference counterpart; the reference's
+ * GPU pass is order-fixed, hydro_ve/momentum_energy_gpu.cu:53-144).  on = 0 (default): when the
+ * lists cover every particle, each pair whose two ends list each other is evaluated once and the
+ * neighbour's share is added with FP64 atomics, so the last bits of ax ay az du can differ from
+ * run to run.  on = 1: every list owner sums its own pairs in list order, bitwise reproducible. */
+int sphgb_set_deterministic(sphgb_ctx* ctx, int32_t on);
 int sphgb_default_params(sphgb_params* params);
 /* kernel normalisation constant K used by the pair passes */
 int sphgb_get_kernel_K(sphgb_ctx* ctx, double* K);

@@ -25,27 +25,25 @@ namespace {
 
 constexpr int kAdjBlock = 128;
 
-// interpolant value and slope (dw/dv) of the interval holding v
-__device__ __forceinline__ double lookupSlope(const double* __restrict__ tab, double v, double& slope)
+// interpolant value and slope (dw/dv) of the interval holding v, from the interleaved table
+// {t[k], t[k+1] - t[k]} with the interval taken from the bits of v / dx (as the forward passes)
+__device__ __forceinline__ double lookupSlope(const double2* __restrict__ tabX, double v, double& slope)
 {
-    constexpr int nInt = kTableSize - 1;
-    constexpr double dx = 2.0 / double(nInt);
-    constexpr double invDx = 1.0 / dx;
-    int idx = int(v * invDx);
-    if (idx >= nInt) {
+    const TabSlot s = tabSlot(v * kTabInvDx);
+    if (s.k < 0) {
         slope = 0.0;
         return 0.0;
     }
-    double a = __ldg(tab + idx), b = __ldg(tab + idx + 1);
-    slope = (b - a) * invDx;
-    return a + slope * (v - double(idx) * dx);
+    const double2 t = __ldg(tabX + s.k);
+    slope = t.y * kTabInvDx;
+    return fma(t.y, s.frac, t.x);
 }
 
 struct AdjArgs {
     // forward state
     const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *rho, *p, *c;
     const double *c11, *c12, *c13, *c22, *c23, *c33;
-    const double* wh;
+    const double2* wh;  // interleaved {t[k], t[k+1] - t[k]}
     double K, gamma;
     DevBox box;
     // lists: own (transposed layout) and incoming (CSR by neighbour)
@@ -111,15 +109,10 @@ __device__ __forceinline__ Side loadPos(const AdjArgs& a, int64_t i)
 // r = x_i - x_j with the legacy periodic fold at 2 h_i (box.hpp:216-238)
 __device__ __forceinline__ void pairR(const DevBox& b, const Side& I, const Side& J, double r[3])
 {
-    const double twoH = 2.0 * I.h;
+    const long long twoHBits = __double_as_longlong(2.0 * I.h);
     const double d[3] = {I.x - J.x, I.y - J.y, I.z - J.z};
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double v = d[k];
-        if (b.pbc[k] && v > twoH) v -= b.L[k];
-        else if (b.pbc[k] && v < -twoH) v += b.L[k];
-        r[k] = v;
-    }
+    for (int k = 0; k < 3; ++k) r[k] = b.pbc[k] ? CoordFp64::wrapLegacy(d[k], twoHBits, b.L[k]) : d[k];
 }
 
 __device__ __forceinline__ void symv(const double C[6], const double r[3], double out[3])
@@ -149,7 +142,7 @@ struct PairGrad {
 };
 
 template<bool WantI, bool WantJ>
-__device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, const Side& I, const Side& J,
+__device__ __forceinline__ void mePairAdj(const DevBox& b, const double2* tab, const Side& I, const Side& J,
                                           const double gA[3], double gE, PairGrad& g)
 {
     double r[3];
@@ -168,7 +161,8 @@ __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, co
     const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
     const double W = rv * rinv;
     const double cs = I.c + J.c;
-    const double visc = W < 0.0 ? 0.5 * (-(0.5 * cs - 2.0 * W) * W) : 0.0;
+    const bool approaching = negative(W);
+    const double visc = approaching ? 0.5 * (-(0.5 * cs - 2.0 * W) * W) : 0.0;
     const double qi = J.m * I.poR2, si = I.moR, tj = J.moR, uj = J.poR;
     const double alpha = Wi * (qi + visc * si), beta = tj * Wj * (uj + visc);
     const double alphaP = Wi * (2.0 * qi + visc * si), betaP = visc * tj * Wj;
@@ -195,7 +189,7 @@ __device__ __forceinline__ void mePairAdj(const DevBox& b, const double* tab, co
     const double buj = bBeta * tj * Wj;
 
     double bW = 0.0, bcs = 0.0;
-    if (W < 0.0) {
+    if (approaching) {
         bW = bVisc * 0.5 * (-0.5 * cs + 4.0 * W);
         bcs = bVisc * 0.5 * (-0.5 * W);
     }
@@ -697,7 +691,7 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     a.c22 = static_cast<const double*>(p->c22);
     a.c23 = static_cast<const double*>(p->c23);
     a.c33 = static_cast<const double*>(p->c33);
-    a.wh = c->wh64.as<double>();
+    a.wh = c->whx64.as<double2>();
     a.K = c->K;
     a.gamma = c->prm.gamma;
     a.box = c->box;

@@ -137,7 +137,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
-                    &c->whdx64};
+                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->meAcc};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -160,6 +160,13 @@ int sphgb_set_params(sphgb_ctx* c, const sphgb_params* p)
     bool tables = p->sincIndex != c->prm.sincIndex || !c->tablesReady;
     c->prm = *p;
     if (tables) SPHGB_TRY(buildTables(c));
+    return SPHGB_OK;
+}
+
+int sphgb_set_deterministic(sphgb_ctx* c, int32_t on)
+{
+    if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;
+    c->deterministic = on != 0;
     return SPHGB_OK;
 }
 

@@ -98,6 +98,14 @@ struct sphgb_ctx {
     uint32_t nbrNgmax = 0;
     sphgb::DBuf nbr, ncount, active, counters;
     bool haveNbr = false;
+    // owned pair lists of the pair-once momentum-energy pass: owned[k * stride + (i - first)] =
+    // j | mutual << 31 for the pairs i evaluates, ownedCount per particle; valid for epoch ownedEpoch
+    sphgb::DBuf owned, ownedCount;
+    int64_t ownedEpoch = -1;
+    // summation mode of the FP64 VE momentum-energy pass, and its per-particle accumulators
+    // (mx, my, mz, en, avE as doubles, the signal-velocity maximum as ordered bits)
+    bool deterministic = false;
+    sphgb::DBuf meAcc;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -36,6 +36,7 @@ __global__ void veAuxKernel(int64_t n, const void* m, const void* kx, const void
     if (prho) aux[3 * n + i] = mi * ld<T>(prho, i);
     if constexpr (std::is_same_v<T, double>) aux[4 * n + i] = log(xmi);
     else aux[4 * n + i] = log2f(xmi);
+    aux[5 * n + i] = T(1) / rho;
 }
 
 template<class P>
@@ -43,7 +44,7 @@ int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 {
     using T = typename P::T;
     const int64_t n = p->n;
-    SPHGB_TRY(c->aux.ensure(sizeof(T) * 5 * n));
+    SPHGB_TRY(c->aux.ensure(sizeof(T) * 6 * n));
     veAuxKernel<T><<<gridFor(n, 256), 256, 0, c->stream>>>(n, p->m, p->kx, p->xm, p->prho, c->aux.as<T>());
     return launched(c, "veAuxKernel");
 }
@@ -397,8 +398,8 @@ struct MeVeArgs {
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
     const void* wh;
-    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3
-    const void* aux;       // rho, m/rho, xm/kx, m*prho, ln xm (5 x n)
+    const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
+    const void* aux;       // rho, m/rho, xm/kx, m*prho, ln xm, 1/rho (6 x n)
     int64_t n;
     double K;
     float Kcour;
@@ -406,6 +407,11 @@ struct MeVeArgs {
     double* du;
     float* groupDt;
     unsigned long long* minDt;
+    // pair-once form: owned pair lists (j | mutual << 31) with their counts, and the accumulators
+    // (mx my mz en avE, maxv bits) x n
+    const uint32_t* owned;
+    const uint32_t* ownedCount;
+    double* acc;
 };
 
 template<class T>
@@ -626,6 +632,145 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
     if (a.minDt) blockMinDt(dt, a.minDt);
 }
 
+// FP64 VE momentum-energy with one evaluation per mutual pair, for lists that cover every particle.
+// i walks its owned list: every pair of its list that j does not list back, and half of the
+// mutual pairs (the other half is in the owned lists of the other ends).  The two ends' terms follow from one
+// another (momentum_energy_kern.hpp:125-210): r and v_ij change sign, so G = c r changes sign at
+// both ends and v_ij . G does not; W_i and W_j, the Atwood weights (a_mom, b_mom), m_j and m_i, and
+// 1/rho_i and 1/rho_j trade places; the viscosity and the signal velocity are symmetric.  i's terms
+// stay in registers; j's go to its accumulators with FP64 atomics (the signal-velocity maximum as an
+// integer maximum of non-negative bit patterns).
+__global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordFp64 cf, MeVeArgs a)
+{
+    using T = double;
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned nOwned = __ldg(a.ownedCount + ii);
+    const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+    const T* aux = static_cast<const T*>(a.aux);
+    const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n,
+            *auxRhoInv = aux + 5 * a.n;
+    const double* hInv3 = a.hInv64 + a.n;
+    const double* hInvDx = a.hInv64 + 2 * a.n;
+    const T *vxA = static_cast<const T*>(a.vx), *vyA = static_cast<const T*>(a.vy),
+            *vzA = static_cast<const T*>(a.vz), *prhoA = static_cast<const T*>(a.prho);
+    constexpr T Atmin = 0.1, Atmax = 0.2, ramp = 1.0 / (Atmax - Atmin);
+
+    const T hi = ld<T>(a.h, i), mi = ld<T>(a.m, i), ci = ld<T>(a.c, i), ai = ld<T>(a.alpha, i);
+    const T xmi = ld<T>(a.xm, i), prhoi = prhoA[i];
+    const T rhoi = auxRho[i], lnxmi = auxLnXm[i], rhoiInv = auxRhoInv[i], moRi = auxMoR[i], mprhoi = auxMprho[i];
+    const T vxi = vxA[i], vyi = vyA[i], vzi = vzA[i];
+    const T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
+    const T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
+    const T xmi2 = xmi * xmi;
+    auto t = cf.target(i);
+    const T hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
+    const bool wrap = cf.needsWrap(t, twoH);
+    T mx = 0, my = 0, mz = 0, en = 0, avE = 0;
+    long long maxvBits = 0;
+    double *accX = a.acc, *accY = a.acc + a.n, *accZ = a.acc + 2 * a.n, *accE = a.acc + 3 * a.n,
+           *accV = a.acc + 4 * a.n;
+    long long* accS = reinterpret_cast<long long*>(a.acc + 5 * a.n);
+    for (unsigned k = 0; k < nOwned; ++k) {
+        const uint32_t e = __ldg(a.owned + int64_t(k) * lv.stride + ii);
+        const uint32_t j = e & 0x7fffffffu;
+        const bool mutual = (e >> 31) != 0;
+        T rx, ry, rz;
+        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+        T r2 = rx * rx + ry * ry + rz * rz;
+        T rinv = invDist(r2);
+        T dist = r2 * rinv;
+        T vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
+        T Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
+        T Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
+        T gix = c11i * rx + c12i * ry + c13i * rz;
+        T giy = c12i * rx + c22i * ry + c23i * rz;
+        T giz = c13i * rx + c23i * ry + c33i * rz;
+        T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
+        T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
+        T gjx = c11j * rx + c12j * ry + c13j * rz;
+        T gjy = c12j * rx + c22j * ry + c23j * rz;
+        T gjz = c13j * rx + c23j * ry + c33j * rz;
+        T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
+        T rhoj = __ldg(auxRho + j);
+        T rv = rx * vxij + ry * vyij + rz * vzij;
+        T wij = rv * rinv;
+        T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
+        const T vsig = T(0.5) * (ci + cj) - T(2) * wij;
+        maxvBits = maxBitsNonNeg(maxvBits, vsig);
+        T dr = fabs(rhoi - rhoj), sr = rhoi + rhoj;
+        T am, bm;
+        if (lessNonNeg(dr, Atmin * sr)) {
+            am = xmi2;
+            bm = xmj * xmj;
+        } else if (lessNonNeg(Atmax * sr, dr)) {
+            am = xmi * xmj;
+            bm = am;
+        } else {
+            T s = ramp * (dr / sr - Atmin);
+            T q = exp(s * (__ldg(auxLnXm + j) - lnxmi));
+            am = xmi2 * q;
+            bm = xmj * xmj / q;
+        }
+        T si = vxij * gix + vyij * giy + vzij * giz;
+        T sj = vxij * gjx + vyij * gjy + vzij * gjz;
+        {  // i's terms
+            T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
+            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
+            T avWi = av * Wi, bvWj = bv * Wj;
+            T ki = momi * Wi + T(0.5) * avWi, kj = momj * Wj + T(0.5) * bvWj;
+            mx -= ki * gix + kj * gjx;
+            my -= ki * giy + kj * gjy;
+            mz -= ki * giz + kj * gjz;
+            en -= mj * am * Wi * si;
+            avE -= T(0.5) * (avWi * si + bvWj * sj);
+        }
+        if (mutual) {  // j's terms of the same pair
+            T av = mi * __ldg(auxRhoInv + j) * visc, bv = moRi * visc;
+            T momi = mi * prhoA[j] * bm, momj = mprhoi * am;
+            T avWj = av * Wj, bvWi = bv * Wi;
+            T kj = momi * Wj + T(0.5) * avWj, ki = momj * Wi + T(0.5) * bvWi;
+            atomicAdd(accX + j, kj * gjx + ki * gix);
+            atomicAdd(accY + j, kj * gjy + ki * giy);
+            atomicAdd(accZ + j, kj * gjz + ki * giz);
+            atomicAdd(accE + j, -(mi * bm * Wj * sj));
+            atomicAdd(accV + j, -T(0.5) * (avWj * sj + bvWi * si));
+            atomicMax(accS + j, __double_as_longlong(vsig));
+        }
+    }
+    atomicAdd(accX + i, mx);
+    atomicAdd(accY + i, my);
+    atomicAdd(accZ + i, mz);
+    atomicAdd(accE + i, en);
+    atomicAdd(accV + i, avE);
+    atomicMax(accS + i, maxvBits);
+}
+
+__global__ void __launch_bounds__(kPairBlock) meVeOnceFinish(ListView lv, MeVeArgs a)
+{
+    const int64_t i0 = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const bool valid = i0 < lv.last;
+    double dt = INFINITY;
+    if (valid) {
+        const int64_t i = i0;
+        const double prhoi = ld<double>(a.prho, i);
+        const double avE = fmax(0.0, a.acc[4 * a.n + i]);
+        a.du[i] = a.K * (prhoi * a.acc[3 * a.n + i] + 0.5 * avE);
+        st<double>(a.ax, i, -a.K * a.acc[i]);
+        st<double>(a.ay, i, -a.K * a.acc[a.n + i]);
+        st<double>(a.az, i, -a.K * a.acc[2 * a.n + i]);
+        const long long mb = reinterpret_cast<const long long*>(a.acc + 5 * a.n)[i];
+        dt = courantDt(__longlong_as_double(mb), ld<double>(a.h, i), ld<double>(a.c, i), a.Kcour);
+    }
+    if (a.groupDt) {
+        double g = dt;
+        for (int o = 16; o > 0; o >>= 1) g = fmin(g, __shfl_xor_sync(0xffffffffu, g, o));
+        if ((threadIdx.x & 31) == 0 && i0 < lv.last) a.groupDt[(i0 - lv.first) / 32] = float(g);
+    }
+    if (a.minDt) blockMinDt(dt, a.minDt);
+}
+
 }  // namespace
 
 int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
@@ -792,6 +937,21 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {
         a.wh = c->whx64.p;
+        // one evaluation per mutual pair when the lists cover all particles and the order may vary
+        const bool once = !avClean && !c->deterministic && c->ownedEpoch == c->nbrEpoch && first == 0 &&
+                          last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
+        if (once) {
+            SPHGB_TRY(c->meAcc.ensure(sizeof(double) * 6 * size_t(p->n)));
+            SPHGB_CUDA(cudaMemsetAsync(c->meAcc.p, 0, sizeof(double) * 6 * size_t(p->n), c->stream));
+            a.owned = c->owned.as<uint32_t>();
+            a.ownedCount = c->ownedCount.as<uint32_t>();
+            a.acc = c->meAcc.as<double>();
+            meVeOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a);
+            SPHGB_TRY(launched(c, "meVeOnceKernel"));
+            meVeOnceFinish<<<blocks, kPairBlock, 0, c->stream>>>(lv, a);
+            SPHGB_TRY(launched(c, "meVeOnceFinish"));
+            return endDtReduction(c, a.minDt, minDt);
+        }
         if (avClean) meVeKernel<Fp64Tag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<Fp64Tag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     }

@@ -343,6 +343,112 @@ __global__ void exportKernel(const uint32_t* __restrict__ nbr, const uint32_t* _
     for (uint32_t q = 0; q < c; ++q) out[k * ngmax + q] = nbr[int64_t(q) * stride + k];
 }
 
+// ---- owned pair lists for the pair-once momentum-energy pass ----
+// Pair (i, j) is mutual when the k-th neighbour j of i also lists i: j has a list (inside the
+// searched range), i lies within j's capped list (the ngmax smallest indices), and |x_i - x_j|^2 <
+// 4 h_j^2 in the reference's distanceSq semantics for target j (rint minimum image when the 2h box of
+// j leaves the periodic box).  Decided in FP32 on the grid form with a relative margin of 2^-17 (the
+// grid-form d2 and the FP32 radius are within a few 2^-24 relative of the exact values); pairs inside
+// the margin or crossing a periodic face take the exact FP64 test.
+// i owns every non-mutual entry and half of its mutual ones: the mutual pair {i, j} belongs to the
+// smaller index when i + j is odd and to the larger when it is even, so each particle owns about
+// half of its mutual pairs wherever it sits in the SFC order.  The owned entries are written
+// compacted, owned[k * stride + (i - first)] = j | mutual << 31, with their count per particle.
+struct MutualArgs {
+    const double *x, *y, *z;
+    const void* h;
+    int hIsFloat;
+    const u64* cell;
+    const float4* loc;
+    float u[3];
+    DevBox box;
+    int64_t first, last, stride;
+    uint32_t ngmax;
+    const uint32_t* nbr;
+    const uint32_t* count;
+    uint32_t* owned;
+    uint32_t* ownedCount;
+};
+
+__device__ bool mutualExact(const MutualArgs& a, int64_t i, int64_t j, double hj)
+{
+    const DevBox& b = a.box;
+    const double r2 = __dmul_rn(__dmul_rn(4.0, hj), hj);
+    const double twoH = __dmul_rn(2.0, hj);
+    const double xj = a.x[j], yj = a.y[j], zj = a.z[j];
+    bool usePbc = false;
+    if (b.pbc[0] | b.pbc[1] | b.pbc[2]) {
+        const bool inside = __dsub_rn(xj, twoH) >= b.lo[0] && __dsub_rn(yj, twoH) >= b.lo[1] &&
+                            __dsub_rn(zj, twoH) >= b.lo[2] && __dadd_rn(xj, twoH) <= b.hi[0] &&
+                            __dadd_rn(yj, twoH) <= b.hi[1] && __dadd_rn(zj, twoH) <= b.hi[2];
+        usePbc = !inside;
+    }
+    double dx = __dsub_rn(a.x[i], xj), dy = __dsub_rn(a.y[i], yj), dz = __dsub_rn(a.z[i], zj);
+    if (usePbc) {
+        if (b.pbc[0]) dx = foldRint(dx, b, 0);
+        if (b.pbc[1]) dy = foldRint(dy, b, 1);
+        if (b.pbc[2]) dz = foldRint(dz, b, 2);
+    }
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return d2 < r2;
+}
+
+__device__ bool mutualPair(const MutualArgs& a, int64_t i, int ci[3], float4 li, int64_t j)
+{
+    if (j < a.first || j >= a.last) return false;
+    const int64_t jj = j - a.first;
+    if (__ldg(a.count + jj) > a.ngmax && i > int64_t(__ldg(a.nbr + int64_t(a.ngmax - 1) * a.stride + jj)))
+        return false;
+    int cj[3];
+    unpackCell(__ldg(a.cell + j), cj);
+    const float4 lj = __ldg(a.loc + j);
+    const float lv[3] = {li.x - lj.x, li.y - lj.y, li.z - lj.z};
+    constexpr int R = 1 << kGridBits;
+    bool wrapped = false;
+    float r[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int d = ci[k] - cj[k];
+        if (a.box.pbc[k]) {
+            if (d > R / 2) {
+                d -= R;
+                wrapped = true;
+            } else if (d < -R / 2) {
+                d += R;
+                wrapped = true;
+            }
+        }
+        r[k] = fmaf(float(d), a.u[k], lv[k]);
+    }
+    const double hj = loadH(a.h, a.hIsFloat, j);
+    if (wrapped) return mutualExact(a, i, j, hj);
+    const float d2 = fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2]));
+    const float tf = 2.f * float(hj);
+    const float R2 = tf * tf, eps = 0x1p-17f * R2;
+    if (d2 < R2 - eps) return true;
+    if (d2 > R2 + eps) return false;
+    return mutualExact(a, i, j, hj);
+}
+
+__global__ void __launch_bounds__(128) ownedListKernel(MutualArgs a)
+{
+    const int64_t i = a.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= a.last) return;
+    const int64_t ii = i - a.first;
+    const unsigned nc = min(__ldg(a.count + ii), a.ngmax);
+    int ci[3];
+    unpackCell(__ldg(a.cell + i), ci);
+    const float4 li = __ldg(a.loc + i);
+    unsigned cnt = 0;
+    for (unsigned k = 0; k < nc; ++k) {
+        const uint32_t j = __ldg(a.nbr + int64_t(k) * a.stride + ii);
+        const bool m = mutualPair(a, i, ci, li, j);
+        const bool own = !m || ((((i ^ int64_t(j)) & 1) != 0) == (i < int64_t(j)));
+        if (own) a.owned[int64_t(cnt++) * a.stride + ii] = j | (m ? 0x80000000u : 0u);
+    }
+    a.ownedCount[ii] = cnt;
+}
+
 __global__ void fillOnes(uint32_t* p, int64_t n)
 {
     int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -402,6 +508,35 @@ int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, c
     unsigned blocks = unsigned((groups + kWarpsPerBlock - 1) / kWarpsPerBlock);
     nbrGroupKernel<<<blocks, kNbrBlock, 0, c->stream>>>(a);
     return launched(c, "nbrGroupKernel");
+}
+
+int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int hIsFloat)
+{
+    const int64_t nWork = c->nbrLast - c->nbrFirst;
+    SPHGB_TRY(c->owned.ensure(sizeof(uint32_t) * size_t(c->nbrNgmax) * size_t(c->nbrStride)));
+    SPHGB_TRY(c->ownedCount.ensure(sizeof(uint32_t) * size_t(c->nbrStride)));
+    MutualArgs a;
+    a.x = x;
+    a.y = y;
+    a.z = z;
+    a.h = h;
+    a.hIsFloat = hIsFloat;
+    a.cell = c->gridKey.as<u64>();
+    a.loc = c->gridLoc.as<float4>();
+    for (int k = 0; k < 3; ++k) a.u[k] = float(c->box.L[k] / double(1 << kGridBits));
+    a.box = c->box;
+    a.first = c->nbrFirst;
+    a.last = c->nbrLast;
+    a.stride = c->nbrStride;
+    a.ngmax = c->nbrNgmax;
+    a.nbr = c->nbr.as<uint32_t>();
+    a.count = c->ncount.as<uint32_t>();
+    a.owned = c->owned.as<uint32_t>();
+    a.ownedCount = c->ownedCount.as<uint32_t>();
+    ownedListKernel<<<gridFor(nWork, 128), 128, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "ownedListKernel"));
+    c->ownedEpoch = c->nbrEpoch;
+    return SPHGB_OK;
 }
 
 int prepareLists(sphgb_ctx* c, const double* x, const double* y, const double* z, int64_t first, int64_t last,
@@ -492,6 +627,8 @@ int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     c->haveNbr = true;
     c->precisionBuilt = p->precision;
     c->xBuilt = p->x;
+    // the pair-once FP64 momentum-energy pass reads the owned lists; the mixed passes do not
+    if (p->precision == SPHGB_FP64) SPHGB_TRY(buildOwned(c, p->x, p->y, p->z, p->h, hf));
     return c->stats.h_fails > 0 ? SPHGB_ERR_NOCONV : SPHGB_OK;
 }
 
@@ -515,6 +652,7 @@ int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const dou
     c->haveNbr = true;
     c->precisionBuilt = hPrec;
     c->xBuilt = x;
+    if (hPrec == SPHGB_FP64) SPHGB_TRY(buildOwned(c, x, y, z, h, 0));
     return SPHGB_OK;
 }
 

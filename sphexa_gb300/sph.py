@@ -75,6 +75,11 @@ class Context:
             setattr(self.params, k, v)
         check(self.lib.sphgb_set_params(self.h, C.byref(self.params)), "sphgb_set_params")
 
+    def set_deterministic(self, on: bool) -> None:
+        """True: every pass sums in list order (bitwise reproducible); False (default): the FP64 VE
+        momentum-energy pass evaluates mutual pairs once and scatters with FP64 atomics."""
+        check(self.lib.sphgb_set_deterministic(self.h, int(bool(on))), "sphgb_set_deterministic")
+
     @property
     def K(self) -> float:
         k = C.c_double()

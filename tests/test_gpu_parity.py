@@ -173,6 +173,47 @@ def test_fp64_against_live_oracle_midsize(gpu_ctx, port, case):
             assert err <= tol, f"{case} {variant} {f}: {err:.3e} (bar {tol:.1e})"
 
 
+@pytest.mark.parametrize("case", ["fourier", "sphere", "random_open_capped"])
+def test_pair_once_momentum_energy_matches_ordered_sums(gpu_ctx, case):
+    """The FP64 VE momentum-energy pass with one evaluation per mutual pair (atomics) against the
+    order-fixed pass on the same lists: rounding-level agreement, identical Courant dt, and the
+    pair-once path is the one that ran (one more launch: accumulate + finish)."""
+    from sphexa_gb300 import sph, workloads as W
+    wl = {"fourier": lambda: W.fourier(16, seed=51, rho_seed=52, v_seed=53),
+          "sphere": lambda: W.sphere(20000, seed=54),
+          "random_open_capped": lambda: W.random_cube(6000, seed=55, periodic=False, h=0.09)}[case]()
+    ctx = gpu_ctx
+    ctx.set_params(ngmax=wl.params["ngmax"], ng0=wl.params["ng0"])
+    out, launches = {}, {}
+    for det in (True, False):
+        ctx.set_deterministic(det)
+        d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+        box = sph.Box(wl.box.copy(), wl.bc.copy())
+        sph.Domain(ctx, box).sync(d)
+        # fixed h (cstone::findNeighbors): lists above ngmax stay capped
+        sph.find_neighbors(ctx, d.x, d.y, d.z, d.h, 0, wl.n, int(wl.params["ngmax"]))
+        sph.compute_xmass(ctx, d)
+        sph.compute_ve_def_gradh(ctx, d)
+        sph.compute_eos(ctx, d)
+        sph.compute_iad_divv_curlv(ctx, d)
+        sph.compute_av_switches(ctx, d)
+        l0 = ctx.launches()
+        sph.compute_momentum_energy(ctx, d, False)
+        launches[det] = ctx.launches() - l0
+        out[det] = {f: getattr(d, f).cpu().numpy() for f in ("ax", "ay", "az", "du")}
+        out[det]["minDt"] = d.minDtCourant
+    ctx.set_deterministic(False)
+    assert launches[False] == launches[True] + 1
+    a0 = np.stack([out[True][f] for f in ("ax", "ay", "az")], 1)
+    a1 = np.stack([out[False][f] for f in ("ax", "ay", "az")], 1)
+    assert np.max(np.abs(a1 - a0)) <= 1e-12 * np.max(np.abs(a0))
+    du0, du1 = out[True]["du"], out[False]["du"]
+    assert np.max(np.abs(du1 - du0)) <= 1e-12 * max(np.max(np.abs(du0)), 1e-300)
+    assert out[False]["minDt"] == out[True]["minDt"]
+    if case == "random_open_capped":
+        assert ctx.stats()["capped"] > 0
+
+
 def test_individual_passes_equal_sweep(gpu_ctx):
     """The reference-named entry points called one by one give the sweep's results."""
     import torch
