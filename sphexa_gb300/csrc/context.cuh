@@ -102,10 +102,10 @@ struct sphgb_ctx {
     // j | mutual << 31 for the pairs i evaluates, ownedCount per particle; valid for epoch ownedEpoch
     sphgb::DBuf owned, ownedCount;
     int64_t ownedEpoch = -1;
-    // summation mode of the FP64 VE momentum-energy pass, and its per-particle accumulators
-    // (mx, my, mz, en, avE as doubles, the signal-velocity maximum as ordered bits)
+    // summation mode of the FP64 passes (order-fixed, or one evaluation per mutual pair) and the
+    // per-particle accumulators of the pair-once passes (up to 6 x n doubles)
     bool deterministic = false;
-    sphgb::DBuf meAcc;
+    sphgb::DBuf pairAcc;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -61,6 +61,45 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
     }
 }
 
+// FP64 xmass / density with one evaluation per mutual pair over the owned lists: i adds
+// W(d / h_i) m_j, and for a mutual pair j receives W(d / h_j) m_i by an FP64 atomic
+__global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
+                                                               const double* h, const double* m, const double2* tab,
+                                                               const double* hInvDx, double* acc)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned no = ov.size(ii);
+    auto t = cf.target(i);
+    const double hi = h[i], mi = m[i], twoH = 2.0 * hi, hiInvDx = hInvDx[i];
+    const bool wrap = cf.needsWrap(t, twoH);
+    double rho0 = 0.0;
+    for (unsigned k = 0; k < no; ++k) {
+        bool mutual;
+        const uint32_t j = ov.at(ii, k, mutual);
+        double rx, ry, rz;
+        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double dist = r2 * invDist(r2);
+        rho0 += lookupX(tab, dist * hiInvDx) * __ldg(m + j);
+        if (mutual) atomicAdd(acc + j, lookupX(tab, dist * __ldg(hInvDx + j)) * mi);
+    }
+    atomicAdd(acc + i, rho0);
+}
+
+template<bool StoreRho>
+__global__ void xmassOnceFinish(int64_t first, int64_t last, const double* h, const double* m, double K,
+                                const double* acc, double* out)
+{
+    const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    const double hi = h[i], mi = m[i];
+    const double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
+    const double xm = mi / ((mi + acc[i]) * K * h3Inv);
+    out[i] = StoreRho ? mi / xm : xm;
+}
+
 // ---------------------------------------------------------------- EOS
 template<class P>
 __global__ void eosStdKernel(int64_t first, int64_t last, const double* u, const void* rho, double gamma, void* p,
@@ -328,6 +367,26 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
     CoordMixed cm = coordMixed(c);
     const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->wh32.p;
     unsigned blocks = gridFor(last - first, kPairBlock);
+    // pair-once for the VE xmass; the std density keeps the order-fixed walk
+    if (std::is_same_v<P, Fp64Tag> && !storeRho && pairOnce(c, p, first, last)) {
+        const int64_t n = p->n;
+        SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * size_t(n)));
+        SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * size_t(n), c->stream));
+        xmassOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
+            lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
+            c->whx64.as<double2>(), c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
+        SPHGB_TRY(launched(c, "xmassOnceKernel"));
+        const unsigned eb = gridFor(last - first, 256);
+        if (storeRho)
+            xmassOnceFinish<true><<<eb, 256, 0, c->stream>>>(first, last, static_cast<const double*>(p->h),
+                                                              static_cast<const double*>(p->m), c->K,
+                                                              c->pairAcc.as<double>(), static_cast<double*>(out));
+        else
+            xmassOnceFinish<false><<<eb, 256, 0, c->stream>>>(first, last, static_cast<const double*>(p->h),
+                                                               static_cast<const double*>(p->m), c->K,
+                                                               c->pairAcc.as<double>(), static_cast<double*>(out));
+        return launched(c, "xmassOnceFinish");
+    }
     if (storeRho)
         xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
     else

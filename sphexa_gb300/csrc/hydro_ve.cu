@@ -306,6 +306,22 @@ struct AvArgs {
     void* alpha;
 };
 
+// alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
+template<class T>
+__device__ __forceinline__ T avAlpha(const AvArgs& a, T alpha_i, T hi, T ci, T divvi, T vsig_i, T gx, T gy, T gz)
+{
+    T gdv = sqrt(gx * gx + gy * gy + gz * gz);
+    T aloc = 0.0;
+    if (divvi < T(0)) {
+        T ac = hi * hi * gdv;
+        aloc = T(a.alphamax) * ac / (ac + hi * fabs(divvi) + T(0.05) * ci);
+    }
+    if (aloc >= alpha_i) return aloc;
+    T decay = hi / (T(a.decay) * vsig_i);
+    T adot = (aloc >= T(a.alphamin)) ? (aloc - alpha_i) / decay : (T(a.alphamin) - alpha_i) / decay;
+    return alpha_i + adot * T(a.dt);
+}
+
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf, CoordMixed cm, AvArgs a)
 {
@@ -375,21 +391,7 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
         gy = T(-double(kh3) * (double(c12) * Sx + double(c22) * Sy + double(c23) * Sz));
         gz = T(-double(kh3) * (double(c13) * Sx + double(c23) * Sy + double(c33) * Sz));
     }
-    // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
-    T alpha_i = ld<T>(a.alpha, i);
-    T gdv = sqrt(gx * gx + gy * gy + gz * gz);
-    T aloc = 0.0;
-    if (divvi < T(0)) {
-        T ac = hi * hi * gdv;
-        aloc = T(a.alphamax) * ac / (ac + hi * fabs(divvi) + T(0.05) * ci);
-    }
-    if (aloc >= alpha_i) alpha_i = aloc;
-    else {
-        T decay = hi / (T(a.decay) * vsig_i);
-        T adot = (aloc >= T(a.alphamin)) ? (aloc - alpha_i) / decay : (T(a.alphamin) - alpha_i) / decay;
-        alpha_i += adot * T(a.dt);
-    }
-    st<T>(a.alpha, i, alpha_i);
+    st<T>(a.alpha, i, avAlpha<T>(a, ld<T>(a.alpha, i), hi, ci, divvi, vsig_i, gx, gy, gz));
 }
 
 // ---------------------------------------------------------------- momentum and energy (VE)
@@ -632,6 +634,150 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
     if (a.minDt) blockMinDt(dt, a.minDt);
 }
 
+// FP64 gradh with one evaluation per mutual pair over the owned lists.  i adds w_i xm_j,
+// dterh_i xm_j and dterh_i m_j (veDefGradhJLoop, ve_def_gradh_kern.hpp:64-78); a mutual pair also
+// gives j its terms at v_j = d / h_j with xm_i and m_i, by FP64 atomics.  The self terms and the
+// epilogue (ve_def_gradh_kern.hpp:60-62, 80-88) run in gradhOnceFinish.
+__global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
+                                                               const double* h, const double* m, const double* xm,
+                                                               const double2* tw, const double2* tdw,
+                                                               const double* hInv64, int64_t n, double* acc)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned no = ov.size(ii);
+    const double* hInv = hInv64;
+    const double* hInvDx = hInv64 + 2 * n;
+    auto t = cf.target(i);
+    const double hi = h[i], mi = m[i], xmi = xm[i], twoH = 2.0 * hi, hiInv = hInv[i], hiInvDx = hInvDx[i];
+    const bool wrap = cf.needsWrap(t, twoH);
+    double kx = 0.0, whom = 0.0, wr0 = 0.0;
+    for (unsigned k = 0; k < no; ++k) {
+        bool mutual;
+        const uint32_t j = ov.at(ii, k, mutual);
+        double rx, ry, rz;
+        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double dist = r2 * invDist(r2);
+        {
+            const double v = dist * hiInv;
+            const TabSlot sl = tabSlot(dist * hiInvDx);
+            const double w = lookupX(tw, sl), dw = lookupX(tdw, sl);
+            const double dterh = -(3.0 * w + v * dw);
+            const double xmj = __ldg(xm + j);
+            kx += w * xmj;
+            whom += dterh * xmj;
+            wr0 += dterh * __ldg(m + j);
+        }
+        if (mutual) {
+            const double v = dist * __ldg(hInv + j);
+            const TabSlot sl = tabSlot(dist * __ldg(hInvDx + j));
+            const double w = lookupX(tw, sl), dw = lookupX(tdw, sl);
+            const double dterh = -(3.0 * w + v * dw);
+            atomicAdd(acc + j, w * xmi);
+            atomicAdd(acc + n + j, dterh * xmi);
+            atomicAdd(acc + 2 * n + j, dterh * mi);
+        }
+    }
+    atomicAdd(acc + i, kx);
+    atomicAdd(acc + n + i, whom);
+    atomicAdd(acc + 2 * n + i, wr0);
+}
+
+__global__ void gradhOnceFinish(int64_t first, int64_t last, int64_t n, const double* h, const double* m,
+                                const double* xm, double K, const double* acc, double* kxOut, double* gradhOut)
+{
+    const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    const double hi = h[i], mi = m[i], xmi = xm[i];
+    const double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
+    double kxi = xmi + acc[i], whomega = -3.0 * xmi + acc[n + i], wrho0 = -3.0 * mi + acc[2 * n + i];
+    kxi *= K * h3Inv;
+    whomega *= K * h3Inv * hInv;
+    wrho0 *= K * h3Inv * hInv;
+    whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
+    const double rhoi = kxi * mi / xmi;
+    const double dhdrho = -hi / (rhoi * 3.0);
+    kxOut[i] = kxi;
+    gradhOut[i] = 1.0 - dhdrho * whomega;
+}
+
+// FP64 AV switches with one evaluation per mutual pair over the owned lists.  i's sum is
+// S_i = sum vol_j (divv_i - divv_j) W_i r (r = x_i - x_j; c_i is applied after the walk), j's term of
+// the same pair is vol_i (divv_i - divv_j) W_j r (r and the divv difference both change sign);
+// the signal-velocity candidate c_i + c_j - 3 (r.v) / |r| of approaching pairs is symmetric.
+__global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, AvArgs a,
+                                                            const double* hInv64, int64_t n, double* acc)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned no = ov.size(ii);
+    const double2* tabX = static_cast<const double2*>(a.wh);
+    const double* hInvDx = hInv64 + 2 * n;
+    const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
+                 *vz = static_cast<const double*>(a.vz), *c = static_cast<const double*>(a.c),
+                 *divv = static_cast<const double*>(a.divv), *vol = static_cast<const double*>(a.vol);
+    auto t = cf.target(i);
+    const double hi = ld<double>(a.h, i), ci = c[i], divvi = divv[i], voli = vol[i];
+    const double vxi = vx[i], vyi = vy[i], vzi = vz[i], twoH = 2.0 * hi, hiInvDx = hInvDx[i];
+    const bool wrap = cf.needsWrap(t, twoH);
+    double Sx = 0, Sy = 0, Sz = 0;
+    long long vsigBits = 0;
+    long long* accV = reinterpret_cast<long long*>(acc + 3 * n);
+    for (unsigned k = 0; k < no; ++k) {
+        bool mutual;
+        const uint32_t j = ov.at(ii, k, mutual);
+        double rx, ry, rz;
+        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double rinv = invDist(r2);
+        const double dist = r2 * rinv;
+        const double rv = rx * (vxi - vx[j]) + ry * (vyi - vy[j]) + rz * (vzi - vz[j]);
+        const bool approaching = negative(rv);
+        double vs = 0.0;
+        if (approaching) {
+            vs = ci + c[j] - 3.0 * rv * rinv;
+            vsigBits = maxBitsNonNeg(vsigBits, vs);
+        }
+        const double dd = divvi - divv[j];
+        const double fw = vol[j] * dd * lookupX(tabX, dist * hiInvDx);
+        Sx += fw * rx;
+        Sy += fw * ry;
+        Sz += fw * rz;
+        if (mutual) {
+            const double fwj = voli * dd * lookupX(tabX, dist * __ldg(hInvDx + j));
+            atomicAdd(acc + j, fwj * rx);
+            atomicAdd(acc + n + j, fwj * ry);
+            atomicAdd(acc + 2 * n + j, fwj * rz);
+            if (approaching) atomicMax(accV + j, __double_as_longlong(vs));
+        }
+    }
+    atomicAdd(acc + i, Sx);
+    atomicAdd(acc + n + i, Sy);
+    atomicAdd(acc + 2 * n + i, Sz);
+    atomicMax(accV + i, vsigBits);
+}
+
+__global__ void avOnceFinish(int64_t first, int64_t last, int64_t n, AvArgs a, const double* acc)
+{
+    const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    const double hi = ld<double>(a.h, i), ci = ld<double>(a.c, i), divvi = ld<double>(a.divv, i);
+    const double hiInv = 1.0 / hi, kh3 = a.K * hiInv * hiInv * hiInv;
+    const double c11 = ld<double>(a.c11, i), c12 = ld<double>(a.c12, i), c13 = ld<double>(a.c13, i);
+    const double c22 = ld<double>(a.c22, i), c23 = ld<double>(a.c23, i), c33 = ld<double>(a.c33, i);
+    const double Sx = acc[i], Sy = acc[n + i], Sz = acc[2 * n + i];
+    const double gx = -kh3 * (c11 * Sx + c12 * Sy + c13 * Sz);
+    const double gy = -kh3 * (c12 * Sx + c22 * Sy + c23 * Sz);
+    const double gz = -kh3 * (c13 * Sx + c23 * Sy + c33 * Sz);
+    // vsig_i starts at 1e-40 c_i (av_switches_kern.hpp:66); both candidates are >= 0
+    const long long vb = max(__double_as_longlong(1.e-40 * ci), reinterpret_cast<const long long*>(acc + 3 * n)[i]);
+    st<double>(a.alpha, i,
+               avAlpha<double>(a, ld<double>(a.alpha, i), hi, ci, divvi, __longlong_as_double(vb), gx, gy, gz));
+}
+
 // FP64 VE momentum-energy with one evaluation per mutual pair, for lists that cover every particle.
 // i walks its owned list: every pair of its list that j does not list back, and half of the
 // mutual pairs (the other half is in the owned lists of the other ends).  The two ends' terms follow from one
@@ -781,6 +927,21 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     lv.first = first;
     lv.last = last;
     unsigned blocks = gridFor(last - first, kPairBlock);
+    if (pairOnce(c, p, first, last)) {
+        const int64_t n = p->n;
+        SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 3 * size_t(n)));
+        SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 3 * size_t(n), c->stream));
+        gradhOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
+            lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
+            static_cast<const double*>(p->xm), c->whx64.as<double2>(), c->whdx64.as<double2>(),
+            c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+        SPHGB_TRY(launched(c, "gradhOnceKernel"));
+        gradhOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(
+            first, last, n, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
+            static_cast<const double*>(p->xm), c->K, c->pairAcc.as<double>(), static_cast<double*>(p->kx),
+            static_cast<double*>(p->gradh));
+        return launched(c, "gradhOnceFinish");
+    }
     if (p->precision == SPHGB_MIXED)
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                     p->xm, c->wh32.p, c->whd32.p, c->K, p->kx,
@@ -874,6 +1035,16 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
     if (mixed) {
         a.wh = c->wh32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+    } else if (pairOnce(c, p, first, last)) {
+        const int64_t n = p->n;
+        a.wh = c->whx64.p;
+        SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 4 * size_t(n)));
+        SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 4 * size_t(n), c->stream));
+        avOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, ownedView(c), coordFp64(c, p), a,
+                                                            c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+        SPHGB_TRY(launched(c, "avOnceKernel"));
+        avOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
+        return launched(c, "avOnceFinish");
     } else {
         a.wh = c->whx64.p;
         avKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
@@ -938,14 +1109,13 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     } else {
         a.wh = c->whx64.p;
         // one evaluation per mutual pair when the lists cover all particles and the order may vary
-        const bool once = !avClean && !c->deterministic && c->ownedEpoch == c->nbrEpoch && first == 0 &&
-                          last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
+        const bool once = !avClean && pairOnce(c, p, first, last);
         if (once) {
-            SPHGB_TRY(c->meAcc.ensure(sizeof(double) * 6 * size_t(p->n)));
-            SPHGB_CUDA(cudaMemsetAsync(c->meAcc.p, 0, sizeof(double) * 6 * size_t(p->n), c->stream));
+            SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 6 * size_t(p->n)));
+            SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 6 * size_t(p->n), c->stream));
             a.owned = c->owned.as<uint32_t>();
             a.ownedCount = c->ownedCount.as<uint32_t>();
-            a.acc = c->meAcc.as<double>();
+            a.acc = c->pairAcc.as<double>();
             meVeOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a);
             SPHGB_TRY(launched(c, "meVeOnceKernel"));
             meVeOnceFinish<<<blocks, kPairBlock, 0, c->stream>>>(lv, a);

@@ -79,7 +79,7 @@ __device__ __forceinline__ void gridOffset(const NbrArgs& a, const int cj[3], fl
 
 struct WarpSmem {
     int32_t stack[kStack];
-    float fx[kWarp], fy[kWarp], fz[kWarp];
+    float4 f[kWarp];  // staged candidates: offsets from the group origin
 };
 
 __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
@@ -153,51 +153,68 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         Rg = fmaxf(Rg, fmaxf(fabsf(gmin[k]), fabsf(gmax[k])));
     }
     // FP32 decision margin on d2: covers the rounding of cell edge, offsets and the squared sum;
-    // pairs inside the margin get the exact FP64 test
+    // pairs inside the margin get the exact FP64 test (every pair when exactOnly)
     const float r2f = float(r2);
     const float margin = 64.f * 0x1p-24f * (Rg + rf) * (Rg + rf);
+    const float inBelow = r2f - margin;   // d2f < inBelow: neighbour
+    const float outAbove = r2f + margin;  // d2f > outAbove: not a neighbour
 
     unsigned cnt = 0;
     unsigned long long tested = 0, rechecked = 0;
     const int64_t ii = i - a.first;
+    const uint32_t iu = uint32_t(i);
+    uint32_t* outp = a.nbr + ii;  // row cnt of this target's transposed list
 
+    // the reference's distanceSq decision in FP64 (findneighbors.hpp:33-60)
+    auto exactIn = [&](uint32_t j) {
+        ++rechecked;
+        double dx = __dsub_rn(a.x[j], a.x[i]), dy = __dsub_rn(a.y[j], a.y[i]), dz = __dsub_rn(a.z[j], a.z[i]);
+        if (usePbc) {
+            if (b.pbc[0]) dx = foldRint(dx, b, 0);
+            if (b.pbc[1]) dy = foldRint(dy, b, 1);
+            if (b.pbc[2]) dz = foldRint(dz, b, 2);
+        }
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        return d2 < r2;
+    };
+    auto take = [&](uint32_t j) {
+        if (j != iu) {
+            if (cnt < a.ngmax) *outp = j;
+            outp += a.stride;
+            ++cnt;
+        }
+    };
+
+    // one chunk of m <= 32 contiguous candidates [ja, ja + m), staged by the warp.  Every target
+    // tests all 32 slots with a fixed trip count; slots >= m hold a far-away sentinel whose FP32
+    // distance is +inf.  Groups that need the exact test for every pair loop over the m slots.
     auto flush = [&](int64_t ja, int m) {
+        float4 fj = make_float4(1e30f, 1e30f, 1e30f, 0.f);
         if (lane < m) {
             const int64_t j = ja + lane;
             int cj[3];
             unpackCell(a.cell[j], cj);
             float rj[3];
             gridOffset(a, cj, a.loc[j], co, lo, rj);
-            sm.fx[lane] = rj[0];
-            sm.fy[lane] = rj[1];
-            sm.fz[lane] = rj[2];
+            fj = make_float4(rj[0], rj[1], rj[2], 0.f);
         }
+        sm.f[lane] = fj;
         __syncwarp();
         if (valid) {
             tested += m;
-            for (int t = 0; t < m; ++t) {
-                const float ex = dxi - sm.fx[t], ey = dyi - sm.fy[t], ez = dzi - sm.fz[t];
-                const float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                bool in;
-                if (!exactOnly && d2f < r2f - margin) in = true;
-                else if (!exactOnly && d2f > r2f + margin) in = false;
-                else {
-                    ++rechecked;
-                    const int64_t j = ja + t;
-                    double dx = __dsub_rn(a.x[j], a.x[i]), dy = __dsub_rn(a.y[j], a.y[i]),
-                           dz = __dsub_rn(a.z[j], a.z[i]);
-                    if (usePbc) {
-                        if (b.pbc[0]) dx = foldRint(dx, b, 0);
-                        if (b.pbc[1]) dy = foldRint(dy, b, 1);
-                        if (b.pbc[2]) dz = foldRint(dz, b, 2);
-                    }
-                    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-                    in = d2 < r2;
-                }
-                const int64_t j = ja + t;
-                if (in && j != i) {
-                    if (cnt < a.ngmax) a.nbr[int64_t(cnt) * a.stride + ii] = uint32_t(j);
-                    ++cnt;
+            const uint32_t j0 = uint32_t(ja);
+            if (exactOnly) {
+                for (int t = 0; t < m; ++t)
+                    if (exactIn(j0 + uint32_t(t))) take(j0 + uint32_t(t));
+            } else {
+#pragma unroll 8
+                for (int t = 0; t < kWarp; ++t) {
+                    const float4 f = sm.f[t];
+                    const float ex = dxi - f.x, ey = dyi - f.y, ez = dzi - f.z;
+                    const float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                    if (d2f > outAbove) continue;
+                    const uint32_t j = j0 + uint32_t(t);
+                    if (d2f < inBelow || exactIn(j)) take(j);
                 }
             }
         }

@@ -44,6 +44,36 @@ inline ListView listView(const sphgb_ctx* c)
                     c->nbrNgmax};
 }
 
+// ---- owned lists: the pairs particle i evaluates in the pair-once FP64 passes ----
+// owned[k * stride + (i - first)] = j | mutual << 31, k < count[i - first]: every pair of i's list
+// that j does not list back, and half of the mutual pairs (the other half sits in the owned lists
+// of the other ends).  A mutual pair's evaluation also produces j's terms, added with FP64 atomics.
+struct OwnedView {
+    const uint32_t* owned;
+    const uint32_t* count;
+    int64_t stride;
+    __device__ __forceinline__ unsigned size(int64_t ii) const { return __ldg(count + ii); }
+    __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k, bool& mutual) const
+    {
+        const uint32_t e = __ldg(owned + int64_t(k) * stride + ii);
+        mutual = (e >> 31) != 0;
+        return e & 0x7fffffffu;
+    }
+};
+
+inline OwnedView ownedView(const sphgb_ctx* c)
+{
+    return OwnedView{c->owned.as<uint32_t>(), c->ownedCount.as<uint32_t>(), c->nbrStride};
+}
+
+// a pass over [first, last) may evaluate pairs once: FP64 fields, order-free summation allowed,
+// owned lists of the current neighbour lists, and lists covering every particle
+inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last)
+{
+    return !c->deterministic && p->precision == SPHGB_FP64 && c->ownedEpoch == c->nbrEpoch && first == 0 &&
+           last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
+}
+
 // ---- FP64 coordinates: reference distancePBC / legacy applyPBC (box.hpp:216-254) ----
 struct CoordFp64 {
     const double *x, *y, *z;
