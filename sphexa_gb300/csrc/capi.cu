@@ -300,6 +300,11 @@ int sphgb_sweep_passes(sphgb_ctx* c, sphgb_particles* p, int32_t variant, int32_
         if (s != SPHGB_OK && s != SPHGB_ERR_NOCONV) return s;
     }
     int st = s;
+    struct SweepScope {  // precomputes once per sweep, released on every exit path
+        sphgb_ctx* c;
+        explicit SweepScope(sphgb_ctx* cc) : c(cc) { c->inSweep = true, c->sweepPrepared = false; }
+        ~SweepScope() { c->inSweep = false, c->sweepPrepared = false; }
+    } scope(c);
     auto stage = [&](int k, auto&& fn) {
         StageTimer t(c, kStagePass0 + k);
         int r = fn();

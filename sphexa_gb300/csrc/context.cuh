@@ -106,6 +106,8 @@ struct sphgb_ctx {
     // per-particle accumulators of the pair-once passes (up to 6 x n doubles)
     bool deterministic = false;
     sphgb::DBuf pairAcc;
+    // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
+    bool inSweep = false, sweepPrepared = false;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -23,30 +23,41 @@ namespace sphgb {
 namespace {
 
 // ---------------------------------------------------------------- per-particle quotients
-template<class T>
+// aux = {rho, m/rho, xm/kx, m*prho, ln xm, 1/rho} x n; a pass asks only for the parts it reads
+enum AuxPart : int { kAuxVol = 1, kAuxMe = 2 };
+
+template<class T, int Parts>
 __global__ void veAuxKernel(int64_t n, const void* m, const void* kx, const void* xm, const void* prho, T* aux)
 {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
     T mi = ld<T>(m, i), kxi = ld<T>(kx, i), xmi = ld<T>(xm, i);
-    T rho = kxi * mi / xmi;
-    aux[i] = rho;
-    aux[n + i] = mi / rho;
-    aux[2 * n + i] = xmi / kxi;
-    if (prho) aux[3 * n + i] = mi * ld<T>(prho, i);
-    if constexpr (std::is_same_v<T, double>) aux[4 * n + i] = log(xmi);
-    else aux[4 * n + i] = log2f(xmi);
-    aux[5 * n + i] = T(1) / rho;
+    if constexpr ((Parts & kAuxVol) != 0) aux[2 * n + i] = xmi / kxi;
+    if constexpr ((Parts & kAuxMe) != 0) {
+        T rho = kxi * mi / xmi;
+        aux[i] = rho;
+        aux[n + i] = mi / rho;
+        aux[3 * n + i] = mi * ld<T>(prho, i);
+        if constexpr (std::is_same_v<T, double>) aux[4 * n + i] = log(xmi);
+        else aux[4 * n + i] = log2f(xmi);
+        aux[5 * n + i] = T(1) / rho;
+    }
 }
 
-template<class P>
+template<class P, int Parts>
 int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 {
     using T = typename P::T;
     const int64_t n = p->n;
     SPHGB_TRY(c->aux.ensure(sizeof(T) * 6 * n));
-    veAuxKernel<T><<<gridFor(n, 256), 256, 0, c->stream>>>(n, p->m, p->kx, p->xm, p->prho, c->aux.as<T>());
+    veAuxKernel<T, Parts><<<gridFor(n, 256), 256, 0, c->stream>>>(n, p->m, p->kx, p->xm, p->prho, c->aux.as<T>());
     return launched(c, "veAuxKernel");
+}
+
+template<int Parts>
+int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
+{
+    return p->precision == SPHGB_MIXED ? launchVeAux<MixedTag, Parts>(c, p) : launchVeAux<Fp64Tag, Parts>(c, p);
 }
 
 // ---------------------------------------------------------------- gradh (kx, gradh)
@@ -976,7 +987,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     const bool gradV = p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33;
     SPHGB_TRY(checkPass(c, p, first, last));
     const bool mixed = p->precision == SPHGB_MIXED;
-    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
+    SPHGB_TRY(launchVeAux<kAuxVol>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
@@ -1023,7 +1034,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
     const bool mixed = p->precision == SPHGB_MIXED;
-    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
+    SPHGB_TRY(launchVeAux<kAuxVol>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
@@ -1061,7 +1072,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     if (avClean && !(p->dV11 && p->dV12 && p->dV13 && p->dV22 && p->dV23 && p->dV33)) return SPHGB_ERR_ARG;
     SPHGB_TRY(checkPass(c, p, first, last));
     const bool mixed = p->precision == SPHGB_MIXED;
-    SPHGB_TRY(mixed ? launchVeAux<MixedTag>(c, p) : launchVeAux<Fp64Tag>(c, p));
+    SPHGB_TRY(launchVeAux<kAuxMe>(c, p));
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;

@@ -151,8 +151,11 @@ int checkPass(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t las
     if (first < c->nbrFirst || last > c->nbrLast || first >= last || p->n < last) return SPHGB_ERR_ARG;
     if (p->precision != SPHGB_FP64 && p->precision != SPHGB_MIXED) return SPHGB_ERR_ARG;
     sphgb_particles* q = const_cast<sphgb_particles*>(p);
-    if (p->precision == SPHGB_MIXED) return prepareMixed(c, q, first, last);
-    return prepareFp64(c, q);
+    // inside one sweep positions and h stay put after the neighbour search: prepare once
+    if (c->sweepPrepared) return SPHGB_OK;
+    const int s = p->precision == SPHGB_MIXED ? prepareMixed(c, q, first, last) : prepareFp64(c, q);
+    if (s == SPHGB_OK && c->inSweep) c->sweepPrepared = true;
+    return s;
 }
 
 int beginDtReduction(sphgb_ctx* c, unsigned long long** dst)
