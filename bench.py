@@ -41,8 +41,9 @@ UNIT = "particles/s"
 VE_FLOPS_PER_PAIR = {"xmass": 20.2, "gradh": 34.4, "iad_divv": 37.6 + 59.3, "av": 55.3, "me": 136.2}
 STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
-# dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count
-NCU_DRAM_BYTES_PER_PARTICLE = {"me": 692.8, "iad_divv": 585.8}
+# dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count.
+# "me" and "av" are the pair-once kernels of the default (non-deterministic) FP64 mode.
+NCU_DRAM_BYTES_PER_PARTICLE = {"me": 584.7, "iad_divv": 564.3, "av": 381.7}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
 
 
