@@ -137,7 +137,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
-                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc};
+                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)

@@ -108,6 +108,8 @@ struct sphgb_ctx {
     sphgb::DBuf pairAcc;
     // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
     bool inSweep = false, sweepPrepared = false;
+    // packed neighbour-side records of the mixed pair passes (float4 x 4 per particle)
+    sphgb::DBuf pack;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -425,6 +425,9 @@ struct MeVeArgs {
     const uint32_t* owned;
     const uint32_t* ownedCount;
     double* acc;
+    // mixed form: packed neighbour records {vx vy vz c} {c11 c12 c13 c22} {c23 c33 m xm}
+    // {alpha rho m/rho m*prho} per particle
+    const float4* pack;
 };
 
 template<class T>
@@ -449,6 +452,19 @@ __device__ __forceinline__ T avRv(T rx, T ry, T rz, T eta, T etaCrit, const T gi
     T Ap1 = T(1) + A;
     T phi = T(0.5) * d3 * fmax(T(0), fmin(T(1), T(4) * A / (Ap1 * Ap1)));
     return -phi * (d1 + d2);
+}
+
+// neighbour-side fields of the mixed momentum-energy pass as four 16-byte records per particle
+__global__ void meVePackKernel(int64_t n, MeVeArgs a, float4* __restrict__ pack)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    const float m = ld<float>(a.m, j), xm = ld<float>(a.xm, j), kx = ld<float>(a.kx, j);
+    const float rho = kx * m / xm;
+    pack[4 * j] = make_float4(ld<float>(a.vx, j), ld<float>(a.vy, j), ld<float>(a.vz, j), ld<float>(a.c, j));
+    pack[4 * j + 1] = make_float4(ld<float>(a.c11, j), ld<float>(a.c12, j), ld<float>(a.c13, j), ld<float>(a.c22, j));
+    pack[4 * j + 2] = make_float4(ld<float>(a.c23, j), ld<float>(a.c33, j), m, xm);
+    pack[4 * j + 3] = make_float4(ld<float>(a.alpha, j), rho, m / rho, m * ld<float>(a.prho, j));
 }
 
 template<class P, bool AvClean>
@@ -568,6 +584,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             dt = courantDt(__longlong_as_double(maxvBits), hi, ci, a.Kcour);
         }
     } else {
+        // neighbour fields from the packed records (4 x 16 B per particle, meVePackKernel): six
+        // gathers per pair (cell, offset, 4 records) instead of seventeen scalar ones
         auto t = cm.target(i);
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         T rhoiInv = __frcp_rn(rhoi);
@@ -576,23 +594,25 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
+            const float4 pv = __ldg(a.pack + 4 * int64_t(j));      // vx vy vz c
+            const float4 pc = __ldg(a.pack + 4 * int64_t(j) + 1);  // c11 c12 c13 c22
+            const float4 pd = __ldg(a.pack + 4 * int64_t(j) + 2);  // c23 c33 m xm
+            const float4 pe = __ldg(a.pack + 4 * int64_t(j) + 3);  // alpha rho m/rho m*prho
             T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
             T rinv = rsqrtf(r2);
             T dist = r2 * rinv;
-            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            T vxij = vxi - pv.x, vyij = vyi - pv.y, vzij = vzi - pv.z;
             T v1 = dist * hiInv, v2 = dist * hjInv;
             T Wi = hiInv3 * tableLookup(tab, v1);
             T Wj = (hjInv * hjInv * hjInv) * tableLookup(tab, v2);
-            T a1i = -(c11i * rx + c12i * ry + c13i * rz) * Wi;
-            T a2i = -(c12i * rx + c22i * ry + c23i * rz) * Wi;
-            T a3i = -(c13i * rx + c23i * ry + c33i * rz) * Wi;
-            T c11j = ld<T>(a.c11, j), c12j = ld<T>(a.c12, j), c13j = ld<T>(a.c13, j);
-            T c22j = ld<T>(a.c22, j), c23j = ld<T>(a.c23, j), c33j = ld<T>(a.c33, j);
-            T a1j = -(c11j * rx + c12j * ry + c13j * rz) * Wj;
-            T a2j = -(c12j * rx + c22j * ry + c23j * rz) * Wj;
-            T a3j = -(c13j * rx + c23j * ry + c33j * rz) * Wj;
-            T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
-            T rhoj = __ldg(auxRho + j);
+            T gix = c11i * rx + c12i * ry + c13i * rz;
+            T giy = c12i * rx + c22i * ry + c23i * rz;
+            T giz = c13i * rx + c23i * ry + c33i * rz;
+            T gjx = pc.x * rx + pc.y * ry + pc.z * rz;
+            T gjy = pc.y * rx + pc.w * ry + pd.x * rz;
+            T gjz = pc.z * rx + pd.x * ry + pd.y * rz;
+            T mj = pd.z, cj = pv.w, xmj = pd.w;
+            T rhoj = pe.y;
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
@@ -600,7 +620,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
                 rv += avRv<T>(rx, ry, rz, fminf(v1, v2), etaCrit, gi, gj);
             }
             T wij = rv * rinv;
-            T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
+            T visc = artificialViscosity<T>(ai, pe.x, ci, cj, wij);
             T vsig = T(0.5) * (ci + cj) - T(2) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
             T dr = fabsf(rhoi - rhoj), sr = rhoi + rhoj;
@@ -613,20 +633,23 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
                 bm = am;
             } else {
                 T s = ramp * (__fdividef(dr, sr) - Atmin);
-                T q = exp2f(s * (__ldg(auxLnXm + j) - lnxmi));
+                T q = exp2f(s * (log2f(xmj) - lnxmi));
                 am = xmi2 * q;
                 bm = xmj * xmj * __frcp_rn(q);
             }
-            T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
-            T avx = T(0.5) * (av * a1i + bv * a1j);
-            T avy = T(0.5) * (av * a2i + bv * a2j);
-            T avz = T(0.5) * (av * a3i + bv * a3j);
-            avE.add(avx * vxij + avy * vyij + avz * vzij);
-            en.add(mj * am * (vxij * a1i + vyij * a2i + vzij * a3i));
-            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
-            mx.add(momi * a1i + momj * a1j + avx);
-            my.add(momi * a2i + momj * a2j + avy);
-            mz.add(momi * a3i + momj * a3j + avz);
+            T av = mj * rhoiInv * visc, bv = pe.z * visc;
+            T momi = mj * prhoi * am, momj = pe.w * bm;
+            T si = vxij * gix + vyij * giy + vzij * giz;
+            T sj = vxij * gjx + vyij * gjy + vzij * gjz;
+            T avWi = av * Wi, bvWj = bv * Wj;
+            // a_i = -G_i W_i, a_j = -G_j W_j: momentum momi a_i + momj a_j + 0.5 (av a_i + bv a_j),
+            // energy mj am (v_ij . a_i), viscous work 0.5 (av v_ij . a_i + bv v_ij . a_j)
+            T ki = momi * Wi + T(0.5) * avWi, kj = momj * Wj + T(0.5) * bvWj;
+            mx.add(-(ki * gix + kj * gjx));
+            my.add(-(ki * giy + kj * gjy));
+            mz.add(-(ki * giz + kj * gjz));
+            en.add(-(mj * am * Wi * si));
+            avE.add(T(-0.5) * (avWi * si + bvWj * sj));
         }
         if (valid) {
             double ave = fmax(0.0, avE.value64());
@@ -1115,6 +1138,10 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     auto cm = coordMixed(c);
     if (mixed) {
         a.wh = c->wh32.p;
+        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));
+        meVePackKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>());
+        SPHGB_TRY(launched(c, "meVePackKernel"));
+        a.pack = c->pack.as<float4>();
         if (avClean) meVeKernel<MixedTag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {

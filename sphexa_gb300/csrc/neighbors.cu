@@ -322,7 +322,9 @@ __global__ void hIterKernel(const uint32_t* __restrict__ count, Th* __restrict__
     active[k] = go ? 1u : 0u;
 }
 
-__global__ void ncOutKernel(const uint32_t* __restrict__ count, const uint8_t* __restrict__ iters, int64_t nWork,
+constexpr int kNcOutBlock = 256;
+
+__global__ void __launch_bounds__(kNcOutBlock) ncOutKernel(const uint32_t* __restrict__ count, const uint8_t* __restrict__ iters, int64_t nWork,
                             uint32_t ngmax, uint32_t* __restrict__ nc, int addSelf,
                             unsigned long long* __restrict__ counters)
 {
@@ -343,7 +345,24 @@ __global__ void ncOutKernel(const uint32_t* __restrict__ count, const uint8_t* _
         fails += __shfl_xor_sync(0xffffffffu, fails, o);
         mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
+    // one atomic per block and counter: same-address atomics from every warp serialise in L2
+    __shared__ unsigned long long sS[kNcOutBlock / kWarp], sC[kNcOutBlock / kWarp], sF[kNcOutBlock / kWarp];
+    __shared__ unsigned sM[kNcOutBlock / kWarp];
+    const int w = threadIdx.x / kWarp;
     if ((threadIdx.x & 31) == 0) {
+        sS[w] = sum;
+        sC[w] = capped;
+        sF[w] = fails;
+        sM[w] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < kNcOutBlock / kWarp; ++q) {
+            sum += sS[q];
+            capped += sC[q];
+            fails += sF[q];
+            mx = max(mx, sM[q]);
+        }
         atomicAdd(&counters[3], sum);
         atomicAdd(&counters[4], capped);
         atomicMax(&counters[5], (unsigned long long)mx);
@@ -484,8 +503,10 @@ __global__ void gridFormKernel(const double* __restrict__ x, const double* __res
     float l[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+        // cell = floor((x - lo) / u) by a multiply: a cell off by one near a boundary only gives an
+        // offset just outside [0, u), which the FP32 offset still holds to 2^-24 of u
         double u = box.L[k] / double(1 << kGridBits);
-        double g = floor((c[k] - box.lo[k]) / u);
+        double g = floor((c[k] - box.lo[k]) * (double(1 << kGridBits) * box.iL[k]));
         g = fmin(fmax(g, 0.0), double(kGridMask));
         ic[k] = unsigned(g);
         l[k] = float(c[k] - (box.lo[k] + g * u));
@@ -636,7 +657,7 @@ int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
         ++rounds;
         SPHGB_TRY(runSearch(c, p->x, p->y, p->z, p->h, hf, first, last, ngmax, active));
     }
-    ncOutKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->ncount.as<uint32_t>(), iters, nWork, ngmax,
+    ncOutKernel<<<gridFor(nWork, kNcOutBlock), kNcOutBlock, 0, c->stream>>>(c->ncount.as<uint32_t>(), iters, nWork, ngmax,
                                                              p->nc ? p->nc + first : nullptr, 1, ctr);
     SPHGB_TRY(launched(c, "ncOutKernel"));
     SPHGB_TRY(finishStats(c, rounds));
@@ -656,7 +677,7 @@ int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const dou
     SPHGB_TRY(prepareLists(c, x, y, z, first, last, ngmax));
     const int64_t nWork = last - first;
     SPHGB_TRY(runSearch(c, x, y, z, h, hPrec == SPHGB_MIXED, first, last, ngmax, nullptr));
-    ncOutKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(c->ncount.as<uint32_t>(), nullptr, nWork, ngmax, ncOut, 0,
+    ncOutKernel<<<gridFor(nWork, kNcOutBlock), kNcOutBlock, 0, c->stream>>>(c->ncount.as<uint32_t>(), nullptr, nWork, ngmax, ncOut, 0,
                                                              c->counters.as<unsigned long long>());
     SPHGB_TRY(launched(c, "ncOutKernel"));
     if (nbrOut) {

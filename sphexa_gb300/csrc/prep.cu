@@ -55,8 +55,10 @@ __global__ void mixedCoordsKernel(const double* __restrict__ x, const double* __
     float l[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+        // cell = floor((x - lo) / u) by a multiply: a cell off by one near a boundary only gives an
+        // offset just outside [0, u), which the FP32 offset still holds to 2^-24 of u
         double u = box.L[k] / double(1 << kGridBits);
-        double g = floor((c[k] - box.lo[k]) / u);
+        double g = floor((c[k] - box.lo[k]) * (double(1 << kGridBits) * box.iL[k]));
         g = fmin(fmax(g, 0.0), double(kGridMask));
         ic[k] = unsigned(g);
         l[k] = float(c[k] - (box.lo[k] + g * u));
