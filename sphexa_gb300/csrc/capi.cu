@@ -134,10 +134,10 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->internalTmp,   &c->internalCodes, &c->leaves,  &c->layout,        &c->prefixes,
                     &c->childOffsets,  &c->internalToLeaf, &c->nodeCenter, &c->nodeSize,  &c->nodeBoxF,
                     &c->levelRangeDev, &c->nbr,     &c->ncount,        &c->active,        &c->counters,
-                    &c->wh64,     &c->whd64,        &c->wh32,          &c->whd32,         &c->gridKey,
+                    &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
-                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack};
+                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)

@@ -135,20 +135,6 @@ __device__ __forceinline__ u64 sfcKey(double x, double y, double z, const DevBox
     return hilbertEncode(ic[0], ic[1], ic[2]);
 }
 
-// ---- lt::lookup (sph/include/sph/table_lookup.hpp:10-26) ----
-template<class T>
-__device__ __forceinline__ T tableLookup(const T* __restrict__ tab, T v)
-{
-    constexpr int nInt = kTableSize - 1;
-    constexpr T dx = T(2.0) / T(nInt);
-    constexpr T invDx = T(1) / dx;
-    int idx = int(v * invDx);
-    if (idx >= nInt) return T(0);
-    T a = __ldg(tab + idx), b = __ldg(tab + idx + 1);
-    T der = (b - a) * invDx;
-    return a + der * (v - T(idx) * dx);
-}
-
 // ---- status word bits set by kernels ----
 enum DevFlag : int {
     kFlagStackOverflow = 1,

@@ -113,9 +113,9 @@ struct sphgb_ctx {
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 
-    // kernel tables (FP64 and FP32)
-    sphgb::DBuf wh64, whd64, wh32, whd32;
-    sphgb::DBuf whx64, whdx64;  // FP64 tables interleaved {t[k], t[k+1] - t[k]}
+    // kernel tables W and dW/dv, FP64 and FP32, interleaved {t[k], t[k+1] - t[k]}
+    sphgb::DBuf whx64, whdx64;
+    sphgb::DBuf whx32, whdx32;
 
     // mixed precision grid-local coordinates: packed cell (21 bits per axis) + float4 {dx,dy,dz,1/h}
     sphgb::DBuf gridKey, gridLoc;

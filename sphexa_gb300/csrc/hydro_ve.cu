@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         st<double>(kxOut, i, kxi);
         st<double>(gradhOut, i, 1.0 - dhdrho * whomega);
     } else {
-        const float *tw = static_cast<const float*>(wh), *tdw = static_cast<const float*>(whd);
+        const float2 *tw = static_cast<const float2*>(wh), *tdw = static_cast<const float2*>(whd);
         auto t = cm.target(i);
         float mi = ld<float>(m, i), xmi = ld<float>(xm, i);
         KSum kx, whom, wr0;
@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             cm.diff(t, j, rx, ry, rz, hjInv);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             float v = dist * t.hInv;
-            float w = tableLookup(tw, v), dw = tableLookup(tdw, v);
+            float w, dw;
+            lookupX32Pair(tw, tdw, v, w, dw);
             float dterh = -(3.f * w + v * dw);
             float xmj = ld<float>(xm, j);
             kx.add(w * xmj);
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         }
     } else {
         using T = float;
-        const float* tab = static_cast<const float*>(a.wh);
+        const float2* tab = static_cast<const float2*>(a.wh);
         auto t = cm.target(i);
         const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
         // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             T rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            T w = tableLookup(tab, dist * t.hInv);
+            T w = lookupX32(tab, dist * t.hInv);
             T vw = ld<T>(a.vol, j) * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             t11.add(rx * rxv);
@@ -392,7 +393,8 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + ld<T>(a.c, j) - 3.f * rv * rinv);
-            T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) * tableLookup(tab, dist * t.hInv);
+            T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) *
+                   lookupX32(reinterpret_cast<const float2*>(a.wh), dist * t.hInv);
             sx.add(fw * rx);
             sy.add(fw * ry);
             sz.add(fw * rz);
@@ -603,8 +605,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T dist = r2 * rinv;
             T vxij = vxi - pv.x, vyij = vyi - pv.y, vzij = vzi - pv.z;
             T v1 = dist * hiInv, v2 = dist * hjInv;
-            T Wi = hiInv3 * tableLookup(tab, v1);
-            T Wj = (hjInv * hjInv * hjInv) * tableLookup(tab, v2);
+            T Wi = hiInv3 * lookupX32(reinterpret_cast<const float2*>(a.wh), v1);
+            T Wj = (hjInv * hjInv * hjInv) * lookupX32(reinterpret_cast<const float2*>(a.wh), v2);
             T gix = c11i * rx + c12i * ry + c13i * rz;
             T giy = c12i * rx + c22i * ry + c23i * rz;
             T giz = c13i * rx + c23i * ry + c33i * rz;
@@ -978,7 +980,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     }
     if (p->precision == SPHGB_MIXED)
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                    p->xm, c->wh32.p, c->whd32.p, c->K, p->kx,
+                                                                    p->xm, c->whx32.p, c->whdx32.p, c->K, p->kx,
                                                                     p->gradh);
     else
         gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
@@ -1042,7 +1044,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     }
     unsigned blocks = gridFor(last - first, kPairBlock);
     if (mixed) {
-        a.wh = c->wh32.p;
+        a.wh = c->whx32.p;
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else {
         a.wh = c->whx64.p;
@@ -1067,7 +1069,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
              c->K,   c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant, p->alpha};
     unsigned blocks = gridFor(last - first, kPairBlock);
     if (mixed) {
-        a.wh = c->wh32.p;
+        a.wh = c->whx32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else if (pairOnce(c, p, first, last)) {
         const int64_t n = p->n;
@@ -1137,7 +1139,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     auto cf = coordFp64(c, p);
     auto cm = coordMixed(c);
     if (mixed) {
-        a.wh = c->wh32.p;
+        a.wh = c->whx32.p;
         SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));
         meVePackKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>());
         SPHGB_TRY(launched(c, "meVePackKernel"));

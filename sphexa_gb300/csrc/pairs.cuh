@@ -214,6 +214,34 @@ __device__ __forceinline__ double lookupX(const double2* __restrict__ tabX, doub
     return lookupX(tabX, tabSlot(x));
 }
 
+// FP32 lookup on the interleaved FP32 table {t[k], t[k+1] - t[k]}: one 8-byte load per lookup
+__device__ __forceinline__ float lookupX32(const float2* __restrict__ tab, float v)
+{
+    constexpr int nInt = kTableSize - 1;
+    const float x = v * float(kTabInvDx);
+    const int k = int(x);
+    if (k >= nInt) return 0.f;
+    const float2 t = __ldg(tab + k);
+    return fmaf(t.y, x - float(k), t.x);
+}
+
+// W and dW/dv at the same v from the two interleaved FP32 tables
+__device__ __forceinline__ void lookupX32Pair(const float2* __restrict__ tw, const float2* __restrict__ tdw, float v,
+                                              float& w, float& dw)
+{
+    constexpr int nInt = kTableSize - 1;
+    const float x = v * float(kTabInvDx);
+    const int k = int(x);
+    if (k >= nInt) {
+        w = dw = 0.f;
+        return;
+    }
+    const float f = x - float(k);
+    const float2 a = __ldg(tw + k), b = __ldg(tdw + k);
+    w = fmaf(a.y, f, a.x);
+    dw = fmaf(b.y, f, b.x);
+}
+
 // ---- Mixed coordinates: 21-bit grid cell per axis packed in 64 bits + FP32 in-cell offset ----
 constexpr int kGridBits = 21;
 constexpr int kGridMask = (1 << kGridBits) - 1;

@@ -99,16 +99,8 @@ int buildTables(sphgb_ctx* c)
         wdf[i] = float(whd[i]);
     }
     c->K = kernelNormalisation(n);
-    SPHGB_TRY(c->wh64.ensure(sizeof(double) * kTableSize));
-    SPHGB_TRY(c->whd64.ensure(sizeof(double) * kTableSize));
-    SPHGB_TRY(c->wh32.ensure(sizeof(float) * kTableSize));
-    SPHGB_TRY(c->whd32.ensure(sizeof(float) * kTableSize));
-    SPHGB_CUDA(cudaMemcpy(c->wh64.p, wh.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice));
-    SPHGB_CUDA(cudaMemcpy(c->whd64.p, whd.data(), sizeof(double) * kTableSize, cudaMemcpyHostToDevice));
-    SPHGB_CUDA(cudaMemcpy(c->wh32.p, wf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
-    SPHGB_CUDA(cudaMemcpy(c->whd32.p, wdf.data(), sizeof(float) * kTableSize, cudaMemcpyHostToDevice));
-    // FP64 lookups read {t[k], t[k+1] - t[k]} in one 16-byte load; the difference is the one the
-    // reference interpolant forms (sph/include/sph/table_lookup.hpp:23)
+    // lookups read {t[k], t[k+1] - t[k]} in one load; the difference is the one the reference
+    // interpolant forms (sph/include/sph/table_lookup.hpp:23)
     std::vector<double> wx(2 * kTableSize), wdx(2 * kTableSize);
     for (int i = 0; i < kTableSize; ++i) {
         const bool last = i + 1 == kTableSize;
@@ -117,6 +109,18 @@ int buildTables(sphgb_ctx* c)
         wdx[2 * i] = whd[i];
         wdx[2 * i + 1] = last ? 0.0 : whd[i + 1] - whd[i];
     }
+    std::vector<float> wx32(2 * kTableSize), wdx32(2 * kTableSize);
+    for (int i = 0; i < kTableSize; ++i) {
+        const bool last = i + 1 == kTableSize;
+        wx32[2 * i] = wf[i];
+        wx32[2 * i + 1] = last ? 0.f : wf[i + 1] - wf[i];
+        wdx32[2 * i] = wdf[i];
+        wdx32[2 * i + 1] = last ? 0.f : wdf[i + 1] - wdf[i];
+    }
+    SPHGB_TRY(c->whx32.ensure(sizeof(float) * 2 * kTableSize));
+    SPHGB_TRY(c->whdx32.ensure(sizeof(float) * 2 * kTableSize));
+    SPHGB_CUDA(cudaMemcpy(c->whx32.p, wx32.data(), sizeof(float) * 2 * kTableSize, cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->whdx32.p, wdx32.data(), sizeof(float) * 2 * kTableSize, cudaMemcpyHostToDevice));
     SPHGB_TRY(c->whx64.ensure(sizeof(double) * 2 * kTableSize));
     SPHGB_TRY(c->whdx64.ensure(sizeof(double) * 2 * kTableSize));
     SPHGB_CUDA(cudaMemcpy(c->whx64.p, wx.data(), sizeof(double) * 2 * kTableSize, cudaMemcpyHostToDevice));
