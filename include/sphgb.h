@@ -85,6 +85,8 @@ typedef struct {
     int64_t h_fails;          /* particles that hit the 10-iteration limit */
     int64_t candidates;       /* candidate pairs tested by the last neighbour search */
     int64_t fp64_rechecks;    /* candidate pairs that needed the exact FP64 test */
+    int64_t refined_gradh;    /* mixed form: particles whose gradh was recomputed in FP64 (last pass) */
+    int64_t refined_divv;     /* mixed form: particles whose divv sign was settled in FP64 (last pass) */
 } sphgb_stats;
 
 /* ---- context ---- */
@@ -102,6 +104,11 @@ int sphgb_set_params(sphgb_ctx* ctx, const sphgb_params* params);
  * neighbour's share is added with FP64 atomics, so the last bits of ax ay az du can differ from
  * run to run.  on = 1: every list owner sums its own pairs in list order, bitwise reproducible. */
 int sphgb_set_deterministic(sphgb_ctx* ctx, int32_t on);
+/* Mixed form only (no reference counterpart): on = 1 (default) recomputes in FP64, from the exact
+ * inputs, the particles whose gradh is near 0 (|gradh| < 0.1) or whose divv sign lies within the
+ * FP32 error bound, with the neighbour shells their values depend on; on = 0 leaves the FP32
+ * results.  The counts of the last sweep are in sphgb_stats.refined_gradh / refined_divv. */
+int sphgb_set_mixed_refinement(sphgb_ctx* ctx, int32_t on);
 int sphgb_default_params(sphgb_params* params);
 /* kernel normalisation constant K used by the pair passes */
 int sphgb_get_kernel_K(sphgb_ctx* ctx, double* K);

@@ -52,7 +52,8 @@ class SphgbStats(C.Structure):
     _fields_ = [("num_leaves", C.c_int64), ("num_nodes", C.c_int64), ("num_internal", C.c_int64),
                 ("level_range", C.c_int32 * 23), ("nc_sum", C.c_int64), ("nc_max", C.c_uint32),
                 ("capped", C.c_int64), ("h_iterations", C.c_int64), ("h_fails", C.c_int64),
-                ("candidates", C.c_int64), ("fp64_rechecks", C.c_int64)]
+                ("candidates", C.c_int64), ("fp64_rechecks", C.c_int64), ("refined_gradh", C.c_int64),
+                ("refined_divv", C.c_int64)]
 
 
 class SphgbSeeds(C.Structure):
@@ -76,6 +77,7 @@ SIGNATURES = {
     "sphgb_set_params": [_P, C.POINTER(SphgbParams)],
     "sphgb_default_params": [C.POINTER(SphgbParams)],
     "sphgb_set_deterministic": [_P, C.c_int32],
+    "sphgb_set_mixed_refinement": [_P, C.c_int32],
     "sphgb_get_kernel_K": [_P, C.POINTER(C.c_double)],
     "sphgb_domain_sync": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox)],
     "sphgb_get_tree": [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),

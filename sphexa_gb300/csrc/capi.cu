@@ -137,7 +137,8 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
-                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32};
+                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32,    &c->refMask,
+                    &c->refFp64,    &c->divvBound};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -167,6 +168,13 @@ int sphgb_set_deterministic(sphgb_ctx* c, int32_t on)
 {
     if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;
     c->deterministic = on != 0;
+    return SPHGB_OK;
+}
+
+int sphgb_set_mixed_refinement(sphgb_ctx* c, int32_t on)
+{
+    if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;
+    c->refineMixed = on != 0;
     return SPHGB_OK;
 }
 
@@ -358,6 +366,8 @@ int sphgb_get_stats(sphgb_ctx* c, sphgb_stats* s)
 {
     if (!c || !s) return SPHGB_ERR_ARG;
     *s = c->stats;
+    s->refined_gradh = c->stats_refinedGradh;
+    s->refined_divv = c->stats_refinedDivv;
     return SPHGB_OK;
 }
 

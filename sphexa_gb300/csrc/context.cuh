@@ -110,6 +110,11 @@ struct sphgb_ctx {
     bool inSweep = false, sweepPrepared = false;
     // packed neighbour-side records of the mixed pair passes (float4 x 4 per particle)
     sphgb::DBuf pack;
+    // mixed form: FP64 refinement of ill-conditioned particles (masks, FP64 xm/kx/gradh scratch,
+    // divv error bound per particle) and the counts of the last passes
+    bool refineMixed = true;
+    sphgb::DBuf refMask, refFp64, divvBound;
+    int64_t stats_refinedGradh = 0, stats_refinedDivv = 0;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 
@@ -174,6 +179,8 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
 
 int buildTranspose(sphgb_ctx* c);
 int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic);
+int refineMixedGradh(sphgb_ctx* c, sphgb_particles* p);
+int refineMixedDivv(sphgb_ctx* c, sphgb_particles* p, const float* bound);
 
 // min-reduction of per-block Courant dt partials into one double on the host
 int reduceMinDt(sphgb_ctx* c, const double* partials, int count, double* out);

@@ -155,7 +155,8 @@ __global__ void eosVeKernel(int64_t first, int64_t last, const double* u, const 
 // ---------------------------------------------------------------- IAD + divv/curlv
 struct IadDivvArgs {
     const void *h, *vx, *vy, *vz, *xm, *kx, *wh;
-    const void* vol;  // aux: xm/kx per particle
+    const void* vol;    // aux: xm/kx per particle
+    float* divvBound;   // mixed: error bound of divv per particle (refinement flag), may be null
     double K;
     void *c11, *c12, *c13, *c22, *c23, *c33, *divv, *curlv;
     void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
         KSum t11, t12, t13, t22, t23, t33;
         KSum M[9];
+        float Aabs = 0.f;  // sum over pairs of |xm_j W| |v_j - v_i|_1 |r|_1 >= sum |term| of every M entry
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz, hjInv;
@@ -261,7 +263,9 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             t23.add(rz * ryv);
             t33.add(rz * rzv);
             T xw = ld<T>(a.xm, j) * w;
-            T sx = (ld<T>(a.vx, j) - vxi) * xw, sy = (ld<T>(a.vy, j) - vyi) * xw, sz = (ld<T>(a.vz, j) - vzi) * xw;
+            const T dvx = ld<T>(a.vx, j) - vxi, dvy = ld<T>(a.vy, j) - vyi, dvz = ld<T>(a.vz, j) - vzi;
+            T sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
+            Aabs = fmaf(fabsf(xw) * (fabsf(dvx) + fabsf(dvy) + fabsf(dvz)), fabsf(rx) + fabsf(ry) + fabsf(rz), Aabs);
             M[0].add(sx * rx);
             M[1].add(sx * ry);
             M[2].add(sx * rz);
@@ -295,6 +299,14 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         double hInv = 1.0 / hi;
         double nk = a.K * (hInv * hInv * hInv) / double(ld<T>(a.kx, i));
         st<T>(a.divv, i, T(nk * (gx[0] + gy[1] + gz[2])));
+        if (a.divvBound) {
+            // divv = -nk sum_ac C_ac M_ac with S = nk sum|C| sum|terms| >= every partial sum.  Its
+            // FP32 error is at most (eps_terms + eps_c + eps_xm + eps_kx) S with the measured input
+            // errors (1e-7, 7e-7, 4e-7, 2e-7 relative): about 1.4e-6 S; the flag bound is 4e-6 S
+            const double sC = fabs(double(cc[0])) + fabs(double(cc[3])) + fabs(double(cc[5])) +
+                              2.0 * (fabs(double(cc[1])) + fabs(double(cc[2])) + fabs(double(cc[4])));
+            a.divvBound[i] = float(4e-6 * fabs(nk) * sC * double(Aabs));
+        }
         if (a.curlv) {
             double cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
             st<T>(a.curlv, i, T(nk * sqrt(cv0 * cv0 + cv1 * cv1 + cv2 * cv2)));
@@ -978,11 +990,15 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
             static_cast<double*>(p->gradh));
         return launched(c, "gradhOnceFinish");
     }
-    if (p->precision == SPHGB_MIXED)
+    if (p->precision == SPHGB_MIXED) {
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                     p->xm, c->whx32.p, c->whdx32.p, c->K, p->kx,
                                                                     p->gradh);
-    else
+        SPHGB_TRY(launched(c, "gradhKernel"));
+        if (first == 0 && last == p->n) return refineMixedGradh(c, p);
+        c->stats_refinedGradh = 0;
+        return SPHGB_OK;
+    } else
         gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                    p->xm, c->whx64.p, c->whdx64.p, c->K, p->kx,
                                                                    p->gradh);
@@ -1045,7 +1061,14 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     unsigned blocks = gridFor(last - first, kPairBlock);
     if (mixed) {
         a.wh = c->whx32.p;
+        const bool refine = c->refineMixed && first == 0 && last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
+        if (refine) {
+            SPHGB_TRY(c->divvBound.ensure(sizeof(float) * size_t(p->n)));
+            a.divvBound = c->divvBound.as<float>();
+        }
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+        SPHGB_TRY(launched(c, "iadDivvKernel"));
+        return refineMixedDivv(c, p, refine ? a.divvBound : nullptr);
     } else {
         a.wh = c->whx64.p;
         iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);

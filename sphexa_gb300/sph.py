@@ -80,6 +80,11 @@ class Context:
         momentum-energy pass evaluates mutual pairs once and scatters with FP64 atomics."""
         check(self.lib.sphgb_set_deterministic(self.h, int(bool(on))), "sphgb_set_deterministic")
 
+    def set_mixed_refinement(self, on: bool) -> None:
+        """Mixed form: recompute ill-conditioned particles (gradh near 0, divv sign within the FP32
+        error) in FP64 from the exact inputs (default True)."""
+        check(self.lib.sphgb_set_mixed_refinement(self.h, int(bool(on))), "sphgb_set_mixed_refinement")
+
     @property
     def K(self) -> float:
         k = C.c_double()

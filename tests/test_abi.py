@@ -74,4 +74,4 @@ def test_struct_layouts_match_header_sizes():
     assert C.sizeof(_lib.SphgbBox) == 56
     assert C.sizeof(_lib.SphgbParams) == 72
     assert C.sizeof(_lib.SphgbParticles) == 8 + 8 + 8 + 8 * (5 + 30) + 8
-    assert C.sizeof(_lib.SphgbStats) == 24 + 92 + 4 + 8 + 8 + 8 * 5
+    assert C.sizeof(_lib.SphgbStats) == 24 + 92 + 4 + 8 + 8 + 8 * 7
