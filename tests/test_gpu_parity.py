@@ -173,6 +173,35 @@ def test_fp64_against_live_oracle_midsize(gpu_ctx, port, case):
             assert err <= tol, f"{case} {variant} {f}: {err:.3e} (bar {tol:.1e})"
 
 
+@pytest.mark.parametrize("variant", ["std", "ve"])
+def test_sedov_50_cubed_against_oracle(gpu_ctx, port, variant):
+    """The 50^3 = 125,000-particle Sedov lattice (periodic [-0.5, 0.5]^3, Sedov u, v = 0, ng0 100,
+    ngmax 150): keys, order, leaves, octree arrays, neighbour sets and counts bit-exact against the
+    oracle's full sweep, every field within the FP64 bar."""
+    from sphexa_gb300 import workloads as W
+    wl = W.sedov(50)
+    ref = port.sweep(wl, variant, False)
+    r = run_gpu(gpu_ctx, wl, variant, False, "fp64")
+    np.testing.assert_array_equal(r["keys"], ref["keys"])
+    np.testing.assert_array_equal(r["order"], ref["order"].astype(np.int64))
+    t = r["tree"]
+    np.testing.assert_array_equal(t["leaves"], ref["leaves"])
+    np.testing.assert_array_equal(np.diff(t["layout"].astype(np.int64)), ref["counts"].astype(np.int64))
+    for k in ("prefixes", "child_offsets", "internal_to_leaf", "level_range"):
+        np.testing.assert_array_equal(t[k], ref[k])
+    np.testing.assert_array_equal(r["nc"], ref["nc"])
+    ng = int(wl.params["ngmax"])
+    np.testing.assert_array_equal(flat_sets(r["nbr"], r["nc"], ng), flat_sets(ref["nbr"], ref["nc"], ng))
+    fields = ("rho", "p", "c", "c11", "c12", "c13", "c22", "c23", "c33", "ax", "ay", "az", "du")
+    if variant == "ve":
+        fields += ("xm", "kx", "gradh", "prho", "divv", "curlv", "alpha")
+    for f in fields:
+        err = np.max(np.abs(r[f] - ref[f])) / field_scale(ref, f)
+        tol = fp64_tol(ref, f, variant)
+        assert err <= tol, f"sedov50 {variant} {f}: {err:.3e} (bar {tol:.1e})"
+    assert r["minDt"] == pytest.approx(float(ref["minDtCourant"]), rel=1e-12)
+
+
 @pytest.mark.parametrize("case", ["fourier", "sphere", "random_open_capped"])
 def test_pair_once_passes_match_ordered_sums(gpu_ctx, case):
     """The FP64 VE passes with one evaluation per mutual pair (owned lists, FP64 atomics: xmass,
