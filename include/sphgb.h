@@ -37,7 +37,9 @@ typedef enum {
 } sphgb_status;
 
 typedef enum { SPHGB_FP64 = 0, SPHGB_MIXED = 1 } sphgb_precision;
-typedef enum { SPHGB_BC_OPEN = 0, SPHGB_BC_PERIODIC = 1 } sphgb_boundary;
+/* cstone::BoundaryType (domain/include/cstone/sfc/box.hpp:80-85); fixed boundaries act as open in
+ * the key, tree and pair passes and freeze resting particles next to them in the position update */
+typedef enum { SPHGB_BC_OPEN = 0, SPHGB_BC_PERIODIC = 1, SPHGB_BC_FIXED = 2 } sphgb_boundary;
 typedef enum { SPHGB_STD = 0, SPHGB_VE = 1 } sphgb_variant;
 
 typedef struct sphgb_ctx sphgb_ctx;
@@ -219,6 +221,45 @@ int sphgb_kernel_launches(sphgb_ctx* ctx, int64_t* launches);
  * with a dependent-chain probe kernel; the roofline denominator of the pair passes (no
  * reference counterpart: the reference records no performance figures) */
 int sphgb_measure_fma_peak(sphgb_ctx* ctx, int32_t fp64, double* flops_per_s);
+
+/* ---- time integration and reductions (one time step for all particles, no rungs) ---- */
+
+/* Timestep state of sphexa::ParticlesData used by sph::computeTimestep (ts_global.hpp:97-113). */
+typedef struct {
+    double minDt, minDt_m1, ttot;   /* in/out: current and previous step, elapsed time */
+    double minDtCourant;            /* in: Courant limit from the momentum-energy pass */
+    double minDtRho;                /* in: divv limit (sphgb_rho_timestep), INFINITY if unused */
+    double maxDtIncrease;           /* in: growth limit, 1.1 in the reference (particles_data.hpp:141) */
+    double g, etaAcc, eps;          /* in: acceleration limit when g != 0 (ts_global.hpp:36-57);
+                                       reference defaults etaAcc 0.2, eps 0.005 (particles_data.hpp:112-114) */
+} sphgb_timestep;
+
+/* sph::computePositions (sph/include/sph/positions.hpp:180-200; GPU computePositionsKernel,
+ * positions_gpu.cu:118-165) on [first, last) with dt = ts->minDt and dt_m1 = ts->minDt_m1: Press
+ * position update with the periodic put-in-box, velocities at n+1, X_n+1 - X_n into x_m1 y_m1 z_m1,
+ * Adams-Bashforth update of u with du_m1 <- du; particles at rest within 2h of a fixed boundary do
+ * not move.  x_m1 y_m1 z_m1 du_m1 have the precision's hydro type (double or float). */
+int sphgb_compute_positions(sphgb_ctx* ctx, sphgb_particles* p, const sphgb_box* box, void* x_m1, void* y_m1,
+                            void* z_m1, void* du_m1, const sphgb_timestep* ts, int64_t first, int64_t last);
+/* sph::updateSmoothingLength (sph/include/sph/update_h.hpp:26-45, updateH kernels.hpp:26-32):
+ * h <- h/2 (1 + 1023 ng0 / nc)^(1/10) with nc the neighbour counts of the last search (p->nc) */
+int sphgb_update_smoothing_length(sphgb_ctx* ctx, sphgb_particles* p, int64_t first, int64_t last);
+/* sph::rhoTimestep (ts_global.hpp:72-95): Krho / |max divv| over [first, last); the reference's
+ * Krho is 0.06 (particles_data.hpp:107) */
+int sphgb_rho_timestep(sphgb_ctx* ctx, const sphgb_particles* p, int64_t first, int64_t last, double Krho,
+                       double* dt);
+/* sph::accelerationTimestep (ts_global.hpp:36-57): etaAcc sqrt(eps / sqrt(max |a|^2)) */
+int sphgb_acceleration_timestep(sphgb_ctx* ctx, const sphgb_particles* p, int64_t first, int64_t last,
+                                double etaAcc, double eps, double* dt);
+/* sph::computeTimestep at one rank (ts_global.hpp:97-113): min of the acceleration limit (g != 0),
+ * minDtCourant, minDtRho and maxDtIncrease * minDt; updates ttot, minDt_m1, minDt */
+int sphgb_compute_timestep(sphgb_ctx* ctx, const sphgb_particles* p, int64_t first, int64_t last,
+                           sphgb_timestep* ts);
+/* sphexa::localConservedQuantities (main/src/observables/conserved_quantities.hpp:49-113; GPU
+ * conservedQuantitiesGpu, conserved_gpu.cu:71-95) with u: out = {eKin, eInt, px, py, pz, Lx, Ly, Lz},
+ * FP64 sums in a fixed order (run-to-run identical) */
+int sphgb_conserved_quantities(sphgb_ctx* ctx, const sphgb_particles* p, int64_t first, int64_t last,
+                               double out[8]);
 
 /* ---- allocation-free entry point ----
  * No counterpart in the reference.  For callers that must not let a library call cudaMalloc or

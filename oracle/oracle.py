@@ -185,3 +185,36 @@ def sorted_sets(nbr: np.ndarray, nc: np.ndarray, ngmax: int) -> np.ndarray:
     a.sort(axis=1)
     a[mask] = -1
     return a
+
+def _dptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def run_positions(lib, f: dict, dt: float, dt_m1: float, box, bc) -> None:
+    """oracle_positions on numpy float64 arrays in f (x y z vx vy vz ax ay az xm1 ym1 zm1 u du dum1 h),
+    updated in place"""
+    fn = lib.oracle_positions
+    fn.argtypes = [C.c_int64] + [C.c_void_p] * 16 + [C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    c = np.ascontiguousarray(bc, dtype=np.uint8)
+    names = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "xm1", "ym1", "zm1", "u", "du", "dum1", "h"]
+    rc = fn(len(f["x"]), *[_dptr(f.get(k)) for k in names], dt, dt_m1, b.ctypes.data, c.ctypes.data)
+    assert rc == 0
+
+
+def run_update_h(lib, ng0: int, nc: np.ndarray, h: np.ndarray) -> None:
+    fn = lib.oracle_update_h
+    fn.argtypes = [C.c_int64, C.c_uint32, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    assert fn(len(h), ng0, nc.ctypes.data, h.ctypes.data) == 0
+
+
+def run_conserved(lib, f: dict) -> np.ndarray:
+    fn = lib.oracle_conserved
+    fn.argtypes = [C.c_int64] + [C.c_void_p] * 9
+    fn.restype = C.c_int
+    out = np.zeros(8)
+    names = ["x", "y", "z", "vx", "vy", "vz", "m", "u"]
+    assert fn(len(f["x"]), *[_dptr(f.get(k)) for k in names], out.ctypes.data) == 0
+    return out

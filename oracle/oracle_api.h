@@ -111,6 +111,21 @@ int oracle_jloop(const oracle_jloop_in* in, double* out);
 double oracle_kernel_K(double sincIndex);
 void oracle_tables(double sincIndex, double* wh, double* whd); /* 20000 each */
 
+/* One integration step for all particles (FP64 fields), the semantics of the reference GPU path
+ * (computePositionsKernel, sph/include/sph/positions_gpu.cu:118-165): Press position update with
+ * put-in-box, velocities at n+1, X_n+1 - X_n into xm1, Adams-Bashforth u update with dum1 <- du;
+ * particles at rest within 2h of a fixed boundary (bc 2) are left untouched. */
+int oracle_positions(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                     const double* ax, const double* ay, const double* az, double* xm1, double* ym1, double* zm1,
+                     double* u, const double* du, double* dum1, const double* h, double dt, double dt_m1,
+                     const double box[6], const uint8_t bc[3]);
+/* updateH (sph/include/sph/kernels.hpp:26-32) for every particle */
+int oracle_update_h(int64_t n, uint32_t ng0, const uint32_t* nc, double* h);
+/* localConservedQuantities with u (main/src/observables/conserved_quantities.hpp:49-113):
+ * out = {eKin, eInt, px, py, pz, Lx, Ly, Lz}, sequential sums in index order */
+int oracle_conserved(int64_t n, const double* x, const double* y, const double* z, const double* vx,
+                     const double* vy, const double* vz, const double* m, const double* u, double out[8]);
+
 #ifdef __cplusplus
 }
 #endif

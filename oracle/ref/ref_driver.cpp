@@ -39,6 +39,7 @@
 #include "sph/hydro_ve/iad_divv_curlv.hpp"
 #include "sph/hydro_ve/av_switches.hpp"
 #include "sph/hydro_ve/momentum_energy.hpp"
+#include "sph/positions.hpp"
 
 using KeyType = uint64_t;
 using Dataset = sphexa::ParticlesData<cstone::CpuTag>;
@@ -345,5 +346,67 @@ extern "C" int oracle_jloop(const oracle_jloop_in* in, double* out)
         }
         default: return 2;
     }
+    return 0;
+}
+
+/* ---- one integration step through the reference's own functions ----
+ * sph::positionUpdate, sph::energyUpdate, sph::fbcCheck (sph/include/sph/positions.hpp:46-85), in the
+ * loop structure of the GPU kernel (positions_gpu.cu:118-165), and sph::updateH (kernels.hpp:26-32). */
+extern "C" int oracle_positions(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                                const double* ax, const double* ay, const double* az, double* xm1, double* ym1,
+                                double* zm1, double* u, const double* du, double* dum1, const double* h, double dt,
+                                double dt_m1, const double box[6], const uint8_t bc[3])
+{
+    auto bt = [](uint8_t b) {
+        return b == 1 ? cstone::BoundaryType::periodic : (b == 2 ? cstone::BoundaryType::fixed : cstone::BoundaryType::open);
+    };
+    cstone::Box<double> B(box[0], box[1], box[2], box[3], box[4], box[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
+    const bool fbcX = B.boundaryX() == cstone::BoundaryType::fixed, fbcY = B.boundaryY() == cstone::BoundaryType::fixed,
+               fbcZ = B.boundaryZ() == cstone::BoundaryType::fixed;
+    const bool anyFBC = fbcX || fbcY || fbcZ;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        if (anyFBC && vx[i] == 0.0 && vy[i] == 0.0 && vz[i] == 0.0 &&
+            (sph::fbcCheck(x[i], h[i], B.xmax(), B.xmin(), fbcX) || sph::fbcCheck(y[i], h[i], B.ymax(), B.ymin(), fbcY) ||
+             sph::fbcCheck(z[i], h[i], B.zmax(), B.zmin(), fbcZ)))
+            continue;
+        cstone::Vec3<double> A{ax[i], ay[i], az[i]}, X{x[i], y[i], z[i]}, Xm1{xm1[i], ym1[i], zm1[i]}, V;
+        util::tie(X, V, Xm1) = sph::positionUpdate(dt, dt_m1, X, A, Xm1, B);
+        x[i] = X[0], y[i] = X[1], z[i] = X[2];
+        xm1[i] = Xm1[0], ym1[i] = Xm1[1], zm1[i] = Xm1[2];
+        vx[i] = V[0], vy[i] = V[1], vz[i] = V[2];
+        if (u) {
+            u[i] = sph::energyUpdate(u[i], dt, dt_m1, du[i], dum1[i]);
+            dum1[i] = du[i];
+        }
+    }
+    return 0;
+}
+
+extern "C" int oracle_update_h(int64_t n, uint32_t ng0, const uint32_t* nc, double* h)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) h[i] = sph::updateH(ng0, nc[i], h[i]);
+    return 0;
+}
+
+/* conserved_quantities.hpp includes <mpi.h> and cannot be compiled here: the restatement of the
+ * port is the only implementation of oracle_conserved (pinned by tests against numpy sums) */
+extern "C" int oracle_conserved(int64_t n, const double* x, const double* y, const double* z, const double* vx,
+                                const double* vy, const double* vz, const double* m, const double* u, double out[8])
+{
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t i = 0; i < n; ++i) {
+        cstone::Vec3<double> X{x[i], y[i], z[i]}, V{vx[i], vy[i], vz[i]};
+        s[0] += m[i] * norm2(V);
+        s[1] += u ? u[i] * m[i] : 0.0;
+        auto L = cross(X, V);
+        for (int k = 0; k < 3; ++k) {
+            s[2 + k] += m[i] * V[k];
+            s[5 + k] += m[i] * L[k];
+        }
+    }
+    out[0] = 0.5 * s[0];
+    for (int q = 1; q < 8; ++q) out[q] = s[q];
     return 0;
 }

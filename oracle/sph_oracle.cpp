@@ -989,3 +989,76 @@ extern "C" int oracle_jloop(const oracle_jloop_in* in, double* out)
     }
     return 0;
 }
+
+/* ---- one integration step (port) ----
+ * positionUpdate / energyUpdate / fbcCheck of sph/include/sph/positions.hpp:46-85 and putInBox of
+ * domain/include/cstone/sfc/box.hpp:193-214, with the GPU kernel's handling of particles frozen next
+ * to a fixed boundary (sph/include/sph/positions_gpu.cu:131-139: neither position nor energy moves). */
+extern "C" int oracle_positions(int64_t n, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                                const double* ax, const double* ay, const double* az, double* xm1, double* ym1,
+                                double* zm1, double* u, const double* du, double* dum1, const double* h, double dt,
+                                double dt_m1, const double box[6], const uint8_t bc[3])
+{
+    const bool fixed[3] = {bc[0] == 2, bc[1] == 2, bc[2] == 2};
+    const bool anyFixed = fixed[0] || fixed[1] || fixed[2];
+    auto nearFixed = [&](double c, double hi, int k) {
+        return fixed[k] && (std::abs(box[2 * k + 1] - c) < 2.0 * hi || std::abs(box[2 * k] - c) < 2.0 * hi);
+    };
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        if (anyFixed && vx[i] == 0.0 && vy[i] == 0.0 && vz[i] == 0.0 &&
+            (nearFixed(x[i], h[i], 0) || nearFixed(y[i], h[i], 1) || nearFixed(z[i], h[i], 2)))
+            continue;
+        double* X[3] = {x + i, y + i, z + i};
+        double* dX[3] = {xm1 + i, ym1 + i, zm1 + i};
+        double* V[3] = {vx + i, vy + i, vz + i};
+        const double A[3] = {ax[i], ay[i], az[i]};
+        const double idt = 1.0 / dt_m1, halfDtm1 = 0.5 * dt_m1;
+        for (int k = 0; k < 3; ++k) {
+            const double vn = *dX[k] * idt + halfDtm1 * A[k];
+            const double vnp1 = vn + A[k] * dt;
+            const double dxn = (vn + 0.5 * A[k] * std::abs(dt)) * dt;
+            double xn = *X[k] + dxn;
+            const double lo = box[2 * k], hi = box[2 * k + 1];
+            if (bc[k] == 1) {
+                if (xn > hi) xn -= hi - lo;
+                else if (xn < lo) xn += hi - lo;
+            }
+            *X[k] = xn;
+            *dX[k] = dxn;
+            *V[k] = vnp1;
+        }
+        if (u) {
+            double un = u[i] + du[i] * dt + 0.5 * (du[i] - dum1[i]) / dt_m1 * std::abs(dt) * dt;
+            if (un < 0.0) un = u[i] * std::exp(un * dt / u[i]);
+            u[i] = un;
+            dum1[i] = du[i];
+        }
+    }
+    return 0;
+}
+
+extern "C" int oracle_update_h(int64_t n, uint32_t ng0, const uint32_t* nc, double* h)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) h[i] = updateH(ng0, nc[i], h[i]);
+    return 0;
+}
+
+extern "C" int oracle_conserved(int64_t n, const double* x, const double* y, const double* z, const double* vx,
+                                const double* vy, const double* vz, const double* m, const double* u, double out[8])
+{
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t i = 0; i < n; ++i) {
+        const double X[3] = {x[i], y[i], z[i]}, V[3] = {vx[i], vy[i], vz[i]}, mi = m[i];
+        s[0] += mi * (V[0] * V[0] + (V[1] * V[1] + V[2] * V[2]));
+        s[1] += u ? u[i] * mi : 0.0;
+        for (int k = 0; k < 3; ++k) s[2 + k] += mi * V[k];
+        s[5] += mi * (X[1] * V[2] - X[2] * V[1]);
+        s[6] += mi * (X[2] * V[0] - X[0] * V[2]);
+        s[7] += mi * (X[0] * V[1] - X[1] * V[0]);
+    }
+    out[0] = 0.5 * s[0];
+    for (int q = 1; q < 8; ++q) out[q] = s[q];
+    return 0;
+}

@@ -64,6 +64,11 @@ class SphgbGrads(C.Structure):
     _fields_ = [(f, C.c_void_p) for f in ("x", "y", "z", "vx", "vy", "vz", "h", "u")]
 
 
+class SphgbTimestep(C.Structure):
+    _fields_ = [(f, C.c_double) for f in ("minDt", "minDt_m1", "ttot", "minDtCourant", "minDtRho", "maxDtIncrease",
+                                          "g", "etaAcc", "eps")]
+
+
 # name -> (argtypes); every function returns int status unless listed in RESTYPES
 _P = C.c_void_p
 _I64 = C.c_int64
@@ -108,6 +113,14 @@ SIGNATURES = {
     "sphgb_kernel_launches": [_P, C.POINTER(C.c_int64)],
     "sphgb_measure_fma_peak": [_P, C.c_int32, C.POINTER(C.c_double)],
     "sphgb_sfc_keys_noalloc": [_P, _P, _P, _I64, C.POINTER(SphgbBox), _P, _P],
+    "sphgb_compute_positions": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox), _P, _P, _P, _P,
+                                C.POINTER(SphgbTimestep), _I64, _I64],
+    "sphgb_update_smoothing_length": [_P, C.POINTER(SphgbParticles), _I64, _I64],
+    "sphgb_rho_timestep": [_P, C.POINTER(SphgbParticles), _I64, _I64, C.c_double, C.POINTER(C.c_double)],
+    "sphgb_acceleration_timestep": [_P, C.POINTER(SphgbParticles), _I64, _I64, C.c_double, C.c_double,
+                                    C.POINTER(C.c_double)],
+    "sphgb_compute_timestep": [_P, C.POINTER(SphgbParticles), _I64, _I64, C.POINTER(SphgbTimestep)],
+    "sphgb_conserved_quantities": [_P, C.POINTER(SphgbParticles), _I64, _I64, C.POINTER(C.c_double)],
 }
 RESTYPES = {"sphgb_status_string": C.c_char_p, "sphgb_last_cuda_error": C.c_char_p}
 

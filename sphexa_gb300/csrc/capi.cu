@@ -53,6 +53,9 @@ int checkRange(const sphgb_particles* p, int64_t first, int64_t last)
 }
 
 }  // namespace
+
+// for the entry points in other translation units
+int useDeviceOf(sphgb_ctx* c) { return useDevice(c); }
 }  // namespace sphgb
 
 using namespace sphgb;
@@ -138,7 +141,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32,    &c->refMask,
-                    &c->refFp64,    &c->divvBound};
+                    &c->refFp64,    &c->divvBound,  &c->intScratch};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)

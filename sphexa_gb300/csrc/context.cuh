@@ -115,6 +115,8 @@ struct sphgb_ctx {
     bool refineMixed = true;
     sphgb::DBuf refMask, refFp64, divvBound;
     int64_t stats_refinedGradh = 0, stats_refinedDivv = 0;
+    // block partials of the integration-step reductions
+    sphgb::DBuf intScratch;
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -353,3 +353,86 @@ def sweep_passes(ctx: Context, d: ParticlesData, variant: str = "ve", av_clean: 
                allow=(0, _lib.SPHGB_ERR_NOCONV))
     d.minDtCourant = dt.value
     return st
+
+# ---------------------------------------------------------------- time integration and reductions
+@dataclass
+class Timestep:
+    """sphexa::ParticlesData time-step state (particles_data.hpp:96-141): current and previous step,
+    elapsed time, the pass limits and the limiter constants."""
+    minDt: float = 1e-12
+    minDt_m1: float = 1e-12
+    ttot: float = 0.0
+    minDtCourant: float = float("inf")
+    minDtRho: float = float("inf")
+    maxDtIncrease: float = 1.1
+    g: float = 0.0
+    etaAcc: float = 0.2
+    eps: float = 0.005
+
+    def to_c(self) -> _lib.SphgbTimestep:
+        t = _lib.SphgbTimestep()
+        for f, _ in t._fields_:
+            setattr(t, f, float(getattr(self, f)))
+        return t
+
+    def update_from(self, t: _lib.SphgbTimestep) -> None:
+        for f, _ in t._fields_:
+            setattr(self, f, getattr(t, f))
+
+
+def compute_positions(ctx: Context, d: ParticlesData, box: Box, x_m1: torch.Tensor, y_m1: torch.Tensor,
+                      z_m1: torch.Tensor, du_m1: torch.Tensor | None, ts: Timestep, first: int = 0,
+                      last: int | None = None) -> None:
+    """sph::computePositions (positions.hpp:180-200) with dt = ts.minDt, dt_m1 = ts.minDt_m1."""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    b = box.to_c()
+    t = ts.to_c()
+    check(ctx.lib.sphgb_compute_positions(ctx.h, C.byref(s), C.byref(b), x_m1.data_ptr(), y_m1.data_ptr(),
+                                          z_m1.data_ptr(), du_m1.data_ptr() if du_m1 is not None else None,
+                                          C.byref(t), first, last), "computePositions")
+
+
+def update_smoothing_length(ctx: Context, d: ParticlesData, first: int = 0, last: int | None = None) -> None:
+    """sph::updateSmoothingLength (update_h.hpp:26-45)"""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    check(ctx.lib.sphgb_update_smoothing_length(ctx.h, C.byref(s), first, last), "updateSmoothingLength")
+
+
+def rho_timestep(ctx: Context, d: ParticlesData, Krho: float = 0.06, first: int = 0, last: int | None = None) -> float:
+    """sph::rhoTimestep (ts_global.hpp:72-95)"""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    v = C.c_double()
+    check(ctx.lib.sphgb_rho_timestep(ctx.h, C.byref(s), first, last, Krho, C.byref(v)), "rhoTimestep")
+    return v.value
+
+
+def acceleration_timestep(ctx: Context, d: ParticlesData, etaAcc: float = 0.2, eps: float = 0.005, first: int = 0,
+                          last: int | None = None) -> float:
+    """sph::accelerationTimestep (ts_global.hpp:36-57)"""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    v = C.c_double()
+    check(ctx.lib.sphgb_acceleration_timestep(ctx.h, C.byref(s), first, last, etaAcc, eps, C.byref(v)),
+          "accelerationTimestep")
+    return v.value
+
+
+def compute_timestep(ctx: Context, d: ParticlesData, ts: Timestep, first: int = 0, last: int | None = None) -> None:
+    """sph::computeTimestep at one rank (ts_global.hpp:97-113): updates ts in place."""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    t = ts.to_c()
+    check(ctx.lib.sphgb_compute_timestep(ctx.h, C.byref(s), first, last, C.byref(t)), "computeTimestep")
+    ts.update_from(t)
+
+
+def conserved_quantities(ctx: Context, d: ParticlesData, first: int = 0, last: int | None = None) -> dict:
+    """sphexa::localConservedQuantities (conserved_quantities.hpp:49-113)"""
+    last = d.n if last is None else last
+    s = d.c_struct()
+    out = (C.c_double * 8)()
+    check(ctx.lib.sphgb_conserved_quantities(ctx.h, C.byref(s), first, last, out), "conservedQuantities")
+    return {"eKin": out[0], "eInt": out[1], "linmom": list(out[2:5]), "angmom": list(out[5:8])}
