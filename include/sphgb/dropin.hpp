@@ -17,6 +17,7 @@
  */
 #pragma once
 
+#include <array>
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
@@ -145,9 +146,11 @@ sphgb_box toBox(const Box& box)
     b.lim[3] = double(box.ymax());
     b.lim[4] = double(box.zmin());
     b.lim[5] = double(box.zmax());
-    b.bc[0] = uint8_t(box.boundaryX()) == 1 ? SPHGB_BC_PERIODIC : SPHGB_BC_OPEN;
-    b.bc[1] = uint8_t(box.boundaryY()) == 1 ? SPHGB_BC_PERIODIC : SPHGB_BC_OPEN;
-    b.bc[2] = uint8_t(box.boundaryZ()) == 1 ? SPHGB_BC_PERIODIC : SPHGB_BC_OPEN;
+    // cstone::BoundaryType and sphgb_boundary share their numbering (open 0, periodic 1, fixed 2)
+    auto bt = [](auto t) { return uint8_t(t) <= SPHGB_BC_FIXED ? uint8_t(t) : uint8_t(SPHGB_BC_OPEN); };
+    b.bc[0] = bt(box.boundaryX());
+    b.bc[1] = bt(box.boundaryY());
+    b.bc[2] = bt(box.boundaryZ());
     return b;
 }
 
@@ -337,6 +340,84 @@ void computeEOS_HydroStd(std::size_t startIndex, std::size_t endIndex, Dataset& 
     sphgb_ctx* c = bind(d);
     sphgb_particles p = particles(d);
     check(sphgb_compute_eos_std(c, &p, int64_t(startIndex), int64_t(endIndex)), "computeEOS_HydroStd");
+}
+
+// ---- time integration and reductions ----
+
+template<class Dataset>
+sphgb_timestep timestepOf(const Dataset& d)
+{
+    sphgb_timestep ts{};
+    ts.minDt = double(d.minDt);
+    ts.minDt_m1 = double(d.minDt_m1);
+    ts.ttot = double(d.ttot);
+    ts.minDtCourant = double(d.minDtCourant);
+    ts.minDtRho = double(d.minDtRho);
+    ts.maxDtIncrease = double(Dataset::maxDtIncrease);
+    ts.g = double(d.g);
+    ts.etaAcc = double(d.etaAcc);
+    ts.eps = double(d.eps);
+    return ts;
+}
+
+//! sph::computePositions (positions.hpp:180-200), every particle on the step d.minDt (no rungs)
+template<class GroupView, class Dataset, class Box>
+void computePositions(const GroupView& grp, Dataset& d, const Box& box)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    auto& dv = d.devData;
+    const sphgb_box b = toBox(box);
+    const sphgb_timestep ts = timestepOf(d);
+    check(sphgb_compute_positions(c, &p, &b, ptr(dv.x_m1), ptr(dv.y_m1), ptr(dv.z_m1), ptr(dv.du_m1), &ts,
+                                  int64_t(grp.firstBody), int64_t(grp.lastBody)),
+          "computePositions");
+}
+
+//! sph::updateSmoothingLength (update_h.hpp:26-45)
+template<class GroupView, class Dataset>
+void updateSmoothingLength(const GroupView& grp, Dataset& d)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    check(sphgb_update_smoothing_length(c, &p, int64_t(grp.firstBody), int64_t(grp.lastBody)),
+          "updateSmoothingLength");
+}
+
+//! sph::rhoTimestep (ts_global.hpp:72-95)
+template<class Dataset>
+double rhoTimestep(std::size_t first, std::size_t last, Dataset& d)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    double dt = 0;
+    check(sphgb_rho_timestep(c, &p, int64_t(first), int64_t(last), double(d.Krho), &dt), "rhoTimestep");
+    return dt;
+}
+
+//! sph::computeTimestep at one rank (ts_global.hpp:97-113): updates d.ttot, d.minDt_m1, d.minDt
+template<class Dataset>
+void computeTimestep(std::size_t first, std::size_t last, Dataset& d)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    sphgb_timestep ts = timestepOf(d);
+    check(sphgb_compute_timestep(c, &p, int64_t(first), int64_t(last), &ts), "computeTimestep");
+    d.ttot = ts.ttot;
+    d.minDt_m1 = ts.minDt_m1;
+    d.minDt = ts.minDt;
+}
+
+//! sphexa::localConservedQuantities (conserved_quantities.hpp:49-113): {eKin, eInt, linmom, angmom}
+template<class Dataset>
+std::tuple<double, double, std::array<double, 3>, std::array<double, 3>>
+localConservedQuantities(std::size_t first, std::size_t last, Dataset& d)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    double o[8];
+    check(sphgb_conserved_quantities(c, &p, int64_t(first), int64_t(last), o), "localConservedQuantities");
+    return {o[0], o[1], {o[2], o[3], o[4]}, {o[5], o[6], o[7]}};
 }
 
 }  // namespace dropin

@@ -86,6 +86,20 @@ int run(const char* in, const char* out, bool ve, double lim[6], int bc[3])
         download(*v, o);
     download(dv.du, o);
     std::fwrite(&d.minDtCourant, sizeof(double), 1, o);
+
+    // the rest of the propagator's step (ve_hydro.hpp:190-204): time step, positions, h, observables
+    for (auto* v : {&dv.x_m1, &dv.y_m1, &dv.z_m1, &dv.du_m1}) v->resize(n);
+    dr::computeTimestep(0, n, d);
+    dr::computePositions(grp, d, domain.box());
+    dr::updateSmoothingLength(grp, d);
+    auto [eKin, eInt, linmom, angmom] = dr::localConservedQuantities(0, n, d);
+    download(dv.x, o);
+    download(dv.vx, o);
+    download(dv.u, o);
+    download(dv.h, o);
+    const double tail[10] = {d.minDt, d.ttot, eKin, eInt, linmom[0], linmom[1], linmom[2],
+                             angmom[0], angmom[1], angmom[2]};
+    std::fwrite(tail, sizeof(double), 10, o);
     std::fclose(o);
     return 0;
 }

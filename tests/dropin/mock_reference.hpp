@@ -3,6 +3,8 @@
 // include/sphgb/dropin.hpp can be compiled and linked without the reference sources.
 #pragma once
 
+#include <cmath>
+
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -27,7 +29,10 @@ public:
         if (p_) cudaFree(p_);
         p_ = nullptr;
         n_ = n;
-        if (n) cudaMalloc(&p_, n * sizeof(T));
+        if (n) {
+            cudaMalloc(&p_, n * sizeof(T));
+            cudaMemset(p_, 0, n * sizeof(T));  // value-initialised, as thrust::device_vector::resize
+        }
     }
     std::size_t size() const { return n_; }
     T* data() { return p_; }
@@ -84,6 +89,7 @@ struct DeviceParticlesData
     DeviceVector<Th> h, vx, vy, vz, alpha, rho, p, c, xm, kx, gradh, prho, divv, curlv, c11, c12, c13, c22, c23, c33,
         ax, ay, az, dV11, dV12, dV13, dV22, dV23, dV33;
     DeviceVector<Tm> m;
+    DeviceVector<Th> x_m1, y_m1, z_m1, du_m1;
     DeviceVector<uint64_t> keys;
     DeviceVector<unsigned> nc;
 };
@@ -95,6 +101,8 @@ struct ParticlesData
     using RealType  = double;
     unsigned ng0{100}, ngmax{150};
     double gamma{5.0 / 3.0}, Kcour{0.2}, sincIndex{6.0}, minDt{1e-6}, minDtCourant{0};
+    double minDt_m1{1e-6}, ttot{0}, minDtRho{INFINITY}, Krho{0.06}, g{0}, etaAcc{0.2}, eps{0.005};
+    constexpr static double maxDtIncrease = 1.1;
     Th alphamin{0.05f}, alphamax{1.0f}, decay_constant{0.2f};
     DeviceParticlesData<Th, Tm> devData;
 };

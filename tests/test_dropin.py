@@ -52,13 +52,33 @@ def test_dropin_sweep_matches_oracle(tmp_path, port, variant, precision):
     n = wl.n
     names = ["rho", "c11", "c12", "ax", "ay", "az", "xm", "kx", "divv", "alpha", "du"]
     got = {k: res[i * n:(i + 1) * n] for i, k in enumerate(names)}
+    min_dt_courant = res[11 * n]
+    step = {k: res[11 * n + 1 + i * n:11 * n + 1 + (i + 1) * n] for i, k in enumerate(["x", "vx", "u", "h"])}
+    tail = res[15 * n + 1:]
     ref = port.sweep(wl, variant, False)
     if precision == "fp64":
         fields = ("rho", "c11", "ax", "du") + (("xm", "kx", "divv", "alpha") if variant == "ve" else ())
         for k in fields:
             err = np.max(np.abs(got[k] - ref[k])) / (np.max(np.abs(ref[k])) + 1e-300)
             assert err <= 1e-12, f"{k}: {err:.3e}"
-        assert res[-1] == pytest.approx(ref["minDtCourant"], rel=1e-12)
+        assert min_dt_courant == pytest.approx(ref["minDtCourant"], rel=1e-12)
+        # the step that follows, computed by the oracle from the oracle's sweep
+        dt = min(ref["minDtCourant"], 1.1 * 1e-6)
+        assert tail[0] == pytest.approx(dt, rel=1e-12) and tail[1] == pytest.approx(dt, rel=1e-12)
+        f = {k: ref[k].copy() for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "u", "du", "h")}
+        for k in ("xm1", "ym1", "zm1", "dum1"):
+            f[k] = np.zeros(n)
+        from oracle import oracle as O
+        O.run_positions(port.lib, f, dt, 1e-6, ref["box"], wl.bc)
+        for k in ("x", "vx", "u"):
+            scale = np.max(np.abs(f[k])) + 1e-300
+            assert np.max(np.abs(step[k] - f[k])) <= 1e-12 * scale, k
+        h = ref["h"].copy()
+        O.run_update_h(port.lib, 100, ref["nc"].astype(np.uint32), h)
+        np.testing.assert_allclose(step["h"], h, rtol=1e-15)
+        f["m"] = ref["m"]
+        cons = O.run_conserved(port.lib, f)
+        np.testing.assert_allclose(tail[2:], cons, rtol=1e-9, atol=1e-14)
     else:
         assert np.max(np.abs(got["rho"] - ref["rho"]) / ref["rho"]) <= 1e-6
         a32 = np.stack([got["ax"], got["ay"], got["az"]], 1)
