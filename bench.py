@@ -269,6 +269,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-integration", action="store_true")
     ap.add_argument("--adjoint-side", type=int, default=100)
     args = ap.parse_args()
 
@@ -435,6 +436,49 @@ def main() -> None:
                       "d2h_bytes_per_step": d2h, "steps": k_e2e,
                       "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
         del d
+
+    # ---------------- integration step on the same particles (FP64): time step, positions, h, sums
+    if not args.no_integration:
+        d = sph.ParticlesData.from_workload(wl, "fp64", dev)
+        boxi = sph.Box(wl.box.copy(), wl.bc.copy())
+        sph.sweep(ctx, d, boxi, args.variant, False)
+        m1 = {k: torch.zeros(n, dtype=torch.float64, device=dev) for k in ("x", "y", "z", "du")}
+        ts = sph.Timestep(minDt=1e-7, minDt_m1=1e-7, minDtCourant=d.minDtCourant)
+
+        def integrate():
+            sph.compute_timestep(ctx, d, ts)
+            sph.compute_positions(ctx, d, boxi, m1["x"], m1["y"], m1["z"], m1["du"], ts)
+            sph.update_smoothing_length(ctx, d)
+            return sph.conserved_quantities(ctx, d)
+
+        for _ in range(max(1, args.warmup)):
+            integrate()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k_int = max(3, args.steps)
+        t0 = time.perf_counter()
+        pos_ms = 0.0
+        for _ in range(k_int):
+            sph.compute_timestep(ctx, d, ts)
+            e0.record()
+            sph.compute_positions(ctx, d, boxi, m1["x"], m1["y"], m1["z"], m1["du"], ts)
+            e1.record()
+            sph.update_smoothing_length(ctx, d)
+            sph.conserved_quantities(ctx, d)
+            torch.cuda.synchronize()
+            pos_ms += e0.elapsed_time(e1)
+        wall = (time.perf_counter() - t0) * 1e3 / k_int
+        pos_ms /= k_int
+        # algorithmic bytes of the position + energy update per particle: reads x y z v a x_m1 u du
+        # du_m1 (15 doubles), writes x y z v x_m1 u du_m1 (11 doubles)
+        bytes_pp = 8 * (15 + 11)
+        out["integration"] = {"step_ms": wall, "positions_ms": pos_ms,
+                              "positions_gbs": n * bytes_pp / (pos_ms * 1e-3) / 1e9,
+                              "positions_hbm_frac": n * bytes_pp / (pos_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                              "bytes_per_particle": bytes_pp,
+                              "what": "computeTimestep + computePositions + updateSmoothingLength + conserved sums"}
+        del d, m1
+        torch.cuda.empty_cache()
 
     # ---------------- adjoint / forward on the adjoint configuration (1M particles, FP64 std chain)
     if not args.no_adjoint:

@@ -28,6 +28,7 @@ struct PosArgs {
     void *vx, *vy, *vz, *xm1, *ym1, *zm1, *dum1;
     const void *ax, *ay, *az, *h;
     double dt, dtm1;
+    double idtm1, halfDtm1, adt;  // 1/dt_m1, 0.5 dt_m1, |dt|: the same values for every particle
     DevBox box;
     int fixed[3];
     int64_t first, last;
@@ -75,15 +76,12 @@ __global__ void __launch_bounds__(kIntBlock) positionsKernel(PosArgs a)
     double* X[3] = {a.x + i, a.y + i, a.z + i};
     T* dX[3] = {xm1 + i, ym1 + i, zm1 + i};
     T* V[3] = {vx + i, vy + i, vz + i};
-    const double idt = __ddiv_rn(1.0, a.dtm1);
-    const double halfDtm1 = __dmul_rn(0.5, a.dtm1);
-    const double adt = fabs(a.dt);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const double vHalf = __dmul_rn(double(*dX[k]), idt);
-        const double vn = __dadd_rn(vHalf, __dmul_rn(halfDtm1, A[k]));
+        const double vHalf = __dmul_rn(double(*dX[k]), a.idtm1);
+        const double vn = __dadd_rn(vHalf, __dmul_rn(a.halfDtm1, A[k]));
         const double vnp1 = __dadd_rn(vn, __dmul_rn(A[k], a.dt));
-        const double dxn = __dmul_rn(__dadd_rn(vn, __dmul_rn(__dmul_rn(0.5, A[k]), adt)), a.dt);
+        const double dxn = __dmul_rn(__dadd_rn(vn, __dmul_rn(__dmul_rn(0.5, A[k]), a.adt)), a.dt);
         double xn = __dadd_rn(*X[k], dxn);
         if (a.box.pbc[k]) {
             if (xn > a.box.hi[k]) xn = __dsub_rn(xn, a.box.L[k]);
@@ -292,6 +290,9 @@ int sphgb_compute_positions(sphgb_ctx* c, sphgb_particles* p, const sphgb_box* b
     a.h = p->h;
     a.dt = ts->minDt;
     a.dtm1 = ts->minDt_m1;
+    a.idtm1 = 1.0 / a.dtm1;  // the host's IEEE division: the value the reference forms per particle
+    a.halfDtm1 = 0.5 * a.dtm1;
+    a.adt = std::fabs(a.dt);
     a.box = makeDevBox(*box);
     for (int k = 0; k < 3; ++k) a.fixed[k] = box->bc[k] == SPHGB_BC_FIXED;
     a.first = first;
@@ -299,9 +300,7 @@ int sphgb_compute_positions(sphgb_ctx* c, sphgb_particles* p, const sphgb_box* b
     const unsigned blocks = gridFor(last - first, kIntBlock);
     if (p->precision == SPHGB_MIXED) positionsKernel<float><<<blocks, kIntBlock, 0, c->stream>>>(a);
     else positionsKernel<double><<<blocks, kIntBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "positionsKernel"));
-    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
-    return SPHGB_OK;
+    return launched(c, "positionsKernel");
 }
 
 int sphgb_update_smoothing_length(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
@@ -316,9 +315,7 @@ int sphgb_update_smoothing_length(sphgb_ctx* c, sphgb_particles* p, int64_t firs
     else
         updateHKernel<double><<<blocks, kIntBlock, 0, c->stream>>>(first, last, c->prm.ng0, p->nc,
                                                                    static_cast<double*>(p->h));
-    SPHGB_TRY(launched(c, "updateHKernel"));
-    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
-    return SPHGB_OK;
+    return launched(c, "updateHKernel");
 }
 
 int sphgb_rho_timestep(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last, double Krho, double* dt)
