@@ -100,7 +100,7 @@ struct sphgb_ctx {
     bool haveNbr = false;
     // owned pair lists of the pair-once momentum-energy pass: owned[k * stride + (i - first)] =
     // j | mutual << 31 for the pairs i evaluates, ownedCount per particle; valid for epoch ownedEpoch
-    sphgb::DBuf owned, ownedCount;
+    sphgb::DBuf owned, ownedCount, ownedR2;
     int64_t ownedEpoch = -1;
     // summation mode of the FP64 passes (order-fixed, or one evaluation per mutual pair) and the
     // per-particle accumulators of the pair-once passes (up to 6 x n doubles)

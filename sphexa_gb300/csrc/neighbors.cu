@@ -402,9 +402,31 @@ struct MutualArgs {
     uint32_t ngmax;
     const uint32_t* nbr;
     const uint32_t* count;
+    // (2 h_j)^2 in FP32 per particle, negative when the 2h box of j leaves the periodic box (j's
+    // search takes the minimum image): no FP64 work per pair outside the rounding margin
+    const float* r2f;
     uint32_t* owned;
     uint32_t* ownedCount;
 };
+
+__global__ void radius2Kernel(const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z, const void* h, int hIsFloat, int64_t n, DevBox b,
+                              float* __restrict__ r2f)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    const double hj = loadH(h, hIsFloat, j);
+    const float tf = 2.f * float(hj);
+    bool usePbc = false;
+    if (b.pbc[0] | b.pbc[1] | b.pbc[2]) {  // the search's decision for target j (nbrGroupKernel)
+        const double twoH = __dmul_rn(2.0, hj);
+        const bool inside = __dsub_rn(x[j], twoH) >= b.lo[0] && __dsub_rn(y[j], twoH) >= b.lo[1] &&
+                            __dsub_rn(z[j], twoH) >= b.lo[2] && __dadd_rn(x[j], twoH) <= b.hi[0] &&
+                            __dadd_rn(y[j], twoH) <= b.hi[1] && __dadd_rn(z[j], twoH) <= b.hi[2];
+        usePbc = !inside;
+    }
+    r2f[j] = usePbc ? -(tf * tf) : tf * tf;
+}
 
 __device__ bool mutualExact(const MutualArgs& a, int64_t i, int64_t j, double hj)
 {
@@ -456,14 +478,14 @@ __device__ bool mutualPair(const MutualArgs& a, int64_t i, int ci[3], float4 li,
         }
         r[k] = fmaf(float(d), a.u[k], lv[k]);
     }
-    const double hj = loadH(a.h, a.hIsFloat, j);
-    if (wrapped) return mutualExact(a, i, j, hj);
+    const float R2s = __ldg(a.r2f + j);
+    // across a periodic face only a target that takes the minimum image can list i
+    if (wrapped && !(R2s < 0.f)) return false;
     const float d2 = fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2]));
-    const float tf = 2.f * float(hj);
-    const float R2 = tf * tf, eps = 0x1p-17f * R2;
+    const float R2 = fabsf(R2s), eps = 0x1p-17f * R2;
     if (d2 < R2 - eps) return true;
     if (d2 > R2 + eps) return false;
-    return mutualExact(a, i, j, hj);
+    return mutualExact(a, i, j, loadH(a.h, a.hIsFloat, j));
 }
 
 __global__ void __launch_bounds__(128) ownedListKernel(MutualArgs a)
@@ -553,6 +575,10 @@ int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, 
     const int64_t nWork = c->nbrLast - c->nbrFirst;
     SPHGB_TRY(c->owned.ensure(sizeof(uint32_t) * size_t(c->nbrNgmax) * size_t(c->nbrStride)));
     SPHGB_TRY(c->ownedCount.ensure(sizeof(uint32_t) * size_t(c->nbrStride)));
+    SPHGB_TRY(c->ownedR2.ensure(sizeof(float) * size_t(c->n)));
+    radius2Kernel<<<gridFor(c->n, 256), 256, 0, c->stream>>>(x, y, z, h, hIsFloat, c->n, c->box,
+                                                            c->ownedR2.as<float>());
+    SPHGB_TRY(launched(c, "radius2Kernel"));
     MutualArgs a;
     a.x = x;
     a.y = y;
@@ -569,6 +595,7 @@ int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, 
     a.ngmax = c->nbrNgmax;
     a.nbr = c->nbr.as<uint32_t>();
     a.count = c->ncount.as<uint32_t>();
+    a.r2f = c->ownedR2.as<float>();
     a.owned = c->owned.as<uint32_t>();
     a.ownedCount = c->ownedCount.as<uint32_t>();
     ownedListKernel<<<gridFor(nWork, 128), 128, 0, c->stream>>>(a);
