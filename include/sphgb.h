@@ -111,6 +111,13 @@ int sphgb_set_deterministic(sphgb_ctx* ctx, int32_t on);
  * FP32 error bound, with the neighbour shells their values depend on; on = 0 leaves the FP32
  * results.  The counts of the last sweep are in sphgb_stats.refined_gradh / refined_divv. */
 int sphgb_set_mixed_refinement(sphgb_ctx* ctx, int32_t on);
+/* Domain mode.  0 (default): every sphgb_domain_sync stands alone (open dimensions take the
+ * particle extrema).  1: the syncs are the steps of one simulation, as cstone::Domain::sync
+ * (domain/include/cstone/domain/assignment.hpp:80-82): from the second sync on, the open-dimension
+ * box follows limitBoxShrinking (box.hpp:397-414) against the previous sync's box.  Setting the
+ * mode starts a new sequence.  The tree is the converged cornerstone tree of each sync in both
+ * modes (the reference's focus tree reaches it by one rebalance step per sync). */
+int sphgb_set_domain_mode(sphgb_ctx* ctx, int32_t mode);
 int sphgb_default_params(sphgb_params* params);
 /* kernel normalisation constant K used by the pair passes */
 int sphgb_get_kernel_K(sphgb_ctx* ctx, double* K);

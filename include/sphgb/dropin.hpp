@@ -161,10 +161,13 @@ template<class KeyType, class T, class Box>
 class SingleRankDomain
 {
 public:
-    SingleRankDomain(int /*rank*/, int /*numRanks*/, unsigned bucketSize, unsigned /*bucketSizeFocus*/,
+    // the tree the reference's octreeProperties() exposes is its focus tree, refined to
+    // bucketSizeFocus (domain/domain.hpp:416-428); the coarser global tree (bucketSize) only assigns
+    // ranks, which has no counterpart at one rank
+    SingleRankDomain(int /*rank*/, int /*numRanks*/, unsigned /*bucketSize*/, unsigned bucketSizeFocus,
                      float /*theta*/, const Box& box, int device = 0)
         : box_(box)
-        , bucket_(bucketSize)
+        , bucket_(bucketSizeFocus)
         , device_(device)
     {
     }
@@ -173,6 +176,10 @@ public:
     void sync(Dataset& d, Props&... extraProperties)
     {
         sphgb_ctx* c = bind(d, device_);
+        if (!started_) {  // this domain's syncs are the steps of one simulation (box shrink limit)
+            check(sphgb_set_domain_mode(c, 1), "sphgb_set_domain_mode");
+            started_ = true;
+        }
         sphgb_params prm{};
         sphgb_default_params(&prm);
         prm.ng0 = d.ng0;
@@ -232,6 +239,7 @@ private:
     Box box_;
     unsigned bucket_;
     int device_;
+    bool started_ = false;
 };
 
 /*! cstone::findNeighbors (domain/include/cstone/findneighbors.hpp:149-170) on the tree of the last

@@ -410,3 +410,17 @@ extern "C" int oracle_conserved(int64_t n, const double* x, const double* y, con
     for (int q = 1; q < 8; ++q) out[q] = s[q];
     return 0;
 }
+
+/* cstone::limitBoxShrinking (domain/include/cstone/sfc/box.hpp:397-414) on limits only */
+extern "C" int oracle_limit_box_shrinking(const double fit[6], const double prev[6], double out[6])
+{
+    using B = cstone::Box<double>;
+    B f(fit[0], fit[1], fit[2], fit[3], fit[4], fit[5], cstone::BoundaryType::open, cstone::BoundaryType::open,
+        cstone::BoundaryType::open);
+    B p(prev[0], prev[1], prev[2], prev[3], prev[4], prev[5], cstone::BoundaryType::open, cstone::BoundaryType::open,
+        cstone::BoundaryType::open);
+    B r = cstone::limitBoxShrinking(f, p);
+    const double o[6] = {r.xmin(), r.xmax(), r.ymin(), r.ymax(), r.zmin(), r.zmax()};
+    for (int k = 0; k < 6; ++k) out[k] = o[k];
+    return 0;
+}

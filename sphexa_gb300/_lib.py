@@ -83,6 +83,7 @@ SIGNATURES = {
     "sphgb_default_params": [C.POINTER(SphgbParams)],
     "sphgb_set_deterministic": [_P, C.c_int32],
     "sphgb_set_mixed_refinement": [_P, C.c_int32],
+    "sphgb_set_domain_mode": [_P, C.c_int32],
     "sphgb_get_kernel_K": [_P, C.POINTER(C.c_double)],
     "sphgb_domain_sync": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox)],
     "sphgb_get_tree": [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),

@@ -174,6 +174,14 @@ int sphgb_set_deterministic(sphgb_ctx* c, int32_t on)
     return SPHGB_OK;
 }
 
+int sphgb_set_domain_mode(sphgb_ctx* c, int32_t mode)
+{
+    if (!c || (mode != 0 && mode != 1)) return SPHGB_ERR_ARG;
+    c->domainMode = mode;
+    c->domainFirst = true;
+    return SPHGB_OK;
+}
+
 int sphgb_set_mixed_refinement(sphgb_ctx* c, int32_t on)
 {
     if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;

@@ -117,6 +117,11 @@ struct sphgb_ctx {
     int64_t stats_refinedGradh = 0, stats_refinedDivv = 0;
     // block partials of the integration-step reductions
     sphgb::DBuf intScratch;
+    // domain mode: 0 every sync stands alone; 1 the syncs are the steps of one simulation (the box
+    // of a later sync is limited in how far it shrinks against the previous one)
+    int domainMode = 0;
+    bool domainFirst = true;
+    sphgb_box prevBox{};
     int precisionBuilt = -1;
     const double* xBuilt = nullptr;
 

@@ -8,6 +8,8 @@
 // pass: particle s is the first particle of every node whose key range also holds key[s+bucket];
 // such a node holds more than `bucket` particles and is split.  The children c >= 1 of all split
 // nodes, plus key 0, are exactly the leaf start keys.
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "context.cuh"
@@ -300,8 +302,21 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
                 b.lim[2 * k + 1] = ext[2 * k + 1];
             }
     }
+    // across the steps of one simulation the box may grow freely but shrinks by at most 5 % of its
+    // previous length per side and sync (limitBoxShrinking, domain/include/cstone/sfc/box.hpp:397-414,
+    // applied from the second sync on, domain/assignment.hpp:80-82)
+    if (c->domainMode == 1 && !c->domainFirst) {
+        const sphgb_box& q = c->prevBox;
+        for (int k = 0; k < 3; ++k) {
+            const double lo = q.lim[2 * k], hi = q.lim[2 * k + 1], len = hi - lo;
+            b.lim[2 * k] = std::min(b.lim[2 * k], lo + 0.05 * len);
+            b.lim[2 * k + 1] = std::max(b.lim[2 * k + 1], hi - 0.05 * len);
+        }
+    }
     for (int k = 0; k < 3; ++k)
         if (!(b.lim[2 * k + 1] > b.lim[2 * k])) return SPHGB_ERR_ARG;
+    c->prevBox = b;
+    c->domainFirst = false;
     *box = b;
     c->hbox = b;
     c->box = makeDevBox(b);

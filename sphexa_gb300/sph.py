@@ -85,6 +85,10 @@ class Context:
         error) in FP64 from the exact inputs (default True)."""
         check(self.lib.sphgb_set_mixed_refinement(self.h, int(bool(on))), "sphgb_set_mixed_refinement")
 
+    def set_domain_mode(self, mode: int) -> None:
+        """0: every sync stands alone; 1: syncs are the steps of one simulation (box shrink limit)."""
+        check(self.lib.sphgb_set_domain_mode(self.h, int(mode)), "sphgb_set_domain_mode")
+
     @property
     def K(self) -> float:
         k = C.c_double()
