@@ -15,6 +15,8 @@
 // runs an FP64 instruction.  Only pairs whose FP32 distance lies within a rounding margin of the
 // radius are re-tested in FP64 from the original coordinates.  Lists are stored transposed,
 // nbr[k * stride + (i - first)], so that the pair passes read them coalesced.
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "pairs.cuh"
@@ -405,6 +407,10 @@ struct MutualArgs {
     // (2 h_j)^2 in FP32 per particle, negative when the 2h box of j leaves the periodic box (j's
     // search takes the minimum image): no FP64 work per pair outside the rounding margin
     const float* r2f;
+    // (L/4)^2 of the smallest periodic box length (INFINITY without periodic axes): pairs whose
+    // larger 2h exceeds L/4 are not evaluated once, because the legacy wrap of the pair loops
+    // (threshold 2h of the list owner, box.hpp:216-238) may then pick different images at the two ends
+    float wrapSafe2;
     uint32_t* owned;
     uint32_t* ownedCount;
 };
@@ -481,6 +487,7 @@ __device__ bool mutualPair(const MutualArgs& a, int64_t i, int ci[3], float4 li,
     const float R2s = __ldg(a.r2f + j);
     // across a periodic face only a target that takes the minimum image can list i
     if (wrapped && !(R2s < 0.f)) return false;
+    if (fmaxf(fabsf(R2s), fabsf(__ldg(a.r2f + i))) > a.wrapSafe2) return false;
     const float d2 = fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2]));
     const float R2 = fabsf(R2s), eps = 0x1p-17f * R2;
     if (d2 < R2 - eps) return true;
@@ -596,6 +603,9 @@ int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, 
     a.nbr = c->nbr.as<uint32_t>();
     a.count = c->ncount.as<uint32_t>();
     a.r2f = c->ownedR2.as<float>();
+    a.wrapSafe2 = INFINITY;
+    for (int k = 0; k < 3; ++k)
+        if (c->box.pbc[k]) a.wrapSafe2 = std::min(a.wrapSafe2, float(0.0625 * c->box.L[k] * c->box.L[k]));
     a.owned = c->owned.as<uint32_t>();
     a.ownedCount = c->ownedCount.as<uint32_t>();
     ownedListKernel<<<gridFor(nWork, 128), 128, 0, c->stream>>>(a);
