@@ -217,6 +217,16 @@ typedef struct {
 int sphgb_adjoint_std(sphgb_ctx* ctx, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads,
                       int32_t deterministic);
 
+/* Reverse mode of the VE chain xmass -> kx/gradh -> EOS -> IAD + divv/curlv (+dV) -> AV switches ->
+ * momentum-energy<av_clean> (ve_hydro.hpp:130-204), for the state left by the last forward VE
+ * passes on the frozen lists of the last search (first = 0, last = n), FP64 form.  alpha_prev is
+ * alpha before the AV switch of that forward (the switch updates p->alpha in place); the time step
+ * of the switch is params.minDt.  Seeds: rho (= kx m / xm), a, du; outputs as sphgb_adjoint_std.
+ * The AV switch and the Atwood weights are differentiated piecewise, on the branch the forward
+ * took; the Courant time step is not differentiated.  deterministic as sphgb_adjoint_std. */
+int sphgb_adjoint_ve(sphgb_ctx* ctx, sphgb_particles* p, const double* alpha_prev, int32_t av_clean,
+                     const sphgb_seeds* seeds, sphgb_grads* grads, int32_t deterministic);
+
 /* ---- statistics and timing ---- */
 int sphgb_get_stats(sphgb_ctx* ctx, sphgb_stats* stats);
 /* milliseconds of the last call of each stage, measured with CUDA events on the context

@@ -109,6 +109,8 @@ SIGNATURES = {
     "sphgb_sweep_passes": [_P, C.POINTER(SphgbParticles), C.c_int32, C.c_int32, C.POINTER(C.c_double)],
     "sphgb_adjoint_std": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbSeeds), C.POINTER(SphgbGrads),
                           C.c_int32],
+    "sphgb_adjoint_ve": [_P, C.POINTER(SphgbParticles), _P, C.c_int32, C.POINTER(SphgbSeeds),
+                         C.POINTER(SphgbGrads), C.c_int32],
     "sphgb_get_stats": [_P, C.POINTER(SphgbStats)],
     "sphgb_get_timings": [_P, C.POINTER(C.c_float), C.c_int32],
     "sphgb_kernel_launches": [_P, C.POINTER(C.c_int64)],

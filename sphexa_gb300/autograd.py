@@ -1,9 +1,10 @@
-"""torch.autograd harness over the hand-written adjoint (sphgb_adjoint_std).
+"""torch.autograd harness over the hand-written adjoints (sphgb_adjoint_std, sphgb_adjoint_ve).
 
 A thin test/analysis harness: the forward runs the std pair passes (density, EOS, IAD,
-momentum-energy) through the C ABI on the neighbour lists frozen by ``FrozenStdSweep.freeze``,
-and the backward calls the adjoint kernels.  Gradients are taken with respect to positions,
-velocities, smoothing lengths and internal energy; masses are constants.
+momentum-energy) or the VE pair passes (xmass, gradh, EOS, IAD + divv/curlv, AV switches,
+momentum-energy) through the C ABI on the neighbour lists frozen by ``freeze``, and the backward
+calls the adjoint kernels.  Gradients are taken with respect to positions, velocities, smoothing
+lengths and internal energy; masses and the alpha before the AV switch are constants.
 """
 
 from __future__ import annotations
@@ -45,24 +46,62 @@ class FrozenStdSweep:
         return tuple(f[k].clone() for k in ("rho", "ax", "ay", "az", "du"))
 
     def backward(self, g_rho, g_ax, g_ay, g_az, g_du):
-        n = self.d.n
-        dev = self.d.device
-        seeds = _lib.SphgbSeeds()
-        keep = []
-        for name, g in (("rho", g_rho), ("ax", g_ax), ("ay", g_ay), ("az", g_az), ("du", g_du)):
-            if g is not None:
-                g = g.detach().to(torch.float64).contiguous()
-                keep.append(g)
-                setattr(seeds, name, g.data_ptr())
-        out = {k: torch.zeros(n, dtype=torch.float64, device=dev) for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u")}
-        grads = _lib.SphgbGrads()
-        for k, t in out.items():
-            setattr(grads, k, t.data_ptr())
-        s = self.d.c_struct()
-        check(self.ctx.lib.sphgb_adjoint_std(self.ctx.h, C.byref(s), C.byref(seeds), C.byref(grads),
-                                            int(self.deterministic)),
-              "sphgb_adjoint_std")
-        return tuple(out[k] for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u"))
+        return _run_adjoint(self, g_rho, g_ax, g_ay, g_az, g_du, "sphgb_adjoint_std",
+                            lambda s, seeds, grads: (C.byref(s), C.byref(seeds), C.byref(grads),
+                                                     int(self.deterministic)))
+
+
+def _run_adjoint(sweep, g_rho, g_ax, g_ay, g_az, g_du, fn, args):
+    """call the adjoint entry ``fn`` with the output seeds; returns the input gradients"""
+    n = sweep.d.n
+    dev = sweep.d.device
+    seeds = _lib.SphgbSeeds()
+    keep = []
+    for name, g in (("rho", g_rho), ("ax", g_ax), ("ay", g_ay), ("az", g_az), ("du", g_du)):
+        if g is not None:
+            g = g.detach().to(torch.float64).contiguous()
+            keep.append(g)
+            setattr(seeds, name, g.data_ptr())
+    out = {k: torch.zeros(n, dtype=torch.float64, device=dev) for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u")}
+    grads = _lib.SphgbGrads()
+    for k, t in out.items():
+        setattr(grads, k, t.data_ptr())
+    s = sweep.d.c_struct()
+    check(getattr(sweep.ctx.lib, fn)(sweep.ctx.h, *args(s, seeds, grads)), fn)
+    return tuple(out[k] for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u"))
+
+
+class FrozenVeSweep(FrozenStdSweep):
+    """VE chain on frozen lists.  The alpha before the AV switch is kept from freeze() on, so that
+    every forward starts from the same alpha; av_clean selects momentumAndEnergy<avClean>."""
+
+    def __init__(self, ctx, d, box, av_clean: bool = False, deterministic: bool = False):
+        super().__init__(ctx, d, box, deterministic)
+        self.av_clean = av_clean
+        self.alpha0 = None
+
+    def freeze(self) -> None:
+        super().freeze()
+        self.alpha0 = self.d.f["alpha"].clone()
+
+    def forward(self, x, y, z, vx, vy, vz, h, u):
+        f = self.d.f
+        for k, t in zip(("x", "y", "z", "vx", "vy", "vz", "h", "u"), (x, y, z, vx, vy, vz, h, u)):
+            f[k].copy_(t.detach())
+        f["alpha"].copy_(self.alpha0)
+        sph.compute_xmass(self.ctx, self.d)
+        sph.compute_ve_def_gradh(self.ctx, self.d)
+        sph.compute_eos(self.ctx, self.d)
+        sph.compute_iad_divv_curlv(self.ctx, self.d)
+        sph.compute_av_switches(self.ctx, self.d)
+        sph.compute_momentum_energy(self.ctx, self.d, self.av_clean)
+        return tuple(f[k].clone() for k in ("rho", "ax", "ay", "az", "du"))
+
+    def backward(self, g_rho, g_ax, g_ay, g_az, g_du):
+        a0 = self.alpha0
+        return _run_adjoint(self, g_rho, g_ax, g_ay, g_az, g_du, "sphgb_adjoint_ve",
+                            lambda s, seeds, grads: (C.byref(s), a0.data_ptr(), int(self.av_clean), C.byref(seeds),
+                                                     C.byref(grads), int(self.deterministic)))
 
 
 class StdSweepFunction(torch.autograd.Function):
@@ -77,6 +116,10 @@ class StdSweepFunction(torch.autograd.Function):
     def backward(fctx, g_rho, g_ax, g_ay, g_az, g_du):
         grads = fctx.sweep.backward(g_rho, g_ax, g_ay, g_az, g_du)
         return (None,) + grads
+
+
+class VeSweepFunction(StdSweepFunction):
+    """(x, y, z, vx, vy, vz, h, u) -> (rho, ax, ay, az, du) of the VE chain on frozen lists."""
 
 
 def loss_rho_a(rho, ax, ay, az, rho_target):

@@ -373,6 +373,14 @@ int sphgb_adjoint_std(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* seeds
     return adjointStd(c, p, seeds, grads, deterministic);
 }
 
+int sphgb_adjoint_ve(sphgb_ctx* c, sphgb_particles* p, const double* alpha_prev, int32_t av_clean,
+                     const sphgb_seeds* seeds, sphgb_grads* grads, int32_t deterministic)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!p || !grads) return SPHGB_ERR_ARG;
+    return adjointVe(c, p, alpha_prev, av_clean, seeds, grads, deterministic);
+}
+
 int sphgb_get_stats(sphgb_ctx* c, sphgb_stats* s)
 {
     if (!c || !s) return SPHGB_ERR_ARG;

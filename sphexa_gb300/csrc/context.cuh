@@ -186,6 +186,8 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
 
 int buildTranspose(sphgb_ctx* c);
 int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic);
+int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avClean, const sphgb_seeds* s,
+              sphgb_grads* g, int deterministic);
 int refineMixedGradh(sphgb_ctx* c, sphgb_particles* p);
 int refineMixedDivv(sphgb_ctx* c, sphgb_particles* p, const float* bound);
 

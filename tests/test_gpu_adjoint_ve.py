@@ -1,0 +1,140 @@
+"""The hand-written adjoint of the VE chain (sphgb_adjoint_ve) against torch autograd through the FP64
+torch restatement of the same chain (tests/torch_reference.py ve_chain) and against FP64 central
+differences.
+
+Workload: the adjoint configuration's generator (jittered periodic lattice, Fourier density
+field, Gaussian velocities) at 10^3 to 12^3 particles, with u, h and the alpha before the AV switch
+varied per particle (so that the AV switch takes both of its branches, the Atwood weights all three
+of theirs and no two h coincide) and an AV time step of 1e-2.  Loss L = sum (rho - rho_target)^2 +
+sum |a|^2 (+ a seed on du for the reference-gradient test) on the frozen neighbour lists.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
+
+
+def setup(side=10, seed=7, av_clean=False, deterministic=False):
+    import torch
+    from sphexa_gb300 import autograd as AG, sph, workloads as W
+    wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    wl.fields["u"] = wl.fields["u"] * rng.uniform(0.8, 1.2, wl.n)
+    wl.fields["h"] = wl.fields["h"] * rng.uniform(0.97, 1.03, wl.n)
+    wl.fields["alpha"] = rng.uniform(0.05, 0.5, wl.n)
+    ctx = sph.Context(0)
+    ctx.set_params(minDt=1e-2)
+    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0", av_clean=av_clean)
+    box = sph.Box(wl.box.copy(), wl.bc.copy())
+    sw = AG.FrozenVeSweep(ctx, d, box, av_clean=av_clean, deterministic=deterministic)
+    sw.freeze()
+    order = sph.Domain(ctx, box).order(wl.n)
+    rho_t = torch.tensor(wl.fields["rho_target"][order], dtype=torch.float64, device="cuda:0")
+    return wl, ctx, sw, rho_t
+
+
+@pytest.mark.parametrize("av_clean", [False, True])
+@pytest.mark.parametrize("deterministic", [False, True])
+def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, deterministic):
+    import torch
+    from sphexa_gb300 import autograd as AG, sph
+    from torch_reference import ve_chain
+    wl, ctx, sw, rho_t = setup(side=10, seed=7, av_clean=av_clean, deterministic=deterministic)
+    n = wl.n
+    ng = int(ctx.params.ngmax)
+    nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
+    cnt = np.minimum(sw.d.nc.cpu().numpy().astype(np.int64) - 1, ng)
+    ei = np.repeat(np.arange(n), cnt)
+    ej = np.concatenate([nb[k, :cnt[k]] for k in range(n)])
+    dev = "cuda:0"
+    wh, whd = port.tables(6.0)
+    tab = torch.tensor(wh, dtype=torch.float64, device=dev)
+    tabd = torch.tensor(whd, dtype=torch.float64, device=dev)
+    p = ctx.params
+    inp = [t.clone().requires_grad_(True) for t in sw.inputs()]
+    out_ref = ve_chain(*inp, sw.d.m.clone(), sw.alpha0.clone(), torch.tensor(ei, device=dev),
+                       torch.tensor(ej, device=dev), tab, tabd, ctx.K, float(p.gamma),
+                       torch.tensor(wl.box[1::2] - wl.box[0::2], dtype=torch.float64), [True, True, True],
+                       float(p.minDt), float(p.alphamin), float(p.alphamax), float(p.decay_constant), av_clean)
+    gen = torch.Generator(device="cpu").manual_seed(3)
+    s_du = torch.randn(n, generator=gen, dtype=torch.float64).to(dev)
+    L_ref = AG.loss_rho_a(*out_ref[:4], rho_t) + (s_du * out_ref[4]).sum()
+    L_ref.backward()
+    g_ref = {f: inp[k].grad.detach().cpu().numpy() for k, f in enumerate(FIELDS)}
+
+    base = [t.detach().clone().requires_grad_(True) for t in sw.inputs()]
+    out = AG.VeSweepFunction.apply(sw, *base)
+    for name, a, b in zip(("rho", "ax", "ay", "az", "du"), out, out_ref):
+        ref = b.detach().cpu().numpy()
+        err = np.max(np.abs(a.detach().cpu().numpy() - ref)) / (np.max(np.abs(ref)) + 1e-300)
+        assert err <= 1e-10, name
+    L = AG.loss_rho_a(*out[:4], rho_t) + (s_du * out[4]).sum()
+    L.backward()
+    for k, f in enumerate(FIELDS):
+        g = base[k].grad.detach().cpu().numpy()
+        err = np.linalg.norm(g - g_ref[f]) / (np.linalg.norm(g_ref[f]) + 1e-300)
+        print(f"VE reference gradient {f:3s}: normwise rel {err:.3e}")
+        assert err <= 1e-9, f
+    ctx.close()
+
+
+def test_deterministic_ve_adjoint_is_bit_reproducible():
+    wl, ctx, sw, rho_t = setup(side=10, seed=9, av_clean=True, deterministic=True)
+    vals = sw.inputs()
+    rho, ax, ay, az, du = sw.forward(*vals)
+    seeds = (2.0 * (rho - rho_t), 2.0 * ax, 2.0 * ay, 2.0 * az, du)
+    g1 = [t.cpu().numpy() for t in sw.backward(*seeds)]
+    g2 = [t.cpu().numpy() for t in sw.backward(*seeds)]
+    for a, b in zip(g1, g2):
+        np.testing.assert_array_equal(a, b)
+    ctx.close()
+
+
+def test_ve_adjoint_requires_alpha_before_the_switch():
+    import ctypes as C
+    from sphexa_gb300 import _lib
+    wl, ctx, sw, rho_t = setup(side=8, seed=11)
+    s = sw.d.c_struct()
+    seeds = _lib.SphgbSeeds()
+    grads = _lib.SphgbGrads()
+    assert ctx.lib.sphgb_adjoint_ve(ctx.h, C.byref(s), None, 0, C.byref(seeds), C.byref(grads), 0) == 1  # SPHGB_ERR_ARG
+    ctx.close()
+
+
+@pytest.mark.parametrize("av_clean", [False, True])
+def test_ve_adjoint_matches_central_differences(av_clean):
+    from sphexa_gb300 import autograd as AG
+    wl, ctx, sw, rho_t = setup(side=12, seed=5, av_clean=av_clean)
+    base = [t.clone().requires_grad_(True) for t in sw.inputs()]
+    rho, ax, ay, az, du = AG.VeSweepFunction.apply(sw, *base)
+    L = AG.loss_rho_a(rho, ax, ay, az, rho_t)
+    L.backward()
+    grads = {f: base[k].grad.detach().cpu().numpy() for k, f in enumerate(FIELDS)}
+    rng = np.random.Generator(np.random.PCG64(55555))
+    picks = [(FIELDS[rng.integers(0, 8)], int(rng.integers(0, wl.n))) for _ in range(64)]
+    rows = []
+    for field, i in picks:
+        k = FIELDS.index(field)
+        vals = [t.detach().clone() for t in base]
+        x0 = float(vals[k][i])
+        eps = 1e-6 * (x0 if field == "h" else 1.0)
+        vals[k][i] = x0 + eps
+        lp = float(AG.loss_rho_a(*sw.forward(*vals)[:4], rho_t).item())
+        vals[k][i] = x0 - eps
+        lm = float(AG.loss_rho_a(*sw.forward(*vals)[:4], rho_t).item())
+        fd = (lp - lm) / (2 * eps)
+        ad = float(grads[field][i])
+        scale = max(abs(fd), 1e-3 * float(np.max(np.abs(grads[field]))), 1e-300)
+        rows.append((field, i, ad, fd, abs(ad - fd) / scale))
+    for f in FIELDS:
+        e = [r[4] for r in rows if r[0] == f]
+        if e:
+            print(f"{f:3s} n={len(e):2d} max rel {max(e):.3e} median {np.median(e):.3e}")
+    # u moves no pair distance and no branch of the AV switch or the Atwood weights: smooth
+    smooth = [r[4] for r in rows if r[0] == "u"]
+    assert smooth and max(smooth) <= 1e-6
+    assert np.median([r[4] for r in rows]) <= 1e-4
+    ctx.close()
