@@ -188,15 +188,16 @@ def cpu_baseline(side: int, threads: int = 0, workload: str = "sedov200_jit", va
                       f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
 
 
-def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int) -> dict:
-    """Forward std chain (density, EOS, IAD, momentum-energy on frozen lists) against its adjoint
-    for the loss sum (rho - rho_target)^2 + sum |a|^2, FP64, CUDA events on the default stream."""
+def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str = "std") -> dict:
+    """Forward chain on frozen lists against its adjoint for the loss sum (rho - rho_target)^2 +
+    sum |a|^2, FP64, CUDA events on the default stream.  chain "std": density, EOS, IAD,
+    momentum-energy; "ve": xmass, gradh, EOS, IAD + divv/curlv, AV switches, momentum-energy."""
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=5, rho_seed=55, v_seed=555, target_seed=5555)
     d = sph.ParticlesData.from_workload(wl, "fp64", dev)
     box = sph.Box(wl.box.copy(), wl.bc.copy())
-    sw = AG.FrozenStdSweep(ctx, d, box)
+    sw = AG.FrozenStdSweep(ctx, d, box) if chain == "std" else AG.FrozenVeSweep(ctx, d, box)
     sw.freeze()
     order = sph.Domain(ctx, box).order(wl.n)
     rho_t = torch.tensor(wl.fields["rho_target"][order], dtype=torch.float64, device=dev)
@@ -226,7 +227,7 @@ def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int) -> dict:
     fwd = timed(lambda: sw.forward(*vals), k)
     adj = timed(lambda: sw.backward(*seeds), k)
     return {"workload": f"adjoint config: jittered Fourier lattice {side}^3 = {wl.n} particles, frozen lists",
-            "form": "fp64 std chain", "forward_ms": fwd, "adjoint_ms": adj, "ratio": adj / fwd,
+            "form": f"fp64 {chain} chain", "forward_ms": fwd, "adjoint_ms": adj, "ratio": adj / fwd,
             "first_adjoint_ms_incl_transpose": first_ms, "steps": k}
 
 
@@ -483,6 +484,7 @@ def main() -> None:
     # ---------------- adjoint / forward on the adjoint configuration (1M particles, FP64 std chain)
     if not args.no_adjoint:
         out["adjoint"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup)
+        out["adjoint"]["ve"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup, chain="ve")
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.cpu_side, workload=args.workload, variant=args.variant)

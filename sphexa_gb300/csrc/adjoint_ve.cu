@@ -46,14 +46,15 @@ struct VeAdjArgs {
     // outputs
     double *bx, *by, *bz, *bvx, *bvy, *bvz, *bh, *bu;
     // per-particle quotients
-    double *hInv, *rho, *vol, *lnxm;
+    double *hInv, *rho, *rhoInv, *vol, *kxInv, *xmInv, *lnxm;
     // forward sums
     double *en, *avE, *G, *vsig, *P, *wom, *wr0;
     uint32_t* vsigArg;
     // adjoints of the intermediate fields
     double *prhoB, *cB, *alphaB, *rhoB, *xmB, *kxB, *CB, *gB, *divvB, *gradhB;
+    double* Rav;  // 3 x n: R_i = sum_j fac_j W_j r_j of the AV pair terms (i's C partials, avCbar)
     // seeds of the pair terms
-    double *GB, *vsigB, *tauB, *PB, *Skx, *Som, *Sr0, *R0b;
+    double *GB, *CGB, *vsigB, *tauB, *PB, *Skx, *Som, *Sr0, *R0b;
 };
 
 constexpr uint32_t kNoPair = 0xffffffffu;
@@ -98,7 +99,9 @@ __device__ __forceinline__ MeSide meSide(const VeAdjArgs& a, int64_t i)
     s.alpha = a.alpha[i];
     s.m = a.m[i];
     s.rho = a.rho[i];
+    s.rhoInv = a.rhoInv[i];
     s.xm = a.xm[i];
+    s.xmInv = a.xmInv[i];
     s.lnxm = a.lnxm[i];
     s.prho = a.prho[i];
 #pragma unroll
@@ -129,9 +132,13 @@ __global__ void veQuotKernel(VeAdjArgs a)
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= a.n) return;
     const double xm = a.xm[i], kx = a.kx[i];
+    const double rho = kx * a.m[i] / xm;
     a.hInv[i] = 1.0 / a.h[i];
-    a.rho[i] = kx * a.m[i] / xm;
+    a.rho[i] = rho;
+    a.rhoInv[i] = 1.0 / rho;
     a.vol[i] = xm / kx;
+    a.kxInv[i] = 1.0 / kx;
+    a.xmInv[i] = 1.0 / xm;
     a.lnxm[i] = log(xm);
 }
 
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
     loadC(a, i, Ci);
     const double hInv = a.hInv[i], ci = a.c[i], divvi = a.divv[i];
     const double Wk0 = a.K * hInv * hInv * hInv;
-    double G[3] = {0.0, 0.0, 0.0}, P[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double S[3] = {0.0, 0.0, 0.0}, P[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     double vsig = 1e-40 * ci, so = -3.0 * a.xm[i], sr = -3.0 * a.m[i];
     uint32_t arg = kNoPair;
     const unsigned nc = a.lv.capped(i);
@@ -191,13 +198,11 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
                 arg = j;
             }
         }
-        double CIr[3];
-        symv(Ci, r, CIr);
-        const double fac = -a.vol[j] * (divvi - a.divv[j]) * Wk0 * w;
+        const double fac = a.vol[j] * (divvi - a.divv[j]) * w;
         const double xw = a.xm[j] * w;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            G[k] += fac * CIr[k];
+            S[k] += fac * r[k];
 #pragma unroll
             for (int t = 0; t < 3; ++t) P[3 * k + t] -= xw * v[k] * r[t];
         }
@@ -205,8 +210,11 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
         so += a.xm[j] * dterh;
         sr += a.m[j] * dterh;
     }
+    // G = -K h^-3 C_i S, S = sum_j vol_j (divv_i - divv_j) w r
+    double G[3];
+    symv(Ci, S, G);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) a.G[k * a.n + i] = G[k];
+    for (int k = 0; k < 3; ++k) a.G[k * a.n + i] = -Wk0 * G[k];
 #pragma unroll
     for (int k = 0; k < 9; ++k) a.P[k * a.n + i] = P[k];
     a.vsig[i] = vsig;
@@ -222,16 +230,21 @@ struct MeSeed {
     bool any;
 };
 
+template<bool WithDu>
 __device__ __forceinline__ MeSeed meSeed(const VeAdjArgs& a, int64_t i)
 {
     MeSeed s;
     s.mb[0] = a.sAx ? -a.K * a.sAx[i] : 0.0;
     s.mb[1] = a.sAy ? -a.K * a.sAy[i] : 0.0;
     s.mb[2] = a.sAz ? -a.K * a.sAz[i] : 0.0;
-    const double du = a.sDu ? a.sDu[i] : 0.0;
-    s.enb = a.K * a.prho[i] * du;
-    s.avEb = a.avE[i] >= 0.0 ? 0.5 * a.K * du : 0.0;
-    s.any = s.mb[0] != 0.0 || s.mb[1] != 0.0 || s.mb[2] != 0.0 || du != 0.0;
+    s.any = s.mb[0] != 0.0 || s.mb[1] != 0.0 || s.mb[2] != 0.0;
+    s.enb = s.avEb = 0.0;
+    if (WithDu) {
+        const double du = a.sDu[i];
+        s.enb = a.K * a.prho[i] * du;
+        s.avEb = a.avE[i] >= 0.0 ? 0.5 * a.K * du : 0.0;
+        s.any = s.any || du != 0.0;
+    }
     return s;
 }
 
@@ -279,6 +292,7 @@ __device__ __forceinline__ void meAddJ(MeAcc& s, const MeGrad& o)
     }
 }
 
+template<bool AvClean>
 __device__ __forceinline__ void meFlush(const VeAdjArgs& a, int64_t k, const MeAcc& s, bool atomic)
 {
     put(a.bx, k, s.x[0], atomic);
@@ -295,11 +309,12 @@ __device__ __forceinline__ void meFlush(const VeAdjArgs& a, int64_t k, const MeA
     put(a.xmB, k, s.xm, atomic);
 #pragma unroll
     for (int q = 0; q < 6; ++q) put(a.CB + q * a.n, k, s.C[q], atomic);
-    if (a.avClean)
+    if (AvClean)
 #pragma unroll
         for (int q = 0; q < 6; ++q) put(a.gB + q * a.n, k, s.g[q], atomic);
 }
 
+template<bool AvClean, bool WithDu>
 __device__ __forceinline__ void mePair(const VeAdjArgs& a, int64_t i, int64_t j, const MeSide& I, const MeSide& J,
                                        double etaCrit, const MeSeed& sd, MeGrad& o)
 {
@@ -308,19 +323,20 @@ __device__ __forceinline__ void mePair(const VeAdjArgs& a, int64_t i, int64_t j,
     vdiff(a, i, j, v);
     double dwi, dwj;
     const double wi = lookupVS(a.wh, d * I.hInv, dwi), wj = lookupVS(a.wh, d * J.hInv, dwj);
-    meAdj(r, d, rinv, v, I, J, wi, dwi, wj, dwj, a.avClean != 0, etaCrit, sd.mb, sd.enb, sd.avEb, o);
+    meAdj<AvClean, WithDu>(r, d, rinv, v, I, J, wi, dwi, wj, dwj, etaCrit, sd.mb, sd.enb, sd.avEb, o);
 }
 
-template<bool TwoSided>
+// WithDu: a du seed is given (the energy sums en, avE of the forward are then needed)
+template<bool TwoSided, bool AvClean, bool WithDu>
 __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     MeAcc s{};
     const MeSide S = meSide(a, k);
-    const MeSeed sd = meSeed(a, k);
+    const MeSeed sd = meSeed<WithDu>(a, k);
     // own terms outside the pairs: du = K (prho en + avE / 2) and the rho seed
-    s.prho = a.sDu ? a.K * a.en[k] * a.sDu[k] : 0.0;
+    s.prho = WithDu ? a.K * a.en[k] * a.sDu[k] : 0.0;
     s.rho = a.sRho ? a.sRho[k] : 0.0;
     if (sd.any) {
         const unsigned nc = a.lv.capped(k);
@@ -329,7 +345,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
             const int64_t j = a.lv.at(k, q);
             const MeSide J = meSide(a, j);
             MeGrad o;
-            mePair(a, k, j, S, J, etaCrit, sd, o);
+            mePair<AvClean, WithDu>(a, k, j, S, J, etaCrit, sd, o);
             meAddI(s, o);
             if (!TwoSided) {
                 atomicAdd(a.bx + j, -o.r[0]);
@@ -346,7 +362,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
                 atomicAdd(a.xmB + j, o.xmJ);
 #pragma unroll
                 for (int t = 0; t < 6; ++t) atomicAdd(a.CB + t * a.n + j, o.CJ[t]);
-                if (a.avClean)
+                if (AvClean)
 #pragma unroll
                     for (int t = 0; t < 6; ++t) atomicAdd(a.gB + t * a.n + j, o.gJ[t]);
             }
@@ -355,15 +371,62 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
     if (TwoSided) {
         for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
             const int64_t i = a.tIdx[e];
-            const MeSeed si = meSeed(a, i);
+            const MeSeed si = meSeed<WithDu>(a, i);
             if (!si.any) continue;
             const MeSide I = meSide(a, i);
             MeGrad o;
-            mePair(a, i, k, I, S, etaCritOf(a.lv.capped(i)), si, o);
+            mePair<AvClean, WithDu>(a, i, k, I, S, etaCritOf(a.lv.capped(i)), si, o);
             meAddJ(s, o);
         }
     }
-    meFlush(a, k, s, !TwoSided);
+    meFlush<AvClean>(a, k, s, !TwoSided);
+}
+
+// one evaluation per owned entry of the owned lists built with the neighbour lists: a mutual pair
+// gives both particles' terms (meAdjMutual), a one-sided entry its owner's (the same function with
+// the neighbour's seeds zero); the neighbour's partials are added with FP64 atomics.  No avClean.
+template<bool WithDu>
+__global__ void __launch_bounds__(kVeAdjBlock) meVeAdjOnceKernel(VeAdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    MeAcc s{};
+    const MeSide S = meSide(a, k);
+    const MeSeed sd = meSeed<WithDu>(a, k);
+    s.prho = WithDu ? a.K * a.en[k] * a.sDu[k] : 0.0;
+    s.rho = a.sRho ? a.sRho[k] : 0.0;
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        MeSeed sj{};
+        if (mutual) sj = meSeed<WithDu>(a, j);
+        if (!sd.any && !sj.any) continue;
+        const MeSide J = meSide(a, j);
+        double r[3], d, rinv, v[3];
+        geom(a, k, j, r, d, rinv);
+        vdiff(a, k, j, v);
+        double dwi, dwj;
+        const double wi = lookupVS(a.wh, d * S.hInv, dwi), wj = lookupVS(a.wh, d * J.hInv, dwj);
+        MeGrad o;
+        meAdjMutual<WithDu>(r, d, rinv, v, S, J, wi, dwi, wj, dwj, sd.mb, sd.enb, sd.avEb, sj.mb, sj.enb, sj.avEb, o);
+        meAddI(s, o);
+        atomicAdd(a.bx + j, -o.r[0]);
+        atomicAdd(a.by + j, -o.r[1]);
+        atomicAdd(a.bz + j, -o.r[2]);
+        atomicAdd(a.bvx + j, -o.v[0]);
+        atomicAdd(a.bvy + j, -o.v[1]);
+        atomicAdd(a.bvz + j, -o.v[2]);
+        atomicAdd(a.bh + j, o.hJ);
+        atomicAdd(a.prhoB + j, o.prhoJ);
+        atomicAdd(a.cB + j, o.c);
+        atomicAdd(a.alphaB + j, o.alpha);
+        atomicAdd(a.rhoB + j, o.rhoJ);
+        atomicAdd(a.xmB + j, o.xmJ);
+#pragma unroll
+        for (int t = 0; t < 6; ++t) atomicAdd(a.CB + t * a.n + j, o.CJ[t]);
+    }
+    meFlush<false>(a, k, s, true);
 }
 
 // ---------------------------------------------------------------- AV switch
@@ -375,8 +438,14 @@ __global__ void veAvSeedKernel(VeAdjArgs a)
     double Gb[3], vsigb, hb, divvb, cb;
     avSeed(a.av, a.alphaB[k], a.alpha0[k], a.h[k], a.c[k], a.divv[k], G, a.vsig[k], Gb, vsigb, hb, divvb, cb);
     if (a.vsigArg[k] == kNoPair) cb += 1e-40 * vsigb;  // vsig = 1e-40 c_i when no pair approaches
+    double C[6], CGb[3];
+    loadC(a, k, C);
+    symv(C, Gb, CGb);
 #pragma unroll
-    for (int t = 0; t < 3; ++t) a.GB[t * a.n + k] = Gb[t];
+    for (int t = 0; t < 3; ++t) {
+        a.GB[t * a.n + k] = Gb[t];
+        a.CGB[t * a.n + k] = CGb[t];
+    }
     a.vsigB[k] = vsigb;
     a.bh[k] += hb;
     a.divvB[k] += divvb;
@@ -384,9 +453,9 @@ __global__ void veAvSeedKernel(VeAdjArgs a)
 }
 
 struct AvSeedV {
-    double Gb[3], vsigb;
+    double Gb[3], CGb[3], vsigb;
     uint32_t arg;
-    bool any;
+    bool any, gAny;  // gAny: a G seed; without one only the pair that set vsig has partials
 };
 
 __device__ __forceinline__ AvSeedV avSeedOf(const VeAdjArgs& a, int64_t i)
@@ -395,14 +464,16 @@ __device__ __forceinline__ AvSeedV avSeedOf(const VeAdjArgs& a, int64_t i)
     s.Gb[0] = a.GB[i];
     s.Gb[1] = a.GB[a.n + i];
     s.Gb[2] = a.GB[2 * a.n + i];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) s.CGb[t] = a.CGB[t * a.n + i];
     s.vsigb = a.vsigB[i];
     s.arg = a.vsigArg[i];
-    s.any = s.Gb[0] != 0.0 || s.Gb[1] != 0.0 || s.Gb[2] != 0.0 || s.vsigb != 0.0;
+    s.gAny = s.Gb[0] != 0.0 || s.Gb[1] != 0.0 || s.Gb[2] != 0.0;
+    s.any = s.gAny || s.vsigb != 0.0;
     return s;
 }
 
-__device__ __forceinline__ void avPair(const VeAdjArgs& a, int64_t i, int64_t j, const double Ci[6],
-                                       const AvSeedV& sd, AvGrad& o)
+__device__ __forceinline__ void avPair(const VeAdjArgs& a, int64_t i, int64_t j, const AvSeedV& sd, AvGrad& o)
 {
     double r[3], d, rinv, v[3];
     geom(a, i, j, r, d, rinv);
@@ -410,7 +481,7 @@ __device__ __forceinline__ void avPair(const VeAdjArgs& a, int64_t i, int64_t j,
     const double hInv = a.hInv[i];
     double dw;
     const double w = lookupVS(a.wh, d * hInv, dw);
-    avAdj(r, d, rinv, v, hInv, w, dw, Ci, a.K, a.vol[j], a.kx[j], a.xm[j], a.divv[i], a.divv[j], sd.Gb, sd.vsigb,
+    avAdj(r, d, rinv, v, hInv, w, dw, a.K, a.vol[j], a.kxInv[j], a.divv[i], a.divv[j], sd.CGb, sd.vsigb,
           uint32_t(j) == sd.arg, o);
 }
 
@@ -419,26 +490,25 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
-    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, c = 0, h = 0, C[6] = {0, 0, 0, 0, 0, 0}, divv = 0, xm = 0, kx = 0;
+    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, c = 0, h = 0, divv = 0, xm = 0, kx = 0;
     const AvSeedV sd = avSeedOf(a, k);
     if (sd.any) {
-        double Ck[6];
-        loadC(a, k, Ck);
+        double R[3] = {0.0, 0.0, 0.0};
         const unsigned nc = a.lv.capped(k);
         for (unsigned q = 0; q < nc; ++q) {
             const int64_t j = a.lv.at(k, q);
+            if (!sd.gAny && uint32_t(j) != sd.arg) continue;
             AvGrad o;
-            avPair(a, k, j, Ck, sd, o);
+            avPair(a, k, j, sd, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] += o.r[t];
                 v[t] += o.v[t];
+                R[t] += o.R[t];
             }
             c += o.cI;
             h += o.hI;
             divv += o.divvI;
-#pragma unroll
-            for (int t = 0; t < 6; ++t) C[t] += o.CI[t];
             if (!TwoSided) {
                 atomicAdd(a.bx + j, -o.r[0]);
                 atomicAdd(a.by + j, -o.r[1]);
@@ -454,16 +524,16 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
                 atomicAdd(a.kxB + j, o.kxJ);
             }
         }
+#pragma unroll
+        for (int t = 0; t < 3; ++t) put(a.Rav + t * a.n, k, R[t], !TwoSided);
     }
     if (TwoSided) {
         for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
             const int64_t i = a.tIdx[e];
             const AvSeedV si = avSeedOf(a, i);
-            if (!si.any) continue;
-            double Ci[6];
-            loadC(a, i, Ci);
+            if (!si.any || (!si.gAny && uint32_t(k) != si.arg)) continue;
             AvGrad o;
-            avPair(a, i, k, Ci, si, o);
+            avPair(a, i, k, si, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] -= o.r[t];
@@ -487,8 +557,106 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
     put(a.divvB, k, divv, at);
     put(a.xmB, k, xm, at);
     put(a.kxB, k, kx, at);
+}
+
+// scatter form over the owned lists: a mutual pair gives both directed terms from one geometry
+__global__ void __launch_bounds__(kVeAdjBlock) veAvAdjOnceKernel(VeAdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, R[3] = {0, 0, 0}, c = 0, h = 0, divv = 0, xm = 0, kx = 0;
+    const AvSeedV sk = avSeedOf(a, k);
+    const double hInvK = a.hInv[k], divvK = a.divv[k], volK = a.vol[k], kxInvK = a.kxInv[k];
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        const bool wantK = sk.any && (sk.gAny || j == sk.arg);
+        AvSeedV sj{};
+        bool wantJ = false;
+        if (mutual) {
+            sj = avSeedOf(a, j);
+            wantJ = sj.any && (sj.gAny || uint32_t(k) == sj.arg);
+        }
+        if (!wantK && !wantJ) continue;
+        double r[3], d, rinv, vv[3];
+        geom(a, k, j, r, d, rinv);
+        vdiff(a, k, j, vv);
+        double rj[3] = {0, 0, 0}, vj[3] = {0, 0, 0}, cj = 0, hj = 0, divvj = 0, xmj = 0, kxj = 0;
+        const double divvJ = a.divv[j];
+        if (wantK) {
+            double dw;
+            const double w = lookupVS(a.wh, d * hInvK, dw);
+            AvGrad o;
+            avAdj(r, d, rinv, vv, hInvK, w, dw, a.K, a.vol[j], a.kxInv[j], divvK, divvJ, sk.CGb, sk.vsigb,
+                  j == sk.arg, o);
 #pragma unroll
-    for (int t = 0; t < 6; ++t) put(a.CB + t * a.n, k, C[t], at);
+            for (int t = 0; t < 3; ++t) {
+                x[t] += o.r[t];
+                v[t] += o.v[t];
+                R[t] += o.R[t];
+                rj[t] -= o.r[t];
+                vj[t] -= o.v[t];
+            }
+            c += o.cI;
+            h += o.hI;
+            divv += o.divvI;
+            cj += o.cJ;
+            divvj += o.divvJ;
+            xmj += o.xmJ;
+            kxj += o.kxJ;
+        }
+        if (wantJ) {
+            const double hInvJ = a.hInv[j];
+            double dw;
+            const double w = lookupVS(a.wh, d * hInvJ, dw);
+            const double rm[3] = {-r[0], -r[1], -r[2]}, vm[3] = {-vv[0], -vv[1], -vv[2]};
+            AvGrad p;
+            avAdj(rm, d, rinv, vm, hInvJ, w, dw, a.K, volK, kxInvK, divvJ, divvK, sj.CGb, sj.vsigb,
+                  uint32_t(k) == sj.arg, p);
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                rj[t] += p.r[t];
+                vj[t] += p.v[t];
+                x[t] -= p.r[t];
+                v[t] -= p.v[t];
+                atomicAdd(a.Rav + t * a.n + j, p.R[t]);
+            }
+            cj += p.cI;
+            c += p.cJ;
+            hj = p.hI;
+            divvj += p.divvI;
+            divv += p.divvJ;
+            xm += p.xmJ;
+            kx += p.kxJ;
+            atomicAdd(a.bh + j, hj);
+        }
+        atomicAdd(a.bx + j, rj[0]);
+        atomicAdd(a.by + j, rj[1]);
+        atomicAdd(a.bz + j, rj[2]);
+        if (vj[0] != 0.0 || vj[1] != 0.0 || vj[2] != 0.0) {
+            atomicAdd(a.bvx + j, vj[0]);
+            atomicAdd(a.bvy + j, vj[1]);
+            atomicAdd(a.bvz + j, vj[2]);
+            atomicAdd(a.cB + j, cj);
+        }
+        atomicAdd(a.divvB + j, divvj);
+        atomicAdd(a.xmB + j, xmj);
+        atomicAdd(a.kxB + j, kxj);
+    }
+    atomicAdd(a.bx + k, x[0]);
+    atomicAdd(a.by + k, x[1]);
+    atomicAdd(a.bz + k, x[2]);
+    atomicAdd(a.bvx + k, v[0]);
+    atomicAdd(a.bvy + k, v[1]);
+    atomicAdd(a.bvz + k, v[2]);
+    atomicAdd(a.cB + k, c);
+    atomicAdd(a.bh + k, h);
+    atomicAdd(a.divvB + k, divv);
+    atomicAdd(a.xmB + k, xm);
+    atomicAdd(a.kxB + k, kx);
+#pragma unroll
+    for (int t = 0; t < 3; ++t) atomicAdd(a.Rav + t * a.n + k, R[t]);
 }
 
 // ---------------------------------------------------------------- IAD + divv
@@ -502,6 +670,11 @@ __global__ void veIadSeedKernel(VeAdjArgs a)
     for (int t = 0; t < 6; ++t) {
         Cb[t] = a.CB[t * a.n + k];
         gb[t] = a.avClean ? a.gB[t * a.n + k] : 0.0;
+    }
+    {  // C partials of the AV pair terms
+        const double Gb[3] = {a.GB[k], a.GB[a.n + k], a.GB[2 * a.n + k]};
+        const double R[3] = {a.Rav[k], a.Rav[a.n + k], a.Rav[2 * a.n + k]};
+        avCbar(Gb, R, Cb);
     }
 #pragma unroll
     for (int t = 0; t < 9; ++t) P[t] = a.P[t * a.n + k];
@@ -524,7 +697,7 @@ __device__ __forceinline__ void iadPair(const VeAdjArgs& a, int64_t i, int64_t j
     const double hInv = a.hInv[i];
     double dw;
     const double w = lookupVS(a.wh, d * hInv, dw);
-    iadDivvAdj(r, d, rinv, v, hInv, w, dw, a.vol[j], a.kx[j], a.xm[j], tauB, PB, o);
+    iadDivvAdj(r, d, rinv, v, hInv, w, dw, a.vol[j], a.kxInv[j], a.xm[j], tauB, PB, o);
 }
 
 __device__ __forceinline__ void iadSeedOf(const VeAdjArgs& a, int64_t i, double tauB[6], double PB[9])
@@ -593,6 +766,76 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjKernel(VeAdjArgs a)
     put(a.bh, k, h, at);
     put(a.xmB, k, xm, at);
     put(a.kxB, k, kx, at);
+}
+
+// scatter form over the owned lists: a mutual pair gives both directed terms from one geometry
+// (the neighbour's term with r -> -r, v -> -v and the roles swapped), a one-sided entry its owner's
+__global__ void __launch_bounds__(kVeAdjBlock) veIadAdjOnceKernel(VeAdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, h = 0, xm = 0, kx = 0;
+    double tauK[6], PK[9];
+    iadSeedOf(a, k, tauK, PK);
+    const double hInvK = a.hInv[k];
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double r[3], d, rinv, vv[3];
+        geom(a, k, j, r, d, rinv);
+        vdiff(a, k, j, vv);
+        double dw;
+        double w = lookupVS(a.wh, d * hInvK, dw);
+        IadGrad o;
+        iadDivvAdj(r, d, rinv, vv, hInvK, w, dw, a.vol[j], a.kxInv[j], a.xm[j], tauK, PK, o);
+        double rj[3], vj[3], hj = 0.0;
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            x[t] += o.r[t];
+            v[t] += o.v[t];
+            rj[t] = -o.r[t];
+            vj[t] = -o.v[t];
+        }
+        h += o.hI;
+        if (mutual) {
+            double tauJ[6], PJ[9];
+            iadSeedOf(a, j, tauJ, PJ);
+            const double hInvJ = a.hInv[j];
+            const double rm[3] = {-r[0], -r[1], -r[2]}, vm[3] = {-vv[0], -vv[1], -vv[2]};
+            w = lookupVS(a.wh, d * hInvJ, dw);
+            IadGrad p;
+            iadDivvAdj(rm, d, rinv, vm, hInvJ, w, dw, a.vol[k], a.kxInv[k], a.xm[k], tauJ, PJ, p);
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                rj[t] += p.r[t];
+                vj[t] += p.v[t];
+                x[t] -= p.r[t];
+                v[t] -= p.v[t];
+            }
+            hj = p.hI;
+            xm += p.xmJ;
+            kx += p.kxJ;
+            atomicAdd(a.bh + j, hj);
+        }
+        atomicAdd(a.bx + j, rj[0]);
+        atomicAdd(a.by + j, rj[1]);
+        atomicAdd(a.bz + j, rj[2]);
+        atomicAdd(a.bvx + j, vj[0]);
+        atomicAdd(a.bvy + j, vj[1]);
+        atomicAdd(a.bvz + j, vj[2]);
+        atomicAdd(a.xmB + j, o.xmJ);
+        atomicAdd(a.kxB + j, o.kxJ);
+    }
+    atomicAdd(a.bx + k, x[0]);
+    atomicAdd(a.by + k, x[1]);
+    atomicAdd(a.bz + k, x[2]);
+    atomicAdd(a.bvx + k, v[0]);
+    atomicAdd(a.bvy + k, v[1]);
+    atomicAdd(a.bvz + k, v[2]);
+    atomicAdd(a.bh + k, h);
+    atomicAdd(a.xmB + k, xm);
+    atomicAdd(a.kxB + k, kx);
 }
 
 // ---------------------------------------------------------------- EOS, gradh, xmass
@@ -672,6 +915,57 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjKernel(VeAdjArgs a)
     put(a.xmB, k, xm, at);
 }
 
+__global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjOnceKernel(VeAdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double x[3] = {0, 0, 0}, h = 0, xm = 0;
+    const double hInvK = a.hInv[k], skx = a.Skx[k], som = a.Som[k], sr0 = a.Sr0[k];
+    const double xmK = a.xm[k], mK = a.m[k];
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double r[3], d, rinv;
+        geom(a, k, j, r, d, rinv);
+        double dw, dwd;
+        double w = lookupVS(a.wh, d * hInvK, dw), wd = lookupVS(a.whd, d * hInvK, dwd);
+        GradhGrad o;
+        gradhAdj(r, d, rinv, hInvK, w, dw, wd, dwd, a.xm[j], a.m[j], skx, som, sr0, o);
+        double rj[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            x[t] += o.r[t];
+            rj[t] = -o.r[t];
+        }
+        h += o.hI;
+        if (mutual) {
+            const double hInvJ = a.hInv[j];
+            const double rm[3] = {-r[0], -r[1], -r[2]};
+            w = lookupVS(a.wh, d * hInvJ, dw);
+            wd = lookupVS(a.whd, d * hInvJ, dwd);
+            GradhGrad p;
+            gradhAdj(rm, d, rinv, hInvJ, w, dw, wd, dwd, xmK, mK, a.Skx[j], a.Som[j], a.Sr0[j], p);
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                rj[t] += p.r[t];
+                x[t] -= p.r[t];
+            }
+            xm += p.xmJ;
+            atomicAdd(a.bh + j, p.hI);
+        }
+        atomicAdd(a.bx + j, rj[0]);
+        atomicAdd(a.by + j, rj[1]);
+        atomicAdd(a.bz + j, rj[2]);
+        atomicAdd(a.xmB + j, o.xmJ);
+    }
+    atomicAdd(a.bx + k, x[0]);
+    atomicAdd(a.by + k, x[1]);
+    atomicAdd(a.bz + k, x[2]);
+    atomicAdd(a.bh + k, h);
+    atomicAdd(a.xmB + k, xm);
+}
+
 __global__ void veXmassSeedKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -728,10 +1022,49 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjKernel(VeAdjArgs a)
     put(a.bh, k, h, at);
 }
 
+__global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjOnceKernel(VeAdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double x[3] = {0, 0, 0}, h = 0;
+    const double hInvK = a.hInv[k], r0b = a.R0b[k], mK = a.m[k];
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double r[3], d, rinv;
+        geom(a, k, j, r, d, rinv);
+        double dw;
+        lookupVS(a.wh, d * hInvK, dw);
+        double rb[3], hIb;
+        xmassAdj(r, d, rinv, hInvK, dw, a.m[j], r0b, rb, hIb);
+        h += hIb;
+        if (mutual) {
+            const double hInvJ = a.hInv[j];
+            const double rm[3] = {-r[0], -r[1], -r[2]};
+            lookupVS(a.wh, d * hInvJ, dw);
+            double pb[3], hJb;
+            xmassAdj(rm, d, rinv, hInvJ, dw, mK, a.R0b[j], pb, hJb);
+#pragma unroll
+            for (int t = 0; t < 3; ++t) rb[t] -= pb[t];
+            atomicAdd(a.bh + j, hJb);
+        }
+#pragma unroll
+        for (int t = 0; t < 3; ++t) x[t] += rb[t];
+        atomicAdd(a.bx + j, -rb[0]);
+        atomicAdd(a.by + j, -rb[1]);
+        atomicAdd(a.bz + j, -rb[2]);
+    }
+    atomicAdd(a.bx + k, x[0]);
+    atomicAdd(a.by + k, x[1]);
+    atomicAdd(a.bz + k, x[2]);
+    atomicAdd(a.bh + k, h);
+}
+
 }  // namespace
 
 // number of n-sized double sections of the VE adjoint state
-constexpr int kVeAdjSections = 65;
+constexpr int kVeAdjSections = 74;
 
 int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avClean, const sphgb_seeds* s,
               sphgb_grads* g, int deterministic)
@@ -818,10 +1151,14 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     a.gB = take(6);
     a.divvB = take(1);
     a.gradhB = take(1);
-    const int64_t accSections = 20;
+    a.Rav = take(3);
+    const int64_t accSections = 23;
     a.hInv = take(1);
     a.rho = take(1);
+    a.rhoInv = take(1);
     a.vol = take(1);
+    a.kxInv = take(1);
+    a.xmInv = take(1);
     a.lnxm = take(1);
     a.en = take(1);
     a.avE = take(1);
@@ -832,6 +1169,7 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     a.wr0 = take(1);
     a.vsigArg = reinterpret_cast<uint32_t*>(take(1));
     a.GB = take(3);
+    a.CGB = take(3);
     a.vsigB = take(1);
     a.tauB = take(6);
     a.PB = take(9);
@@ -849,21 +1187,39 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     const bool two = deterministic != 0;
     veQuotKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veQuotKernel"));
-    vePreMeKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "vePreMeKernel"));
+    const bool withDu = a.sDu != nullptr;
+    if (withDu) {  // en and avE enter only through the du seed
+        vePreMeKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "vePreMeKernel"));
+    }
     vePreKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "vePreKernel"));
-    if (two) meVeAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    else meVeAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "meVeAdjKernel"));
+    {
+        using K = void (*)(VeAdjArgs);
+        // [two-sided][avClean][du seed]
+        const K me[2][2][2] = {{{meVeAdjKernel<false, false, false>, meVeAdjKernel<false, false, true>},
+                                {meVeAdjKernel<false, true, false>, meVeAdjKernel<false, true, true>}},
+                               {{meVeAdjKernel<true, false, false>, meVeAdjKernel<true, false, true>},
+                                {meVeAdjKernel<true, true, false>, meVeAdjKernel<true, true, true>}}};
+        // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
+        if (!two && !c->deterministic && !a.avClean && c->ownedEpoch == c->nbrEpoch) {
+            if (withDu) meVeAdjOnceKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+            else meVeAdjOnceKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        } else
+            me[two][a.avClean][withDu]<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "meVeAdjKernel"));
+    }
     veAvSeedKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veAvSeedKernel"));
+    const bool once = !two && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
     if (two) veAvAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+    else if (once) veAvAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else veAvAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veAvAdjKernel"));
     veIadSeedKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veIadSeedKernel"));
     if (two) veIadAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+    else if (once) veIadAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else veIadAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veIadAdjKernel"));
     veEosAdjKernel<<<eb, 256, 0, c->stream>>>(a);
@@ -871,11 +1227,13 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     veGradhSeedKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veGradhSeedKernel"));
     if (two) veGradhAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+    else if (once) veGradhAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else veGradhAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veGradhAdjKernel"));
     veXmassSeedKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veXmassSeedKernel"));
     if (two) veXmassAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+    else if (once) veXmassAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else veXmassAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veXmassAdjKernel"));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));

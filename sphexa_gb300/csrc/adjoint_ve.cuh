@@ -89,7 +89,7 @@ VEAD_HD double dWdh(double hInv, double w, double dw, double v)
 
 // ------------------------------------------------------------------ momentum-energy
 struct MeSide {
-    double hInv, c, alpha, m, rho, xm, lnxm, prho;
+    double hInv, c, alpha, m, rho, rhoInv, xm, xmInv, lnxm, prho;
     double C[6], g[6];
 };
 
@@ -100,7 +100,7 @@ struct MeFwd {
     double d1, d2, d3, e, A, praw, pc, phi;
     bool etaIsV2, etaBelow, clampActive;
     int branch;
-    double dr, sr, At, s, am, bm;
+    double srInv, At, s, am, bm;
     double av, bv, avv[3];
 };
 
@@ -145,27 +145,28 @@ VEAD_HD void meFwd(const double r[3], double d, double rinv, const double v[3], 
     f.asum = I.alpha + J.alpha;
     f.csum = I.c + J.c;
     f.visc = f.approaching ? -(0.25 * f.asum * f.csum - 2.0 * f.wij) * f.wij : 0.0;
-    f.dr = fabs(I.rho - J.rho);
-    f.sr = I.rho + J.rho;
-    f.At = f.dr / f.sr;
-    f.s = 0.0;
-    if (f.dr < kAtmin * f.sr) {
+    // Atwood number |rho_i - rho_j| / (rho_i + rho_j) against Atmin / Atmax without dividing
+    const double dr = fabs(I.rho - J.rho), sr = I.rho + J.rho;
+    f.s = f.At = f.srInv = 0.0;
+    if (dr < kAtmin * sr) {
         f.branch = 0;
         f.am = I.xm * I.xm;
         f.bm = J.xm * J.xm;
-    } else if (kAtmax * f.sr < f.dr) {
+    } else if (kAtmax * sr < dr) {
         f.branch = 2;
         f.am = I.xm * J.xm;
         f.bm = f.am;
     } else {
         f.branch = 1;
+        f.srInv = 1.0 / sr;
+        f.At = dr * f.srInv;
         f.s = kRamp * (f.At - kAtmin);
         const double q = exp(f.s * (J.lnxm - I.lnxm));
         f.am = I.xm * I.xm * q;
         f.bm = J.xm * J.xm / q;
     }
-    f.av = J.m / I.rho * f.visc;
-    f.bv = J.m / J.rho * f.visc;
+    f.av = J.m * I.rhoInv * f.visc;
+    f.bv = J.m * J.rhoInv * f.visc;
     for (int k = 0; k < 3; ++k) f.avv[k] = 0.5 * (f.av * f.Ai[k] + f.bv * f.Aj[k]);
 }
 
@@ -182,71 +183,43 @@ struct MeGrad {
     double hJ, prhoJ, rhoJ, xmJ, CJ[6], gJ[6];   // j's fields
 };
 
-// seeds of i's pair terms: mb = dL/d(sum of momentum terms) = -K abar_i, enb = K prho_i dubar_i,
-// avEb = K/2 dubar_i where the sum avE_i >= 0 (0 otherwise)
-VEAD_HD void meAdj(const double r[3], double d, double rinv, const double v[3], const MeSide& I, const MeSide& J,
-                   double wi, double dwi, double wj, double dwj, bool avClean, double etaCrit, const double mb[3],
-                   double enb, double avEb, MeGrad& o)
+// adjoints of the pair's shared intermediates, set by the seed-dependent head
+struct MeBar {
+    double Aib[3], Ajb[3], amb, bmb, viscb;
+};
+
+// from the intermediates' adjoints to the pair's inputs (common to one term and to a mutual pair)
+template<bool AvClean>
+VEAD_HD void meTail(const double r[3], double rinv, const double v[3], const MeSide& I, const MeSide& J, double wi,
+                    double dwi, double wj, double dwj, const MeFwd& f, const MeBar& b, MeGrad& o)
 {
-    MeFwd f;
-    meFwd(r, d, rinv, v, I, J, wi, wj, avClean, etaCrit, f);
-    for (int k = 0; k < 3; ++k) o.r[k] = o.v[k] = 0.0;
-    for (int q = 0; q < 6; ++q) o.CI[q] = o.CJ[q] = o.gI[q] = o.gJ[q] = 0.0;
-    o.c = o.alpha = 0.0;
-    o.xmI = o.xmJ = 0.0;
-
-    const double mj = J.m;
-    double avvb[3], Aib[3], Ajb[3];
-    double mbAi = 0.0, mbAj = 0.0, vAi = 0.0;
-    for (int k = 0; k < 3; ++k) {
-        avvb[k] = mb[k] + avEb * v[k];
-        mbAi += mb[k] * f.Ai[k];
-        mbAj += mb[k] * f.Aj[k];
-        vAi += v[k] * f.Ai[k];
-    }
-    for (int k = 0; k < 3; ++k) {
-        o.v[k] = avEb * f.avv[k] + enb * mj * f.am * f.Ai[k];
-        Aib[k] = mb[k] * mj * I.prho * f.am + enb * mj * f.am * v[k] + 0.5 * f.av * avvb[k];
-        Ajb[k] = mb[k] * mj * J.prho * f.bm + 0.5 * f.bv * avvb[k];
-    }
-    const double amb = mbAi * mj * I.prho + enb * mj * vAi;
-    const double bmb = mbAj * mj * J.prho;
-    o.prhoI = mbAi * mj * f.am;
-    o.prhoJ = mbAj * mj * f.bm;
-    const double avb = 0.5 * (avvb[0] * f.Ai[0] + avvb[1] * f.Ai[1] + avvb[2] * f.Ai[2]);
-    const double bvb = 0.5 * (avvb[0] * f.Aj[0] + avvb[1] * f.Aj[1] + avvb[2] * f.Aj[2]);
-    const double viscb = avb * mj / I.rho + bvb * mj / J.rho;
-    o.rhoI = -avb * f.av / I.rho;
-    o.rhoJ = -bvb * f.bv / J.rho;
-
     // Atwood weights
     if (f.branch == 0) {
-        o.xmI += 2.0 * amb * I.xm;
-        o.xmJ += 2.0 * bmb * J.xm;
+        o.xmI += 2.0 * b.amb * I.xm;
+        o.xmJ += 2.0 * b.bmb * J.xm;
     } else if (f.branch == 2) {
-        o.xmI += (amb + bmb) * J.xm;
-        o.xmJ += (amb + bmb) * I.xm;
+        o.xmI += (b.amb + b.bmb) * J.xm;
+        o.xmJ += (b.amb + b.bmb) * I.xm;
     } else {
-        o.xmI += amb * (2.0 - f.s) * f.am / I.xm + bmb * f.s * f.bm / I.xm;
-        o.xmJ += amb * f.s * f.am / J.xm + bmb * (2.0 - f.s) * f.bm / J.xm;
-        const double sb = (amb * f.am - bmb * f.bm) * (J.lnxm - I.lnxm);
-        const double Atb = sb * kRamp;
+        const double pa = b.amb * f.am, pb = b.bmb * f.bm;
+        o.xmI += ((2.0 - f.s) * pa + f.s * pb) * I.xmInv;
+        o.xmJ += (f.s * pa + (2.0 - f.s) * pb) * J.xmInv;
+        const double Atb = (pa - pb) * (J.lnxm - I.lnxm) * kRamp;
         const double sgn = I.rho > J.rho ? 1.0 : (I.rho < J.rho ? -1.0 : 0.0);
-        o.rhoI += Atb * (sgn - f.At) / f.sr;
-        o.rhoJ += Atb * (-sgn - f.At) / f.sr;
+        o.rhoI += Atb * (sgn - f.At) * f.srInv;
+        o.rhoJ += Atb * (-sgn - f.At) * f.srInv;
     }
-
     // viscosity
     double wijb = 0.0;
     if (f.approaching) {
-        wijb = viscb * (-0.25 * f.asum * f.csum + 4.0 * f.wij);
-        o.c = viscb * (-0.25 * f.asum * f.wij);
-        o.alpha = viscb * (-0.25 * f.csum * f.wij);
+        wijb = b.viscb * (-0.25 * f.asum * f.csum + 4.0 * f.wij);
+        o.c = b.viscb * (-0.25 * f.asum * f.wij);
+        o.alpha = b.viscb * (-0.25 * f.csum * f.wij);
     }
     const double rvb = wijb * rinv;
     double db = -wijb * f.wij * rinv;
     double v1b = 0.0, v2b = 0.0;
-    if (avClean) {
+    if (AvClean) {
         const double phib = -rvb * (f.d1 + f.d2);
         double d1b = -rvb * f.phi, d2b = -rvb * f.phi;
         const double pcb = phib * 0.5 * f.d3;
@@ -272,19 +245,117 @@ VEAD_HD void meAdj(const double r[3], double d, double rinv, const double v[3], 
         o.v[k] += rvb * r[k];
     }
     // A_i = -W_i C_i r, A_j = -W_j C_j r
-    const double Wib = -(Aib[0] * f.CIr[0] + Aib[1] * f.CIr[1] + Aib[2] * f.CIr[2]);
-    const double Wjb = -(Ajb[0] * f.CJr[0] + Ajb[1] * f.CJr[1] + Ajb[2] * f.CJr[2]);
-    symvAdj(Aib, r, -f.Wi, o.CI);
-    symvAdj(Ajb, r, -f.Wj, o.CJ);
+    const double Wib = -(b.Aib[0] * f.CIr[0] + b.Aib[1] * f.CIr[1] + b.Aib[2] * f.CIr[2]);
+    const double Wjb = -(b.Ajb[0] * f.CJr[0] + b.Ajb[1] * f.CJr[1] + b.Ajb[2] * f.CJr[2]);
+    symvAdj(b.Aib, r, -f.Wi, o.CI);
+    symvAdj(b.Ajb, r, -f.Wj, o.CJ);
     double CAi[3], CAj[3];
-    symv(I.C, Aib, CAi);
-    symv(J.C, Ajb, CAj);
+    symv(I.C, b.Aib, CAi);
+    symv(J.C, b.Ajb, CAj);
     for (int k = 0; k < 3; ++k) o.r[k] += -f.Wi * CAi[k] - f.Wj * CAj[k];
     // W_i = h_i^-3 w(d / h_i)
     o.hI = Wib * dWdh(I.hInv, wi, dwi, f.v1) - v1b * f.v1 * I.hInv;
     o.hJ = Wjb * dWdh(J.hInv, wj, dwj, f.v2) - v2b * f.v2 * J.hInv;
     db += Wib * f.hi3 * dwi * I.hInv + Wjb * f.hj3 * dwj * J.hInv + v1b * I.hInv + v2b * J.hInv;
     for (int k = 0; k < 3; ++k) o.r[k] += db * r[k] * rinv;
+}
+
+VEAD_HD void meGradZero(MeGrad& o)
+{
+    for (int k = 0; k < 3; ++k) o.r[k] = o.v[k] = 0.0;
+    for (int q = 0; q < 6; ++q) o.CI[q] = o.CJ[q] = o.gI[q] = o.gJ[q] = 0.0;
+    o.c = o.alpha = o.xmI = o.xmJ = 0.0;
+}
+
+// i's term of one pair.  Seeds of i: mb = dL/d(sum of momentum terms) = -K abar_i, enb = K prho_i
+// dubar_i, avEb = K/2 dubar_i where the sum avE_i >= 0 (0 otherwise).  WithDu = false: enb = avEb
+// = 0 (no du seed) and the energy terms drop out; AvClean selects momentumAndEnergy<avClean>.
+template<bool AvClean, bool WithDu>
+VEAD_HD void meAdj(const double r[3], double d, double rinv, const double v[3], const MeSide& I, const MeSide& J,
+                   double wi, double dwi, double wj, double dwj, double etaCrit, const double mb[3], double enb,
+                   double avEb, MeGrad& o)
+{
+    MeFwd f;
+    meFwd(r, d, rinv, v, I, J, wi, wj, AvClean, etaCrit, f);
+    meGradZero(o);
+    const double mj = J.m;
+    MeBar b;
+    double avvb[3], mbAi = 0.0, mbAj = 0.0, vAi = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        avvb[k] = WithDu ? mb[k] + avEb * v[k] : mb[k];
+        mbAi += mb[k] * f.Ai[k];
+        mbAj += mb[k] * f.Aj[k];
+        if (WithDu) vAi += v[k] * f.Ai[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (WithDu) o.v[k] = avEb * f.avv[k] + enb * mj * f.am * f.Ai[k];
+        b.Aib[k] = mb[k] * mj * I.prho * f.am + 0.5 * f.av * avvb[k];
+        if (WithDu) b.Aib[k] += enb * mj * f.am * v[k];
+        b.Ajb[k] = mb[k] * mj * J.prho * f.bm + 0.5 * f.bv * avvb[k];
+    }
+    b.amb = WithDu ? mbAi * mj * I.prho + enb * mj * vAi : mbAi * mj * I.prho;
+    b.bmb = mbAj * mj * J.prho;
+    o.prhoI = mbAi * mj * f.am;
+    o.prhoJ = mbAj * mj * f.bm;
+    const double avb = 0.5 * (avvb[0] * f.Ai[0] + avvb[1] * f.Ai[1] + avvb[2] * f.Ai[2]);
+    const double bvb = 0.5 * (avvb[0] * f.Aj[0] + avvb[1] * f.Aj[1] + avvb[2] * f.Aj[2]);
+    b.viscb = (avb * I.rhoInv + bvb * J.rhoInv) * mj;
+    o.rhoI = -avb * f.av * I.rhoInv;
+    o.rhoJ = -bvb * f.bv * J.rhoInv;
+    meTail<AvClean>(r, rinv, v, I, J, wi, dwi, wj, dwj, f, b, o);
+}
+
+// both terms of a mutual pair (i's term of j and j's term of i, same image, no avClean correction)
+// from one evaluation.  With r_ji = -r, v_ji = -v the two terms share every intermediate and
+// their seeds enter only through s = m_j mb_i - m_i mb_j, sigma = m_j avEb_i + m_i avEb_j and the
+// energy seeds.
+template<bool WithDu>
+VEAD_HD void meAdjMutual(const double r[3], double d, double rinv, const double v[3], const MeSide& I,
+                         const MeSide& J, double wi, double dwi, double wj, double dwj, const double mbI[3],
+                         double enbI, double avEbI, const double mbJ[3], double enbJ, double avEbJ, MeGrad& o)
+{
+    MeFwd f;
+    meFwd(r, d, rinv, v, I, J, wi, wj, false, 0.0, f);
+    meGradZero(o);
+    double sv[3], ui[3], uj[3], t[3];
+    const double sigma = WithDu ? J.m * avEbI + I.m * avEbJ : 0.0;
+    for (int k = 0; k < 3; ++k) {
+        sv[k] = J.m * mbI[k] - I.m * mbJ[k];
+        ui[k] = I.prho * sv[k];
+        uj[k] = J.prho * sv[k];
+        t[k] = sv[k];
+        if (WithDu) {
+            ui[k] += enbI * J.m * v[k];
+            uj[k] += enbJ * I.m * v[k];
+            t[k] += sigma * v[k];
+        }
+    }
+    double sAi = 0.0, sAj = 0.0, tAi = 0.0, tAj = 0.0, uAi = 0.0, uAj = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        sAi += sv[k] * f.Ai[k];
+        sAj += sv[k] * f.Aj[k];
+        tAi += t[k] * f.Ai[k];
+        tAj += t[k] * f.Aj[k];
+        uAi += ui[k] * f.Ai[k];
+        uAj += uj[k] * f.Aj[k];
+    }
+    const double hvi = 0.5 * f.visc * I.rhoInv, hvj = 0.5 * f.visc * J.rhoInv;
+    MeBar b;
+    for (int k = 0; k < 3; ++k) {
+        b.Aib[k] = f.am * ui[k] + hvi * t[k];
+        b.Ajb[k] = f.bm * uj[k] + hvj * t[k];
+        if (WithDu)
+            o.v[k] = enbI * J.m * f.am * f.Ai[k] + enbJ * I.m * f.bm * f.Aj[k] +
+                     sigma * (hvi * f.Ai[k] + hvj * f.Aj[k]);
+    }
+    b.amb = uAi;
+    b.bmb = uAj;
+    b.viscb = 0.5 * (tAi * I.rhoInv + tAj * J.rhoInv);
+    o.prhoI = f.am * sAi;
+    o.prhoJ = f.bm * sAj;
+    o.rhoI = -hvi * tAi * I.rhoInv;
+    o.rhoJ = -hvj * tAj * J.rhoInv;
+    meTail<false>(r, rinv, v, I, J, wi, dwi, wj, dwj, f, b, o);
 }
 
 // ------------------------------------------------------------------ AV switches
@@ -332,42 +403,37 @@ VEAD_HD void avSeed(const AvPrm& P, double alphab, double alpha0, double h, doub
 
 struct AvGrad {
     double r[3], v[3], cI, cJ;
-    double hI, CI[6], divvI;
+    double hI, divvI, R[3];   // R: this pair's part of sum_j fac_j W_j r_j (i's C partials, see avCbar)
     double divvJ, xmJ, kxJ;
 };
 
-// pair term of G_i (and, for the pair that set vsig_i, the signal velocity c_i + c_j - 3 rv / d)
+// pair term of G_i = sum_j fac_j t_j, fac_j = vol_j (divv_i - divv_j), t_j = -W_j C_i r_j,
+// W_j = K h_i^-3 w(d_j / h_i), given Gb (dL/dG_i) through CGb = C_i Gb (C symmetric): the pair
+// needs only r . CGb; i's C partials are -sym(Gb R^T) with R = sum_j fac_j W_j r_j (avCbar).  For
+// the pair that set vsig_i, the signal velocity c_i + c_j - 3 rv / d as well.
 VEAD_HD void avAdj(const double r[3], double d, double rinv, const double v[3], double hiInv, double wi, double dwi,
-                   const double Ci[6], double K, double volj, double kxj, double xmj, double divvi, double divvj,
-                   const double Gb[3], double vsigb, bool isVsigPair, AvGrad& o)
+                   double K, double volj, double kxInvj, double divvi, double divvj, const double CGb[3],
+                   double vsigb, bool isVsigPair, AvGrad& o)
 {
-    double CIr[3];
-    symv(Ci, r, CIr);
     const double hi3 = hiInv * hiInv * hiInv;
     const double Wk = K * hi3 * wi;
     const double ddiv = divvi - divvj;
     const double fac = volj * ddiv;
-    double facb = 0.0, tb[3];
-    for (int k = 0; k < 3; ++k) {
-        facb += Gb[k] * (-Wk * CIr[k]);
-        tb[k] = fac * Gb[k];
-    }
+    const double rc = r[0] * CGb[0] + r[1] * CGb[1] + r[2] * CGb[2];
+    const double facb = -Wk * rc;
+    const double Wkb = -fac * rc;
     const double volb = facb * ddiv;
     o.divvI = facb * volj;
     o.divvJ = -facb * volj;
-    o.xmJ = volb / kxj;
-    o.kxJ = -volb * volj / kxj;
-    (void)xmj;
-    const double Wkb = -(tb[0] * CIr[0] + tb[1] * CIr[1] + tb[2] * CIr[2]);
-    for (int q = 0; q < 6; ++q) o.CI[q] = 0.0;
-    symvAdj(tb, r, -Wk, o.CI);
-    double Ct[3];
-    symv(Ci, tb, Ct);
+    o.xmJ = volb * kxInvj;
+    o.kxJ = -volb * volj * kxInvj;
     const double v1 = d * hiInv;
     o.hI = Wkb * K * dWdh(hiInv, wi, dwi, v1);
     double db = Wkb * K * hi3 * dwi * hiInv;
+    const double fw = fac * Wk;
     for (int k = 0; k < 3; ++k) {
-        o.r[k] = -Wk * Ct[k];
+        o.r[k] = -fw * CGb[k];
+        o.R[k] = fw * r[k];
         o.v[k] = 0.0;
     }
     o.cI = o.cJ = 0.0;
@@ -384,6 +450,9 @@ VEAD_HD void avAdj(const double r[3], double d, double rinv, const double v[3], 
     }
     for (int k = 0; k < 3; ++k) o.r[k] += db * r[k] * rinv;
 }
+
+// i's C partials from the AV pair sum: Cb += -sym(Gb R^T), R = sum_j fac_j W_j r_j
+VEAD_HD void avCbar(const double Gb[3], const double R[3], double Cb[6]) { symvAdj(Gb, R, -1.0, Cb); }
 
 // ------------------------------------------------------------------ IAD + divv
 // per-particle part: from Cb (6), divvb and gb (6, the avClean velocity gradient) of particle i and
@@ -463,7 +532,7 @@ struct IadGrad {
 
 // pair terms of tau_i (vol_j w r r^T) and P_i (xm_j w (v_j - v_i) r^T)
 VEAD_HD void iadDivvAdj(const double r[3], double d, double rinv, const double v[3], double hiInv, double wi,
-                        double dwi, double volj, double kxj, double xmj, const double tauB[6], const double PB[9],
+                        double dwi, double volj, double kxInvj, double xmj, const double tauB[6], const double PB[9],
                         IadGrad& o)
 {
     double Tr[3];
@@ -475,8 +544,8 @@ VEAD_HD void iadDivvAdj(const double r[3], double d, double rinv, const double v
     const double vPr = -(v[0] * PBr[0] + v[1] * PBr[1] + v[2] * PBr[2]);
     const double wb = volj * Q + xmj * vPr;
     const double volb = wi * Q;
-    o.xmJ = volb / kxj + wi * vPr;
-    o.kxJ = -volb * volj / kxj;
+    o.xmJ = volb * kxInvj + wi * vPr;
+    o.kxJ = -volb * volj * kxInvj;
     for (int a = 0; a < 3; ++a) o.v[a] = -xmj * wi * PBr[a];
     for (int q = 0; q < 3; ++q) {
         const double PtV = -(v[0] * PB[q] + v[1] * PB[3 + q] + v[2] * PB[6 + q]);

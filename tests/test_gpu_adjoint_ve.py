@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
 
 
-def setup(side=10, seed=7, av_clean=False, deterministic=False):
+def setup(side=10, seed=7, av_clean=False, deterministic=False, ordered_forward=False):
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
@@ -27,6 +27,8 @@ def setup(side=10, seed=7, av_clean=False, deterministic=False):
     wl.fields["alpha"] = rng.uniform(0.05, 0.5, wl.n)
     ctx = sph.Context(0)
     ctx.set_params(minDt=1e-2)
+    if ordered_forward:  # forward passes in list order; the scatter adjoint then walks the full lists
+        ctx.set_deterministic(True)
     d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0", av_clean=av_clean)
     box = sph.Box(wl.box.copy(), wl.bc.copy())
     sw = AG.FrozenVeSweep(ctx, d, box, av_clean=av_clean, deterministic=deterministic)
@@ -37,12 +39,15 @@ def setup(side=10, seed=7, av_clean=False, deterministic=False):
 
 
 @pytest.mark.parametrize("av_clean", [False, True])
-@pytest.mark.parametrize("deterministic", [False, True])
-def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, deterministic):
+@pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided"])
+def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, form):
+    """pair-once: one evaluation per mutual pair of the owned lists; scatter: every list entry
+    once with atomics (context in deterministic mode); two-sided: bit-reproducible form"""
     import torch
     from sphexa_gb300 import autograd as AG, sph
     from torch_reference import ve_chain
-    wl, ctx, sw, rho_t = setup(side=10, seed=7, av_clean=av_clean, deterministic=deterministic)
+    wl, ctx, sw, rho_t = setup(side=10, seed=7, av_clean=av_clean, deterministic=form == "two-sided",
+                               ordered_forward=form == "scatter")
     n = wl.n
     ng = int(ctx.params.ngmax)
     nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
