@@ -114,9 +114,11 @@ int sphgb_set_mixed_refinement(sphgb_ctx* ctx, int32_t on);
 /* Domain mode.  0 (default): every sphgb_domain_sync stands alone (open dimensions take the
  * particle extrema).  1: the syncs are the steps of one simulation, as cstone::Domain::sync
  * (domain/include/cstone/domain/assignment.hpp:80-82): from the second sync on, the open-dimension
- * box follows limitBoxShrinking (box.hpp:397-414) against the previous sync's box.  Setting the
- * mode starts a new sequence.  The tree is the converged cornerstone tree of each sync in both
- * modes (the reference's focus tree reaches it by one rebalance step per sync). */
+ * box follows limitBoxShrinking (box.hpp:397-414) against the previous sync's box, and the tree is
+ * the reference's single-rank focus tree: converged at the first sync, then updated once per sync
+ * from the previous tree and the previous sync's counts (focus/octree_focus_mpi.hpp:88-253,
+ * domain/domain.hpp:199-211), so a leaf may hold more than bucket particles until the next sync
+ * splits it.  Setting the mode starts a new sequence.  Mode 0 builds the converged tree every sync. */
 int sphgb_set_domain_mode(sphgb_ctx* ctx, int32_t mode);
 int sphgb_default_params(sphgb_params* params);
 /* kernel normalisation constant K used by the pair passes */

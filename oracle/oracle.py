@@ -218,3 +218,64 @@ def run_conserved(lib, f: dict) -> np.ndarray:
     names = ["x", "y", "z", "vx", "vy", "vz", "m", "u"]
     assert fn(len(f["x"]), *[_dptr(f.get(k)) for k in names], out.ctypes.data) == 0
     return out
+
+
+# ---- single-rank focus tree across syncs (restatement, numpy) ----
+KEY_END = np.uint64(1) << np.uint64(63)
+MAX_LEVEL = 21
+
+
+def _node_range(level: int) -> int:
+    return 1 << (3 * (MAX_LEVEL - level))
+
+
+def focus_rebalance_once(leaves: np.ndarray, counts: np.ndarray, bucket: int) -> np.ndarray:
+    """One update of the single-rank focus tree (CombinedUpdate::updateFocus,
+    domain/include/cstone/focus/octree_focus.hpp:65-113, with the decisions of
+    focus/rebalance.hpp:32-66 and protectAncestors :152-165 at one rank, where the focus range is
+    the whole key range, so the MAC criterion never decides and the mandatory keys 0 and 2^63 are
+    always present).  leaves: cornerstone leaves (L + 1 keys); counts: particle counts of the L
+    leaves from the previous sync.  A leaf whose parent holds more than bucket particles splits in
+    8 (if it holds more than bucket itself and lies above the last level) or stays; otherwise the
+    whole subtree under its highest ancestor holding at most bucket particles collapses into that
+    ancestor, whose left-most leaf keeps the start key."""
+    lv = [int(k) for k in leaves]
+    L = len(lv) - 1
+    layout = np.concatenate([[0], np.cumsum(np.asarray(counts, dtype=np.int64))])
+    import bisect
+
+    def count(start: int, level: int) -> int:
+        a = bisect.bisect_left(lv, start)
+        b = bisect.bisect_left(lv, start + _node_range(level))
+        return int(layout[b] - layout[a])
+
+    out = []
+    for k in range(L):
+        s, span = lv[k], lv[k + 1] - lv[k]
+        level = MAX_LEVEL - (span.bit_length() - 1) // 3
+        if level == 0:
+            op = 8 if counts[k] > bucket else 1
+        else:
+            ps = s & ~(_node_range(level - 1) - 1)
+            if count(ps, level - 1) > bucket:
+                op = 8 if (counts[k] > bucket and level < MAX_LEVEL) else 1
+            else:
+                a_s, a_l = ps, level - 1
+                while a_l > 0:
+                    pp = a_s & ~(_node_range(a_l - 1) - 1)
+                    if count(pp, a_l - 1) > bucket:
+                        break
+                    a_s, a_l = pp, a_l - 1
+                op = 1 if s == a_s else 0
+        if op == 1:
+            out.append(s)
+        elif op == 8:
+            out.extend(s + c * _node_range(level + 1) for c in range(8))
+    out.append(int(KEY_END))
+    return np.array(out, dtype=np.uint64)
+
+
+def leaf_counts(leaves: np.ndarray, sorted_keys: np.ndarray) -> np.ndarray:
+    """particles per leaf cell of a cornerstone leaf array"""
+    pos = np.searchsorted(sorted_keys, leaves)
+    return np.diff(pos)

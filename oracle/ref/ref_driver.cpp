@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cstone/findneighbors.hpp"
+#include "cstone/focus/octree_focus.hpp"
 #include "cstone/focus/source_center.hpp"
 #include "cstone/primitives/gather.hpp"
 #include "cstone/sfc/sfc.hpp"
@@ -422,5 +423,57 @@ extern "C" int oracle_limit_box_shrinking(const double fit[6], const double prev
     B r = cstone::limitBoxShrinking(f, p);
     const double o[6] = {r.xmin(), r.xmax(), r.ymin(), r.ymax(), r.zmin(), r.zmax()};
     for (int k = 0; k < 6; ++k) out[k] = o[k];
+    return 0;
+}
+
+/* The single-rank focus tree across the syncs of one simulation: FocusedOctree
+ * (domain/include/cstone/focus/octree_focus_mpi.hpp:40-253) driven as Domain::sync does
+ * (domain/domain.hpp:199-211): converge() at the first sync, then updateMinMac + updateTree +
+ * updateCounts at every sync.  One rank: the focus range is the whole key range, there are no peers
+ * and every leaf count comes from the local keys; the rebalance itself is the reference's
+ * CombinedUpdate::updateFocus (focus/octree_focus.hpp:65-113).  keys: the sorted keys of each step,
+ * n per step.  leaves_out: the cornerstone leaves after each step, concatenated (at most cap keys);
+ * nleaves[s]: the number of leaf cells of step s. */
+extern "C" int oracle_focus_steps(int64_t n, int32_t steps, const uint64_t* keys, uint32_t bucket,
+                                  uint64_t* leaves_out, int64_t cap, int64_t* nleaves)
+{
+    using K = uint64_t;
+    std::vector<K> leaves{0, cstone::nodeRange<K>(0)};
+    cstone::OctreeData<K, cstone::CpuTag> tree;
+    tree.resize(cstone::nNodes(leaves));
+    cstone::updateInternalTree<K>(leaves, tree.data());
+    std::vector<unsigned> counts{bucket + 1};  // the constructor's root count forces the first split
+    std::vector<char> macs(1, 1);
+    std::vector<unsigned> leafCounts;
+    auto updateCounts = [&](const K* k) {
+        leafCounts.assign(cstone::nNodes(leaves), 0);
+        cstone::computeNodeCounts<K>(leaves.data(), leafCounts.data(), cstone::nNodes(leaves), std::span<const K>(k, n),
+                                     std::numeric_limits<unsigned>::max(), true);
+        counts.assign(tree.numNodes, 0);
+        cstone::scatter<cstone::TreeNodeIndex>(cstone::leafToInternal(tree), leafCounts.data(), counts.data());
+        cstone::upsweep(tree.levelRange, tree.childOffsets, counts.data(), cstone::NodeCount<unsigned>{});
+    };
+    auto updateTree = [&]() {
+        macs.assign(tree.numNodes, 0);  // updateMinMac: no node lies outside the focus at one rank
+        return cstone::CombinedUpdate<K>::updateFocus(tree, leaves, bucket, K(0), cstone::nodeRange<K>(0), {}, counts,
+                                                     macs);
+    };
+    int64_t used = 0;
+    for (int32_t s = 0; s < steps; ++s) {
+        const K* k = keys + int64_t(s) * n;
+        if (s == 0) {
+            bool converged = false;
+            while (!converged) {
+                converged = updateTree();
+                updateCounts(k);
+            }
+        }
+        updateTree();
+        updateCounts(k);
+        if (used + int64_t(leaves.size()) > cap) return 1;
+        std::copy(leaves.begin(), leaves.end(), leaves_out + used);
+        used += int64_t(leaves.size());
+        nleaves[s] = int64_t(leaves.size()) - 1;
+    }
     return 0;
 }

@@ -163,7 +163,7 @@ namespace sphgb {
 // per-translation-unit entry points used by capi.cu
 int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box);
 int applyOrder(sphgb_ctx* c, void* field, int esz);
-int buildTree(sphgb_ctx* c);
+int buildTree(sphgb_ctx* c, bool rebalance);
 int buildTables(sphgb_ctx* c);
 int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
 int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,

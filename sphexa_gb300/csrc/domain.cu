@@ -128,6 +128,104 @@ __global__ void splitEmitKernel(const u64* __restrict__ keys, int64_t n, int buc
     }
 }
 
+// ---- one rebalance of the previous sync's tree (the single-rank focus tree across syncs) ----
+__device__ __forceinline__ int leafLevel(u64 span) { return kMaxLevel - (63 - __clzll((long long)span)) / 3; }
+
+__device__ __forceinline__ int64_t lowerBoundLeaves(const u64* __restrict__ a, int64_t n, u64 v);
+
+// particles of the node [start, start + nodeRange(level)) in the previous tree: node boundaries are
+// leaf boundaries of that tree, so two positions in its leaf array and its layout give the count
+__device__ __forceinline__ uint32_t prevNodeCount(const u64* __restrict__ leaves, int64_t numLeaves,
+                                                  const uint32_t* __restrict__ layout, u64 start, int level)
+{
+    const int64_t a = lowerBoundLeaves(leaves, numLeaves + 1, start);
+    const int64_t b = lowerBoundLeaves(leaves, numLeaves + 1, start + nodeRange(level));
+    return layout[b] - layout[a];
+}
+
+// per leaf of the previous tree: 8 = split, 1 = keep, 0 = merged away (CombinedUpdate::updateFocus,
+// domain/include/cstone/focus/octree_focus.hpp:65-113, decisions of focus/rebalance.hpp:32-66 and
+// protectAncestors :152-165, at one rank where the focus is the whole key range).  A leaf whose
+// parent holds more than bucket particles splits when it holds more than bucket itself, else stays;
+// otherwise the subtree under its highest ancestor holding at most bucket particles collapses into
+// that ancestor, whose left-most leaf keeps the start key.
+__global__ void rebalanceOpsKernel(const u64* __restrict__ leaves, const uint32_t* __restrict__ layout,
+                                   int64_t numLeaves, uint32_t bucket, uint32_t* __restrict__ ops)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k > numLeaves) return;
+    if (k == numLeaves) {
+        ops[k] = 0;  // closes the exclusive scan
+        return;
+    }
+    const u64 s = leaves[k];
+    const int level = leafLevel(leaves[k + 1] - s);
+    const uint32_t own = layout[k + 1] - layout[k];
+    uint32_t op;
+    if (level == 0) op = own > bucket ? 8u : 1u;
+    else {
+        const u64 ps = s & ~(nodeRange(level - 1) - 1);
+        if (prevNodeCount(leaves, numLeaves, layout, ps, level - 1) > bucket)
+            op = (own > bucket && level < kMaxLevel) ? 8u : 1u;
+        else {
+            u64 as = ps;
+            int al = level - 1;
+            while (al > 0) {
+                const u64 pp = as & ~(nodeRange(al - 1) - 1);
+                if (prevNodeCount(leaves, numLeaves, layout, pp, al - 1) > bucket) break;
+                as = pp;
+                --al;
+            }
+            op = s == as ? 1u : 0u;
+        }
+    }
+    ops[k] = op;
+}
+
+__global__ void rebalanceEmitKernel(const u64* __restrict__ leaves, int64_t numLeaves, const uint32_t* __restrict__ ops,
+                                    const uint32_t* __restrict__ off, u64* __restrict__ out)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= numLeaves) return;
+    const uint32_t op = ops[k];
+    if (op == 0) return;
+    const u64 s = leaves[k];
+    const uint32_t o = off[k];
+    if (op == 1) out[o] = s;
+    else {
+        const u64 step = nodeRange(leafLevel(leaves[k + 1] - s) + 1);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) out[o + c] = s + u64(c) * step;
+    }
+}
+
+// internal nodes of a cornerstone leaf array: leaf k (start s, level l) is the left-most leaf of the
+// nodes that start at s on the levels d..l-1, d the level of the last non-zero octal digit of s
+__device__ __forceinline__ int alignLevel(u64 s) { return s == 0 ? 0 : kMaxLevel - (__ffsll((long long)s) - 1) / 3; }
+
+__global__ void internalCountKernel(const u64* __restrict__ leaves, int64_t numLeaves, uint32_t* __restrict__ cnt)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k > numLeaves) return;
+    if (k == numLeaves) {
+        cnt[k] = 0;
+        return;
+    }
+    const int l = leafLevel(leaves[k + 1] - leaves[k]), d = alignLevel(leaves[k]);
+    cnt[k] = l > d ? uint32_t(l - d) : 0u;
+}
+
+__global__ void internalEmitKernel(const u64* __restrict__ leaves, int64_t numLeaves, const uint32_t* __restrict__ off,
+                                   u64* __restrict__ codes)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= numLeaves) return;
+    const u64 s = leaves[k];
+    const int l = leafLevel(leaves[k + 1] - s), d = alignLevel(s);
+    uint32_t o = off[k];
+    for (int q = d; q < l; ++q) codes[o++] = placeholder(s, q);
+}
+
 __global__ void levelRangeKernel(const u64* __restrict__ codes, int64_t numInternal, int32_t* __restrict__ out)
 {
     // out[0..22]: first internal node of each level (level-major order); out[23..45]: levelRange
@@ -166,6 +264,11 @@ __device__ __forceinline__ int64_t lowerBoundKeys(const u64* __restrict__ a, int
         else hi = mid;
     }
     return lo;
+}
+
+__device__ __forceinline__ int64_t lowerBoundLeaves(const u64* __restrict__ a, int64_t n, u64 v)
+{
+    return lowerBoundKeys(a, n, v);
 }
 
 __global__ void octreeNodesKernel(const u64* __restrict__ internalCodes, const int32_t* __restrict__ ranges,
@@ -315,6 +418,9 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
     }
     for (int k = 0; k < 3; ++k)
         if (!(b.lim[2 * k + 1] > b.lim[2 * k])) return SPHGB_ERR_ARG;
+    // across the syncs of one simulation the tree is updated once per sync from the previous tree
+    // and its counts (the reference's focus tree, converged only at the first sync)
+    const bool rebalance = c->domainMode == 1 && !c->domainFirst && c->haveTree;
     c->prevBox = b;
     c->domainFirst = false;
     *box = b;
@@ -376,59 +482,102 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
     if (p->keys) SPHGB_CUDA(cudaMemcpyAsync(p->keys, c->keys.p, sizeof(u64) * n, cudaMemcpyDeviceToDevice, st));
     c->haveSync = true;
     c->haveNbr = false;
-    return buildTree(c);
+    return buildTree(c, rebalance);
 }
 
-int buildTree(sphgb_ctx* c)
+// exclusive sum of cnt[0..count) into off[0..count), returns off[count - 1] + cnt[count - 1]
+static int scanCounts(sphgb_ctx* c, uint32_t* cnt, uint32_t* off, int64_t count, int64_t* total)
+{
+    size_t tmp = 0;
+    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt, off, int(count), c->stream));
+    SPHGB_TRY(c->sortTemp.ensure(tmp));
+    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(c->sortTemp.p, tmp, cnt, off, int(count), c->stream));
+    c->launches += 2;
+    uint32_t t = 0;
+    SPHGB_CUDA(cudaMemcpyAsync(&t, off + count - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    *total = t;  // cnt[count - 1] is 0 by construction
+    return SPHGB_OK;
+}
+
+// rebalance = false: the converged cornerstone tree of the sorted keys (leaves split until no leaf
+// holds more than bucket particles).  rebalance = true: one update of the previous sync's tree with
+// the previous sync's counts, as the reference's focus tree evolves between syncs.
+int buildTree(sphgb_ctx* c, bool rebalance)
 {
     const int64_t n = c->n;
     cudaStream_t st = c->stream;
     const int bucket = int(c->prm.bucket);
     const u64* keys = c->keys.as<u64>();
+    int64_t S = 0, L = 0;
 
-    SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (n + 1)));
-    SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (n + 1)));
-    splitCountKernel<<<gridFor(n + 1, kBlock), kBlock, 0, st>>>(keys, n, bucket, c->splitCount.as<uint32_t>());
-    SPHGB_TRY(launched(c, "splitCountKernel"));
-    size_t tmp = 0;
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, c->splitCount.as<uint32_t>(),
-                                             c->splitOffset.as<uint32_t>(), int(n + 1), st));
-    SPHGB_TRY(c->sortTemp.ensure(tmp));
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(c->sortTemp.p, tmp, c->splitCount.as<uint32_t>(),
-                                             c->splitOffset.as<uint32_t>(), int(n + 1), st));
-    c->launches += 2;
-    uint32_t S32 = 0;
-    SPHGB_CUDA(cudaMemcpyAsync(&S32, c->splitOffset.as<uint32_t>() + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaStreamSynchronize(st));
-    const int64_t S = S32;
-    const int64_t L = 7 * S + 1;
+    if (!rebalance) {
+        SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (n + 1)));
+        SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (n + 1)));
+        splitCountKernel<<<gridFor(n + 1, kBlock), kBlock, 0, st>>>(keys, n, bucket, c->splitCount.as<uint32_t>());
+        SPHGB_TRY(launched(c, "splitCountKernel"));
+        SPHGB_TRY(scanCounts(c, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(), n + 1, &S));
+        L = 7 * S + 1;
+        SPHGB_TRY(c->leafKeysTmp.ensure(sizeof(u64) * (L + 1)));
+        SPHGB_TRY(c->leaves.ensure(sizeof(u64) * (L + 1)));
+        SPHGB_TRY(c->internalTmp.ensure(sizeof(u64) * (S + 1)));
+        SPHGB_TRY(c->internalCodes.ensure(sizeof(u64) * (S + 1)));
+        splitEmitKernel<<<gridFor(n, kBlock), kBlock, 0, st>>>(keys, n, bucket, c->splitOffset.as<uint32_t>(), S,
+                                                               c->leafKeysTmp.as<u64>(), c->internalTmp.as<u64>());
+        SPHGB_TRY(launched(c, "splitEmitKernel"));
+        if (L > 1) {
+            size_t tmp = 0;
+            SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->leafKeysTmp.as<u64>(), c->leaves.as<u64>(),
+                                                      int(L), 0, 63, st));
+            SPHGB_TRY(c->sortTemp.ensure(tmp));
+            SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->leafKeysTmp.as<u64>(),
+                                                      c->leaves.as<u64>(), int(L), 0, 63, st));
+            c->launches += 4;
+        } else {
+            SPHGB_CUDA(cudaMemsetAsync(c->leaves.p, 0, sizeof(u64), st));
+        }
+    } else {
+        // the previous tree: c->leaves (numLeaves + 1 keys) and its layout of the previous keys
+        const int64_t Lp = c->numLeaves;
+        SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (Lp + 1)));
+        SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (Lp + 1)));
+        rebalanceOpsKernel<<<gridFor(Lp + 1, kBlock), kBlock, 0, st>>>(c->leaves.as<u64>(), c->layout.as<uint32_t>(), Lp,
+                                                                      uint32_t(bucket), c->splitCount.as<uint32_t>());
+        SPHGB_TRY(launched(c, "rebalanceOpsKernel"));
+        SPHGB_TRY(scanCounts(c, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(), Lp + 1, &L));
+        SPHGB_TRY(c->leafKeysTmp.ensure(sizeof(u64) * (L + 1)));
+        rebalanceEmitKernel<<<gridFor(Lp, kBlock), kBlock, 0, st>>>(c->leaves.as<u64>(), Lp, c->splitCount.as<uint32_t>(),
+                                                                   c->splitOffset.as<uint32_t>(), c->leafKeysTmp.as<u64>());
+        SPHGB_TRY(launched(c, "rebalanceEmitKernel"));
+        setKey<<<1, 1, 0, st>>>(c->leafKeysTmp.as<u64>() + L, kKeyEnd);
+        SPHGB_TRY(launched(c, "setKey"));
+        // internal nodes of the new leaves
+        SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (L + 1)));
+        SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (L + 1)));
+        internalCountKernel<<<gridFor(L + 1, kBlock), kBlock, 0, st>>>(c->leafKeysTmp.as<u64>(), L,
+                                                                      c->splitCount.as<uint32_t>());
+        SPHGB_TRY(launched(c, "internalCountKernel"));
+        SPHGB_TRY(scanCounts(c, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(), L + 1, &S));
+        if (7 * S + 1 != L) return SPHGB_ERR_STATE;  // not a cornerstone leaf array
+        SPHGB_TRY(c->internalTmp.ensure(sizeof(u64) * (S + 1)));
+        SPHGB_TRY(c->internalCodes.ensure(sizeof(u64) * (S + 1)));
+        internalEmitKernel<<<gridFor(L, kBlock), kBlock, 0, st>>>(c->leafKeysTmp.as<u64>(), L,
+                                                                 c->splitOffset.as<uint32_t>(), c->internalTmp.as<u64>());
+        SPHGB_TRY(launched(c, "internalEmitKernel"));
+        SPHGB_TRY(c->leaves.ensure(sizeof(u64) * (L + 1)));
+        SPHGB_CUDA(cudaMemcpyAsync(c->leaves.p, c->leafKeysTmp.p, sizeof(u64) * L, cudaMemcpyDeviceToDevice, st));
+    }
     c->numInternal = S;
     c->numLeaves = L;
     c->numNodes = L + S;
-
-    SPHGB_TRY(c->leafKeysTmp.ensure(sizeof(u64) * (L + 1)));
-    SPHGB_TRY(c->leaves.ensure(sizeof(u64) * (L + 1)));
-    SPHGB_TRY(c->internalTmp.ensure(sizeof(u64) * (S + 1)));
-    SPHGB_TRY(c->internalCodes.ensure(sizeof(u64) * (S + 1)));
-    splitEmitKernel<<<gridFor(n, kBlock), kBlock, 0, st>>>(keys, n, bucket, c->splitOffset.as<uint32_t>(), S,
-                                                           c->leafKeysTmp.as<u64>(), c->internalTmp.as<u64>());
-    SPHGB_TRY(launched(c, "splitEmitKernel"));
-    if (L > 1) {
-        tmp = 0;
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->leafKeysTmp.as<u64>(), c->leaves.as<u64>(), int(L),
-                                                  0, 63, st));
-        SPHGB_TRY(c->sortTemp.ensure(tmp));
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->leafKeysTmp.as<u64>(), c->leaves.as<u64>(),
-                                                  int(L), 0, 63, st));
-        tmp = 0;
+    if (S > 0) {
+        size_t tmp = 0;
         SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->internalTmp.as<u64>(), c->internalCodes.as<u64>(),
                                                   int(S), 0, 62, st));
         SPHGB_TRY(c->sortTemp.ensure(tmp));
         SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->internalTmp.as<u64>(),
                                                   c->internalCodes.as<u64>(), int(S), 0, 62, st));
-        c->launches += 8;
-    } else {
-        SPHGB_CUDA(cudaMemsetAsync(c->leaves.p, 0, sizeof(u64), st));
+        c->launches += 4;
     }
     setKey<<<1, 1, 0, st>>>(c->leaves.as<u64>() + L, kKeyEnd);
     SPHGB_TRY(launched(c, "setKey"));
