@@ -321,8 +321,9 @@ int sphgb_sweep_passes(sphgb_ctx* c, sphgb_particles* p, int32_t variant, int32_
     int st = s;
     struct SweepScope {  // precomputes once per sweep, released on every exit path
         sphgb_ctx* c;
-        explicit SweepScope(sphgb_ctx* cc) : c(cc) { c->inSweep = true, c->sweepPrepared = false; }
-        ~SweepScope() { c->inSweep = false, c->sweepPrepared = false; }
+        explicit SweepScope(sphgb_ctx* cc) : c(cc) { reset(true); }
+        ~SweepScope() { reset(false); }
+        void reset(bool in) { c->inSweep = in, c->sweepPrepared = c->eosFused = c->auxReady = false; }
     } scope(c);
     auto stage = [&](int k, auto&& fn) {
         StageTimer t(c, kStagePass0 + k);

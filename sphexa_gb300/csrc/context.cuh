@@ -108,6 +108,8 @@ struct sphgb_ctx {
     sphgb::DBuf pairAcc;
     // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
     bool inSweep = false, sweepPrepared = false;
+    // within one sweep: the EOS ran in the gradh epilogue / the per-particle quotients are formed
+    bool eosFused = false, auxReady = false;
     // packed neighbour-side records of the mixed pair passes (float4 x 4 per particle)
     sphgb::DBuf pack;
     // mixed form: FP64 refinement of ill-conditioned particles (masks, FP64 xm/kx/gradh scratch,

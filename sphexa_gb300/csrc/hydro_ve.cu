@@ -44,6 +44,20 @@ __global__ void veAuxKernel(int64_t n, const void* m, const void* kx, const void
     }
 }
 
+// all aux parts of particle i from its own m, kx, xm, prho (the sweep forms them once, fused)
+template<class T>
+__device__ __forceinline__ void veAuxAll(int64_t n, int64_t i, T mi, T kxi, T xmi, T prhoi, T* aux)
+{
+    const T rho = kxi * mi / xmi;
+    aux[i] = rho;
+    aux[n + i] = mi / rho;
+    aux[2 * n + i] = xmi / kxi;
+    aux[3 * n + i] = mi * prhoi;
+    if constexpr (std::is_same_v<T, double>) aux[4 * n + i] = log(xmi);
+    else aux[4 * n + i] = log2f(xmi);
+    aux[5 * n + i] = T(1) / rho;
+}
+
 template<class P, int Parts>
 int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 {
@@ -57,6 +71,7 @@ int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 template<int Parts>
 int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 {
+    if (c->inSweep && c->auxReady) return SPHGB_OK;  // formed by the fused EOS of this sweep
     return p->precision == SPHGB_MIXED ? launchVeAux<MixedTag, Parts>(c, p) : launchVeAux<Fp64Tag, Parts>(c, p);
 }
 
@@ -135,6 +150,22 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
 }
 
 // ---------------------------------------------------------------- EOS (ideal gas, VE)
+// computeIdealGasEOS_Impl (hydro_ve/eos.hpp:52-94) for particle i; returns prho in the field type
+template<class T>
+__device__ __forceinline__ T eosVe(int64_t i, double ui, T mi, T kxi, T xmi, T gradhi, double gamma, void* prho,
+                                   void* c, void* rho, void* p)
+{
+    T rhoi = kxi * mi / xmi;
+    double tmp = ui * (gamma - 1.0);
+    double pi = double(rhoi) * tmp;
+    const T prhoi = T(pi / double(kxi * mi * mi * gradhi));
+    st<T>(prho, i, prhoi);
+    st<T>(c, i, T(sqrt(gamma * tmp)));
+    if (rho) st<T>(rho, i, rhoi);
+    if (p) st<T>(p, i, T(pi));
+    return prhoi;
+}
+
 template<class P>
 __global__ void eosVeKernel(int64_t first, int64_t last, const double* u, const void* m, const void* kx,
                             const void* xm, const void* gradh, double gamma, void* prho, void* c, void* rho, void* p)
@@ -142,14 +173,21 @@ __global__ void eosVeKernel(int64_t first, int64_t last, const double* u, const 
     using T = typename P::T;
     int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= last) return;
-    T kxi = ld<T>(kx, i), mi = ld<T>(m, i), xmi = ld<T>(xm, i);
-    T rhoi = kxi * mi / xmi;
-    double tmp = u[i] * (gamma - 1.0);
-    double pi = double(rhoi) * tmp;
-    st<T>(prho, i, T(pi / double(kxi * mi * mi * ld<T>(gradh, i))));
-    st<T>(c, i, T(sqrt(gamma * tmp)));
-    if (rho) st<T>(rho, i, rhoi);
-    if (p) st<T>(p, i, T(pi));
+    eosVe<T>(i, u[i], ld<T>(m, i), ld<T>(kx, i), ld<T>(xm, i), ld<T>(gradh, i), gamma, prho, c, rho, p);
+}
+
+// EOS fused with the per-particle quotients of the later passes (one read of m, kx, xm, gradh)
+template<class P>
+__global__ void eosAuxVeKernel(int64_t n, const double* u, const void* m, const void* kx, const void* xm,
+                               const void* gradh, double gamma, void* prho, void* c, void* rho, void* p,
+                               typename P::T* aux)
+{
+    using T = typename P::T;
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const T mi = ld<T>(m, i), kxi = ld<T>(kx, i), xmi = ld<T>(xm, i);
+    const T prhoi = eosVe<T>(i, u[i], mi, kxi, xmi, ld<T>(gradh, i), gamma, prho, c, rho, p);
+    veAuxAll<T>(n, i, mi, kxi, xmi, prhoi, aux);
 }
 
 // ---------------------------------------------------------------- IAD + divv/curlv
@@ -751,6 +789,29 @@ __global__ void gradhOnceFinish(int64_t first, int64_t last, int64_t n, const do
     gradhOut[i] = 1.0 - dhdrho * whomega;
 }
 
+// the same epilogue fused with the EOS and the quotients of the later passes (inside a sweep)
+__global__ void gradhEosFinish(int64_t n, const double* h, const double* m, const double* xm, double K,
+                               const double* acc, double* kxOut, double* gradhOut, const double* u, double gamma,
+                               void* prho, void* c, void* rho, void* p, double* aux)
+{
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const double hi = h[i], mi = m[i], xmi = xm[i];
+    const double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
+    double kxi = xmi + acc[i], whomega = -3.0 * xmi + acc[n + i], wrho0 = -3.0 * mi + acc[2 * n + i];
+    kxi *= K * h3Inv;
+    whomega *= K * h3Inv * hInv;
+    wrho0 *= K * h3Inv * hInv;
+    whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
+    const double rhoi = kxi * mi / xmi;
+    const double dhdrho = -hi / (rhoi * 3.0);
+    const double gradhi = 1.0 - dhdrho * whomega;
+    kxOut[i] = kxi;
+    gradhOut[i] = gradhi;
+    const double prhoi = eosVe<double>(i, u[i], mi, kxi, xmi, gradhi, gamma, prho, c, rho, p);
+    veAuxAll<double>(n, i, mi, kxi, xmi, prhoi, aux);
+}
+
 // FP64 AV switches with one evaluation per mutual pair over the owned lists.  i's sum is
 // S_i = sum vol_j (divv_i - divv_j) W_i r (r = x_i - x_j; c_i is applied after the walk), j's term of
 // the same pair is vol_i (divv_i - divv_j) W_j r (r and the divv difference both change sign);
@@ -984,6 +1045,15 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
             static_cast<const double*>(p->xm), c->whx64.as<double2>(), c->whdx64.as<double2>(),
             c->hInv64.as<double>(), n, c->pairAcc.as<double>());
         SPHGB_TRY(launched(c, "gradhOnceKernel"));
+        if (c->inSweep && p->u && p->prho && p->c) {  // EOS and quotients fused into the epilogue
+            SPHGB_TRY(c->aux.ensure(sizeof(double) * 6 * n));
+            gradhEosFinish<<<gridFor(n, 256), 256, 0, c->stream>>>(
+                n, static_cast<const double*>(p->h), static_cast<const double*>(p->m), static_cast<const double*>(p->xm),
+                c->K, c->pairAcc.as<double>(), static_cast<double*>(p->kx), static_cast<double*>(p->gradh), p->u,
+                c->prm.gamma, p->prho, p->c, p->rho, p->p, c->aux.as<double>());
+            c->eosFused = c->auxReady = true;
+            return launched(c, "gradhEosFinish");
+        }
         gradhOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(
             first, last, n, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
             static_cast<const double*>(p->xm), c->K, c->pairAcc.as<double>(), static_cast<double*>(p->kx),
@@ -1010,7 +1080,22 @@ int passEosVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     if (!p->u || !p->m || !p->kx || !p->xm || !p->gradh || !p->prho || !p->c || first < 0 || last > p->n ||
         first >= last)
         return SPHGB_ERR_ARG;
+    if (c->inSweep && c->eosFused) return SPHGB_OK;  // done in the gradh epilogue of this sweep
     unsigned blocks = gridFor(last - first, 256);
+    if (c->inSweep && first == 0 && last == p->n) {  // EOS and the quotients of the later passes together
+        const int64_t n = p->n;
+        if (p->precision == SPHGB_MIXED) {
+            SPHGB_TRY(c->aux.ensure(sizeof(float) * 6 * n));
+            eosAuxVeKernel<MixedTag><<<blocks, 256, 0, c->stream>>>(n, p->u, p->m, p->kx, p->xm, p->gradh, c->prm.gamma,
+                                                                   p->prho, p->c, p->rho, p->p, c->aux.as<float>());
+        } else {
+            SPHGB_TRY(c->aux.ensure(sizeof(double) * 6 * n));
+            eosAuxVeKernel<Fp64Tag><<<blocks, 256, 0, c->stream>>>(n, p->u, p->m, p->kx, p->xm, p->gradh, c->prm.gamma,
+                                                                  p->prho, p->c, p->rho, p->p, c->aux.as<double>());
+        }
+        c->auxReady = true;
+        return launched(c, "eosAuxVeKernel");
+    }
     if (p->precision == SPHGB_MIXED)
         eosVeKernel<MixedTag><<<blocks, 256, 0, c->stream>>>(first, last, p->u, p->m, p->kx, p->xm, p->gradh,
                                                             c->prm.gamma, p->prho, p->c, p->rho, p->p);
