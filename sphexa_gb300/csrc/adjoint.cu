@@ -15,8 +15,6 @@
 // once by thread i over its list for the partials of i's quantities and once by thread j over the
 // transposed list for the partials of j's quantities.  Each thread writes only its own particle,
 // so the sums are deterministic.  No per-pair value is stored.
-#include <cub/cub.cuh>
-
 #include "pairs.cuh"
 
 namespace sphgb {
@@ -623,12 +621,7 @@ int buildTranspose(sphgb_ctx* c)
     SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (nWork + 1)));
     cappedCountKernel<<<gridFor(nWork + 1, 256), 256, 0, c->stream>>>(lv, c->splitCount.as<uint32_t>());
     SPHGB_TRY(launched(c, "cappedCountKernel"));
-    size_t tmp = 0;
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(),
-                                             int(nWork + 1), c->stream));
-    SPHGB_TRY(c->sortTemp.ensure(tmp));
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(c->sortTemp.p, tmp, c->splitCount.as<uint32_t>(),
-                                             c->splitOffset.as<uint32_t>(), int(nWork + 1), c->stream));
+    SPHGB_TRY(exclusiveScan(c, c->splitCount.as<uint32_t>(), c->splitOffset.as<uint32_t>(), nWork + 1));
     uint32_t pairs32 = 0;
     SPHGB_CUDA(cudaMemcpyAsync(&pairs32, c->splitOffset.as<uint32_t>() + nWork, sizeof(uint32_t),
                                cudaMemcpyDeviceToHost, c->stream));
@@ -641,14 +634,8 @@ int buildTranspose(sphgb_ctx* c)
     pairKeysKernel<<<gridFor(nWork, 256), 256, 0, c->stream>>>(lv, c->splitOffset.as<uint32_t>(),
                                                               c->adjKeysAlt.as<u64>());
     SPHGB_TRY(launched(c, "pairKeysKernel"));
-    if (pairs > 0) {
-        tmp = 0;
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->adjKeysAlt.as<u64>(), c->adjKeys.as<u64>(),
-                                                  int(pairs), 0, 64, c->stream));
-        SPHGB_TRY(c->sortTemp.ensure(tmp));
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->adjKeysAlt.as<u64>(), c->adjKeys.as<u64>(),
-                                                  int(pairs), 0, 64, c->stream));
-    }
+    if (pairs > 0)  // keys (j << 32 | i) with j < 2^31: 63 bits
+        SPHGB_TRY(radixSort(c, c->adjKeysAlt.as<u64>(), c->adjKeys.as<u64>(), nullptr, nullptr, pairs, 63));
     int64_t work = pairs > 0 ? pairs : nWork + 1;
     csrFromKeysKernel<<<gridFor(work, 256), 256, 0, c->stream>>>(c->adjKeys.as<u64>(), pairs, nWork,
                                                                 c->tOff.as<uint32_t>(), c->tIdx.as<uint32_t>());

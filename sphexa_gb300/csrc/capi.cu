@@ -141,7 +141,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32,    &c->refMask,
-                    &c->refFp64,    &c->divvBound,  &c->intScratch};
+                    &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)

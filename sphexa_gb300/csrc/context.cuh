@@ -142,6 +142,7 @@ struct sphgb_ctx {
     // adjoint: incoming lists as CSR (tOff, tIdx) built from sorted (j<<32|i) keys, and the
     // per-particle adjoint state of the intermediate fields
     sphgb::DBuf adjKeys, adjKeysAlt, tOff, tIdx, adjState;
+    sphgb::DBuf scanTemp;  // tile sums of exclusiveScan
     int64_t transEpoch = -1, transPairs = 0;
     // validity of the precomputes: the lists' epoch and the field pointers they were made from
     int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;
@@ -187,6 +188,11 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
                          double* minDt);
 
 int buildTranspose(sphgb_ctx* c);
+// stable LSD radix sort of 64-bit keys (bits [0, endBit)) with optional 32-bit values, out of place
+int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* valsIn, uint32_t* valsOut, int64_t n,
+              int endBit);
+// exclusive prefix sum of n 32-bit counts (out may not alias in)
+int exclusiveScan(sphgb_ctx* c, const uint32_t* in, uint32_t* out, int64_t n);
 int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic);
 int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avClean, const sphgb_seeds* s,
               sphgb_grads* g, int deterministic);

@@ -10,7 +10,6 @@
 // nodes, plus key 0, are exactly the leaf start keys.
 #include <algorithm>
 
-#include <cub/cub.cuh>
 
 #include "context.cuh"
 
@@ -436,15 +435,8 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
     keysKernel<<<gridFor(n, kBlock), kBlock, 0, st>>>(p->x, p->y, p->z, n, c->box, c->keysAlt.as<u64>(),
                                                        c->orderAlt.as<uint32_t>());
     SPHGB_TRY(launched(c, "keysKernel"));
-    size_t tmp = 0;
-    SPHGB_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, c->keysAlt.as<u64>(), c->keys.as<u64>(),
-                                               c->orderAlt.as<uint32_t>(), c->order.as<uint32_t>(), int(n), 0, 63,
-                                               st));
-    SPHGB_TRY(c->sortTemp.ensure(tmp));
-    SPHGB_CUDA(cub::DeviceRadixSort::SortPairs(c->sortTemp.p, tmp, c->keysAlt.as<u64>(), c->keys.as<u64>(),
-                                               c->orderAlt.as<uint32_t>(), c->order.as<uint32_t>(), int(n), 0, 63,
-                                               st));
-    c->launches += 4;  // upsweep/downsweep passes of the library sort (counted once per pass group)
+    SPHGB_TRY(radixSort(c, c->keysAlt.as<u64>(), c->keys.as<u64>(), c->orderAlt.as<uint32_t>(),
+                        c->order.as<uint32_t>(), n, 63));
 
     // permute the conserved fields in place (the reference's particleProperties of sync)
     const size_t hs = p->precision == SPHGB_MIXED ? 4 : 8;
@@ -488,11 +480,7 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
 // exclusive sum of cnt[0..count) into off[0..count), returns off[count - 1] + cnt[count - 1]
 static int scanCounts(sphgb_ctx* c, uint32_t* cnt, uint32_t* off, int64_t count, int64_t* total)
 {
-    size_t tmp = 0;
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt, off, int(count), c->stream));
-    SPHGB_TRY(c->sortTemp.ensure(tmp));
-    SPHGB_CUDA(cub::DeviceScan::ExclusiveSum(c->sortTemp.p, tmp, cnt, off, int(count), c->stream));
-    c->launches += 2;
+    SPHGB_TRY(exclusiveScan(c, cnt, off, count));
     uint32_t t = 0;
     SPHGB_CUDA(cudaMemcpyAsync(&t, off + count - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
@@ -526,13 +514,7 @@ int buildTree(sphgb_ctx* c, bool rebalance)
                                                                c->leafKeysTmp.as<u64>(), c->internalTmp.as<u64>());
         SPHGB_TRY(launched(c, "splitEmitKernel"));
         if (L > 1) {
-            size_t tmp = 0;
-            SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->leafKeysTmp.as<u64>(), c->leaves.as<u64>(),
-                                                      int(L), 0, 63, st));
-            SPHGB_TRY(c->sortTemp.ensure(tmp));
-            SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->leafKeysTmp.as<u64>(),
-                                                      c->leaves.as<u64>(), int(L), 0, 63, st));
-            c->launches += 4;
+            SPHGB_TRY(radixSort(c, c->leafKeysTmp.as<u64>(), c->leaves.as<u64>(), nullptr, nullptr, L, 63));
         } else {
             SPHGB_CUDA(cudaMemsetAsync(c->leaves.p, 0, sizeof(u64), st));
         }
@@ -570,15 +552,7 @@ int buildTree(sphgb_ctx* c, bool rebalance)
     c->numInternal = S;
     c->numLeaves = L;
     c->numNodes = L + S;
-    if (S > 0) {
-        size_t tmp = 0;
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, c->internalTmp.as<u64>(), c->internalCodes.as<u64>(),
-                                                  int(S), 0, 62, st));
-        SPHGB_TRY(c->sortTemp.ensure(tmp));
-        SPHGB_CUDA(cub::DeviceRadixSort::SortKeys(c->sortTemp.p, tmp, c->internalTmp.as<u64>(),
-                                                  c->internalCodes.as<u64>(), int(S), 0, 62, st));
-        c->launches += 4;
-    }
+    if (S > 0) SPHGB_TRY(radixSort(c, c->internalTmp.as<u64>(), c->internalCodes.as<u64>(), nullptr, nullptr, S, 62));
     setKey<<<1, 1, 0, st>>>(c->leaves.as<u64>() + L, kKeyEnd);
     SPHGB_TRY(launched(c, "setKey"));
 

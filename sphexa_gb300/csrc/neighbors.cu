@@ -17,7 +17,6 @@
 // nbr[k * stride + (i - first)], so that the pair passes read them coalesced.
 #include <algorithm>
 
-#include <cub/cub.cuh>
 
 #include "pairs.cuh"
 

@@ -133,3 +133,21 @@ def test_sizes_rejected_before_any_access(gpu_ctx):
     assert lib.sphgb_domain_sync(gpu_ctx.h, C.byref(p), C.byref(b)) == 1
     p.n = 0
     assert lib.sphgb_domain_sync(gpu_ctx.h, C.byref(p), C.byref(b)) == 1
+
+
+def test_duplicate_positions_sort_stably(gpu_ctx, port):
+    """20 particles on each point of a 10^3 lattice: equal keys keep their input order (the
+    reference's stable sort_by_key), and the tree and lists stay those of the oracle"""
+    from oracle import oracle as O
+    from sphexa_gb300 import sph, workloads as W
+    wl = W.random_cube(20000, seed=93, periodic=True)
+    g = (np.arange(20000) % 1000)
+    for k, f in enumerate(("x", "y", "z")):
+        wl.fields[f] = -0.5 + (((g // 10 ** k) % 10) + 0.5) / 10.0
+    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+    dom = sph.Domain(gpu_ctx, sph.Box(wl.box.copy(), wl.bc.copy()))
+    dom.sync(d)
+    ref = port.sweep(wl, "ve", stages=O.OS_KEYS | O.OS_TREE, want_nbr=False)
+    np.testing.assert_array_equal(d.keys.cpu().numpy().view(np.uint64), ref["keys"])
+    np.testing.assert_array_equal(dom.order(wl.n), ref["order"].astype(np.int64))
+    np.testing.assert_array_equal(dom.tree()["leaves"], ref["leaves"])
