@@ -143,6 +143,7 @@ struct sphgb_ctx {
     // per-particle adjoint state of the intermediate fields
     sphgb::DBuf adjKeys, adjKeysAlt, tOff, tIdx, adjState;
     sphgb::DBuf scanTemp;  // tile sums of exclusiveScan
+    bool sortSmemSet = false;
     int64_t transEpoch = -1, transPairs = 0;
     // validity of the precomputes: the lists' epoch and the field pointers they were made from
     int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;

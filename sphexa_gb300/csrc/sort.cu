@@ -8,8 +8,8 @@
 //   scan        exclusive prefix of that matrix: each (digit, tile) gets its first output slot
 //   scatter     each tile ranks its keys per digit in index order (warp match for the lanes of one
 //               round, per-warp prefix in shared memory, a running base across the tile's rounds)
-//               and writes key and value to slot + rank: equal digits keep their input order, so
-//               every pass, and the sort, is stable.
+//               into shared memory, grouped by digit, then writes each digit's run to its slots:
+//               equal digits keep their input order, so every pass, and the sort, is stable.
 // Scan: per-tile sums, one block scanning the sums, per-tile scan with its base.
 #include "context.cuh"
 
@@ -22,6 +22,7 @@ constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;
 constexpr int kWarps = kThreads / 32;
 constexpr int kRadix = 256;
+constexpr size_t kStageKeys = sizeof(u64) * kTile, kStagePairs = (sizeof(u64) + sizeof(uint32_t)) * kTile;
 
 __global__ void __launch_bounds__(kThreads) radixHistKernel(const u64* __restrict__ keys, int64_t n, int shift,
                                                             int64_t tiles, uint32_t* __restrict__ counts)
@@ -39,17 +40,30 @@ __global__ void __launch_bounds__(kThreads) radixHistKernel(const u64* __restric
     counts[int64_t(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* sh, uint32_t& blockTotal);
+
+// ranks the tile's keys per digit in index order into shared memory (tile-local digit runs), then
+// writes the runs out: consecutive slots of one digit go to consecutive global slots (coalesced)
 template<bool WithVals>
 __global__ void __launch_bounds__(kThreads) radixScatterKernel(const u64* __restrict__ keysIn,
                                                                const uint32_t* __restrict__ valsIn,
                                                                u64* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
                                                                int64_t n, int shift, int64_t tiles,
+                                                               const uint32_t* __restrict__ counts,
                                                                const uint32_t* __restrict__ offsets)
 {
-    __shared__ uint32_t base[kRadix];
+    extern __shared__ u64 staged[];  // kTile keys, then kTile values
+    uint32_t* stagedVals = reinterpret_cast<uint32_t*>(staged + kTile);
+    __shared__ uint32_t base[kRadix], localStart[kRadix], globalStart[kRadix];
     __shared__ uint32_t warpCnt[kWarps][kRadix];
+    __shared__ uint32_t sh[32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    base[tid] = offsets[int64_t(tid) * tiles + blockIdx.x];
+    const int64_t cell = int64_t(tid) * tiles + blockIdx.x;
+    uint32_t tileTotal;
+    const uint32_t ls = blockExclusiveScan(counts[cell], sh, tileTotal);
+    localStart[tid] = ls;
+    base[tid] = ls;
+    globalStart[tid] = offsets[cell];
     const int64_t tileStart = int64_t(blockIdx.x) * kTile;
     for (int r = 0; r < kItems; ++r) {
 #pragma unroll
@@ -74,11 +88,19 @@ __global__ void __launch_bounds__(kThreads) radixScatterKernel(const u64* __rest
         __syncthreads();
         if (valid) {
             const uint32_t pos = base[digit] + warpCnt[warp][digit] + rankInWarp;
-            keysOut[pos] = key;
-            if (WithVals) valsOut[pos] = val;
+            staged[pos] = key;
+            if (WithVals) stagedVals[pos] = val;
         }
         __syncthreads();
         base[tid] += total;
+    }
+    __syncthreads();
+    for (uint32_t t = tid; t < tileTotal; t += kThreads) {
+        const u64 key = staged[t];
+        const unsigned d = unsigned(key >> shift) & (kRadix - 1);
+        const uint32_t pos = globalStart[d] + (t - localStart[d]);
+        keysOut[pos] = key;
+        if (WithVals) valsOut[pos] = stagedVals[t];
     }
 }
 
@@ -210,6 +232,13 @@ int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* val
     uint32_t* offsets = reinterpret_cast<uint32_t*>(base + bKeys + bVals + bCells);
     uint32_t* scan = reinterpret_cast<uint32_t*>(base + bKeys + bVals + 2 * bCells);
 
+    if (!c->sortSmemSet) {  // the staged tile of (key, value) pairs exceeds the default 48 KB
+        SPHGB_CUDA(cudaFuncSetAttribute(radixScatterKernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(kStagePairs)));
+        SPHGB_CUDA(cudaFuncSetAttribute(radixScatterKernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(kStageKeys)));
+        c->sortSmemSet = true;
+    }
     const int passes = (endBit + 7) / 8;
     const u64* kSrc = keysIn;
     const uint32_t* vSrc = valsIn;
@@ -223,11 +252,11 @@ int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* val
         SPHGB_TRY(launched(c, "radixHistKernel"));
         SPHGB_TRY(exclusiveScan(c, counts, offsets, cells, scan));
         if (withVals)
-            radixScatterKernel<true><<<unsigned(tiles), kThreads, 0, st>>>(kSrc, vSrc, kDst, vDst, n, shift, tiles,
-                                                                          offsets);
+            radixScatterKernel<true><<<unsigned(tiles), kThreads, kStagePairs, st>>>(kSrc, vSrc, kDst, vDst, n, shift,
+                                                                                    tiles, counts, offsets);
         else
-            radixScatterKernel<false><<<unsigned(tiles), kThreads, 0, st>>>(kSrc, nullptr, kDst, nullptr, n, shift,
-                                                                           tiles, offsets);
+            radixScatterKernel<false><<<unsigned(tiles), kThreads, kStageKeys, st>>>(kSrc, nullptr, kDst, nullptr, n,
+                                                                                    shift, tiles, counts, offsets);
         SPHGB_TRY(launched(c, "radixScatterKernel"));
         kSrc = kDst;
         vSrc = vDst;
