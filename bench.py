@@ -296,9 +296,10 @@ def main() -> None:
     fp64_peak = ctx.fma_peak(True)
     fp32_peak = ctx.fma_peak(False)
 
+    from sphexa_gb300 import replicas as R
+
     def barrier():
-        if world > 1:
-            dist.barrier()
+        R.barrier(world)
 
     def timed_sweeps(d, box, steps, warmup):
         for _ in range(warmup):
@@ -319,11 +320,7 @@ def main() -> None:
         torch.cuda.synchronize()
         barrier()
         ck = clocks.stop()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = R.max_over_ranks(e0.elapsed_time(e1), world, dev)
         return ms, stage_sum / steps, ctx.launches() - l0, ck
 
     # ---------------- FP64 form (headline)
@@ -332,7 +329,7 @@ def main() -> None:
     ms64, st64, launches, clocks = timed_sweeps(d64, box, args.steps, args.warmup)
     stats = ctx.stats()
     pairs = stats["nc_sum"]
-    value = n * args.steps * world / (ms64 * 1e-3)
+    value = R.job_throughput(n, args.steps, world, ms64)
 
     # dominant kernel: largest per-stage time of the FP64 sweep
     names = STAGES_VE if args.variant == "ve" else ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
@@ -376,7 +373,7 @@ def main() -> None:
         d32 = sph.ParticlesData.from_workload(wl, "mixed", dev)
         box32 = sph.Box(wl.box.copy(), wl.bc.copy())
         ms32, st32, _, _ = timed_sweeps(d32, box32, args.steps, args.warmup)
-        v32 = n * args.steps * world / (ms32 * 1e-3)
+        v32 = R.job_throughput(n, args.steps, world, ms32)
         r32 = {k: d32.f[k].double().cpu().numpy() for k in ref64}
         a64 = np.stack([ref64["ax"], ref64["ay"], ref64["az"]], 1)
         a32 = np.stack([r32["ax"], r32["ay"], r32["az"]], 1)
@@ -432,8 +429,8 @@ def main() -> None:
         for _ in range(k_e2e):
             e2e_step()
         barrier()
-        wall = time.perf_counter() - t0
-        out["e2e"] = {"value": n * k_e2e * world / wall, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        wall_ms = R.max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+        out["e2e"] = {"value": R.job_throughput(n, k_e2e, world, wall_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "steps": k_e2e,
                       "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
         del d
