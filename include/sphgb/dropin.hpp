@@ -428,5 +428,39 @@ localConservedQuantities(std::size_t first, std::size_t last, Dataset& d)
     return {o[0], o[1], {o[2], o[3], o[4]}, {o[5], o[6], o[7]}};
 }
 
+/*! Gradients of one forward pass sequence (no reference counterpart).  Seeds and results are device
+ *  arrays of n doubles in SFC order (a null seed counts as zero); the lists are those of the last
+ *  neighbour search, the state that of the last forward passes (FP64 fields). */
+struct Seeds {
+    const double *rho = nullptr, *ax = nullptr, *ay = nullptr, *az = nullptr, *du = nullptr;
+};
+struct Grads {
+    double *x, *y, *z, *vx, *vy, *vz, *h, *u;
+};
+
+//! adjoint of the std chain computeDensity -> computeEOS_HydroStd -> computeIAD -> computeMomentumEnergySTD
+template<class Dataset>
+void adjointStd(Dataset& d, const Seeds& s, const Grads& g, bool deterministic = false)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    sphgb_seeds sd{s.rho, s.ax, s.ay, s.az, s.du};
+    sphgb_grads gr{g.x, g.y, g.z, g.vx, g.vy, g.vz, g.h, g.u};
+    check(sphgb_adjoint_std(c, &p, &sd, &gr, deterministic ? 1 : 0), "adjointStd");
+}
+
+/*! adjoint of the VE chain computeXMass -> computeVeDefGradh -> computeEOS -> computeIadDivvCurlv ->
+ *  computeAVswitches -> computeMomentumEnergy<avClean>; alphaPrev: a device copy of alpha taken
+ *  before computeAVswitches (which updates alpha in place) */
+template<bool avClean, class Dataset>
+void adjointVe(Dataset& d, const double* alphaPrev, const Seeds& s, const Grads& g, bool deterministic = false)
+{
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    sphgb_seeds sd{s.rho, s.ax, s.ay, s.az, s.du};
+    sphgb_grads gr{g.x, g.y, g.z, g.vx, g.vy, g.vz, g.h, g.u};
+    check(sphgb_adjoint_ve(c, &p, alphaPrev, avClean ? 1 : 0, &sd, &gr, deterministic ? 1 : 0), "adjointVe");
+}
+
 }  // namespace dropin
 }  // namespace sphgb

@@ -1,7 +1,8 @@
 // A VE and a std sweep written the way the reference's propagators call them
 // (main/src/propagator/ve_hydro.hpp:130-204, std_hydro.hpp:124-168), through the drop-in adapter.
 // Reads binary particle fields (x y z h m u vx vy vz alpha as FP64) from argv[1], writes the
-// outputs in SFC order to argv[2].  Precision: "fp64" or "mixed" in argv[3], variant "ve"/"std" in argv[4].
+// outputs in SFC order to argv[2].  Precision: "fp64" or "mixed" in argv[3], variant "ve"/"std" in argv[4];
+// argv[3] = "adjoint": the VE adjoint check of runAdjoint instead.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -104,6 +105,94 @@ int run(const char* in, const char* out, bool ve, double lim[6], int bc[3])
     return 0;
 }
 
+// The VE adjoint through the adapter: L = sum |a|^2 after the VE passes; writes the derivative of L
+// along a fixed +-1 direction in u from adjointVe and from a central difference of the passes on
+// the frozen lists (u moves no pair distance).
+int runAdjoint(const char* in, const char* out, double lim[6], int bc[3])
+{
+    using Th = double;
+    std::FILE* f = std::fopen(in, "rb");
+    if (!f) return 2;
+    long long n = 0;
+    if (std::fread(&n, sizeof(n), 1, f) != 1) return 2;
+    std::vector<double> a(10 * n);
+    if (std::fread(a.data(), sizeof(double), a.size(), f) != a.size()) return 2;
+    std::fclose(f);
+    auto col = [&](int k) { return std::vector<double>(a.begin() + k * n, a.begin() + (k + 1) * n); };
+    ParticlesData<Th, Th> d;
+    auto& dv = d.devData;
+    DeviceVector<double>* inputs[] = {&dv.x, &dv.y, &dv.z, &dv.h, &dv.m, &dv.u, &dv.vx, &dv.vy, &dv.vz, &dv.alpha};
+    for (int k = 0; k < 10; ++k) upload(*inputs[k], col(k));
+    for (auto* v : {&dv.rho, &dv.p, &dv.c, &dv.xm, &dv.kx, &dv.gradh, &dv.prho, &dv.divv, &dv.curlv, &dv.c11, &dv.c12,
+                    &dv.c13, &dv.c22, &dv.c23, &dv.c33, &dv.ax, &dv.ay, &dv.az, &dv.du})
+        v->resize(n);
+    dv.keys.resize(n);
+    dv.nc.resize(n);
+    auto bt = [](int b) { return b == 1 ? BoundaryType::periodic : BoundaryType::open; };
+    Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
+    dr::SingleRankDomain<uint64_t, double, Box<double>> domain(0, 1, 64, 64, 0.5f, box);
+    domain.sync(d);
+    GroupView grp{0, uint32_t(n), 1, nullptr, nullptr};
+    dr::findNeighborsSfc(0, n, d, domain.box());
+    DeviceVector<double> alphaPrev(n);
+    cudaMemcpy(rawPtr(alphaPrev), rawPtr(dv.alpha), n * sizeof(double), cudaMemcpyDeviceToDevice);
+    auto host = [&](DeviceVector<double>& v) {
+        std::vector<double> h(n);
+        cudaMemcpy(h.data(), rawPtr(v), n * sizeof(double), cudaMemcpyDeviceToHost);
+        return h;
+    };
+    auto forward = [&]() {  // the VE passes on the frozen lists, from the same alpha; returns L
+        cudaMemcpy(rawPtr(dv.alpha), rawPtr(alphaPrev), n * sizeof(double), cudaMemcpyDeviceToDevice);
+        dr::computeXMass(grp, d, domain.box());
+        dr::computeVeDefGradh(grp, d, domain.box());
+        dr::computeEOS(0, n, d);
+        dr::computeIadDivvCurlv(grp, d, domain.box());
+        dr::computeAVswitches(grp, d, domain.box());
+        dr::computeMomentumEnergy<false>(grp, nullptr, d, domain.box());
+        auto ax = host(dv.ax), ay = host(dv.ay), az = host(dv.az);
+        double L = 0;
+        for (long long i = 0; i < n; ++i) L += ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i];
+        return L;
+    };
+    forward();
+    std::vector<double> s[3] = {host(dv.ax), host(dv.ay), host(dv.az)};
+    DeviceVector<double> seed[3], grad[8];
+    for (int k = 0; k < 3; ++k) {
+        for (auto& v : s[k]) v *= 2.0;
+        upload(seed[k], s[k]);
+    }
+    for (auto& g : grad) g.resize(n);
+    dr::Seeds sd;
+    sd.ax = rawPtr(seed[0]);
+    sd.ay = rawPtr(seed[1]);
+    sd.az = rawPtr(seed[2]);
+    dr::Grads gr{rawPtr(grad[0]), rawPtr(grad[1]), rawPtr(grad[2]), rawPtr(grad[3]),
+                 rawPtr(grad[4]), rawPtr(grad[5]), rawPtr(grad[6]), rawPtr(grad[7])};
+    dr::adjointVe<false>(d, rawPtr(alphaPrev), sd, gr);
+    auto gu = host(grad[7]);
+    auto u0 = host(dv.u);
+    std::vector<double> dir(n), up(n);
+    unsigned long long st = 12345;
+    double ad = 0;
+    for (long long i = 0; i < n; ++i) {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        dir[i] = (st >> 63) ? 1.0 : -1.0;
+        ad += gu[i] * dir[i];
+    }
+    const double eps = 1e-6;
+    for (long long i = 0; i < n; ++i) up[i] = u0[i] + eps * dir[i];
+    upload(dv.u, up);
+    const double lp = forward();
+    for (long long i = 0; i < n; ++i) up[i] = u0[i] - eps * dir[i];
+    upload(dv.u, up);
+    const double lm = forward();
+    const double res[2] = {ad, (lp - lm) / (2 * eps)};
+    std::FILE* o = std::fopen(out, "wb");
+    std::fwrite(res, sizeof(double), 2, o);
+    std::fclose(o);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 5) return 1;
@@ -113,6 +202,7 @@ int main(int argc, char** argv)
     for (int k = 0; k < 3; ++k) bc[k] = std::atoi(argv[11 + k]);
     bool ve = std::string(argv[4]) == "ve";
     try {
+        if (std::string(argv[3]) == "adjoint") return runAdjoint(argv[1], argv[2], lim, bc);
         if (std::string(argv[3]) == "mixed") return run<float>(argv[1], argv[2], ve, lim, bc);
         return run<double>(argv[1], argv[2], ve, lim, bc);
     } catch (const std::exception& e) {

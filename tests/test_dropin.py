@@ -84,3 +84,23 @@ def test_dropin_sweep_matches_oracle(tmp_path, port, variant, precision):
         a32 = np.stack([got["ax"], got["ay"], got["az"]], 1)
         a64 = np.stack([ref["ax"], ref["ay"], ref["az"]], 1)
         assert np.linalg.norm(a32 - a64) / np.linalg.norm(a64) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_dropin_ve_adjoint_matches_central_difference(tmp_path):
+    """dropin::adjointVe on the adapter's state against a central difference of the VE passes (u)"""
+    from sphexa_gb300 import workloads as W
+    exe = build_driver(tmp_path)
+    wl = W.fourier(12, seed=74, rho_seed=75, v_seed=76)
+    cols = ["x", "y", "z", "h", "m", "u", "vx", "vy", "vz", "alpha"]
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([wl.n], dtype=np.int64).tofile(f)
+        np.concatenate([wl.fields[c] for c in cols]).astype(np.float64).tofile(f)
+    out = tmp_path / "adj.bin"
+    args = [str(exe), str(inp), str(out), "adjoint", "ve"] + [repr(float(v)) for v in wl.box] + \
+           [str(int(b)) for b in wl.bc]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    ad, fd = np.fromfile(out, dtype=np.float64)
+    assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
