@@ -617,6 +617,8 @@ int buildTranspose(sphgb_ctx* c)
     if (c->transEpoch == c->nbrEpoch) return SPHGB_OK;
     ListView lv = listView(c);
     const int64_t nWork = lv.last - lv.first;
+    // list entries are counted and sorted with 32-bit offsets
+    if (nWork * int64_t(c->nbrNgmax) >= (int64_t(1) << 32)) return SPHGB_ERR_TOO_LARGE;
     SPHGB_TRY(c->splitCount.ensure(sizeof(uint32_t) * (nWork + 1)));
     SPHGB_TRY(c->splitOffset.ensure(sizeof(uint32_t) * (nWork + 1)));
     cappedCountKernel<<<gridFor(nWork + 1, 256), 256, 0, c->stream>>>(lv, c->splitCount.as<uint32_t>());

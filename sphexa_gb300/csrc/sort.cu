@@ -189,6 +189,7 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 int exclusiveScan(sphgb_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scratch)
 {
     if (n <= 0) return SPHGB_OK;
+    if (n >= (int64_t(1) << 32)) return SPHGB_ERR_TOO_LARGE;
     const int64_t tiles = (n + kTile - 1) / kTile;
     scanReduceKernel<<<unsigned(tiles), kThreads, 0, c->stream>>>(in, n, scratch);
     SPHGB_TRY(launched(c, "scanReduceKernel"));
@@ -211,6 +212,7 @@ int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* val
 {
     if (n <= 0) return SPHGB_OK;
     if (endBit < 1 || endBit > 64 || (valsIn == nullptr) != (valsOut == nullptr)) return SPHGB_ERR_ARG;
+    if (n >= (int64_t(1) << 32)) return SPHGB_ERR_TOO_LARGE;  // output slots are 32-bit
     cudaStream_t st = c->stream;
     if (n == 1) {
         SPHGB_CUDA(cudaMemcpyAsync(keysOut, keysIn, sizeof(u64), cudaMemcpyDeviceToDevice, st));
