@@ -215,7 +215,8 @@ typedef struct {
 /* deterministic = 0: every pair is differentiated once and the neighbour's partials are added
  * with FP64 atomics (fastest; sums in arrival order).  deterministic = 1: every pair is
  * differentiated from both ends, the neighbour end walking an incoming-list CSR built once per
- * list set, and each particle sums its own terms in a fixed order (bit-reproducible). */
+ * list set, and each particle sums its own terms in a fixed order (bit-reproducible); that CSR
+ * takes fewer than 2^32 list entries (SPHGB_ERR_TOO_LARGE otherwise). */
 int sphgb_adjoint_std(sphgb_ctx* ctx, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads,
                       int32_t deterministic);
 
