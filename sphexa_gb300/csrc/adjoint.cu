@@ -15,6 +15,7 @@
 // once by thread i over its list for the partials of i's quantities and once by thread j over the
 // transposed list for the partials of j's quantities.  Each thread writes only its own particle,
 // so the sums are deterministic.  No per-pair value is stored.
+#include "adjoint_std.cuh"
 #include "pairs.cuh"
 
 namespace sphgb {
@@ -561,6 +562,179 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjScatterKernel(AdjArgs a)
     atomicAdd(a.bh + k, bh);
 }
 
+// ---- one evaluation per owned entry of the owned lists (mutual pairs give both directed terms) ----
+__device__ __forceinline__ stdad::MeSide stdSide(const AdjArgs& a, int64_t i)
+{
+    stdad::MeSide s;
+    s.hInv = a.hInv[i];
+    s.c = a.c[i];
+    s.m = a.m[i];
+    s.rhoInv = a.rhoInv[i];
+    s.poR = a.pOverRho[i];
+    s.poR2 = a.pOverRho2[i];
+    s.C[0] = a.c11[i];
+    s.C[1] = a.c12[i];
+    s.C[2] = a.c13[i];
+    s.C[3] = a.c22[i];
+    s.C[4] = a.c23[i];
+    s.C[5] = a.c33[i];
+    return s;
+}
+
+// r = x_i - x_j with the legacy periodic fold at 2 h_i, d = |r|
+__device__ __forceinline__ void pairGeom(const AdjArgs& a, int64_t i, int64_t j, double r[3], double& d, double& rinv)
+{
+    const long long twoHBits = __double_as_longlong(2.0 * a.h[i]);
+    const double dd[3] = {a.x[i] - a.x[j], a.y[i] - a.y[j], a.z[i] - a.z[j]};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = a.box.pbc[k] ? CoordFp64::wrapLegacy(dd[k], twoHBits, a.box.L[k]) : dd[k];
+    const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    rinv = rsqrt(r2);
+    d = r2 * rinv;
+}
+
+__global__ void __launch_bounds__(kAdjBlock) meAdjOnceKernel(AdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double gA[3], gE;
+    const bool anyK = seedsOf(a, k, gA, gE);
+    double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
+    const stdad::MeSide S = stdSide(a, k);
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double gAj[3] = {0.0, 0.0, 0.0}, gEj = 0.0;
+        const bool anyJ = mutual && seedsOf(a, j, gAj, gEj);
+        if (!anyK && !anyJ) continue;
+        const stdad::MeSide J = stdSide(a, j);
+        double r[3], d, rinv;
+        pairGeom(a, k, j, r, d, rinv);
+        const double v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
+        double dwi, dwj;
+        const double wi = lookupSlope(a.wh, d * S.hInv, dwi), wj = lookupSlope(a.wh, d * J.hInv, dwj);
+        const double zero[3] = {0.0, 0.0, 0.0};
+        stdad::MeGrad o;
+        stdad::meStdAdjPair(r, d, rinv, v, S, J, wi, dwi, wj, dwj, anyK ? gA : zero, anyK ? gE : 0.0, gAj, gEj, o);
+        for (int t = 0; t < 3; ++t) {
+            bx[t] += o.r[t];
+            bv[t] += o.v[t];
+        }
+        bh += o.hI;
+        brho += o.rhoI;
+        bp += o.pI;
+        bc += o.c;
+        for (int t = 0; t < 6; ++t) bC[t] += o.CI[t];
+        atomicAdd(a.bx + j, -o.r[0]);
+        atomicAdd(a.by + j, -o.r[1]);
+        atomicAdd(a.bz + j, -o.r[2]);
+        atomicAdd(a.bvx + j, -o.v[0]);
+        atomicAdd(a.bvy + j, -o.v[1]);
+        atomicAdd(a.bvz + j, -o.v[2]);
+        atomicAdd(a.bh + j, o.hJ);
+        atomicAdd(a.bRho + j, o.rhoJ);
+        atomicAdd(a.bP + j, o.pJ);
+        atomicAdd(a.bC + j, o.c);
+        for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + j, o.CJ[t]);
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bvx + k, bv[0]);
+    atomicAdd(a.bvy + k, bv[1]);
+    atomicAdd(a.bvz + k, bv[2]);
+    atomicAdd(a.bh + k, bh);
+    atomicAdd(a.bRho + k, brho + (a.sRho ? a.sRho[k] : 0.0));
+    atomicAdd(a.bP + k, bp);
+    atomicAdd(a.bC + k, bc);
+    for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + k, bC[t]);
+}
+
+__device__ __forceinline__ void tauOf(const AdjArgs& a, int64_t i, double t[6])
+{
+#pragma unroll
+    for (int q = 0; q < 6; ++q) t[q] = a.tauBar[q * a.n + i];
+}
+
+__global__ void __launch_bounds__(kAdjBlock) iadAdjOnceKernel(AdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double bx[3] = {0, 0, 0}, bh = 0, brho = 0, tauK[6];
+    tauOf(a, k, tauK);
+    const double hInvK = a.hInv[k], volK = a.mOverRho[k], rhoInvK = a.rhoInv[k];
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double r[3], d, rinv, dw;
+        pairGeom(a, k, j, r, d, rinv);
+        double w = lookupSlope(a.wh, d * hInvK, dw);
+        double rb[3], hIb, rhoJb;
+        stdad::iadAdjTerm(r, d, rinv, hInvK, w, dw, a.mOverRho[j], a.rhoInv[j], tauK, rb, hIb, rhoJb);
+        bh += hIb;
+        if (mutual) {  // j's term of the same pair: r -> -r, roles swapped
+            double tauJ[6];
+            tauOf(a, j, tauJ);
+            const double hInvJ = a.hInv[j];
+            const double rm[3] = {-r[0], -r[1], -r[2]};
+            w = lookupSlope(a.wh, d * hInvJ, dw);
+            double pb[3], hJb, rhoKb;
+            stdad::iadAdjTerm(rm, d, rinv, hInvJ, w, dw, volK, rhoInvK, tauJ, pb, hJb, rhoKb);
+            for (int t = 0; t < 3; ++t) rb[t] -= pb[t];
+            brho += rhoKb;
+            atomicAdd(a.bh + j, hJb);
+        }
+        for (int t = 0; t < 3; ++t) bx[t] += rb[t];
+        atomicAdd(a.bx + j, -rb[0]);
+        atomicAdd(a.by + j, -rb[1]);
+        atomicAdd(a.bz + j, -rb[2]);
+        atomicAdd(a.bRho + j, rhoJb);
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bh + k, bh);
+    atomicAdd(a.bRho + k, brho);
+}
+
+__global__ void __launch_bounds__(kAdjBlock) densityAdjOnceKernel(AdjArgs a, OwnedView ov)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const double rhobK = a.bRho[k], hInvK = a.hInv[k], mK = a.m[k];
+    double bx[3] = {0, 0, 0}, bh = rhobK * (-3.0 * a.rho[k] * hInvK);
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        double r[3], d, rinv, dw;
+        pairGeom(a, k, j, r, d, rinv);
+        lookupSlope(a.wh, d * hInvK, dw);
+        double rb[3], hIb;
+        stdad::densityAdjTerm(r, d, rinv, hInvK, dw, a.m[j], a.K, rhobK, rb, hIb);
+        bh += hIb;
+        if (mutual) {
+            const double hInvJ = a.hInv[j];
+            const double rm[3] = {-r[0], -r[1], -r[2]};
+            lookupSlope(a.wh, d * hInvJ, dw);
+            double pb[3], hJb;
+            stdad::densityAdjTerm(rm, d, rinv, hInvJ, dw, mK, a.K, a.bRho[j], pb, hJb);
+            for (int t = 0; t < 3; ++t) rb[t] -= pb[t];
+            atomicAdd(a.bh + j, hJb);
+        }
+        for (int t = 0; t < 3; ++t) bx[t] += rb[t];
+        atomicAdd(a.bx + j, -rb[0]);
+        atomicAdd(a.by + j, -rb[1]);
+        atomicAdd(a.bz + j, -rb[2]);
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bh + k, bh);
+}
+
 __global__ void adjQuotientsKernel(AdjArgs a, double* q)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -718,6 +892,8 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     const unsigned blocks = gridFor(n, kAdjBlock);
     adjQuotientsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a, quot);
     SPHGB_TRY(launched(c, "adjQuotientsKernel"));
+    // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
+    const bool once = !deterministic && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
     if (deterministic) {
         meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "meAdjKernel"));
@@ -726,17 +902,20 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
         for (double* q : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h})
             SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
         SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(double) * 9 * n, c->stream));
-        meAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        if (once) meAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        else meAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "meAdjScatterKernel"));
     }
     iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "iadPrepKernel"));
     if (deterministic) iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else if (once) iadAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else iadAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "iadAdjKernel"));
     eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "eosAdjKernel"));
     if (deterministic) densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else if (once) densityAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
     else densityAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "densityAdjKernel"));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
