@@ -1,5 +1,5 @@
-"""The arithmetic of the hand-written VE adjoint (sphexa_gb300/csrc/adjoint_ve.cuh, the functions the
-device kernels call) against torch autograd on the CPU, without a GPU.
+"""The arithmetic of the hand-written adjoints (sphexa_gb300/csrc/adjoint_ve.cuh and adjoint_std.cuh,
+the functions the device kernels call) against torch autograd on the CPU, without a GPU.
 
 tests/adjoint_host/ve_adjoint_host.cpp runs the device pass sequence as sequential loops over the
 oracle's neighbour lists and forward state (the oracle port's VE sweep); the reference gradient is
@@ -31,20 +31,87 @@ class HostIn(C.Structure):
                 + [(k, P) for k in "sRho sAx sAy sAz sDu gx gy gz gvx gvy gvz gh gu".split()])
 
 
-@pytest.fixture(scope="module")
-def host_lib(tmp_path_factory):
+def _build(tmp_path_factory, name: str) -> C.CDLL:
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("g++ not available")
-    so = tmp_path_factory.mktemp("adjhost") / "libveadjhost.so"
+    so = tmp_path_factory.mktemp("adjhost") / f"lib{name}.so"
     cmd = [gxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", str(ROOT / "sphexa_gb300" / "csrc"),
-           str(ROOT / "tests" / "adjoint_host" / "ve_adjoint_host.cpp"), "-o", str(so)]
+           str(ROOT / "tests" / "adjoint_host" / f"{name}.cpp"), "-o", str(so)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    lib = C.CDLL(str(so))
+    return C.CDLL(str(so))
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    lib = _build(tmp_path_factory, "ve_adjoint_host")
     lib.ve_adj_host.argtypes = [C.POINTER(HostIn), C.c_int]
     lib.ve_adj_host.restype = C.c_int
     return lib
+
+
+class StdHostIn(C.Structure):
+    _fields_ = ([("n", C.c_int64)] + [(k, P) for k in "x y z vx vy vz h u m rho p c".split()]
+                + [("C", P * 6), ("off", P), ("idx", P), ("wh", P), ("ntab", C.c_int64), ("K", C.c_double),
+                   ("gamma", C.c_double), ("L", C.c_double * 3), ("pbc", C.c_int * 3)]
+                + [(k, P) for k in "sRho sAx sAy sAz sDu gx gy gz gvx gvy gvz gh gu".split()])
+
+
+def test_std_adjoint_arithmetic_matches_autograd(port, tmp_path_factory):
+    torch = pytest.importorskip("torch")
+    from sphexa_gb300 import workloads as W
+    from torch_reference import std_chain
+    lib = _build(tmp_path_factory, "std_adjoint_host")
+    lib.std_adj_host.argtypes = [C.POINTER(StdHostIn), C.c_int]
+    port.lib.oracle_kernel_K.restype = C.c_double
+    wl = W.fourier(10, seed=7, rho_seed=55, v_seed=555)
+    rng = np.random.Generator(np.random.PCG64(2))
+    wl.fields["u"] = wl.fields["u"] * rng.uniform(0.8, 1.2, wl.n)
+    wl.fields["h"] = wl.fields["h"] * rng.uniform(0.97, 1.03, wl.n)
+    ref = port.sweep(wl, "std", False)
+    n, ng, p = wl.n, wl.params["ngmax"], wl.params
+    nb = ref["nbr"].reshape(n, ng).astype(np.int64)
+    cnt = np.minimum(ref["nc"].astype(np.int64) - 1, ng)
+    off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    ej = np.concatenate([nb[k, :cnt[k]] for k in range(n)]).astype(np.int64)
+    ei = np.repeat(np.arange(n), cnt)
+    wh, _ = port.tables(6.0)
+    K = port.lib.oracle_kernel_K(6.0)
+    seeds = {k: rng.normal(size=n) for k in ("rho", "ax", "ay", "az", "du")}
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64)
+    names = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
+    inp = [t(ref[k]).requires_grad_(True) for k in names]
+    out = std_chain(*inp, t(ref["m"]), torch.tensor(ei), torch.tensor(ej), t(wh), K, p["gamma"],
+                    t(wl.box[1::2] - wl.box[0::2]), [True] * 3)
+    L = sum((o * t(seeds[k])).sum() for o, k in zip(out, ("rho", "ax", "ay", "az", "du")))
+    L.backward()
+    a = StdHostIn()
+    keep = []
+
+    def ptr(arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        keep.append(arr)
+        return arr.ctypes.data
+
+    a.n = n
+    for k in "x y z vx vy vz h u m rho p c".split():
+        setattr(a, k, ptr(ref[k]))
+    for q, k in enumerate(("c11", "c12", "c13", "c22", "c23", "c33")):
+        a.C[q] = ptr(ref[k])
+    a.off, a.idx, a.wh, a.ntab, a.K, a.gamma = off.ctypes.data, ej.ctypes.data, ptr(wh), len(wh), K, p["gamma"]
+    for k in range(3):
+        a.L[k] = wl.box[2 * k + 1] - wl.box[2 * k]
+        a.pbc[k] = 1
+    a.sRho, a.sAx, a.sAy, a.sAz, a.sDu = (ptr(seeds[k]) for k in ("rho", "ax", "ay", "az", "du"))
+    g = {k: np.zeros(n) for k in names}
+    a.gx, a.gy, a.gz, a.gvx, a.gvy, a.gvz, a.gh, a.gu = (g[k].ctypes.data for k in names)
+    for mode in (0, 1):
+        assert lib.std_adj_host(C.byref(a), mode) == 0
+        for k, ti in zip(names, inp):
+            gr = ti.grad.numpy()
+            err = np.linalg.norm(g[k] - gr) / np.linalg.norm(gr)
+            assert err <= 1e-12, f"mode {mode} {k}: {err:.3e}"
 
 
 @pytest.mark.parametrize("av_clean", [False, True])
