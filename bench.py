@@ -188,14 +188,17 @@ def cpu_baseline(side: int, threads: int = 0, workload: str = "sedov200_jit", va
                       f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
 
 
-def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str = "std") -> dict:
+def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str = "std",
+                   precision: str = "fp64"):
     """Forward chain on frozen lists against its adjoint for the loss sum (rho - rho_target)^2 +
-    sum |a|^2, FP64, CUDA events on the default stream.  chain "std": density, EOS, IAD,
-    momentum-energy; "ve": xmass, gradh, EOS, IAD + divv/curlv, AV switches, momentum-energy."""
+    sum |a|^2, CUDA events on the default stream.  chain "std": density, EOS, IAD, momentum-energy;
+    "ve": xmass, gradh, EOS, IAD + divv/curlv, AV switches, momentum-energy.  precision "mixed"
+    (std chain): the mixed forward and the FP32-arithmetic adjoint.  Returns the timing record
+    and the first backward's gradients (x y z vx vy vz h u, FP64 on the host)."""
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=5, rho_seed=55, v_seed=555, target_seed=5555)
-    d = sph.ParticlesData.from_workload(wl, "fp64", dev)
+    d = sph.ParticlesData.from_workload(wl, precision, dev)
     box = sph.Box(wl.box.copy(), wl.bc.copy())
     sw = AG.FrozenStdSweep(ctx, d, box) if chain == "std" else AG.FrozenVeSweep(ctx, d, box)
     sw.freeze()
@@ -217,9 +220,10 @@ def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str
     rho, ax, ay, az, du = outs
     seeds = (2.0 * (rho - rho_t), 2.0 * ax, 2.0 * ay, 2.0 * az, None)
     t0 = time.perf_counter()
-    sw.backward(*seeds)  # first call also builds the incoming (transposed) lists
+    grads = sw.backward(*seeds)  # first call also builds the incoming (transposed) lists
     torch.cuda.synchronize()
     first_ms = (time.perf_counter() - t0) * 1e3
+    grads = [g.to(torch.float64).cpu().numpy() for g in grads]
     for _ in range(max(1, warmup)):
         sw.forward(*vals)
         sw.backward(*seeds)
@@ -227,8 +231,8 @@ def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str
     fwd = timed(lambda: sw.forward(*vals), k)
     adj = timed(lambda: sw.backward(*seeds), k)
     return {"workload": f"adjoint config: jittered Fourier lattice {side}^3 = {wl.n} particles, frozen lists",
-            "form": f"fp64 {chain} chain", "forward_ms": fwd, "adjoint_ms": adj, "ratio": adj / fwd,
-            "first_adjoint_ms_incl_transpose": first_ms, "steps": k}
+            "form": f"{precision} {chain} chain", "forward_ms": fwd, "adjoint_ms": adj, "ratio": adj / fwd,
+            "first_adjoint_ms_incl_transpose": first_ms, "steps": k}, grads
 
 
 def run_reference(args) -> None:
@@ -480,8 +484,12 @@ def main() -> None:
 
     # ---------------- adjoint / forward on the adjoint configuration (1M particles, FP64 std chain)
     if not args.no_adjoint:
-        out["adjoint"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup)
-        out["adjoint"]["ve"] = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup, chain="ve")
+        out["adjoint"], g64 = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup)
+        out["adjoint"]["ve"], _ = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup, chain="ve")
+        mixed, g32 = adjoint_timing(ctx, dev, args.adjoint_side, args.steps, args.warmup, precision="mixed")
+        mixed["grad_error_vs_fp64"] = {f: float(np.linalg.norm(b - a) / np.linalg.norm(a))
+                                       for f, a, b in zip(("x", "y", "z", "vx", "vy", "vz", "h", "u"), g64, g32)}
+        out["adjoint"]["mixed"] = mixed
 
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.cpu_side, workload=args.workload, variant=args.variant)

@@ -198,7 +198,10 @@ int sphgb_sweep_passes(sphgb_ctx* ctx, sphgb_particles* p, int32_t variant, int3
 /* ---- adjoint ----
  * No reference counterpart (the reference has no gradients).  Reverse mode of the std chain
  * density -> EOS -> IAD -> momentum-energy, for the state left by the last forward passes on the
- * frozen neighbour lists of the last search (over all particles, first = 0, last = n), FP64 form.
+ * frozen neighbour lists of the last search (over all particles, first = 0, last = n), in the
+ * form of those passes: FP64, or mixed (FP32 pair arithmetic on the forward's grid-form coordinate
+ * differences, FP32 sums, FP64 gradients out; seeds rho, a in the field type; deterministic = 1 is
+ * refused for the mixed form).
  * Seeds are dL/d(output) per particle (device, double; NULL = zero); outputs are dL/d(input)
  * (device, double).  The Courant time step is not differentiated. */
 typedef struct {

@@ -21,8 +21,9 @@ class FrozenStdSweep:
     """Context + particle set whose SFC order, tree and neighbour lists are fixed at freeze()."""
 
     def __init__(self, ctx: sph.Context, d: sph.ParticlesData, box: sph.Box, deterministic: bool = False):
-        if d.precision != "fp64":
-            raise ValueError("the adjoint runs in the FP64 form")
+        # the std adjoint runs in both forms (mixed: FP32 pair arithmetic, scatter form only)
+        if d.precision not in ("fp64", "mixed") or (deterministic and d.precision != "fp64"):
+            raise ValueError("the std adjoint runs in the FP64 form, or in the mixed form without deterministic")
         self.ctx, self.d, self.box = ctx, d, box
         self.deterministic = deterministic
 
@@ -58,8 +59,8 @@ def _run_adjoint(sweep, g_rho, g_ax, g_ay, g_az, g_du, fn, args):
     seeds = _lib.SphgbSeeds()
     keep = []
     for name, g in (("rho", g_rho), ("ax", g_ax), ("ay", g_ay), ("az", g_az), ("du", g_du)):
-        if g is not None:
-            g = g.detach().to(torch.float64).contiguous()
+        if g is not None:  # seeds in the output field's type (du is FP64 in both forms)
+            g = g.detach().to(sweep.d.f[name].dtype).contiguous()
             keep.append(g)
             setattr(seeds, name, g.data_ptr())
     out = {k: torch.zeros(n, dtype=torch.float64, device=dev) for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u")}
@@ -68,7 +69,8 @@ def _run_adjoint(sweep, g_rho, g_ax, g_ay, g_az, g_du, fn, args):
         setattr(grads, k, t.data_ptr())
     s = sweep.d.c_struct()
     check(getattr(sweep.ctx.lib, fn)(sweep.ctx.h, *args(s, seeds, grads)), fn)
-    return tuple(out[k] for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u"))
+    # FP64 gradients, returned in each input's type (float for the mixed form's h and v)
+    return tuple(out[k].to(sweep.d.f[k].dtype) for k in ("x", "y", "z", "vx", "vy", "vz", "h", "u"))
 
 
 class FrozenVeSweep(FrozenStdSweep):
@@ -76,6 +78,8 @@ class FrozenVeSweep(FrozenStdSweep):
     every forward starts from the same alpha; av_clean selects momentumAndEnergy<avClean>."""
 
     def __init__(self, ctx, d, box, av_clean: bool = False, deterministic: bool = False):
+        if d.precision != "fp64":
+            raise ValueError("the VE adjoint runs in the FP64 form")
         super().__init__(ctx, d, box, deterministic)
         self.av_clean = av_clean
         self.alpha0 = None

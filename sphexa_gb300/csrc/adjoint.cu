@@ -233,56 +233,6 @@ __device__ __forceinline__ bool seedsOf(const AdjArgs& a, int64_t i, double gA[3
     return gA[0] != 0.0 || gA[1] != 0.0 || gA[2] != 0.0 || gE != 0.0;
 }
 
-// one evaluation per pair: i's partials summed in registers, j's scattered with atomics
-__global__ void __launch_bounds__(kAdjBlock) meAdjScatterKernel(AdjArgs a)
-{
-    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-    if (k >= a.n) return;
-    double gA[3], gE;
-    double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
-    if (seedsOf(a, k, gA, gE)) {
-        const Side S = loadSide(a, k);
-        const unsigned nc = a.lv.capped(k);
-        for (unsigned q = 0; q < nc; ++q) {
-            const int64_t j = a.lv.at(k, q);
-            const Side J = loadSide(a, j);
-            PairGrad g;
-            mePairAdj<true, true>(a.box, a.wh, S, J, gA, gE, g);
-            for (int t = 0; t < 3; ++t) {
-                bx[t] += g.r[t];
-                bv[t] += g.v[t];
-            }
-            bh += g.hI;
-            brho += g.rhoI;
-            bp += g.pI;
-            bc += g.c;
-            for (int t = 0; t < 6; ++t) bC[t] += g.CI[t];
-            atomicAdd(a.bx + j, -g.r[0]);
-            atomicAdd(a.by + j, -g.r[1]);
-            atomicAdd(a.bz + j, -g.r[2]);
-            atomicAdd(a.bvx + j, -g.v[0]);
-            atomicAdd(a.bvy + j, -g.v[1]);
-            atomicAdd(a.bvz + j, -g.v[2]);
-            atomicAdd(a.bh + j, g.hJ);
-            atomicAdd(a.bRho + j, g.rhoJ);
-            atomicAdd(a.bP + j, g.pJ);
-            atomicAdd(a.bC + j, g.c);
-            for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + j, g.CJ[t]);
-        }
-    }
-    atomicAdd(a.bx + k, bx[0]);
-    atomicAdd(a.by + k, bx[1]);
-    atomicAdd(a.bz + k, bx[2]);
-    atomicAdd(a.bvx + k, bv[0]);
-    atomicAdd(a.bvy + k, bv[1]);
-    atomicAdd(a.bvz + k, bv[2]);
-    atomicAdd(a.bh + k, bh);
-    atomicAdd(a.bRho + k, brho + (a.sRho ? a.sRho[k] : 0.0));
-    atomicAdd(a.bP + k, bp);
-    atomicAdd(a.bC + k, bc);
-    for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + k, bC[t]);
-}
-
 __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -491,35 +441,210 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
     a.bh[k] += bh;
 }
 
-// one evaluation per pair with atomic scatter to the neighbour (IAD)
-__global__ void __launch_bounds__(kAdjBlock) iadAdjScatterKernel(AdjArgs a)
+// ---- scatter form over the full lists, in the pair arithmetic of either precision ----
+// Every list entry is evaluated by its owner; the neighbour's partials go by FP64 atomics.  T is
+// the arithmetic of the pairs: double (FP64 form, with the context in deterministic mode) or float
+// (mixed form: FP64 coordinate differences rounded once, FP32 pair arithmetic, the table interval
+// of the mixed forward); every accumulation is FP64.
+template<class T>
+struct TabOf {
+    using type = double2;
+};
+template<>
+struct TabOf<float> {
+    using type = float2;
+};
+
+__device__ __forceinline__ double lookupSlopeT(const double2* __restrict__ tab, double v, double& slope)
+{
+    return lookupSlope(tab, v, slope);
+}
+
+// the mixed forward's FP32 interval (lookupX32): k = int(v / dx), value and slope of that interval
+__device__ __forceinline__ float lookupSlopeT(const float2* __restrict__ tab, float v, float& slope)
+{
+    constexpr int nInt = kTableSize - 1;
+    const float x = v * float(kTabInvDx);
+    const int k = int(x);
+    if (k >= nInt) {
+        slope = 0.f;
+        return 0.f;
+    }
+    const float2 t = __ldg(tab + k);
+    slope = t.y * float(kTabInvDx);
+    return fmaf(t.y, x - float(k), t.x);
+}
+
+template<class T>
+struct StdScatterArgs {
+    const double *x, *y, *z, *u;
+    const T *vx, *vy, *vz, *h, *m, *rho, *p, *c;
+    const T* C[6];
+    const typename TabOf<T>::type* wh;
+    double K, gamma;
+    DevBox box;
+    ListView lv;
+    int64_t n;
+    const T *sRho, *sAx, *sAy, *sAz;
+    const double* sDu;
+    // adjoints, accumulated in the pair type: the FP64 form writes the caller's gradients and FP64
+    // state, the mixed form FP32 arrays (converted to the FP64 gradients at the end)
+    T *bx, *by, *bz, *bvx, *bvy, *bvz, *bh, *bu;
+    T *bRho, *bP, *bC, *bCij, *tauBar;
+    T *hInv, *moR, *poR, *rhoInv, *poR2;  // per-particle quotients in the pair type
+    CoordMixed cm;                         // mixed form: the grid-form coordinates of the forward passes
+};
+
+template<class T>
+__global__ void stdQuotKernel(StdScatterArgs<T> a)
+{
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= a.n) return;
+    const double rho = double(a.rho[i]), p = double(a.p[i]);
+    a.hInv[i] = T(1.0 / double(a.h[i]));
+    a.moR[i] = T(double(a.m[i]) / rho);
+    a.poR[i] = T(p / rho);
+    a.rhoInv[i] = T(1.0 / rho);
+    a.poR2[i] = T(p / (rho * rho));
+}
+
+template<class T>
+__device__ __forceinline__ stdad::MeSide<T> stdSideT(const StdScatterArgs<T>& a, int64_t i)
+{
+    stdad::MeSide<T> s;
+    s.hInv = a.hInv[i];
+    s.c = a.c[i];
+    s.m = a.m[i];
+    s.rhoInv = a.rhoInv[i];
+    s.poR = a.poR[i];
+    s.poR2 = a.poR2[i];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) s.C[q] = a.C[q][i];
+    return s;
+}
+
+// r = x_i - x_j as the forward passes of that form take it: FP64 differences with the legacy fold
+// at 2 h_i, or (mixed) the FP32 grid form (integer cell difference times the cell edge plus the
+// in-cell offsets, the minimum image across periodic faces)
+template<class T>
+__device__ __forceinline__ void geomT(const StdScatterArgs<T>& a, int64_t i, int64_t j, T r[3], T& d, T& rinv)
+{
+    if constexpr (std::is_same_v<T, double>) {
+        const long long twoHBits = __double_as_longlong(2.0 * a.h[i]);
+        const double dd[3] = {a.x[i] - a.x[j], a.y[i] - a.y[j], a.z[i] - a.z[j]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r[k] = a.box.pbc[k] ? CoordFp64::wrapLegacy(dd[k], twoHBits, a.box.L[k]) : dd[k];
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        rinv = rsqrt(r2);
+        d = r2 * rinv;
+    } else {
+        float hjInv;
+        a.cm.diff(a.cm.target(i), j, r[0], r[1], r[2], hjInv);
+        const float r2 = fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2]));
+        rinv = rsqrtf(r2);
+        d = r2 * rinv;
+    }
+}
+
+template<class T>
+__global__ void __launch_bounds__(kAdjBlock) meAdjScatterT(StdScatterArgs<T> a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
-    const Side S = loadPos(a, k);
-    double bx[3] = {0, 0, 0}, bh = 0;
+    const T gA[3] = {a.sAx ? T(a.K * double(a.sAx[k])) : T(0), a.sAy ? T(a.K * double(a.sAy[k])) : T(0),
+                     a.sAz ? T(a.K * double(a.sAz[k])) : T(0)};
+    const T gE = a.sDu ? T(-0.5 * a.K * a.sDu[k]) : T(0);
+    T bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
+    if (gA[0] != T(0) || gA[1] != T(0) || gA[2] != T(0) || gE != T(0)) {
+        const stdad::MeSide<T> S = stdSideT(a, k);
+        const T zero[3] = {T(0), T(0), T(0)};
+        const unsigned nc = a.lv.capped(k);
+        for (unsigned q = 0; q < nc; ++q) {
+            const int64_t j = a.lv.at(k, q);
+            const stdad::MeSide<T> J = stdSideT(a, j);
+            T r[3], d, rinv;
+            geomT(a, k, j, r, d, rinv);
+            const T v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
+            T dwi, dwj;
+            const T wi = lookupSlopeT(a.wh, d * S.hInv, dwi), wj = lookupSlopeT(a.wh, d * J.hInv, dwj);
+            stdad::MeGrad<T> o;
+            stdad::meStdAdjPair<T>(r, d, rinv, v, S, J, wi, dwi, wj, dwj, gA, gE, zero, T(0), o);
+            for (int t = 0; t < 3; ++t) {
+                bx[t] += o.r[t];
+                bv[t] += o.v[t];
+            }
+            bh += o.hI;
+            brho += o.rhoI;
+            bp += o.pI;
+            bc += o.c;
+            for (int t = 0; t < 6; ++t) bC[t] += o.CI[t];
+            atomicAdd(a.bx + j, -o.r[0]);
+            atomicAdd(a.by + j, -o.r[1]);
+            atomicAdd(a.bz + j, -o.r[2]);
+            atomicAdd(a.bvx + j, -o.v[0]);
+            atomicAdd(a.bvy + j, -o.v[1]);
+            atomicAdd(a.bvz + j, -o.v[2]);
+            atomicAdd(a.bh + j, o.hJ);
+            atomicAdd(a.bRho + j, o.rhoJ);
+            atomicAdd(a.bP + j, o.pJ);
+            atomicAdd(a.bC + j, o.c);
+            for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + j, o.CJ[t]);
+        }
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bvx + k, bv[0]);
+    atomicAdd(a.bvy + k, bv[1]);
+    atomicAdd(a.bvz + k, bv[2]);
+    atomicAdd(a.bh + k, bh);
+    atomicAdd(a.bRho + k, brho + (a.sRho ? a.sRho[k] : T(0)));
+    atomicAdd(a.bP + k, bp);
+    atomicAdd(a.bC + k, bc);
+    for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + k, bC[t]);
+}
+
+template<class T>
+__global__ void iadPrepT(StdScatterArgs<T> a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    double C[6], Cb[6], tauB[6], hb = 0.0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        C[q] = double(a.C[q][k]);
+        Cb[q] = double(a.bCij[q * a.n + k]);
+    }
+    stdad::iadSeed(a.K, double(a.h[k]), C, Cb, tauB, hb);
+    a.bh[k] += T(hb);
+#pragma unroll
+    for (int q = 0; q < 6; ++q) a.tauBar[q * a.n + k] = T(tauB[q]);
+}
+
+template<class T>
+__global__ void __launch_bounds__(kAdjBlock) iadAdjScatterT(StdScatterArgs<T> a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    T tauB[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) tauB[q] = a.tauBar[q * a.n + k];
+    const T hInv = a.hInv[k];
+    T bx[3] = {0, 0, 0}, bh = 0;
     const unsigned nc = a.lv.capped(k);
     for (unsigned q = 0; q < nc; ++q) {
         const int64_t j = a.lv.at(k, q);
-        const Side J = loadPos(a, j);
-        double r[3], Tr[3];
-        pairR(a.box, S, J, r);
-        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-        const double rinv = rsqrt(r2), d = r2 * rinv;
-        double dw;
-        const double w = lookupSlope(a.wh, d * S.hInv, dw);
-        const double Q = quadTau(a, k, r, Tr);
-        const double V = J.moR;
-        double rb[3];
-        for (int t = 0; t < 3; ++t) {
-            rb[t] = V * (2.0 * w * Tr[t] + Q * dw * S.hInv * r[t] * rinv);
-            bx[t] += rb[t];
-        }
-        bh += -V * Q * dw * d * S.hInv * S.hInv;
+        T r[3], d, rinv, dw;
+        geomT(a, k, j, r, d, rinv);
+        const T w = lookupSlopeT(a.wh, d * hInv, dw);
+        T rb[3], hIb, rhoJb;
+        stdad::iadAdjTerm<T>(r, d, rinv, hInv, w, dw, a.moR[j], a.rhoInv[j], tauB, rb, hIb, rhoJb);
+        for (int t = 0; t < 3; ++t) bx[t] += rb[t];
+        bh += hIb;
         atomicAdd(a.bx + j, -rb[0]);
         atomicAdd(a.by + j, -rb[1]);
         atomicAdd(a.bz + j, -rb[2]);
-        atomicAdd(a.bRho + j, -(V * J.rInv) * w * Q);
+        atomicAdd(a.bRho + j, rhoJb);
     }
     atomicAdd(a.bx + k, bx[0]);
     atomicAdd(a.by + k, bx[1]);
@@ -527,35 +652,51 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjScatterKernel(AdjArgs a)
     atomicAdd(a.bh + k, bh);
 }
 
-// one evaluation per pair with atomic scatter to the neighbour (density)
-__global__ void __launch_bounds__(kAdjBlock) densityAdjScatterKernel(AdjArgs a)
+// p = (gamma-1) rho u, c = sqrt(gamma (gamma-1) u)
+template<class T>
+__global__ void eosAdjT(StdScatterArgs<T> a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
-    const Side S = loadPos(a, k);
-    double bx[3] = {0, 0, 0};
-    const double brk = a.bRho[k];
-    const double hi3 = S.hInv * S.hInv * S.hInv;
-    double bh = brk * (-3.0 * a.rho[k] * S.hInv);
+    const double g1 = a.gamma - 1.0;
+    const double u = a.u[k], rho = double(a.rho[k]), c = double(a.c[k]), bp = double(a.bP[k]);
+    a.bRho[k] += T(bp * g1 * u);
+    a.bu[k] = T(bp * g1 * rho + (c > 0.0 ? double(a.bC[k]) * a.gamma * g1 / (2.0 * c) : 0.0));
+}
+
+// the mixed form's FP32 gradients to the caller's FP64 arrays
+__global__ void gradsToDouble(int64_t n, const float* __restrict__ src, double* x, double* y, double* z, double* vx,
+                              double* vy, double* vz, double* h, double* u)
+{
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    double* dst[8] = {x, y, z, vx, vy, vz, h, u};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dst[k][i] = double(src[k * n + i]);
+}
+
+template<class T>
+__global__ void __launch_bounds__(kAdjBlock) densityAdjScatterT(StdScatterArgs<T> a)
+{
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    const T rhob = a.bRho[k];
+    const T hInv = a.hInv[k];
+    T bx[3] = {0, 0, 0}, bh = rhob * (T(-3) * a.rho[k] * hInv);
     const unsigned nc = a.lv.capped(k);
-    double sdw = 0.0;
     for (unsigned q = 0; q < nc; ++q) {
         const int64_t j = a.lv.at(k, q);
-        double r[3];
-        const Side J = loadPos(a, j);
-        pairR(a.box, S, J, r);
-        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-        const double rinv = rsqrt(r2), d = r2 * rinv;
-        double dw;
-        lookupSlope(a.wh, d * S.hInv, dw);
-        const double f = brk * a.K * hi3 * J.m * dw * S.hInv * rinv;
-        for (int t = 0; t < 3; ++t) bx[t] += f * r[t];
-        sdw += J.m * dw * d;
-        atomicAdd(a.bx + j, -f * r[0]);
-        atomicAdd(a.by + j, -f * r[1]);
-        atomicAdd(a.bz + j, -f * r[2]);
+        T r[3], d, rinv, dw;
+        geomT(a, k, j, r, d, rinv);
+        lookupSlopeT(a.wh, d * hInv, dw);
+        T rb[3], hIb;
+        stdad::densityAdjTerm<T>(r, d, rinv, hInv, dw, a.m[j], T(a.K), rhob, rb, hIb);
+        for (int t = 0; t < 3; ++t) bx[t] += rb[t];
+        bh += hIb;
+        atomicAdd(a.bx + j, -rb[0]);
+        atomicAdd(a.by + j, -rb[1]);
+        atomicAdd(a.bz + j, -rb[2]);
     }
-    bh += brk * a.K * hi3 * sdw * (-S.hInv * S.hInv);
     atomicAdd(a.bx + k, bx[0]);
     atomicAdd(a.by + k, bx[1]);
     atomicAdd(a.bz + k, bx[2]);
@@ -563,9 +704,9 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjScatterKernel(AdjArgs a)
 }
 
 // ---- one evaluation per owned entry of the owned lists (mutual pairs give both directed terms) ----
-__device__ __forceinline__ stdad::MeSide stdSide(const AdjArgs& a, int64_t i)
+__device__ __forceinline__ stdad::MeSide<> stdSide(const AdjArgs& a, int64_t i)
 {
-    stdad::MeSide s;
+    stdad::MeSide<> s;
     s.hInv = a.hInv[i];
     s.c = a.c[i];
     s.m = a.m[i];
@@ -600,7 +741,7 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjOnceKernel(AdjArgs a, OwnedVie
     double gA[3], gE;
     const bool anyK = seedsOf(a, k, gA, gE);
     double bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
-    const stdad::MeSide S = stdSide(a, k);
+    const stdad::MeSide<> S = stdSide(a, k);
     const unsigned cnt = ov.size(k);
     for (unsigned q = 0; q < cnt; ++q) {
         bool mutual;
@@ -608,14 +749,14 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjOnceKernel(AdjArgs a, OwnedVie
         double gAj[3] = {0.0, 0.0, 0.0}, gEj = 0.0;
         const bool anyJ = mutual && seedsOf(a, j, gAj, gEj);
         if (!anyK && !anyJ) continue;
-        const stdad::MeSide J = stdSide(a, j);
+        const stdad::MeSide<> J = stdSide(a, j);
         double r[3], d, rinv;
         pairGeom(a, k, j, r, d, rinv);
         const double v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
         double dwi, dwj;
         const double wi = lookupSlope(a.wh, d * S.hInv, dwi), wj = lookupSlope(a.wh, d * J.hInv, dwj);
         const double zero[3] = {0.0, 0.0, 0.0};
-        stdad::MeGrad o;
+        stdad::MeGrad<> o;
         stdad::meStdAdjPair(r, d, rinv, v, S, J, wi, dwi, wj, dwj, anyK ? gA : zero, anyK ? gE : 0.0, gAj, gEj, o);
         for (int t = 0; t < 3; ++t) {
             bx[t] += o.r[t];
@@ -821,15 +962,119 @@ int buildTranspose(sphgb_ctx* c)
     return SPHGB_OK;
 }
 
+// the scatter form in the pair arithmetic T (FP64 form in deterministic context mode, or mixed form)
+template<class T>
+static int adjointStdScatter(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g)
+{
+    const int64_t n = p->n;
+    constexpr bool fp32 = std::is_same_v<T, float>;
+    // state in T: rho, p, c adjoints, C adjoint (6), tau adjoint (6), quotients (5), and for the
+    // mixed form the 8 gradients before their conversion to FP64
+    SPHGB_TRY(c->adjState.ensure(sizeof(T) * (fp32 ? 28 : 20) * n));
+    T* st = c->adjState.as<T>();
+    StdScatterArgs<T> a{};
+    auto f = [](const void* q) { return static_cast<const T*>(q); };
+    a.x = p->x;
+    a.y = p->y;
+    a.z = p->z;
+    a.u = p->u;
+    a.vx = f(p->vx);
+    a.vy = f(p->vy);
+    a.vz = f(p->vz);
+    a.h = f(p->h);
+    a.m = f(p->m);
+    a.rho = f(p->rho);
+    a.p = f(p->p);
+    a.c = f(p->c);
+    const void* Cs[6] = {p->c11, p->c12, p->c13, p->c22, p->c23, p->c33};
+    for (int q = 0; q < 6; ++q) a.C[q] = f(Cs[q]);
+    if constexpr (std::is_same_v<T, double>) a.wh = c->whx64.as<double2>();
+    else a.wh = c->whx32.as<float2>();
+    a.K = c->K;
+    a.gamma = c->prm.gamma;
+    a.box = c->box;
+    a.lv = listView(c);
+    a.n = n;
+    if constexpr (fp32) a.cm = coordMixed(c);
+    if (s) {
+        a.sRho = f(s->rho);
+        a.sAx = f(s->ax);
+        a.sAy = f(s->ay);
+        a.sAz = f(s->az);
+        a.sDu = s->du;
+    }
+    a.bRho = st;
+    a.bP = st + n;
+    a.bC = st + 2 * n;
+    a.bCij = st + 3 * n;
+    a.tauBar = st + 9 * n;
+    T* quot = st + 15 * n;
+    a.hInv = quot;
+    a.moR = quot + n;
+    a.poR = quot + 2 * n;
+    a.rhoInv = quot + 3 * n;
+    a.poR2 = quot + 4 * n;
+    if constexpr (fp32) {
+        T* gr = st + 20 * n;
+        a.bx = gr;
+        a.by = gr + n;
+        a.bz = gr + 2 * n;
+        a.bvx = gr + 3 * n;
+        a.bvy = gr + 4 * n;
+        a.bvz = gr + 5 * n;
+        a.bh = gr + 6 * n;
+        a.bu = gr + 7 * n;
+        SPHGB_CUDA(cudaMemsetAsync(gr, 0, sizeof(T) * 8 * n, c->stream));
+    } else {
+        a.bx = g->x;
+        a.by = g->y;
+        a.bz = g->z;
+        a.bvx = g->vx;
+        a.bvy = g->vy;
+        a.bvz = g->vz;
+        a.bh = g->h;
+        a.bu = g->u;
+        for (double* q : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h})
+            SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
+    }
+    SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(T) * 9 * n, c->stream));
+    const unsigned blocks = gridFor(n, kAdjBlock), eb = gridFor(n, 256);
+    stdQuotKernel<T><<<eb, 256, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "stdQuotKernel"));
+    meAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "meAdjScatterT"));
+    iadPrepT<T><<<eb, 256, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "iadPrepT"));
+    iadAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "iadAdjScatterT"));
+    eosAdjT<T><<<eb, 256, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "eosAdjT"));
+    densityAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    SPHGB_TRY(launched(c, "densityAdjScatterT"));
+    if constexpr (fp32) {
+        gradsToDouble<<<eb, 256, 0, c->stream>>>(n, st + 20 * n, g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h, g->u);
+        SPHGB_TRY(launched(c, "gradsToDouble"));
+    }
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHGB_OK;
+}
+
 int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic)
 {
     if (!c->haveNbr) return SPHGB_ERR_STATE;
-    if (p->precision != SPHGB_FP64) return SPHGB_ERR_ARG;
+    if (p->precision != SPHGB_FP64 && p->precision != SPHGB_MIXED) return SPHGB_ERR_ARG;
     if (c->nbrFirst != 0 || c->nbrLast != p->n) return SPHGB_ERR_ARG;
     if (!p->x || !p->y || !p->z || !p->vx || !p->vy || !p->vz || !p->h || !p->m || !p->u || !p->rho || !p->p ||
         !p->c || !p->c11 || !p->c12 || !p->c13 || !p->c22 || !p->c23 || !p->c33)
         return SPHGB_ERR_ARG;
     if (!g || !g->x || !g->y || !g->z || !g->vx || !g->vy || !g->vz || !g->h || !g->u) return SPHGB_ERR_ARG;
+    if (p->precision == SPHGB_MIXED) {  // FP32 pair arithmetic, FP64 sums; scatter form only
+        if (deterministic) return SPHGB_ERR_ARG;
+        return adjointStdScatter<float>(c, p, s, g);
+    }
+    // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
+    const bool once = !deterministic && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
+    if (!deterministic && !once) return adjointStdScatter<double>(c, p, s, g);
     const int64_t n = p->n;
     if (deterministic) SPHGB_TRY(buildTranspose(c));
     SPHGB_TRY(c->adjState.ensure(sizeof(double) * 20 * n));
@@ -892,8 +1137,6 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     const unsigned blocks = gridFor(n, kAdjBlock);
     adjQuotientsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a, quot);
     SPHGB_TRY(launched(c, "adjQuotientsKernel"));
-    // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
-    const bool once = !deterministic && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
     if (deterministic) {
         meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "meAdjKernel"));
@@ -902,21 +1145,18 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
         for (double* q : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h})
             SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
         SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(double) * 9 * n, c->stream));
-        if (once) meAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-        else meAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "meAdjScatterKernel"));
+        meAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        SPHGB_TRY(launched(c, "meAdjOnceKernel"));
     }
     iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "iadPrepKernel"));
     if (deterministic) iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    else if (once) iadAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else iadAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else iadAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
     SPHGB_TRY(launched(c, "iadAdjKernel"));
     eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "eosAdjKernel"));
     if (deterministic) densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    else if (once) densityAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else densityAdjScatterKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
+    else densityAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
     SPHGB_TRY(launched(c, "densityAdjKernel"));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;

@@ -1,7 +1,9 @@
 // Reverse-mode arithmetic of the standard SPH chain density -> EOS -> IAD -> momentum-energy, one
-// pair or one particle at a time, FP64: pure functions shared by the device kernels (adjoint.cu)
-// and host-side checks.  Conventions as in adjoint_ve.cuh: pair (i, j) of i's list, r = x_i - x_j
-// (legacy fold at 2 h_i), d = |r|, v = v_i - v_j, w / dw the table interpolant and its slope.
+// pair or one particle at a time: pure functions shared by the device kernels (adjoint.cu) and
+// host-side checks.  The pair functions take the arithmetic type T: double for the FP64 form, float
+// for the mixed form (the caller accumulates their results in FP64).  Conventions as in
+// adjoint_ve.cuh: pair (i, j) of i's list, r = x_i - x_j (legacy fold at 2 h_i), d = |r|,
+// v = v_i - v_j, w / dw the table interpolant and its slope.
 //
 // Forward formulas (reference j-loops):
 //   rho_i = K h_i^-3 (m_i + sum_j m_j w(d / h_i))                       hydro_std/density.hpp:41-60
@@ -18,19 +20,44 @@
 namespace sphgb {
 namespace stdad {
 
-using vead::dWdh;
-using vead::symv;
-using vead::symvAdj;
+template<class T>
+VEAD_HD void symv(const T C[6], const T r[3], T o[3])
+{
+    o[0] = C[0] * r[0] + C[1] * r[1] + C[2] * r[2];
+    o[1] = C[1] * r[0] + C[3] * r[1] + C[4] * r[2];
+    o[2] = C[2] * r[0] + C[4] * r[1] + C[5] * r[2];
+}
 
+// Cb += s * d(a . C r) / dC
+template<class T>
+VEAD_HD void symvAdj(const T a[3], const T r[3], T s, T Cb[6])
+{
+    Cb[0] += s * (a[0] * r[0]);
+    Cb[1] += s * (a[0] * r[1] + a[1] * r[0]);
+    Cb[2] += s * (a[0] * r[2] + a[2] * r[0]);
+    Cb[3] += s * (a[1] * r[1]);
+    Cb[4] += s * (a[1] * r[2] + a[2] * r[1]);
+    Cb[5] += s * (a[2] * r[2]);
+}
+
+// d(h^-3 w(d/h))/dh with v = d/h
+template<class T>
+VEAD_HD T dWdh(T hInv, T w, T dw, T v)
+{
+    return -hInv * hInv * hInv * hInv * (T(3) * w + v * dw);
+}
+
+template<class T = double>
 struct MeSide {
-    double hInv, c, m, rhoInv, poR, poR2;  // poR = p / rho, poR2 = p / rho^2
-    double C[6];
+    T hInv, c, m, rhoInv, poR, poR2;  // poR = p / rho, poR2 = p / rho^2
+    T C[6];
 };
 
+template<class T = double>
 struct MeGrad {
-    double r[3], v[3], c;         // r: x_i += , x_j -= ; v: v_i += , v_j -= ; c: both ends
-    double hI, rhoI, pI, CI[6];   // i's fields
-    double hJ, rhoJ, pJ, CJ[6];   // j's fields
+    T r[3], v[3], c;         // r: x_i += , x_j -= ; v: v_i += , v_j -= ; c: both ends
+    T hI, rhoI, pI, CI[6];   // i's fields
+    T hJ, rhoJ, pJ, CJ[6];   // j's fields
 };
 
 // Both momentum-energy terms of one pair: i's term with seeds gAi = K abar_i, gEi = -K/2 dubar_i,
@@ -39,30 +66,30 @@ struct MeGrad {
 //   Ui = alpha gAi - beta2 gAj + (gEi alpha' + gEj beta2') v,  Uj = beta gAi - alpha2 gAj + (gEi beta' + gEj alpha2') v
 // (alpha2 = W_j (q_j + visc t_j), beta2 = s_i W_i (u_i + visc), alpha2' = W_j (2 q_j + visc t_j),
 //  beta2' = visc s_i W_i are j's coefficients).  Zero j seeds give i's term alone.
-VEAD_HD void meStdAdjPair(const double r[3], double d, double rinv, const double v[3], const MeSide& I,
-                          const MeSide& J, double wi, double dwi, double wj, double dwj, const double gAi[3],
-                          double gEi, const double gAj[3], double gEj, MeGrad& o)
+template<class T>
+VEAD_HD void meStdAdjPair(const T r[3], T d, T rinv, const T v[3], const MeSide<T>& I, const MeSide<T>& J, T wi, T dwi,
+                          T wj, T dwj, const T gAi[3], T gEi, const T gAj[3], T gEj, MeGrad<T>& o)
 {
-    const double v1 = d * I.hInv, v2 = d * J.hInv;
-    const double hi3 = I.hInv * I.hInv * I.hInv, hj3 = J.hInv * J.hInv * J.hInv;
-    const double Wi = hi3 * wi, Wj = hj3 * wj;
-    double Ai[3], Aj[3];
-    symv(I.C, r, Ai);
-    symv(J.C, r, Aj);
-    const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
-    const double W = rv * rinv;
-    const double cs = I.c + J.c;
-    const bool approaching = W < 0.0;
-    const double visc = approaching ? 0.5 * (-(0.5 * cs - 2.0 * W) * W) : 0.0;
-    const double qi = J.m * I.poR2, si = I.m * I.rhoInv, tj = J.m * J.rhoInv, uj = J.poR;
-    const double qj = I.m * J.poR2, ui = I.poR;
-    const double alpha = Wi * (qi + visc * si), beta = tj * Wj * (uj + visc);
-    const double alphaP = Wi * (2.0 * qi + visc * si), betaP = visc * tj * Wj;
-    const double alpha2 = Wj * (qj + visc * tj), beta2 = si * Wi * (ui + visc);
-    const double alphaP2 = Wj * (2.0 * qj + visc * tj), betaP2 = visc * si * Wi;
+    const T v1 = d * I.hInv, v2 = d * J.hInv;
+    const T hi3 = I.hInv * I.hInv * I.hInv, hj3 = J.hInv * J.hInv * J.hInv;
+    const T Wi = hi3 * wi, Wj = hj3 * wj;
+    T Ai[3], Aj[3];
+    symv<T>(I.C, r, Ai);
+    symv<T>(J.C, r, Aj);
+    const T rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    const T W = rv * rinv;
+    const T cs = I.c + J.c;
+    const bool approaching = W < T(0);
+    const T visc = approaching ? T(0.5) * (-(T(0.5) * cs - T(2) * W) * W) : T(0);
+    const T qi = J.m * I.poR2, si = I.m * I.rhoInv, tj = J.m * J.rhoInv, uj = J.poR;
+    const T qj = I.m * J.poR2, ui = I.poR;
+    const T alpha = Wi * (qi + visc * si), beta = tj * Wj * (uj + visc);
+    const T alphaP = Wi * (T(2) * qi + visc * si), betaP = visc * tj * Wj;
+    const T alpha2 = Wj * (qj + visc * tj), beta2 = si * Wi * (ui + visc);
+    const T alphaP2 = Wj * (T(2) * qj + visc * tj), betaP2 = visc * si * Wi;
 
-    double Ui[3], Uj[3];
-    double aI = 0, bI = 0, aJ = 0, bJ = 0, vAi = 0, vAj = 0;
+    T Ui[3], Uj[3];
+    T aI = 0, bI = 0, aJ = 0, bJ = 0, vAi = 0, vAj = 0;
     for (int k = 0; k < 3; ++k) {
         Ui[k] = alpha * gAi[k] - beta2 * gAj[k] + (gEi * alphaP + gEj * betaP2) * v[k];
         Uj[k] = beta * gAi[k] - alpha2 * gAj[k] + (gEi * betaP + gEj * alphaP2) * v[k];
@@ -74,47 +101,47 @@ VEAD_HD void meStdAdjPair(const double r[3], double d, double rinv, const double
         vAj += v[k] * Aj[k];
     }
     // adjoints of the scalar coefficients
-    const double bAlpha = aI, bBeta = bI, bAlpha2 = -aJ, bBeta2 = -bJ;
-    const double bAlphaP = gEi * vAi, bBetaP = gEi * vAj, bAlphaP2 = gEj * vAj, bBetaP2 = gEj * vAi;
-    const double bWi = bAlpha * (qi + visc * si) + bAlphaP * (2.0 * qi + visc * si) + bBeta2 * si * (ui + visc) +
-                       bBetaP2 * visc * si;
-    const double bWj = bBeta * tj * (uj + visc) + bBetaP * visc * tj + bAlpha2 * (qj + visc * tj) +
-                       bAlphaP2 * (2.0 * qj + visc * tj);
-    const double bqi = (bAlpha + 2.0 * bAlphaP) * Wi, bqj = (bAlpha2 + 2.0 * bAlphaP2) * Wj;
-    const double bsi = (bAlpha + bAlphaP) * Wi * visc + bBeta2 * Wi * (ui + visc) + bBetaP2 * visc * Wi;
-    const double btj = bBeta * Wj * (uj + visc) + bBetaP * visc * Wj + (bAlpha2 + bAlphaP2) * Wj * visc;
-    const double buj = bBeta * tj * Wj, bui = bBeta2 * si * Wi;
-    const double bVisc = (bAlpha + bAlphaP) * Wi * si + (bBeta + bBetaP) * tj * Wj + (bAlpha2 + bAlphaP2) * Wj * tj +
-                         (bBeta2 + bBetaP2) * si * Wi;
+    const T bAlpha = aI, bBeta = bI, bAlpha2 = -aJ, bBeta2 = -bJ;
+    const T bAlphaP = gEi * vAi, bBetaP = gEi * vAj, bAlphaP2 = gEj * vAj, bBetaP2 = gEj * vAi;
+    const T bWi = bAlpha * (qi + visc * si) + bAlphaP * (T(2) * qi + visc * si) + bBeta2 * si * (ui + visc) +
+                  bBetaP2 * visc * si;
+    const T bWj = bBeta * tj * (uj + visc) + bBetaP * visc * tj + bAlpha2 * (qj + visc * tj) +
+                  bAlphaP2 * (T(2) * qj + visc * tj);
+    const T bqi = (bAlpha + T(2) * bAlphaP) * Wi, bqj = (bAlpha2 + T(2) * bAlphaP2) * Wj;
+    const T bsi = (bAlpha + bAlphaP) * Wi * visc + bBeta2 * Wi * (ui + visc) + bBetaP2 * visc * Wi;
+    const T btj = bBeta * Wj * (uj + visc) + bBetaP * visc * Wj + (bAlpha2 + bAlphaP2) * Wj * visc;
+    const T buj = bBeta * tj * Wj, bui = bBeta2 * si * Wi;
+    const T bVisc = (bAlpha + bAlphaP) * Wi * si + (bBeta + bBetaP) * tj * Wj + (bAlpha2 + bAlphaP2) * Wj * tj +
+                    (bBeta2 + bBetaP2) * si * Wi;
 
     // particle fields
     o.pI = bqi * J.m * I.rhoInv * I.rhoInv + bui * I.rhoInv;
-    o.rhoI = (bqi * (-2.0 * qi) + bsi * (-si) + bui * (-ui)) * I.rhoInv;
+    o.rhoI = (bqi * (T(-2) * qi) + bsi * (-si) + bui * (-ui)) * I.rhoInv;
     o.pJ = buj * J.rhoInv + bqj * I.m * J.rhoInv * J.rhoInv;
-    o.rhoJ = (btj * (-tj) + buj * (-uj) + bqj * (-2.0 * qj)) * J.rhoInv;
+    o.rhoJ = (btj * (-tj) + buj * (-uj) + bqj * (T(-2) * qj)) * J.rhoInv;
     // viscosity
-    double bW = 0.0;
-    o.c = 0.0;
+    T bW = 0;
+    o.c = 0;
     if (approaching) {
-        bW = bVisc * (-0.25 * cs + 2.0 * W);
-        o.c = bVisc * (-0.25 * W);
+        bW = bVisc * (T(-0.25) * cs + T(2) * W);
+        o.c = bVisc * (T(-0.25) * W);
     }
-    const double brv = bW * rinv;
-    double db = -bW * W * rinv;
+    const T brv = bW * rinv;
+    T db = -bW * W * rinv;
     for (int k = 0; k < 3; ++k) {
         o.r[k] = brv * v[k];
         o.v[k] = brv * r[k] + gEi * (alphaP * Ai[k] + betaP * Aj[k]) + gEj * (alphaP2 * Aj[k] + betaP2 * Ai[k]);
     }
     // A = C r
-    for (int q = 0; q < 6; ++q) o.CI[q] = o.CJ[q] = 0.0;
-    symvAdj(Ui, r, 1.0, o.CI);
-    symvAdj(Uj, r, 1.0, o.CJ);
-    double CUi[3], CUj[3];
-    symv(I.C, Ui, CUi);
-    symv(J.C, Uj, CUj);
+    for (int q = 0; q < 6; ++q) o.CI[q] = o.CJ[q] = 0;
+    symvAdj<T>(Ui, r, T(1), o.CI);
+    symvAdj<T>(Uj, r, T(1), o.CJ);
+    T CUi[3], CUj[3];
+    symv<T>(I.C, Ui, CUi);
+    symv<T>(J.C, Uj, CUj);
     // W = h^-3 w(d / h)
-    o.hI = bWi * dWdh(I.hInv, wi, dwi, v1);
-    o.hJ = bWj * dWdh(J.hInv, wj, dwj, v2);
+    o.hI = bWi * dWdh<T>(I.hInv, wi, dwi, v1);
+    o.hJ = bWj * dWdh<T>(J.hInv, wj, dwj, v2);
     db += bWi * hi3 * dwi * I.hInv + bWj * hj3 * dwj * J.hInv;
     for (int k = 0; k < 3; ++k) o.r[k] += CUi[k] + CUj[k] + db * r[k] * rinv;
 }
@@ -150,24 +177,25 @@ VEAD_HD void iadSeed(double K, double h, const double C[6], const double Cb[6], 
 }
 
 // i's IAD term V_j w(d / h_i) r r^T (V_j = m_j / rho_j) with i's tau adjoint: partials of r, h_i, rho_j
-VEAD_HD void iadAdjTerm(const double r[3], double d, double rinv, double hiInv, double wi, double dwi, double Vj,
-                        double rhoInvJ, const double tauB[6], double rb[3], double& hIb, double& rhoJb)
+template<class T>
+VEAD_HD void iadAdjTerm(const T r[3], T d, T rinv, T hiInv, T wi, T dwi, T Vj, T rhoInvJ, const T tauB[6], T rb[3],
+                        T& hIb, T& rhoJb)
 {
-    double Tr[3];
-    symv(tauB, r, Tr);
-    const double Q = r[0] * Tr[0] + r[1] * Tr[1] + r[2] * Tr[2];
-    for (int k = 0; k < 3; ++k) rb[k] = Vj * (2.0 * wi * Tr[k] + Q * dwi * hiInv * r[k] * rinv);
+    T Tr[3];
+    symv<T>(tauB, r, Tr);
+    const T Q = r[0] * Tr[0] + r[1] * Tr[1] + r[2] * Tr[2];
+    for (int k = 0; k < 3; ++k) rb[k] = Vj * (T(2) * wi * Tr[k] + Q * dwi * hiInv * r[k] * rinv);
     hIb = -Vj * Q * dwi * d * hiInv * hiInv;
     rhoJb = -(Vj * rhoInvJ) * wi * Q;
 }
 
 // i's density term K h_i^-3 m_j w(d / h_i) with rhob_i: partials of r and h_i (the pair part; the
 // factor h_i^-3 enters per particle)
-VEAD_HD void densityAdjTerm(const double r[3], double d, double rinv, double hiInv, double dwi, double mj, double K,
-                            double rhob, double rb[3], double& hIb)
+template<class T>
+VEAD_HD void densityAdjTerm(const T r[3], T d, T rinv, T hiInv, T dwi, T mj, T K, T rhob, T rb[3], T& hIb)
 {
-    const double hi3 = hiInv * hiInv * hiInv;
-    const double f = rhob * K * hi3 * mj * dwi * hiInv * rinv;
+    const T hi3 = hiInv * hiInv * hiInv;
+    const T f = rhob * K * hi3 * mj * dwi * hiInv * rinv;
     for (int k = 0; k < 3; ++k) rb[k] = f * r[k];
     hIb = -rhob * K * hi3 * mj * dwi * d * hiInv * hiInv;
 }

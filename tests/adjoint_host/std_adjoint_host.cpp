@@ -45,7 +45,7 @@ extern "C" int std_adj_host(const In* ap, int mutualMode)
     const In& a = *ap;
     int64_t n = a.n;
     auto side = [&](int64_t i) {
-        MeSide s;
+        MeSide<> s;
         s.hInv = 1.0 / a.h[i]; s.c = a.c[i]; s.m = a.m[i]; s.rhoInv = 1.0 / a.rho[i];
         s.poR = a.p[i] / a.rho[i]; s.poR2 = a.p[i] / (a.rho[i] * a.rho[i]);
         for (int q = 0; q < 6; ++q) s.C[q] = a.C[q][i];
@@ -59,7 +59,7 @@ extern "C" int std_adj_host(const In* ap, int mutualMode)
     };
     for (int64_t i = 0; i < n; ++i) {
         rhoB[i] += a.sRho[i];
-        MeSide I = side(i);
+        MeSide<> I = side(i);
         double gAi[3], gEi;
         seeds(i, gAi, gEi);
         for (int64_t q = a.off[i]; q < a.off[i + 1]; ++q) {
@@ -73,10 +73,10 @@ extern "C" int std_adj_host(const In* ap, int mutualMode)
             double r[3], d, rinv;
             pairR(a, i, j, r, d, rinv);
             double v[3] = {a.vx[i] - a.vx[j], a.vy[i] - a.vy[j], a.vz[i] - a.vz[j]};
-            MeSide J = side(j);
+            MeSide<> J = side(j);
             double dwi, dwj;
             double wi = look(a, a.wh, d * I.hInv, dwi), wj = look(a, a.wh, d * J.hInv, dwj);
-            MeGrad o;
+            MeGrad<> o;
             meStdAdjPair(r, d, rinv, v, I, J, wi, dwi, wj, dwj, gAi, gEi, gAj, gEj, o);
             bx[i] += o.r[0]; by[i] += o.r[1]; bz[i] += o.r[2];
             bx[j] -= o.r[0]; by[j] -= o.r[1]; bz[j] -= o.r[2];

@@ -17,14 +17,14 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
 
 
-def setup(side=12, seed=5, deterministic=False, ordered_forward=False):
+def setup(side=12, seed=5, deterministic=False, ordered_forward=False, precision="fp64"):
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
     ctx = sph.Context(0)
     if ordered_forward:  # the scatter adjoint then walks the full lists (no owned lists in use)
         ctx.set_deterministic(True)
-    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+    d = sph.ParticlesData.from_workload(wl, precision, "cuda:0")
     box = sph.Box(wl.box.copy(), wl.bc.copy())
     sw = AG.FrozenStdSweep(ctx, d, box, deterministic=deterministic)
     sw.freeze()
@@ -130,3 +130,25 @@ def test_adjoint_matches_central_differences():
     allrel = [r[4] for r in rows]
     assert np.median(allrel) <= 1e-4
     ctx.close()
+
+
+def test_mixed_adjoint_matches_fp64_gradient():
+    """The mixed form's adjoint (FP32 pair arithmetic on FP64 coordinate differences, FP64 sums) on
+    the mixed forward's state against the FP64 adjoint on the same inputs (the workload's h, m and v
+    are FP32 values, so both forms start from identical inputs).  Bar: normwise 1e-4 per field."""
+    import torch
+    from sphexa_gb300 import autograd as AG
+    grads = {}
+    for prec in ("fp64", "mixed"):
+        wl, ctx, sw, rho_t = setup(side=10, seed=7, precision=prec)
+        base = [t.clone().requires_grad_(True) for t in sw.inputs()]
+        out = AG.StdSweepFunction.apply(sw, *base)
+        L = AG.loss_rho_a(*[o.to(torch.float64) for o in out[:4]], rho_t)
+        L.backward()
+        grads[prec] = [b.grad.detach().to(torch.float64).cpu().numpy() for b in base]
+        ctx.close()
+    for k, f in enumerate(FIELDS):
+        g64, g32 = grads["fp64"][k], grads["mixed"][k]
+        err = np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
+        print(f"mixed adjoint {f:3s}: normwise rel {err:.3e}")
+        assert err <= 1e-4, f
