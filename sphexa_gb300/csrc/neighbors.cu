@@ -80,7 +80,11 @@ __device__ __forceinline__ void gridOffset(const NbrArgs& a, const int cj[3], fl
 
 struct WarpSmem {
     int32_t stack[kStack];
-    float4 f[kWarp];  // staged candidates: offsets from the group origin
+    // staged candidates: negated offsets from the group origin, one array per axis so that one
+    // 16-byte broadcast load gives four candidates' coordinate for the packed FP32x2 arithmetic
+    alignas(16) float nx[kWarp];
+    alignas(16) float ny[kWarp];
+    alignas(16) float nz[kWarp];
 };
 
 __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
@@ -190,16 +194,16 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     // tests all 32 slots with a fixed trip count; slots >= m hold a far-away sentinel whose FP32
     // distance is +inf.  Groups that need the exact test for every pair loop over the m slots.
     auto flush = [&](int64_t ja, int m) {
-        float4 fj = make_float4(1e30f, 1e30f, 1e30f, 0.f);
+        float rj[3] = {1e30f, 1e30f, 1e30f};
         if (lane < m) {
             const int64_t j = ja + lane;
             int cj[3];
             unpackCell(a.cell[j], cj);
-            float rj[3];
             gridOffset(a, cj, a.loc[j], co, lo, rj);
-            fj = make_float4(rj[0], rj[1], rj[2], 0.f);
         }
-        sm.f[lane] = fj;
+        sm.nx[lane] = -rj[0];
+        sm.ny[lane] = -rj[1];
+        sm.nz[lane] = -rj[2];
         __syncwarp();
         if (valid) {
             tested += m;
@@ -208,14 +212,29 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
                 for (int t = 0; t < m; ++t)
                     if (exactIn(j0 + uint32_t(t))) take(j0 + uint32_t(t));
             } else {
-#pragma unroll 8
-                for (int t = 0; t < kWarp; ++t) {
-                    const float4 f = sm.f[t];
-                    const float ex = dxi - f.x, ey = dyi - f.y, ez = dzi - f.z;
-                    const float d2f = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                    if (d2f > outAbove) continue;
-                    const uint32_t j = j0 + uint32_t(t);
-                    if (d2f < inBelow || exactIn(j)) take(j);
+                // four slots per step on packed FP32x2 operations: e = d_i + (-r_j) rounds as
+                // d_i - r_j, and d2 = fma(ex, ex, fma(ey, ey, ez * ez)) per slot as in scalar form
+                const float2 dx2 = make_float2(dxi, dxi), dy2 = make_float2(dyi, dyi), dz2 = make_float2(dzi, dzi);
+#pragma unroll 2
+                for (int t = 0; t < kWarp; t += 4) {
+                    const float4 X = *reinterpret_cast<const float4*>(&sm.nx[t]);
+                    const float4 Y = *reinterpret_cast<const float4*>(&sm.ny[t]);
+                    const float4 Z = *reinterpret_cast<const float4*>(&sm.nz[t]);
+                    const float2 ex0 = __fadd2_rn(dx2, make_float2(X.x, X.y));
+                    const float2 ex1 = __fadd2_rn(dx2, make_float2(X.z, X.w));
+                    const float2 ey0 = __fadd2_rn(dy2, make_float2(Y.x, Y.y));
+                    const float2 ey1 = __fadd2_rn(dy2, make_float2(Y.z, Y.w));
+                    const float2 ez0 = __fadd2_rn(dz2, make_float2(Z.x, Z.y));
+                    const float2 ez1 = __fadd2_rn(dz2, make_float2(Z.z, Z.w));
+                    const float2 q0 = __ffma2_rn(ex0, ex0, __ffma2_rn(ey0, ey0, __fmul2_rn(ez0, ez0)));
+                    const float2 q1 = __ffma2_rn(ex1, ex1, __ffma2_rn(ey1, ey1, __fmul2_rn(ez1, ez1)));
+                    const float d2[4] = {q0.x, q0.y, q1.x, q1.y};
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) {
+                        if (d2[s] > outAbove) continue;
+                        const uint32_t j = j0 + uint32_t(t + s);
+                        if (d2[s] < inBelow || exactIn(j)) take(j);
+                    }
                 }
             }
         }
