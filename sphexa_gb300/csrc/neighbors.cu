@@ -80,11 +80,13 @@ __device__ __forceinline__ void gridOffset(const NbrArgs& a, const int cj[3], fl
 
 struct WarpSmem {
     int32_t stack[kStack];
-    // staged candidates: negated offsets from the group origin, one array per axis so that one
-    // 16-byte broadcast load gives four candidates' coordinate for the packed FP32x2 arithmetic
-    alignas(16) float nx[kWarp];
-    alignas(16) float ny[kWarp];
-    alignas(16) float nz[kWarp];
+    // queue of staged candidates that lie in the group's search box: negated offsets from the
+    // group origin, one array per axis so that one 16-byte broadcast load gives four candidates'
+    // coordinate for the packed FP32x2 arithmetic, and their particle indices (ascending)
+    alignas(16) float nx[2 * kWarp];
+    alignas(16) float ny[2 * kWarp];
+    alignas(16) float nz[2 * kWarp];
+    alignas(16) uint32_t idx[2 * kWarp];
 };
 
 __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
@@ -193,52 +195,115 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     // one chunk of m <= 32 contiguous candidates [ja, ja + m), staged by the warp.  Every target
     // tests all 32 slots with a fixed trip count; slots >= m hold a far-away sentinel whose FP32
     // distance is +inf.  Groups that need the exact test for every pair loop over the m slots.
-    auto flush = [&](int64_t ja, int m) {
-        float rj[3] = {1e30f, 1e30f, 1e30f};
-        if (lane < m) {
-            const int64_t j = ja + lane;
-            int cj[3];
-            unpackCell(a.cell[j], cj);
-            gridOffset(a, cj, a.loc[j], co, lo, rj);
-        }
-        sm.nx[lane] = -rj[0];
-        sm.ny[lane] = -rj[1];
-        sm.nz[lane] = -rj[2];
-        __syncwarp();
-        if (valid) {
-            tested += m;
-            const uint32_t j0 = uint32_t(ja);
-            if (exactOnly) {
-                for (int t = 0; t < m; ++t)
-                    if (exactIn(j0 + uint32_t(t))) take(j0 + uint32_t(t));
-            } else {
-                // four slots per step on packed FP32x2 operations: e = d_i + (-r_j) rounds as
-                // d_i - r_j, and d2 = fma(ex, ex, fma(ey, ey, ez * ez)) per slot as in scalar form
-                const float2 dx2 = make_float2(dxi, dxi), dy2 = make_float2(dyi, dyi), dz2 = make_float2(dzi, dzi);
+    // Candidates are staged 32 at a time (one per lane, coalesced loads of cell and offset); those
+    // outside the group's search box by more than the FP32 rounding of the offsets (cullPad) are
+    // dropped and the rest appended, in ascending index order, to the warp's queue by ballot
+    // compaction.  A dropped candidate is farther than 2h from every target along one axis, so the
+    // reference's FP64 test rejects it too.  Each full queue block of 32 is tested by every target
+    // with a fixed trip count; the last, partial block has far-away sentinels in its empty slots.
+    // Groups that need the exact test for every pair keep every candidate and test the filled slots.
+    const float cullPad = 32.f * 0x1p-24f * (Rg + fmaxf(a.u[0], fmaxf(a.u[1], a.u[2])));
+    const float bxl = gmin[0] - cullPad, bxh = gmax[0] + cullPad;
+    const float byl = gmin[1] - cullPad, byh = gmax[1] + cullPad;
+    const float bzl = gmin[2] - cullPad, bzh = gmax[2] + cullPad;
+    int qn = 0;  // candidates in the queue
+    auto testBlock = [&](int filled) {
+        if (valid) tested += unsigned(filled);
+        if (exactOnly) {
+            if (valid)
+                for (int t = 0; t < filled; ++t) {
+                    const uint32_t j = sm.idx[t];
+                    if (exactIn(j)) take(j);
+                }
+        } else {
+            // four slots per step on packed FP32x2 operations: e = d_i + (-r_j) rounds as
+            // d_i - r_j, and d2 = fma(ex, ex, fma(ey, ey, ez * ez)) per slot as in scalar form.
+            // Every lane runs the loop (the band vote is warp-wide); invalid lanes take nothing.
+            const float2 dx2 = make_float2(dxi, dxi), dy2 = make_float2(dyi, dyi), dz2 = make_float2(dzi, dzi);
 #pragma unroll 2
-                for (int t = 0; t < kWarp; t += 4) {
-                    const float4 X = *reinterpret_cast<const float4*>(&sm.nx[t]);
-                    const float4 Y = *reinterpret_cast<const float4*>(&sm.ny[t]);
-                    const float4 Z = *reinterpret_cast<const float4*>(&sm.nz[t]);
-                    const float2 ex0 = __fadd2_rn(dx2, make_float2(X.x, X.y));
-                    const float2 ex1 = __fadd2_rn(dx2, make_float2(X.z, X.w));
-                    const float2 ey0 = __fadd2_rn(dy2, make_float2(Y.x, Y.y));
-                    const float2 ey1 = __fadd2_rn(dy2, make_float2(Y.z, Y.w));
-                    const float2 ez0 = __fadd2_rn(dz2, make_float2(Z.x, Z.y));
-                    const float2 ez1 = __fadd2_rn(dz2, make_float2(Z.z, Z.w));
-                    const float2 q0 = __ffma2_rn(ex0, ex0, __ffma2_rn(ey0, ey0, __fmul2_rn(ez0, ez0)));
-                    const float2 q1 = __ffma2_rn(ex1, ex1, __ffma2_rn(ey1, ey1, __fmul2_rn(ez1, ez1)));
-                    const float d2[4] = {q0.x, q0.y, q1.x, q1.y};
+            for (int t = 0; t < kWarp; t += 4) {
+                const float4 X = *reinterpret_cast<const float4*>(&sm.nx[t]);
+                const float4 Y = *reinterpret_cast<const float4*>(&sm.ny[t]);
+                const float4 Z = *reinterpret_cast<const float4*>(&sm.nz[t]);
+                const float2 ex0 = __fadd2_rn(dx2, make_float2(X.x, X.y));
+                const float2 ex1 = __fadd2_rn(dx2, make_float2(X.z, X.w));
+                const float2 ey0 = __fadd2_rn(dy2, make_float2(Y.x, Y.y));
+                const float2 ey1 = __fadd2_rn(dy2, make_float2(Y.z, Y.w));
+                const float2 ez0 = __fadd2_rn(dz2, make_float2(Z.x, Z.y));
+                const float2 ez1 = __fadd2_rn(dz2, make_float2(Z.z, Z.w));
+                const float2 q0 = __ffma2_rn(ex0, ex0, __ffma2_rn(ey0, ey0, __fmul2_rn(ez0, ez0)));
+                const float2 q1 = __ffma2_rn(ex1, ex1, __ffma2_rn(ey1, ey1, __fmul2_rn(ez1, ez1)));
+                const float d2[4] = {q0.x, q0.y, q1.x, q1.y};
+                const uint4 J = *reinterpret_cast<const uint4*>(&sm.idx[t]);
+                const uint32_t js[4] = {J.x, J.y, J.z, J.w};
+                bool band = false;
+#pragma unroll
+                for (int s = 0; s < 4; ++s) band |= !(d2[s] < inBelow) && d2[s] <= outAbove;
+                if (__any_sync(0xffffffffu, valid && band)) {
+                    // a pair within the FP32 margin of the radius (rare): slot by slot, exact test
+                    if (valid) {
+#pragma unroll
+                        for (int s = 0; s < 4; ++s)
+                            if (d2[s] <= outAbove && (d2[s] < inBelow || exactIn(js[s]))) take(js[s]);
+                    }
+                } else {
+                    // the common case without divergence: predicated appends
 #pragma unroll
                     for (int s = 0; s < 4; ++s) {
-                        if (d2[s] > outAbove) continue;
-                        const uint32_t j = j0 + uint32_t(t + s);
-                        if (d2[s] < inBelow || exactIn(j)) take(j);
+                        const bool tk = valid && d2[s] < inBelow && js[s] != iu;
+                        if (tk && cnt < a.ngmax) *outp = js[s];
+                        outp += tk ? a.stride : 0;
+                        cnt += tk ? 1u : 0u;
                     }
                 }
             }
         }
         __syncwarp();
+    };
+    auto flush = [&](int64_t ja, int m) {
+        float rj[3];
+        bool keep = false;
+        if (lane < m) {
+            const int64_t j = ja + lane;
+            int cj[3];
+            unpackCell(a.cell[j], cj);
+            gridOffset(a, cj, a.loc[j], co, lo, rj);
+            keep = exactOnly || (rj[0] >= bxl && rj[0] <= bxh && rj[1] >= byl && rj[1] <= byh && rj[2] >= bzl &&
+                                 rj[2] <= bzh);
+        }
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int q = qn + __popc(km & ((1u << lane) - 1u));
+            sm.nx[q] = -rj[0];
+            sm.ny[q] = -rj[1];
+            sm.nz[q] = -rj[2];
+            sm.idx[q] = uint32_t(ja + lane);
+        }
+        qn += __popc(km);
+        __syncwarp();
+        if (qn >= kWarp) {
+            testBlock(kWarp);
+            qn -= kWarp;
+            if (lane < qn) {  // move the queue's tail [32, 32 + qn) to the front
+                sm.nx[lane] = sm.nx[kWarp + lane];
+                sm.ny[lane] = sm.ny[kWarp + lane];
+                sm.nz[lane] = sm.nz[kWarp + lane];
+                sm.idx[lane] = sm.idx[kWarp + lane];
+            }
+            __syncwarp();
+        }
+    };
+    // the partial last block: sentinels (FP32 distance +inf) in the empty slots
+    auto drain = [&]() {
+        if (qn == 0) return;
+        if (lane >= qn) {
+            sm.nx[lane] = -1e30f;
+            sm.ny[lane] = -1e30f;
+            sm.nz[lane] = -1e30f;
+        }
+        __syncwarp();
+        testBlock(qn);
+        qn = 0;
     };
 
     int64_t pa = 0, pb = 0;  // pending contiguous candidate range
@@ -305,6 +370,7 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         flush(pa, m);
         pa += m;
     }
+    drain();
 
     if (valid) a.count[ii] = cnt;
     // warp-aggregated statistics
