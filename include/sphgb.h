@@ -106,6 +106,12 @@ int sphgb_set_params(sphgb_ctx* ctx, const sphgb_params* params);
  * neighbour's share is added with FP64 atomics, so the last bits of ax ay az du can differ from
  * run to run.  on = 1: every list owner sums its own pairs in list order, bitwise reproducible. */
 int sphgb_set_deterministic(sphgb_ctx* ctx, int32_t on);
+/* Forward tape of the VE adjoint (no reference counterpart).  on = 1: the FP64 VE passes over all
+ * particles (gradh, IAD + divv/curlv, AV switches, momentum-energy) keep the per-particle sums
+ * that sphgb_adjoint_ve needs (16 doubles per particle, held by the context), and the adjoint
+ * reads them instead of summing them again over the lists.  The tape belongs to the neighbour
+ * lists it was written on; a later neighbour search invalidates it.  on = 0 (default) frees it. */
+int sphgb_set_adjoint_tape(sphgb_ctx* ctx, int32_t on);
 /* Mixed form only (no reference counterpart): on = 1 (default) recomputes in FP64, from the exact
  * inputs, the particles whose gradh is near 0 (|gradh| < 0.1) or whose divv sign lies within the
  * FP32 error bound, with the neighbour shells their values depend on; on = 0 leaves the FP32

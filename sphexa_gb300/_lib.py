@@ -82,6 +82,7 @@ SIGNATURES = {
     "sphgb_set_params": [_P, C.POINTER(SphgbParams)],
     "sphgb_default_params": [C.POINTER(SphgbParams)],
     "sphgb_set_deterministic": [_P, C.c_int32],
+    "sphgb_set_adjoint_tape": [_P, C.c_int32],
     "sphgb_set_mixed_refinement": [_P, C.c_int32],
     "sphgb_set_domain_mode": [_P, C.c_int32],
     "sphgb_get_kernel_K": [_P, C.POINTER(C.c_double)],

@@ -75,14 +75,17 @@ def _run_adjoint(sweep, g_rho, g_ax, g_ay, g_az, g_du, fn, args):
 
 class FrozenVeSweep(FrozenStdSweep):
     """VE chain on frozen lists.  The alpha before the AV switch is kept from freeze() on, so that
-    every forward starts from the same alpha; av_clean selects momentumAndEnergy<avClean>."""
+    every forward starts from the same alpha; av_clean selects momentumAndEnergy<avClean>.  With
+    tape (default) the context's forward passes keep the sums the backward needs
+    (sphgb_set_adjoint_tape); the backward then reads them from the last forward."""
 
-    def __init__(self, ctx, d, box, av_clean: bool = False, deterministic: bool = False):
+    def __init__(self, ctx, d, box, av_clean: bool = False, deterministic: bool = False, tape: bool = True):
         if d.precision != "fp64":
             raise ValueError("the VE adjoint runs in the FP64 form")
         super().__init__(ctx, d, box, deterministic)
         self.av_clean = av_clean
         self.alpha0 = None
+        ctx.set_adjoint_tape(tape)
 
     def freeze(self) -> None:
         super().freeze()

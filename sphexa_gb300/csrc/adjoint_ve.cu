@@ -167,6 +167,41 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreMeKernel(VeAdjArgs a)
     a.avE[i] = avE;
 }
 
+// the signal velocity of the AV switch (av_switches_kern.hpp:66-86): the first of i's approaching
+// pairs, in list order, with the largest c_i + c_j - 3 (r.v)/|r| sets vsig_i (1e-40 c_i when none)
+__device__ __forceinline__ void vsigStep(const VeAdjArgs& a, int64_t j, const double r[3], double rinv,
+                                         const double v[3], double ci, double& vsig, uint32_t& arg)
+{
+    const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    if (rv < 0.0) {
+        const double vs = ci + a.c[j] - 3.0 * rv * rinv;
+        if (vs > vsig) {
+            vsig = vs;
+            arg = uint32_t(j);
+        }
+    }
+}
+
+// vsig_i and its pair alone, when the forward passes kept the other sums of vePreKernel
+__global__ void __launch_bounds__(kVeAdjBlock) veArgKernel(VeAdjArgs a)
+{
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= a.n) return;
+    const double ci = a.c[i];
+    double vsig = 1e-40 * ci;
+    uint32_t arg = kNoPair;
+    const unsigned nc = a.lv.capped(i);
+    for (unsigned q = 0; q < nc; ++q) {
+        const uint32_t j = a.lv.at(i, q);
+        double r[3], d, rinv, v[3];
+        geom(a, i, j, r, d, rinv);
+        vdiff(a, i, j, v);
+        vsigStep(a, j, r, rinv, v, ci, vsig, arg);
+    }
+    a.vsig[i] = vsig;
+    a.vsigArg[i] = arg;
+}
+
 // forward sums of the AV switch (G_i, vsig_i and the pair that set it), of divv (P_i) and of
 // gradh (whomega0 = K h^-4 S_om, wrho0 = K h^-4 S_r0)
 __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
@@ -190,14 +225,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
         double dw, dwd;
         const double w = lookupVS(a.wh, v1, dw);
         const double wd = lookupVS(a.whd, v1, dwd);
-        const double rv = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
-        if (rv < 0.0) {
-            const double vs = ci + a.c[j] - 3.0 * rv * rinv;
-            if (vs > vsig) {
-                vsig = vs;
-                arg = j;
-            }
-        }
+        vsigStep(a, j, r, rinv, v, ci, vsig, arg);
         const double fac = a.vol[j] * (divvi - a.divv[j]) * w;
         const double xw = a.xm[j] * w;
 #pragma unroll
@@ -1188,12 +1216,33 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     veQuotKernel<<<eb, 256, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "veQuotKernel"));
     const bool withDu = a.sDu != nullptr;
-    if (withDu) {  // en and avE enter only through the du seed
+    // forward sums kept by the forward passes on these lists (sphgb_set_adjoint_tape) are read from
+    // the tape instead of being summed again; vsig_i and its pair are always found here
+    constexpr unsigned kTapeNeeded = kTapeGradh | kTapeIad | kTapeAv;
+    const bool taped = c->tapeEpoch == c->nbrEpoch && c->tapeN == n && (c->tapeMask & kTapeNeeded) == kTapeNeeded;
+    const bool tapedMe = taped && (c->tapeMask & kTapeMe) != 0;
+    if (taped) {
+        double* tp = c->veTape.as<double>();
+        a.G = tp + int64_t(kTapeG) * n;
+        a.P = tp + int64_t(kTapeP) * n;
+        a.wom = tp + int64_t(kTapeWom) * n;
+        a.wr0 = tp + int64_t(kTapeWr0) * n;
+        if (tapedMe) {
+            a.en = tp + int64_t(kTapeEn) * n;
+            a.avE = tp + int64_t(kTapeAvE) * n;
+        }
+    }
+    if (withDu && !tapedMe) {  // en and avE enter only through the du seed
         vePreMeKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "vePreMeKernel"));
     }
-    vePreKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "vePreKernel"));
+    if (taped) {
+        veArgKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veArgKernel"));
+    } else {
+        vePreKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "vePreKernel"));
+    }
     {
         using K = void (*)(VeAdjArgs);
         // [two-sided][avClean][du seed]

@@ -141,7 +141,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pack,       &c->whx32,     &c->whdx32,    &c->refMask,
-                    &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp};
+                    &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -171,6 +171,17 @@ int sphgb_set_deterministic(sphgb_ctx* c, int32_t on)
 {
     if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;
     c->deterministic = on != 0;
+    return SPHGB_OK;
+}
+
+int sphgb_set_adjoint_tape(sphgb_ctx* c, int32_t on)
+{
+    if (!c || (on != 0 && on != 1)) return SPHGB_ERR_ARG;
+    c->tapeOn = on != 0;
+    if (!c->tapeOn) {
+        c->tapeMask = 0;
+        c->veTape.release();
+    }
     return SPHGB_OK;
 }
 

@@ -112,6 +112,13 @@ struct sphgb_ctx {
     bool eosFused = false, auxReady = false;
     // packed neighbour-side records of the mixed pair passes (float4 x 4 per particle)
     sphgb::DBuf pack;
+    // forward tape of the VE adjoint: with tapeOn the FP64 VE passes over all particles keep the
+    // per-particle sums the adjoint needs (kTape* sections x n doubles); tapeMask tells which passes
+    // wrote theirs on the lists of epoch tapeEpoch for tapeN particles
+    bool tapeOn = false;
+    sphgb::DBuf veTape;
+    int64_t tapeEpoch = -1, tapeN = 0;
+    unsigned tapeMask = 0;
     // mixed form: FP64 refinement of ill-conditioned particles (masks, FP64 xm/kx/gradh scratch,
     // divv error bound per particle) and the counts of the last passes
     bool refineMixed = true;

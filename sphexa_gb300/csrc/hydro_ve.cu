@@ -79,7 +79,8 @@ int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
                                                           const void* m, const void* xm, const void* wh,
-                                                          const void* whd, double K, void* kxOut, void* gradhOut)
+                                                          const void* whd, double K, void* kxOut, void* gradhOut,
+                                                          double* tapeWom = nullptr, double* tapeWr0 = nullptr)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -110,6 +111,10 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         kxi *= K * h3Inv;
         whomega *= K * h3Inv * hInv;
         wrho0 *= K * h3Inv * hInv;
+        if (tapeWom) {
+            tapeWom[i] = whomega;
+            tapeWr0[i] = wrho0;
+        }
         whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
         double rhoi = kxi * mi / xmi;
         double dhdrho = -hi / (rhoi * 3.0);
@@ -198,6 +203,8 @@ struct IadDivvArgs {
     double K;
     void *c11, *c12, *c13, *c22, *c23, *c33, *divv, *curlv;
     void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
+    double* tapeP;  // FP64: P_i = sum xm_j W (v_j - v_i) r^T for the VE adjoint (9 x tapeN), or null
+    int64_t tapeN;
 };
 
 template<class P>
@@ -245,6 +252,10 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             M[6] += sz * rx;
             M[7] += sz * ry;
             M[8] += sz * rz;
+        }
+        if (a.tapeP) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) a.tapeP[q * a.tapeN + i] = M[q];
         }
         T cc[6];
         iadInvert<T>(t11, t12, t13, t22, t23, t33, hi, a.K, cc);
@@ -366,6 +377,8 @@ struct AvArgs {
     const void* vol;  // aux: xm/kx
     double K, dt, alphamin, alphamax, decay;
     void* alpha;
+    double* tapeG;  // FP64: G_i (3 x tapeN) for the VE adjoint, or null
+    int64_t tapeN;
 };
 
 // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
@@ -392,7 +405,6 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
-    const T* tab = static_cast<const T*>(a.wh);
     T hi = ld<T>(a.h, i), ci = ld<T>(a.c, i);
     T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
     T c11 = ld<T>(a.c11, i), c12 = ld<T>(a.c12, i), c13 = ld<T>(a.c13, i);
@@ -454,6 +466,13 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
         gy = T(-double(kh3) * (double(c12) * Sx + double(c22) * Sy + double(c23) * Sz));
         gz = T(-double(kh3) * (double(c13) * Sx + double(c23) * Sy + double(c33) * Sz));
     }
+    if constexpr (std::is_same_v<P, Fp64Tag>) {
+        if (a.tapeG) {
+            a.tapeG[i] = gx;
+            a.tapeG[a.tapeN + i] = gy;
+            a.tapeG[2 * a.tapeN + i] = gz;
+        }
+    }
     st<T>(a.alpha, i, avAlpha<T>(a, ld<T>(a.alpha, i), hi, ci, divvi, vsig_i, gx, gy, gz));
 }
 
@@ -480,6 +499,8 @@ struct MeVeArgs {
     // mixed form: packed neighbour records {vx vy vz c} {c11 c12 c13 c22} {c23 c33 m xm}
     // {alpha rho m/rho m*prho} per particle
     const float4* pack;
+    // FP64: the energy sums (en, avE before max(0, .)) for the VE adjoint, or null
+    double *tapeEn, *tapeAvE;
 };
 
 template<class T>
@@ -528,7 +549,6 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
     const int64_t i = valid ? i0 : lv.first;
     const int64_t ii = i - lv.first;
     const unsigned nc = valid ? lv.capped(ii) : 0u;
-    const T* tab = static_cast<const T*>(a.wh);
     const T* aux = static_cast<const T*>(a.aux);
     const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n;
     constexpr T Atmin = T(0.1), Atmax = T(0.2), ramp = T(1) / (Atmax - Atmin);
@@ -628,6 +648,10 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             avE -= T(0.5) * (avWi * si + bvWj * sj);
         }
         if (valid) {
+            if (a.tapeEn) {
+                a.tapeEn[i] = en;
+                a.tapeAvE[i] = avE;
+            }
             avE = fmax(T(0), avE);
             a.du[i] = a.K * (prhoi * en + T(0.5) * avE);
             st<T>(a.ax, i, -a.K * mx);
@@ -772,7 +796,8 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
 }
 
 __global__ void gradhOnceFinish(int64_t first, int64_t last, int64_t n, const double* h, const double* m,
-                                const double* xm, double K, const double* acc, double* kxOut, double* gradhOut)
+                                const double* xm, double K, const double* acc, double* kxOut, double* gradhOut,
+                                double* tapeWom, double* tapeWr0)
 {
     const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= last) return;
@@ -782,6 +807,10 @@ __global__ void gradhOnceFinish(int64_t first, int64_t last, int64_t n, const do
     kxi *= K * h3Inv;
     whomega *= K * h3Inv * hInv;
     wrho0 *= K * h3Inv * hInv;
+    if (tapeWom) {
+        tapeWom[i] = whomega;
+        tapeWr0[i] = wrho0;
+    }
     whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
     const double rhoi = kxi * mi / xmi;
     const double dhdrho = -hi / (rhoi * 3.0);
@@ -792,7 +821,8 @@ __global__ void gradhOnceFinish(int64_t first, int64_t last, int64_t n, const do
 // the same epilogue fused with the EOS and the quotients of the later passes (inside a sweep)
 __global__ void gradhEosFinish(int64_t n, const double* h, const double* m, const double* xm, double K,
                                const double* acc, double* kxOut, double* gradhOut, const double* u, double gamma,
-                               void* prho, void* c, void* rho, void* p, double* aux)
+                               void* prho, void* c, void* rho, void* p, double* aux, double* tapeWom,
+                               double* tapeWr0)
 {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
@@ -802,6 +832,10 @@ __global__ void gradhEosFinish(int64_t n, const double* h, const double* m, cons
     kxi *= K * h3Inv;
     whomega *= K * h3Inv * hInv;
     wrho0 *= K * h3Inv * hInv;
+    if (tapeWom) {
+        tapeWom[i] = whomega;
+        tapeWr0[i] = wrho0;
+    }
     whomega = whomega * mi / xmi + (kxi - K * xmi * h3Inv) * wrho0;
     const double rhoi = kxi * mi / xmi;
     const double dhdrho = -hi / (rhoi * 3.0);
@@ -881,6 +915,11 @@ __global__ void avOnceFinish(int64_t first, int64_t last, int64_t n, AvArgs a, c
     const double gx = -kh3 * (c11 * Sx + c12 * Sy + c13 * Sz);
     const double gy = -kh3 * (c12 * Sx + c22 * Sy + c23 * Sz);
     const double gz = -kh3 * (c13 * Sx + c23 * Sy + c33 * Sz);
+    if (a.tapeG) {
+        a.tapeG[i] = gx;
+        a.tapeG[a.tapeN + i] = gy;
+        a.tapeG[2 * a.tapeN + i] = gz;
+    }
     // vsig_i starts at 1e-40 c_i (av_switches_kern.hpp:66); both candidates are >= 0
     const long long vb = max(__double_as_longlong(1.e-40 * ci), reinterpret_cast<const long long*>(acc + 3 * n)[i]);
     st<double>(a.alpha, i,
@@ -1010,6 +1049,10 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceFinish(ListView lv, MeVeAr
     if (valid) {
         const int64_t i = i0;
         const double prhoi = ld<double>(a.prho, i);
+        if (a.tapeEn) {
+            a.tapeEn[i] = a.acc[3 * a.n + i];
+            a.tapeAvE[i] = a.acc[4 * a.n + i];
+        }
         const double avE = fmax(0.0, a.acc[4 * a.n + i]);
         a.du[i] = a.K * (prhoi * a.acc[3 * a.n + i] + 0.5 * avE);
         st<double>(a.ax, i, -a.K * a.acc[i]);
@@ -1036,6 +1079,10 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     lv.first = first;
     lv.last = last;
     unsigned blocks = gridFor(last - first, kPairBlock);
+    double* tape;
+    SPHGB_TRY(tapeFor(c, p, first, last, kTapeGradh, &tape));
+    double* tWom = tape ? tape + int64_t(kTapeWom) * p->n : nullptr;
+    double* tWr0 = tape ? tape + int64_t(kTapeWr0) * p->n : nullptr;
     if (pairOnce(c, p, first, last)) {
         const int64_t n = p->n;
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 3 * size_t(n)));
@@ -1050,14 +1097,14 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
             gradhEosFinish<<<gridFor(n, 256), 256, 0, c->stream>>>(
                 n, static_cast<const double*>(p->h), static_cast<const double*>(p->m), static_cast<const double*>(p->xm),
                 c->K, c->pairAcc.as<double>(), static_cast<double*>(p->kx), static_cast<double*>(p->gradh), p->u,
-                c->prm.gamma, p->prho, p->c, p->rho, p->p, c->aux.as<double>());
+                c->prm.gamma, p->prho, p->c, p->rho, p->p, c->aux.as<double>(), tWom, tWr0);
             c->eosFused = c->auxReady = true;
             return launched(c, "gradhEosFinish");
         }
         gradhOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(
             first, last, n, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
             static_cast<const double*>(p->xm), c->K, c->pairAcc.as<double>(), static_cast<double*>(p->kx),
-            static_cast<double*>(p->gradh));
+            static_cast<double*>(p->gradh), tWom, tWr0);
         return launched(c, "gradhOnceFinish");
     }
     if (p->precision == SPHGB_MIXED) {
@@ -1071,7 +1118,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     } else
         gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                    p->xm, c->whx64.p, c->whdx64.p, c->K, p->kx,
-                                                                   p->gradh);
+                                                                   p->gradh, tWom, tWr0);
     return launched(c, "gradhKernel");
 }
 
@@ -1156,6 +1203,9 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
         return refineMixedDivv(c, p, refine ? a.divvBound : nullptr);
     } else {
         a.wh = c->whx64.p;
+        SPHGB_TRY(tapeFor(c, p, first, last, kTapeIad, &a.tapeP));
+        if (a.tapeP) a.tapeP += int64_t(kTapeP) * p->n;
+        a.tapeN = p->n;
         iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     }
     return launched(c, "iadDivvKernel");
@@ -1176,6 +1226,11 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
              p->c13, p->c22, p->c23, p->c33,  p->divv, nullptr, c->aux.as<char>() + 2 * es * p->n,
              c->K,   c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant, p->alpha};
     unsigned blocks = gridFor(last - first, kPairBlock);
+    if (!mixed) {
+        SPHGB_TRY(tapeFor(c, p, first, last, kTapeAv, &a.tapeG));
+        if (a.tapeG) a.tapeG += int64_t(kTapeG) * p->n;
+        a.tapeN = p->n;
+    }
     if (mixed) {
         a.wh = c->whx32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
@@ -1256,6 +1311,12 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {
         a.wh = c->whx64.p;
+        double* tape;
+        SPHGB_TRY(tapeFor(c, p, first, last, kTapeMe, &tape));
+        if (tape) {
+            a.tapeEn = tape + int64_t(kTapeEn) * p->n;
+            a.tapeAvE = tape + int64_t(kTapeAvE) * p->n;
+        }
         // one evaluation per mutual pair when the lists cover all particles and the order may vary
         const bool once = !avClean && pairOnce(c, p, first, last);
         if (once) {

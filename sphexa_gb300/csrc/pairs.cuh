@@ -74,6 +74,35 @@ inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first
            last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
 }
 
+// ---- forward tape of the VE adjoint: sections of n doubles in c->veTape ----
+constexpr int kTapeG = 0;      // G_i = -K h_i^-3 C_i S_i of the AV switch (3 sections)
+constexpr int kTapeP = 3;      // P_i = sum xm_j W_ij (v_j - v_i) r_ij^T of divv/curlv, row-major (9)
+constexpr int kTapeWom = 12;   // K h_i^-4 (-3 xm_i + sum xm_j dterh_ij) of gradh
+constexpr int kTapeWr0 = 13;   // K h_i^-4 (-3 m_i + sum m_j dterh_ij)
+constexpr int kTapeEn = 14;    // energy sum of the momentum-energy pass
+constexpr int kTapeAvE = 15;   // viscous energy sum before max(0, .)
+constexpr int kTapeSections = 16;
+enum : unsigned { kTapeGradh = 1, kTapeIad = 2, kTapeAv = 4, kTapeMe = 8 };
+
+// the tape of an FP64 VE pass over all particles (null when the tape is off or the pass covers
+// part of the particles); marks the pass's part as written on the current lists
+inline int tapeFor(sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last, unsigned part,
+                   double** out)
+{
+    *out = nullptr;
+    if (!c->tapeOn || p->precision != SPHGB_FP64 || first != 0 || last != p->n) return SPHGB_OK;
+    const int64_t n = p->n;
+    if (c->tapeEpoch != c->nbrEpoch || c->tapeN != n) {
+        c->tapeMask = 0;
+        c->tapeEpoch = c->nbrEpoch;
+        c->tapeN = n;
+    }
+    SPHGB_TRY(c->veTape.ensure(sizeof(double) * kTapeSections * size_t(n)));
+    c->tapeMask |= part;
+    *out = c->veTape.as<double>();
+    return SPHGB_OK;
+}
+
 // ---- FP64 coordinates: reference distancePBC / legacy applyPBC (box.hpp:216-254) ----
 struct CoordFp64 {
     const double *x, *y, *z;

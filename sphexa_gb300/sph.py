@@ -80,6 +80,10 @@ class Context:
         momentum-energy pass evaluates mutual pairs once and scatters with FP64 atomics."""
         check(self.lib.sphgb_set_deterministic(self.h, int(bool(on))), "sphgb_set_deterministic")
 
+    def set_adjoint_tape(self, on: bool) -> None:
+        """FP64 VE passes keep the sums the VE adjoint needs (sphgb_set_adjoint_tape)."""
+        check(self.lib.sphgb_set_adjoint_tape(self.h, int(bool(on))), "sphgb_set_adjoint_tape")
+
     def set_mixed_refinement(self, on: bool) -> None:
         """Mixed form: recompute ill-conditioned particles (gradh near 0, divv sign within the FP32
         error) in FP64 from the exact inputs (default True)."""

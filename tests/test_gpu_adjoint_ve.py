@@ -143,3 +143,33 @@ def test_ve_adjoint_matches_central_differences(av_clean):
     assert smooth and max(smooth) <= 1e-6
     assert np.median([r[4] for r in rows]) <= 1e-4
     ctx.close()
+
+
+@pytest.mark.parametrize("av_clean", [False, True])
+@pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided"])
+def test_ve_adjoint_tape_matches_recomputed_sums(av_clean, form):
+    """the forward passes' tape (sphgb_set_adjoint_tape) against the adjoint's own re-summation:
+    same gradients to rounding, and with a du seed the energy pre-pass is not launched"""
+    import torch
+    wl, ctx, sw, rho_t = setup(side=10, seed=13, av_clean=av_clean, deterministic=form == "two-sided",
+                               ordered_forward=form == "scatter")
+    gen = torch.Generator(device="cpu").manual_seed(4)
+    s_du = torch.randn(wl.n, generator=gen, dtype=torch.float64).to("cuda:0")
+
+    def grads():
+        vals = sw.inputs()
+        rho, ax, ay, az, du = sw.forward(*vals)
+        l0 = ctx.launches()
+        g = [t.cpu().numpy() for t in sw.backward(2.0 * (rho - rho_t), 2.0 * ax, 2.0 * ay, 2.0 * az, s_du)]
+        return g, ctx.launches() - l0
+
+    grads()  # the first backward also builds the transposed lists of the two-sided form
+    g_tape, n_tape = grads()
+    ctx.set_adjoint_tape(False)
+    g_sum, n_sum = grads()
+    assert n_tape == n_sum - 1  # no energy pre-pass with the tape
+    for f, a, b in zip(FIELDS, g_tape, g_sum):
+        err = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-300)
+        print(f"tape vs re-summed {f:3s}: normwise rel {err:.3e}")
+        assert err <= 1e-12, f
+    ctx.close()
