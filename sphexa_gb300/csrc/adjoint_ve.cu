@@ -50,6 +50,10 @@ struct VeAdjArgs {
     // forward sums
     double *en, *avE, *G, *vsig, *P, *wom, *wr0;
     uint32_t* vsigArg;
+    // FP32 copies {x y z c} and {vx vy vz 0} for the signal-velocity filter, and the bound on the
+    // FP32 error of a position difference per component
+    float4 *xc32, *v32;
+    float ePos;
     // adjoints of the intermediate fields
     double *prhoB, *cB, *alphaB, *rhoB, *xmB, *kxB, *CB, *gB, *divvB, *gradhB;
     double* Rav;  // 3 x n: R_i = sum_j fac_j W_j r_j of the AV pair terms (i's C partials, avCbar)
@@ -140,6 +144,8 @@ __global__ void veQuotKernel(VeAdjArgs a)
     a.kxInv[i] = 1.0 / kx;
     a.xmInv[i] = 1.0 / xm;
     a.lnxm[i] = log(xm);
+    a.xc32[i] = make_float4(float(a.x[i]), float(a.y[i]), float(a.z[i]), float(a.c[i]));
+    a.v32[i] = make_float4(float(a.vx[i]), float(a.vy[i]), float(a.vz[i]), 0.f);
 }
 
 // forward sums of the momentum-energy pass: en_i, avE_i (before max(0, .))
@@ -182,7 +188,12 @@ __device__ __forceinline__ void vsigStep(const VeAdjArgs& a, int64_t j, const do
     }
 }
 
-// vsig_i and its pair alone, when the forward passes kept the other sums of vePreKernel
+// vsig_i and its pair alone, when the forward passes kept the other sums of vePreKernel.  One FP32
+// walk over i's list keeps a lower bound L on vsig_i from the pairs that surely approach; a pair
+// is evaluated in FP64 (vsigStep, in list order) only when its FP32 signal velocity plus the error
+// bound reaches the current L, which every pair able to set vsig_i does, so vsig_i and its pair
+// come out as in vePreKernel.  Particles whose 2h exceeds a quarter of a periodic box edge (where
+// the threshold-2h image rule of the FP64 geometry need not be the minimum image) walk in FP64.
 __global__ void __launch_bounds__(kVeAdjBlock) veArgKernel(VeAdjArgs a)
 {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -191,12 +202,46 @@ __global__ void __launch_bounds__(kVeAdjBlock) veArgKernel(VeAdjArgs a)
     double vsig = 1e-40 * ci;
     uint32_t arg = kNoPair;
     const unsigned nc = a.lv.capped(i);
-    for (unsigned q = 0; q < nc; ++q) {
-        const uint32_t j = a.lv.at(i, q);
+    auto exact = [&](uint32_t j) {
         double r[3], d, rinv, v[3];
         geom(a, i, j, r, d, rinv);
         vdiff(a, i, j, v);
         vsigStep(a, j, r, rinv, v, ci, vsig, arg);
+    };
+    const double twoH = 2.0 * a.h[i];
+    bool fp64Walk = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) fp64Walk |= a.box.pbc[k] && twoH > 0.25 * a.box.L[k];
+    if (fp64Walk) {
+        for (unsigned q = 0; q < nc; ++q) exact(a.lv.at(i, q));
+    } else {
+        const float4 Xi = a.xc32[i], Vi = a.v32[i];
+        const float viMax = fmaxf(fabsf(Vi.x), fmaxf(fabsf(Vi.y), fabsf(Vi.z)));
+        const float dr = 2.f * a.ePos;  // >= |r_f - r| (three components)
+        float L = 0.f;                  // vsig_i > 0
+        for (unsigned q = 0; q < nc; ++q) {
+            const uint32_t j = a.lv.at(i, q);
+            const float4 Xj = a.xc32[j], Vj = a.v32[j];
+            float r[3] = {Xi.x - Xj.x, Xi.y - Xj.y, Xi.z - Xj.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (a.box.pbc[k]) {  // minimum image: |r| <= 2h < L/4 for every listed pair
+                    if (r[k] > 0.5f * a.box.Lf[k]) r[k] -= a.box.Lf[k];
+                    else if (r[k] < -0.5f * a.box.Lf[k]) r[k] += a.box.Lf[k];
+                }
+            const float v[3] = {Vi.x - Vj.x, Vi.y - Vj.y, Vi.z - Vj.z};
+            const float d = sqrtf(fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2])));
+            const float rv = fmaf(r[0], v[0], fmaf(r[1], v[1], r[2] * v[2]));
+            // bounds: |v_f - v| <= dv, |r.v error| <= erv, |signal velocity error| <= ev
+            const float vn = 1.8f * (viMax + fmaxf(fabsf(Vj.x), fmaxf(fabsf(Vj.y), fabsf(Vj.z))));
+            const float dv = 1e-6f * vn;
+            const float erv = dr * vn + d * (dv + 1e-6f * vn);
+            const float vs = Xi.w + Xj.w - 3.f * rv / d;
+            const float ev = 3.f * (4.f * dr * vn / d + 2.f * dv + 1e-6f * vn) +
+                             1e-6f * (Xi.w + Xj.w + 3.f * fabsf(rv) / d);
+            if (!(rv >= erv) && !(vs + ev < L)) exact(j);  // may approach and may reach L (NaN: evaluate)
+            if (rv < -erv) L = fmaxf(L, vs - ev);          // surely approaches
+        }
     }
     a.vsig[i] = vsig;
     a.vsigArg[i] = arg;
@@ -1092,7 +1137,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjOnceKernel(VeAdjArgs a,
 }  // namespace
 
 // number of n-sized double sections of the VE adjoint state
-constexpr int kVeAdjSections = 74;
+constexpr int kVeAdjSections = 78;
 
 int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avClean, const sphgb_seeds* s,
               sphgb_grads* g, int deterministic)
@@ -1142,6 +1187,14 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     a.gamma = c->prm.gamma;
     a.av = AvPrm{c->K, c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant};
     a.box = c->box;
+    {  // FP32 error of a position difference: a few ulp of the largest coordinate plus a box edge
+        double xmax = 0.0, lmax = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            xmax = fmax(xmax, fmax(fabs(c->box.lo[k]), fabs(c->box.hi[k])));
+            lmax = fmax(lmax, c->box.L[k]);
+        }
+        a.ePos = float(4.0 * 0x1p-24 * (xmax + lmax) * 1.001);
+    }
     a.avClean = avClean ? 1 : 0;
     a.lv = listView(c);
     a.tOff = c->tOff.as<uint32_t>();
@@ -1205,6 +1258,9 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
     a.Som = take(1);
     a.Sr0 = take(1);
     a.R0b = take(1);
+    a.xc32 = reinterpret_cast<float4*>(take(2));
+    a.v32 = reinterpret_cast<float4*>(take(2));
+    if ((reinterpret_cast<uintptr_t>(a.xc32) | reinterpret_cast<uintptr_t>(a.v32)) & 15) return SPHGB_ERR_STATE;
     if (q - st > int64_t(kVeAdjSections) * n) return SPHGB_ERR_TOO_LARGE;  // layout and size disagree
 
     for (double* z : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h, g->u})

@@ -146,13 +146,16 @@ def test_ve_adjoint_matches_central_differences(av_clean):
 
 
 @pytest.mark.parametrize("av_clean", [False, True])
-@pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided"])
+@pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided", "large-h"])
 def test_ve_adjoint_tape_matches_recomputed_sums(av_clean, form):
     """the forward passes' tape (sphgb_set_adjoint_tape) against the adjoint's own re-summation:
-    same gradients to rounding, and with a du seed the energy pre-pass is not launched"""
+    same gradients to rounding (vsig_i and its pair found through the FP32 filter, or in FP64 when
+    2h > L/4 as in the 5^3 set), and with a du seed the energy pre-pass is not launched"""
     import torch
-    wl, ctx, sw, rho_t = setup(side=10, seed=13, av_clean=av_clean, deterministic=form == "two-sided",
-                               ordered_forward=form == "scatter")
+    wl, ctx, sw, rho_t = setup(side=5 if form == "large-h" else 10, seed=13, av_clean=av_clean,
+                               deterministic=form == "two-sided", ordered_forward=form == "scatter")
+    if form == "large-h":
+        assert 2.0 * float(sw.d.h.min()) > 0.25 * float(wl.box[1] - wl.box[0])
     gen = torch.Generator(device="cpu").manual_seed(4)
     s_du = torch.randn(wl.n, generator=gen, dtype=torch.float64).to("cuda:0")
 
