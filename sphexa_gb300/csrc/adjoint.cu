@@ -460,7 +460,8 @@ __device__ __forceinline__ double lookupSlopeT(const double2* __restrict__ tab, 
     return lookupSlope(tab, v, slope);
 }
 
-// the mixed forward's FP32 interval (lookupX32): k = int(v / dx), value and slope of that interval
+// FP32 interval of the 20000-entry linear table that the FP64 passes interpolate: k = int(v / dx),
+// value and slope of that interval (the mixed forward's cubic pieces agree with it to ~1e-8)
 __device__ __forceinline__ float lookupSlopeT(const float2* __restrict__ tab, float v, float& slope)
 {
     constexpr int nInt = kTableSize - 1;

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         double xm = mi / (rho0 * K * h3Inv);
         st<double>(out, i, StoreRho ? mi / xm : xm);
     } else {
-        const float2* tab = static_cast<const float2*>(wh);
+        const float4* tab = static_cast<const float4*>(wh);
         auto t = cm.target(i);
         float mi = ld<float>(m, i);
         KSum rho0;
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
             float rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            rho0.add(lookupX32(tab, dist * t.hInv) * ld<float>(m, j));
+            rho0.add(lookupH32(tab, dist * t.hInv) * ld<float>(m, j));
         }
         double hi = double(ld<float>(h, i));
         double rho = rho0.value64() * K / (hi * hi * hi);
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
         st<double>(o.c23, i, cc[4]);
         st<double>(o.c33, i, cc[5]);
     } else {
-        const float2* tab = static_cast<const float2*>(wh);
+        const float4* tab = static_cast<const float4*>(wh);
         auto t = cm.target(i);
         KSum t11, t12, t13, t22, t23, t33;
         for (unsigned k = 0; k < nc; ++k) {
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
             float rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            float w = lookupX32(tab, dist * t.hInv);
+            float w = lookupH32(tab, dist * t.hInv);
             float vw = ld<float>(vol, j) * w;
             t11.add(rx * rx * vw);
             t12.add(rx * ry * vw);
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
         }
     } else {
         auto t = cm.target(i);
-        const float2* tab2 = reinterpret_cast<const float2*>(a.wh);
+        const float4* tab2 = reinterpret_cast<const float4*>(a.wh);
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         KSum mx, my, mz, en;
         for (unsigned k = 0; k < nc; ++k) {
@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
             T v1 = dist * hiInv, v2 = dist * hjInv;
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            T Wi = hiInv3 * lookupX32(tab2, v1);
-            T Wj = (hjInv * hjInv * hjInv) * lookupX32(tab2, v2);
+            T Wi = hiInv3 * lookupH32(tab2, v1);
+            T Wj = (hjInv * hjInv * hjInv) * lookupH32(tab2, v2);
             T a1i = c11i * rx + c12i * ry + c13i * rz;
             T a2i = c12i * rx + c22i * ry + c23i * rz;
             T a3i = c13i * rx + c23i * ry + c33i * rz;
@@ -366,7 +366,7 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
     lv.last = last;
     CoordFp64 cf = coordFp64(c, p);
     CoordMixed cm = coordMixed(c);
-    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whx32.p;
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
     unsigned blocks = gridFor(last - first, kPairBlock);
     // pair-once for the VE xmass; the std density keeps the order-fixed walk
     if (std::is_same_v<P, Fp64Tag> && !storeRho && pairOnce(c, p, first, last)) {
@@ -402,7 +402,7 @@ int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     ListView lv = listView(c);
     lv.first = first;
     lv.last = last;
-    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whx32.p;
+    const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
     iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
         lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, c->K,
         IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
@@ -431,7 +431,7 @@ int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, d
     a.c22 = p->c22;
     a.c23 = p->c23;
     a.c33 = p->c33;
-    a.wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whx32.p;
+    a.wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
     a.hInv64 = c->hInv64.as<double>();
     a.aux = c->aux.p;
     a.n = p->n;

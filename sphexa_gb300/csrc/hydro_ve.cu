@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         st<double>(kxOut, i, kxi);
         st<double>(gradhOut, i, 1.0 - dhdrho * whomega);
     } else {
-        const float2 *tw = static_cast<const float2*>(wh), *tdw = static_cast<const float2*>(whd);
+        const float4 *tw = static_cast<const float4*>(wh), *tdw = static_cast<const float4*>(whd);
         auto t = cm.target(i);
         float mi = ld<float>(m, i), xmi = ld<float>(xm, i);
         KSum kx, whom, wr0;
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             float v = dist * t.hInv;
             float w, dw;
-            lookupX32Pair(tw, tdw, v, w, dw);
+            lookupH32Pair(tw, tdw, v, w, dw);
             float dterh = -(3.f * w + v * dw);
             float xmj = ld<float>(xm, j);
             kx.add(w * xmj);
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
         }
     } else {
         using T = float;
-        const float2* tab = static_cast<const float2*>(a.wh);
+        const float4* tab = static_cast<const float4*>(a.wh);
         auto t = cm.target(i);
         const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
         // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp
             T rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            T w = lookupX32(tab, dist * t.hInv);
+            T w = lookupH32(tab, dist * t.hInv);
             T vw = ld<T>(a.vol, j) * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             t11.add(rx * rxv);
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + ld<T>(a.c, j) - 3.f * rv * rinv);
             T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) *
-                   lookupX32(reinterpret_cast<const float2*>(a.wh), dist * t.hInv);
+                   lookupH32(reinterpret_cast<const float4*>(a.wh), dist * t.hInv);
             sx.add(fw * rx);
             sy.add(fw * ry);
             sz.add(fw * rz);
@@ -679,8 +679,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T dist = r2 * rinv;
             T vxij = vxi - pv.x, vyij = vyi - pv.y, vzij = vzi - pv.z;
             T v1 = dist * hiInv, v2 = dist * hjInv;
-            T Wi = hiInv3 * lookupX32(reinterpret_cast<const float2*>(a.wh), v1);
-            T Wj = (hjInv * hjInv * hjInv) * lookupX32(reinterpret_cast<const float2*>(a.wh), v2);
+            T Wi = hiInv3 * lookupH32(reinterpret_cast<const float4*>(a.wh), v1);
+            T Wj = (hjInv * hjInv * hjInv) * lookupH32(reinterpret_cast<const float4*>(a.wh), v2);
             T gix = c11i * rx + c12i * ry + c13i * rz;
             T giy = c12i * rx + c22i * ry + c23i * rz;
             T giz = c13i * rx + c23i * ry + c33i * rz;
@@ -1109,7 +1109,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     }
     if (p->precision == SPHGB_MIXED) {
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                    p->xm, c->whx32.p, c->whdx32.p, c->K, p->kx,
+                                                                    p->xm, c->whH32.p, c->whdH32.p, c->K, p->kx,
                                                                     p->gradh);
         SPHGB_TRY(launched(c, "gradhKernel"));
         if (first == 0 && last == p->n) return refineMixedGradh(c, p);
@@ -1192,7 +1192,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     }
     unsigned blocks = gridFor(last - first, kPairBlock);
     if (mixed) {
-        a.wh = c->whx32.p;
+        a.wh = c->whH32.p;
         const bool refine = c->refineMixed && first == 0 && last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
         if (refine) {
             SPHGB_TRY(c->divvBound.ensure(sizeof(float) * size_t(p->n)));
@@ -1232,7 +1232,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         a.tapeN = p->n;
     }
     if (mixed) {
-        a.wh = c->whx32.p;
+        a.wh = c->whH32.p;
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else if (pairOnce(c, p, first, last)) {
         const int64_t n = p->n;
@@ -1302,7 +1302,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     auto cf = coordFp64(c, p);
     auto cm = coordMixed(c);
     if (mixed) {
-        a.wh = c->whx32.p;
+        a.wh = c->whH32.p;
         SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));
         meVePackKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>());
         SPHGB_TRY(launched(c, "meVePackKernel"));
