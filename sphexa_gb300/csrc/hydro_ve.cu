@@ -208,7 +208,8 @@ struct IadDivvArgs {
 };
 
 template<class P>
-__global__ void __launch_bounds__(kPairBlock) iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
+__global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
+iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
