@@ -207,6 +207,51 @@ struct IadDivvArgs {
     int64_t tapeN;
 };
 
+// FP64 epilogue of IAD + divv/curlv for particle i from its sums tau = sum vol_j W r r^T and
+// M = sum xm_j W (v_j - v_i) r^T: c_i = tau^-1 (iad_kern.hpp), dV = -M c_i and its trace, curl and
+// symmetric part (divv_curlv_kern.hpp), and the adjoint tape's copy of M
+__device__ __forceinline__ void iadEpilogue64(const IadDivvArgs& a, int64_t i, double hi, const double tau[6],
+                                              const double M[9])
+{
+    using T = double;
+    const T hiInv = 1.0 / hi;
+    if (a.tapeP) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) a.tapeP[q * a.tapeN + i] = M[q];
+    }
+    T cc[6];
+    iadInvert<T>(tau[0], tau[1], tau[2], tau[3], tau[4], tau[5], hi, a.K, cc);
+    st<T>(a.c11, i, cc[0]);
+    st<T>(a.c12, i, cc[1]);
+    st<T>(a.c13, i, cc[2]);
+    st<T>(a.c22, i, cc[3]);
+    st<T>(a.c23, i, cc[4]);
+    st<T>(a.c33, i, cc[5]);
+    // dV[a][b] = -sum_c c_bc M[a][c]
+    const T C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
+    T dVx[3], dVy[3], dVz[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        dVx[b] = -(C[b][0] * M[0] + C[b][1] * M[1] + C[b][2] * M[2]);
+        dVy[b] = -(C[b][0] * M[3] + C[b][1] * M[4] + C[b][2] * M[5]);
+        dVz[b] = -(C[b][0] * M[6] + C[b][1] * M[7] + C[b][2] * M[8]);
+    }
+    T nk = a.K * (hiInv * hiInv * hiInv) / ld<T>(a.kx, i);
+    st<T>(a.divv, i, nk * (dVx[0] + dVy[1] + dVz[2]));
+    if (a.curlv) {
+        T cv0 = dVz[1] - dVy[2], cv1 = dVx[2] - dVz[0], cv2 = dVy[0] - dVx[1];
+        st<T>(a.curlv, i, nk * sqrt(cv0 * cv0 + (cv1 * cv1 + cv2 * cv2)));
+    }
+    if (a.dV11) {
+        st<T>(a.dV11, i, nk * dVx[0]);
+        st<T>(a.dV12, i, nk * (dVx[1] + dVy[0]));
+        st<T>(a.dV13, i, nk * (dVx[2] + dVz[0]));
+        st<T>(a.dV22, i, nk * dVy[1]);
+        st<T>(a.dV23, i, nk * (dVy[2] + dVz[1]));
+        st<T>(a.dV33, i, nk * dVz[2]);
+    }
+}
+
 template<class P>
 __global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
 iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
@@ -219,7 +264,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         using T = double;
         const double2* tab = static_cast<const double2*>(a.wh);
         auto t = cf.target(i);
-        T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi;
+        T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
         const T hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
@@ -254,41 +299,8 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             M[7] += sz * ry;
             M[8] += sz * rz;
         }
-        if (a.tapeP) {
-#pragma unroll
-            for (int q = 0; q < 9; ++q) a.tapeP[q * a.tapeN + i] = M[q];
-        }
-        T cc[6];
-        iadInvert<T>(t11, t12, t13, t22, t23, t33, hi, a.K, cc);
-        st<T>(a.c11, i, cc[0]);
-        st<T>(a.c12, i, cc[1]);
-        st<T>(a.c13, i, cc[2]);
-        st<T>(a.c22, i, cc[3]);
-        st<T>(a.c23, i, cc[4]);
-        st<T>(a.c33, i, cc[5]);
-        // dV[a][b] = -sum_c c_bc M[a][c]
-        const T C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
-        T dVx[3], dVy[3], dVz[3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            dVx[b] = -(C[b][0] * M[0] + C[b][1] * M[1] + C[b][2] * M[2]);
-            dVy[b] = -(C[b][0] * M[3] + C[b][1] * M[4] + C[b][2] * M[5]);
-            dVz[b] = -(C[b][0] * M[6] + C[b][1] * M[7] + C[b][2] * M[8]);
-        }
-        T nk = a.K * hiInv3 / ld<T>(a.kx, i);
-        st<T>(a.divv, i, nk * (dVx[0] + dVy[1] + dVz[2]));
-        if (a.curlv) {
-            T cv0 = dVz[1] - dVy[2], cv1 = dVx[2] - dVz[0], cv2 = dVy[0] - dVx[1];
-            st<T>(a.curlv, i, nk * sqrt(cv0 * cv0 + (cv1 * cv1 + cv2 * cv2)));
-        }
-        if (a.dV11) {
-            st<T>(a.dV11, i, nk * dVx[0]);
-            st<T>(a.dV12, i, nk * (dVx[1] + dVy[0]));
-            st<T>(a.dV13, i, nk * (dVx[2] + dVz[0]));
-            st<T>(a.dV22, i, nk * dVy[1]);
-            st<T>(a.dV23, i, nk * (dVy[2] + dVz[1]));
-            st<T>(a.dV33, i, nk * dVz[2]);
-        }
+        const double tau[6] = {t11, t12, t13, t22, t23, t33};
+        iadEpilogue64(a, i, hi, tau, M);
     } else {
         using T = float;
         const float4* tab = static_cast<const float4*>(a.wh);
@@ -847,6 +859,96 @@ __global__ void gradhEosFinish(int64_t n, const double* h, const double* m, cons
     veAuxAll<double>(n, i, mi, kxi, xmi, prhoi, aux);
 }
 
+// FP64 IAD + divv/curlv with one evaluation per mutual pair over the owned lists.  i adds
+// vol_j W_i r r^T and xm_j W_i (v_j - v_i) r^T (r = x_i - x_j); a mutual pair also gives j
+// vol_i W_j r r^T and xm_i W_j (v_j - v_i) r^T (r and the velocity difference both change sign) by
+// FP64 atomics.  The inversion and divv/curlv follow per particle in iadOnceFinish.
+__global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, IadDivvArgs a,
+                                                             const double* hInv64, int64_t n, double* acc)
+{
+    const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= lv.last) return;
+    const int64_t ii = i - lv.first;
+    const unsigned no = ov.size(ii);
+    const double2* tab = static_cast<const double2*>(a.wh);
+    const double* hInvDx = hInv64 + 2 * n;
+    const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
+                 *vz = static_cast<const double*>(a.vz), *xm = static_cast<const double*>(a.xm),
+                 *vol = static_cast<const double*>(a.vol);
+    auto t = cf.target(i);
+    const double hi = ld<double>(a.h, i), twoH = 2.0 * hi, hiInvDx = hInvDx[i];
+    const bool wrap = cf.needsWrap(t, twoH);
+    const double vxi = vx[i], vyi = vy[i], vzi = vz[i], voli = vol[i], xmi = xm[i];
+    double tau[6] = {0, 0, 0, 0, 0, 0}, M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (unsigned k = 0; k < no; ++k) {
+        bool mutual;
+        const uint32_t j = ov.at(ii, k, mutual);
+        double rx, ry, rz;
+        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double dist = r2 * invDist(r2);
+        const double dvx = vx[j] - vxi, dvy = vy[j] - vyi, dvz = vz[j] - vzi;
+        {
+            const double w = lookupX(tab, dist * hiInvDx);
+            const double vw = vol[j] * w, xw = xm[j] * w;
+            const double rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
+            tau[0] += rx * rxv;
+            tau[1] += ry * rxv;
+            tau[2] += rz * rxv;
+            tau[3] += ry * ryv;
+            tau[4] += rz * ryv;
+            tau[5] += rz * rzv;
+            const double sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
+            M[0] += sx * rx;
+            M[1] += sx * ry;
+            M[2] += sx * rz;
+            M[3] += sy * rx;
+            M[4] += sy * ry;
+            M[5] += sy * rz;
+            M[6] += sz * rx;
+            M[7] += sz * ry;
+            M[8] += sz * rz;
+        }
+        if (mutual) {
+            const double w = lookupX(tab, dist * __ldg(hInvDx + j));
+            const double vw = voli * w, xw = xmi * w;
+            const double rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
+            atomicAdd(acc + j, rx * rxv);
+            atomicAdd(acc + n + j, ry * rxv);
+            atomicAdd(acc + 2 * n + j, rz * rxv);
+            atomicAdd(acc + 3 * n + j, ry * ryv);
+            atomicAdd(acc + 4 * n + j, rz * ryv);
+            atomicAdd(acc + 5 * n + j, rz * rzv);
+            const double sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
+            atomicAdd(acc + 6 * n + j, sx * rx);
+            atomicAdd(acc + 7 * n + j, sx * ry);
+            atomicAdd(acc + 8 * n + j, sx * rz);
+            atomicAdd(acc + 9 * n + j, sy * rx);
+            atomicAdd(acc + 10 * n + j, sy * ry);
+            atomicAdd(acc + 11 * n + j, sy * rz);
+            atomicAdd(acc + 12 * n + j, sz * rx);
+            atomicAdd(acc + 13 * n + j, sz * ry);
+            atomicAdd(acc + 14 * n + j, sz * rz);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) atomicAdd(acc + q * n + i, tau[q]);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) atomicAdd(acc + (6 + q) * n + i, M[q]);
+}
+
+__global__ void iadOnceFinish(int64_t first, int64_t last, int64_t n, IadDivvArgs a, const double* acc)
+{
+    const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    double tau[6], M[9];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) tau[q] = acc[q * n + i];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) M[q] = acc[(6 + q) * n + i];
+    iadEpilogue64(a, i, ld<double>(a.h, i), tau, M);
+}
+
 // FP64 AV switches with one evaluation per mutual pair over the owned lists.  i's sum is
 // S_i = sum vol_j (divv_i - divv_j) W_i r (r = x_i - x_j; c_i is applied after the walk), j's term of
 // the same pair is vol_i (divv_i - divv_j) W_j r (r and the divv difference both change sign);
@@ -1207,6 +1309,16 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
         SPHGB_TRY(tapeFor(c, p, first, last, kTapeIad, &a.tapeP));
         if (a.tapeP) a.tapeP += int64_t(kTapeP) * p->n;
         a.tapeN = p->n;
+        if (pairOnce(c, p, first, last)) {
+            const int64_t n = p->n;
+            SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 15 * size_t(n)));
+            SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 15 * size_t(n), c->stream));
+            iadOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, ownedView(c), coordFp64(c, p), a,
+                                                                 c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+            SPHGB_TRY(launched(c, "iadOnceKernel"));
+            iadOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
+            return launched(c, "iadOnceFinish");
+        }
         iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     }
     return launched(c, "iadDivvKernel");

@@ -205,7 +205,7 @@ def test_sedov_50_cubed_against_oracle(gpu_ctx, port, variant):
 @pytest.mark.parametrize("case", ["fourier", "sphere", "random_open_capped"])
 def test_pair_once_passes_match_ordered_sums(gpu_ctx, case):
     """The FP64 VE passes with one evaluation per mutual pair (owned lists, FP64 atomics: xmass,
-    gradh, AV switches, momentum-energy) against the order-fixed passes on the same lists:
+    gradh, IAD + divv/curlv, AV switches, momentum-energy) against the order-fixed passes on the same lists:
     rounding-level agreement of every output, identical Courant dt, and the pair-once kernels are
     the ones that ran (one extra finishing launch per pass)."""
     from sphexa_gb300 import sph, workloads as W
@@ -214,7 +214,7 @@ def test_pair_once_passes_match_ordered_sums(gpu_ctx, case):
           "random_open_capped": lambda: W.random_cube(6000, seed=55, periodic=False, h=0.09)}[case]()
     ctx = gpu_ctx
     ctx.set_params(ngmax=wl.params["ngmax"], ng0=wl.params["ng0"])
-    fields = ("xm", "kx", "gradh", "prho", "alpha", "ax", "ay", "az", "du")
+    fields = ("xm", "kx", "gradh", "prho", "c11", "c12", "c23", "divv", "curlv", "alpha", "ax", "ay", "az", "du")
     out, launches = {}, {}
     for det in (True, False):
         ctx.set_deterministic(det)
@@ -234,7 +234,7 @@ def test_pair_once_passes_match_ordered_sums(gpu_ctx, case):
         out[det] = {f: getattr(d, f).cpu().numpy() for f in fields}
         out[det]["minDt"] = d.minDtCourant
     ctx.set_deterministic(False)
-    assert launches[False] == launches[True] + 4
+    assert launches[False] == launches[True] + 5
     ref = out[True]
     for f in fields:
         err = np.max(np.abs(out[False][f] - ref[f])) / field_scale(ref, f)
