@@ -100,11 +100,12 @@ int sphgb_create(sphgb_ctx** ctx, int device);
 int sphgb_destroy(sphgb_ctx* ctx);
 int sphgb_set_stream(sphgb_ctx* ctx, void* cuda_stream);
 int sphgb_set_params(sphgb_ctx* ctx, const sphgb_params* params);
-/* Summation order of the FP64 VE momentum-energy pass (no reference counterpart; the reference's
- * GPU pass is order-fixed, hydro_ve/momentum_energy_gpu.cu:53-144).  on = 0 (default): when the
- * lists cover every particle, each pair whose two ends list each other is evaluated once and the
- * neighbour's share is added with FP64 atomics, so the last bits of ax ay az du can differ from
- * run to run.  on = 1: every list owner sums its own pairs in list order, bitwise reproducible. */
+/* Summation order of the FP64 VE passes xmass, gradh, IAD + divv/curlv, AV switches and
+ * momentum-energy (no reference counterpart; the reference's GPU passes are order-fixed, e.g.
+ * hydro_ve/momentum_energy_gpu.cu:53-144).  on = 0 (default): when the lists cover every particle,
+ * each pair whose two ends list each other is evaluated once and the neighbour's share is added
+ * with FP64 atomics, so the last bits of those passes' outputs can differ from run to run.
+ * on = 1: every list owner sums its own pairs in list order, bitwise reproducible. */
 int sphgb_set_deterministic(sphgb_ctx* ctx, int32_t on);
 /* Forward tape of the VE adjoint (no reference counterpart).  on = 1: the FP64 VE passes over all
  * particles (gradh, IAD + divv/curlv, AV switches, momentum-energy) keep the per-particle sums

@@ -77,7 +77,8 @@ class Context:
 
     def set_deterministic(self, on: bool) -> None:
         """True: every pass sums in list order (bitwise reproducible); False (default): the FP64 VE
-        momentum-energy pass evaluates mutual pairs once and scatters with FP64 atomics."""
+        xmass, gradh, IAD + divv/curlv, AV and momentum-energy passes evaluate mutual pairs once and
+        scatter with FP64 atomics."""
         check(self.lib.sphgb_set_deterministic(self.h, int(bool(on))), "sphgb_set_deterministic")
 
     def set_adjoint_tape(self, on: bool) -> None:
