@@ -151,13 +151,20 @@ def test_ve_adjoint_tape_matches_recomputed_sums(av_clean, form):
     """the forward passes' tape (sphgb_set_adjoint_tape) against the adjoint's own re-summation:
     same gradients to rounding (vsig_i and its pair found through the FP32 filter, or in FP64 when
     2h > L/4 as in the 5^3 set), and with a du seed the energy pre-pass is not launched"""
-    import torch
     wl, ctx, sw, rho_t = setup(side=5 if form == "large-h" else 10, seed=13, av_clean=av_clean,
                                deterministic=form == "two-sided", ordered_forward=form == "scatter")
     if form == "large-h":
         assert 2.0 * float(sw.d.h.min()) > 0.25 * float(wl.box[1] - wl.box[0])
+    _tape_vs_resummed(ctx, sw, wl.n, rho_t)
+    ctx.close()
+
+
+def _tape_vs_resummed(ctx, sw, n, rho_t):
+    """backward with the forward tape, then with the tape off: same gradients to rounding, and
+    without the energy pre-pass when the tape holds the momentum-energy sums"""
+    import torch
     gen = torch.Generator(device="cpu").manual_seed(4)
-    s_du = torch.randn(wl.n, generator=gen, dtype=torch.float64).to("cuda:0")
+    s_du = torch.randn(n, generator=gen, dtype=torch.float64).to("cuda:0")
 
     def grads():
         vals = sw.inputs()
@@ -175,4 +182,21 @@ def test_ve_adjoint_tape_matches_recomputed_sums(av_clean, form):
         err = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-300)
         print(f"tape vs re-summed {f:3s}: normwise rel {err:.3e}")
         assert err <= 1e-12, f
+
+
+def test_ve_adjoint_tape_open_box():
+    """the tape and the FP32-filtered signal-velocity walk in an open box (no periodic images),
+    random positions with Gaussian velocities"""
+    import torch
+    from sphexa_gb300 import autograd as AG, sph, workloads as W
+    wl = W.random_cube(3000, seed=61, periodic=False)
+    ctx = sph.Context(0)
+    ctx.set_params(minDt=1e-2, ngmax=250)
+    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+    box = sph.Box(wl.box.copy(), wl.bc.copy())
+    sw = AG.FrozenVeSweep(ctx, d, box)
+    sw.freeze()
+    assert ctx.stats()["capped"] == 0
+    rho_t = torch.ones(wl.n, dtype=torch.float64, device="cuda:0") * float(d.m.sum().item())
+    _tape_vs_resummed(ctx, sw, wl.n, rho_t)
     ctx.close()
