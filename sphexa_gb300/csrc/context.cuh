@@ -136,7 +136,7 @@ struct sphgb_ctx {
 
     // kernel tables W and dW/dv, FP64 and FP32, interleaved {t[k], t[k+1] - t[k]}
     sphgb::DBuf whx64, whdx64;
-    sphgb::DBuf whx32, whdx32;
+    sphgb::DBuf whx32;  // FP32 linear table (the mixed adjoint)
     sphgb::DBuf whH32, whdH32;  // mixed passes: cubic pieces of W and dW/dv (kHermIntervals float4)
 
     // mixed precision grid-local coordinates: packed cell (21 bits per axis) + float4 {dx,dy,dz,1/h}

@@ -60,7 +60,7 @@ int buildTables(sphgb_ctx* c)
 {
     const double n = c->prm.sincIndex;
     std::vector<double> wh(kTableSize), whd(kTableSize);
-    std::vector<float> wf(kTableSize), wdf(kTableSize);
+    std::vector<float> wf(kTableSize);
     // tabulateFunction on [0, 2] (sph/include/sph/sph_kernel_tables.hpp:81-95)
     const double dx = (2.0 - 0.0) / (kTableSize - 1);
     for (int i = 0; i < kTableSize; ++i) {
@@ -68,7 +68,6 @@ int buildTables(sphgb_ctx* c)
         wh[i] = std::pow(sincStd(v), n);
         whd[i] = n * std::pow(sincStd(v), n - 1) * sincStdDeriv(v);
         wf[i] = float(wh[i]);
-        wdf[i] = float(whd[i]);
     }
     c->K = kernelNormalisation(n);
     // lookups read {t[k], t[k+1] - t[k]} in one load; the difference is the one the reference
@@ -81,18 +80,16 @@ int buildTables(sphgb_ctx* c)
         wdx[2 * i] = whd[i];
         wdx[2 * i + 1] = last ? 0.0 : whd[i + 1] - whd[i];
     }
-    std::vector<float> wx32(2 * kTableSize), wdx32(2 * kTableSize);
+    // FP32 copy of the linear table for the mixed adjoint, which differentiates the interpolant of
+    // the FP64 passes
+    std::vector<float> wx32(2 * kTableSize);
     for (int i = 0; i < kTableSize; ++i) {
         const bool last = i + 1 == kTableSize;
         wx32[2 * i] = wf[i];
         wx32[2 * i + 1] = last ? 0.f : wf[i + 1] - wf[i];
-        wdx32[2 * i] = wdf[i];
-        wdx32[2 * i + 1] = last ? 0.f : wdf[i + 1] - wdf[i];
     }
     SPHGB_TRY(c->whx32.ensure(sizeof(float) * 2 * kTableSize));
-    SPHGB_TRY(c->whdx32.ensure(sizeof(float) * 2 * kTableSize));
     SPHGB_CUDA(cudaMemcpy(c->whx32.p, wx32.data(), sizeof(float) * 2 * kTableSize, cudaMemcpyHostToDevice));
-    SPHGB_CUDA(cudaMemcpy(c->whdx32.p, wdx32.data(), sizeof(float) * 2 * kTableSize, cudaMemcpyHostToDevice));
     {  // the mixed passes' cubic pieces of W and dW/dv
         std::vector<float> hw, hd;
         tables::hermitePieces(n, kHermIntervals, hw, hd);
