@@ -241,8 +241,8 @@ def run_reference(args) -> None:
         return
     side = args.cpu_side
     vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_baseline(max(side // 2, 20), workload=args.workload, variant=args.variant)
+    for _ in range(args.warmup):  # untimed, the same bounded sample as a timed step
+        cpu_baseline(side, workload=args.workload, variant=args.variant)
     t_all = time.perf_counter()
     last = None
     for _ in range(args.steps):
