@@ -76,11 +76,20 @@ int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 }
 
 // ---------------------------------------------------------------- gradh (kx, gradh)
+// neighbour-side fields of the mixed gradh pass as one 8-byte record {xm m} per particle
+__global__ void packGradhKernel(int64_t n, const void* xm, const void* m, float2* __restrict__ rec)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    rec[j] = make_float2(ld<float>(xm, j), ld<float>(m, j));
+}
+
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
                                                           const void* m, const void* xm, const void* wh,
                                                           const void* whd, double K, void* kxOut, void* gradhOut,
-                                                          double* tapeWom = nullptr, double* tapeWr0 = nullptr)
+                                                          double* tapeWom = nullptr, double* tapeWr0 = nullptr,
+                                                          const float2* rec = nullptr)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -137,10 +146,10 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             float w, dw;
             lookupH32Pair(tw, tdw, v, w, dw);
             float dterh = -(3.f * w + v * dw);
-            float xmj = ld<float>(xm, j);
-            kx.add(w * xmj);
-            whom.add(dterh * xmj);
-            wr0.add(dterh * ld<float>(m, j));
+            const float2 Q = rec[j];  // {xm m}
+            kx.add(w * Q.x);
+            whom.add(dterh * Q.x);
+            wr0.add(dterh * Q.y);
         }
         double hi = double(ld<float>(h, i)), hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
         double kxi = kx.value64() * (K * h3Inv);
@@ -205,7 +214,17 @@ struct IadDivvArgs {
     void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
     double* tapeP;  // FP64: P_i = sum xm_j W (v_j - v_i) r^T for the VE adjoint (9 x tapeN), or null
     int64_t tapeN;
+    const float4* rec;  // mixed: neighbour records {vx vy vz vol} (packIadKernel)
 };
+
+// neighbour-side fields of the mixed IAD + divv/curlv pass as one 16-byte record per particle
+__global__ void packIadKernel(int64_t n, const void* vx, const void* vy, const void* vz, const void* vol,
+                              float4* __restrict__ rec)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    rec[j] = make_float4(ld<float>(vx, j), ld<float>(vy, j), ld<float>(vz, j), ld<float>(vol, j));
+}
 
 // FP64 epilogue of IAD + divv/curlv for particle i from its sums tau = sum vol_j W r r^T and
 // M = sum xm_j W (v_j - v_i) r^T: c_i = tau^-1 (iad_kern.hpp), dV = -M c_i and its trace, curl and
@@ -314,9 +333,10 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz, hjInv;
             cm.diff(t, j, rx, ry, rz, hjInv);
+            const float4 R = a.rec[j];  // {vx vy vz vol}
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             T w = lookupH32(tab, dist * t.hInv);
-            T vw = ld<T>(a.vol, j) * w;
+            T vw = R.w * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             t11.add(rx * rxv);
             t12.add(ry * rxv);
@@ -325,7 +345,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             t23.add(rz * ryv);
             t33.add(rz * rzv);
             T xw = ld<T>(a.xm, j) * w;
-            const T dvx = ld<T>(a.vx, j) - vxi, dvy = ld<T>(a.vy, j) - vyi, dvz = ld<T>(a.vz, j) - vzi;
+            const T dvx = R.x - vxi, dvy = R.y - vyi, dvz = R.z - vzi;
             T sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
             Aabs = fmaf(fabsf(xw) * (fabsf(dvx) + fabsf(dvy) + fabsf(dvz)), fabsf(rx) + fabsf(ry) + fabsf(rz), Aabs);
             M[0].add(sx * rx);
@@ -392,7 +412,18 @@ struct AvArgs {
     void* alpha;
     double* tapeG;  // FP64: G_i (3 x tapeN) for the VE adjoint, or null
     int64_t tapeN;
+    const float4* rec;   // mixed: neighbour records {vx vy vz c} and {vol divv} (packAvKernel)
+    const float2* rec2;
 };
+
+// neighbour-side fields of the mixed AV-switch pass as a 16-byte and an 8-byte record per particle
+__global__ void packAvKernel(int64_t n, AvArgs a, float4* __restrict__ rec, float2* __restrict__ rec2)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    rec[j] = make_float4(ld<float>(a.vx, j), ld<float>(a.vy, j), ld<float>(a.vz, j), ld<float>(a.c, j));
+    rec2[j] = make_float2(ld<float>(a.vol, j), ld<float>(a.divv, j));
+}
 
 // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
 template<class T>
@@ -465,11 +496,12 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
             T rinv = rsqrtf(r2);
             T dist = r2 * rinv;
-            T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
+            const float4 R = a.rec[j];   // {vx vy vz c}
+            const float2 Q = a.rec2[j];  // {vol divv}
+            T vxij = vxi - R.x, vyij = vyi - R.y, vzij = vzi - R.z;
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + ld<T>(a.c, j) - 3.f * rv * rinv);
-            T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) *
-                   lookupH32(reinterpret_cast<const float4*>(a.wh), dist * t.hInv);
+            if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + R.w - 3.f * rv * rinv);
+            T fw = Q.x * (divvi - Q.y) * lookupH32(reinterpret_cast<const float4*>(a.wh), dist * t.hInv);
             sx.add(fw * rx);
             sy.add(fw * ry);
             sz.add(fw * rz);
@@ -1211,9 +1243,13 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         return launched(c, "gradhOnceFinish");
     }
     if (p->precision == SPHGB_MIXED) {
+        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
+        float2* rec = reinterpret_cast<float2*>(c->pack.p);
+        packGradhKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->xm, p->m, rec);
+        SPHGB_TRY(launched(c, "packGradhKernel"));
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                     p->xm, c->whH32.p, c->whdH32.p, c->K, p->kx,
-                                                                    p->gradh);
+                                                                    p->gradh, nullptr, nullptr, rec);
         SPHGB_TRY(launched(c, "gradhKernel"));
         if (first == 0 && last == p->n) return refineMixedGradh(c, p);
         c->stats_refinedGradh = 0;
@@ -1301,6 +1337,11 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
             SPHGB_TRY(c->divvBound.ensure(sizeof(float) * size_t(p->n)));
             a.divvBound = c->divvBound.as<float>();
         }
+        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
+        a.rec = c->pack.as<float4>();
+        packIadKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->vx, p->vy, p->vz, a.vol,
+                                                                  c->pack.as<float4>());
+        SPHGB_TRY(launched(c, "packIadKernel"));
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
         SPHGB_TRY(launched(c, "iadDivvKernel"));
         return refineMixedDivv(c, p, refine ? a.divvBound : nullptr);
@@ -1346,6 +1387,12 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
     }
     if (mixed) {
         a.wh = c->whH32.p;
+        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
+        a.rec = c->pack.as<float4>();
+        a.rec2 = reinterpret_cast<const float2*>(c->pack.as<float4>() + p->n);
+        packAvKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>(),
+                                                                 reinterpret_cast<float2*>(c->pack.as<float4>() + p->n));
+        SPHGB_TRY(launched(c, "packAvKernel"));
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else if (pairOnce(c, p, first, last)) {
         const int64_t n = p->n;
