@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kThreads) radixScatterKernel(const u64* __rest
         const unsigned rankInWarp = __popc(peers & ((1u << lane) - 1u));
         if (valid && rankInWarp == 0) warpCnt[warp][digit] = __popc(peers);
         __syncthreads();
-        uint32_t total = 0;  // keys of digit tid in this round; warpCnt becomes the prefix over warps
+        uint32_t total = 0;  // keys of digit tid in this pass; warpCnt becomes the prefix over warps
 #pragma unroll
         for (int w = 0; w < kWarps; ++w) {
             const uint32_t t = warpCnt[w][tid];

@@ -10,7 +10,7 @@ reference headers (oracle/Makefile) and records
   * sweep_*.npz   - small seeded workloads (sphexa_gb300/workloads.py) run through the full
                     reference chain: keys, order, cornerstone leaves, octree, neighbour counts
                     and sorted sets, and every output field.
-The GPU machine has no reference sources; tests there compare against these files.
+Where the reference sources are absent, the tests compare against these files.
 
     python tests/golden/make_golden.py
 """
