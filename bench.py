@@ -349,6 +349,10 @@ def main() -> None:
                     "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
                     "algorithmic": f"{pairs} pairs x {flops_pp} flop/pair per launch",
                     "hbm_peak_gbs": peaks.get("hbm_gbs")}
+        if traffic and peaks.get("hbm_gbs"):  # the same kernel against HBM: DRAM bytes over its time
+            gbs = traffic * n / (st64[dom] * 1e-3) / 1e9
+            roofline["hbm_achieved_gbs"] = gbs
+            roofline["hbm_frac"] = gbs / peaks["hbm_gbs"]
     else:
         roofline = {"bound": "hbm", "kernel": names[dom], "achieved": None, "peak": peaks.get("hbm_gbs"),
                     "unit": "GB/s", "frac": None, "traffic": None}
