@@ -350,7 +350,7 @@ def main() -> None:
                     "algorithmic": f"{pairs} pairs x {flops_pp} flop/pair per launch",
                     "hbm_peak_gbs": peaks.get("hbm_gbs")}
         if traffic and peaks.get("hbm_gbs"):  # the same kernel against HBM: DRAM bytes over its time
-            gbs = traffic * n / (st64[dom] * 1e-3) / 1e9
+            gbs = float(traffic * n / (st64[dom] * 1e-3) / 1e9)
             roofline["hbm_achieved_gbs"] = gbs
             roofline["hbm_frac"] = gbs / peaks["hbm_gbs"]
     else:
