@@ -33,7 +33,9 @@ typedef enum {
     SPHGB_ERR_TRAVERSAL = 5,  /* octree traversal stack overflow (reference: 0xFFFFFFFF stack flag) */
     SPHGB_ERR_NOCONV = 6,     /* h / neighbour-count iteration did not converge for some particles */
     SPHGB_ERR_NOTFOUND = 7,   /* no CUDA device / extension not usable */
-    SPHGB_ERR_TOO_LARGE = 8   /* request exceeds a fixed capacity */
+    SPHGB_ERR_TOO_LARGE = 8,  /* request exceeds a fixed capacity */
+    SPHGB_ERR_INPUT = 9       /* a coordinate, h or box limit is not finite, or h <= 0; found by a check
+                                 pass before any key, tree or search kernel runs on the data */
 } sphgb_status;
 
 typedef enum { SPHGB_FP64 = 0, SPHGB_MIXED = 1 } sphgb_precision;
@@ -295,14 +297,18 @@ int sphgb_conserved_quantities(sphgb_ctx* ctx, const sphgb_particles* p, int64_t
  * No counterpart in the reference.  For callers that must not let a library call cudaMalloc or
  * cudaFree (their device memory is owned by their own pool allocator, or they cannot afford the
  * implicit device synchronisation of allocation inside a time-step loop): fits the open box
- * dimensions to the particle extrema like sphgb_domain_sync and writes the Hilbert key of every
- * particle, in input order, into `keys` (device, n entries).  x, y, z are device pointers;
- * `box` is a host struct, updated in place.  Needs no context and allocates nothing: its
- * reduction scratch is a fixed 3 MiB device array inside the library (held by every GPU that
- * loads it until the process exits), which caps n at 268,435,456; larger n returns
- * SPHGB_ERR_TOO_LARGE.  The first call on a device looks up that array's device address, so make
- * it before any stream capture.  Every call shares the array: calls that overlap on the GPU, on
- * one device, race.  Runs on `stream` (0 = legacy default) and returns after synchronising it. */
+ * dimensions to the particle extrema like the first sphgb_domain_sync of a simulation (it keeps no
+ * previous box, so the limitBoxShrinking of domain mode 1 does not apply) and writes the Hilbert
+ * key of every particle, in input order, into `keys` (device, n entries).  x, y, z are device
+ * pointers; `box` is a host struct, updated in place.  Needs no context and allocates nothing: its
+ * reduction scratch is a fixed 3 MiB device array inside the library (held by every GPU that loads
+ * it until the process exits), which caps n at 268,435,456; larger n returns SPHGB_ERR_TOO_LARGE.
+ * The first call on a device looks up that array's device address with cudaGetSymbolAddress (a
+ * runtime call that must not run while a stream is being captured), so make the first call on each
+ * device before any stream capture begins; the address is kept for the life of the process, so do
+ * not call this entry point on a device after cudaDeviceReset of that device.  Every call shares the
+ * array: calls that overlap on the GPU, on one device, race.  Runs on `stream` (0 = legacy default)
+ * and returns after synchronising it. */
 int sphgb_sfc_keys_noalloc(const double* x, const double* y, const double* z, int64_t n, sphgb_box* box,
                            uint64_t* keys, void* stream);
 

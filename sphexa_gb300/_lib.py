@@ -14,13 +14,16 @@ LIB_PATH = PKG / "libsphgb.so"
 
 SPHGB_OK = 0
 SPHGB_ERR_NOCONV = 6
+SPHGB_ERR_TOO_LARGE = 8
+SPHGB_ERR_INPUT = 9
 SPHGB_FP64, SPHGB_MIXED = 0, 1
 SPHGB_STD, SPHGB_VE = 0, 1
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "device allocation failed",
                 4: "call out of order", 5: "octree traversal stack overflow",
                 6: "h / neighbour-count iteration did not converge", 7: "no usable CUDA device",
-                8: "request exceeds a fixed capacity"}
+                8: "request exceeds a fixed capacity",
+                9: "non-finite coordinate, smoothing length or box limit, or h <= 0"}
 
 
 class SphgbBox(C.Structure):

@@ -74,6 +74,7 @@ const char* sphgb_status_string(int s)
     case SPHGB_ERR_NOCONV: return "h / neighbour-count iteration did not converge for some particles";
     case SPHGB_ERR_NOTFOUND: return "no usable CUDA device";
     case SPHGB_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+    case SPHGB_ERR_INPUT: return "non-finite coordinate, smoothing length or box limit, or h <= 0";
     default: return "unknown status";
     }
 }
@@ -141,7 +142,8 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pack,       &c->whx32,     &c->whH32, &c->whdH32,    &c->refMask,
-                    &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape};
+                    &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape,
+                    &c->checkWord};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -374,7 +376,11 @@ int sphgb_sweep(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box, int32_t varian
         t.stop();
         if (s != SPHGB_OK) return s;
     }
-    return sphgb_sweep_passes(c, p, variant, avClean, minDtCourant);
+    // the sync validated the fields and nothing can change them before the search of this call
+    c->inputsChecked = true;
+    const int s = sphgb_sweep_passes(c, p, variant, avClean, minDtCourant);
+    c->inputsChecked = false;
+    return s;
 }
 
 int sphgb_adjoint_std(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* seeds, sphgb_grads* grads,

@@ -162,6 +162,10 @@ struct sphgb_ctx {
 
     // device status word and small counters
     int* dFlags = nullptr;
+    // input validation word (validate.cu); inputsChecked: the fields were validated within the
+    // current sphgb_sweep call and cannot have changed since
+    sphgb::DBuf checkWord;
+    bool inputsChecked = false;
 
     // statistics and timing
     sphgb_stats stats{};
@@ -178,6 +182,9 @@ int applyOrder(sphgb_ctx* c, void* field, int esz);
 int buildTree(sphgb_ctx* c, bool rebalance);
 int buildTables(sphgb_ctx* c);
 int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last);
+// SPHGB_ERR_INPUT when a coordinate of [0, n) is not finite or h (if non-null) is not finite or <= 0
+int validateParticles(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int hIsFloat,
+                      int64_t n);
 int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,
                        int32_t hPrec, int64_t first, int64_t last, uint32_t ngmax, uint32_t* nbrOut, uint32_t* ncOut);
 int exportNeighbors(sphgb_ctx* c, uint32_t* out);

@@ -11,6 +11,8 @@
 #include <algorithm>
 
 
+#include <cmath>
+
 #include "context.cuh"
 
 namespace sphgb {
@@ -383,6 +385,10 @@ int domainSync(sphgb_ctx* c, sphgb_particles* p, sphgb_box* box)
     const int64_t n = p->n;
     if (n <= 0 || n >= (int64_t(1) << 31) || !p->x || !p->y || !p->z) return SPHGB_ERR_ARG;
     cudaStream_t st = c->stream;
+    for (int k = 0; k < 6; ++k)
+        if (!std::isfinite(box->lim[k])) return SPHGB_ERR_INPUT;
+    // no key, sort or tree kernel sees a non-finite coordinate or smoothing length
+    SPHGB_TRY(validateParticles(c, p->x, p->y, p->z, p->h, p->precision == SPHGB_MIXED, n));
     c->n = n;
 
     // box: periodic dims keep their limits, open dims take the particle extrema

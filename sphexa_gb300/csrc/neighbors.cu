@@ -748,6 +748,9 @@ int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
     if (!p->x || !p->y || !p->z || !p->h) return SPHGB_ERR_ARG;
     const uint32_t ngmax = c->prm.ngmax;
     if (c->prm.ng0 > ngmax) return SPHGB_ERR_ARG;  // reference: "ng0 should be smaller than ngmax"
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    if (!c->inputsChecked)
+        SPHGB_TRY(validateParticles(c, p->x, p->y, p->z, p->h, p->precision == SPHGB_MIXED, c->n));
     SPHGB_TRY(prepareLists(c, p->x, p->y, p->z, first, last, ngmax));
     const int64_t nWork = last - first;
     const int hf = p->precision == SPHGB_MIXED;
@@ -795,6 +798,8 @@ int findNeighborsFixed(sphgb_ctx* c, const double* x, const double* y, const dou
                        int64_t first, int64_t last, uint32_t ngmax, uint32_t* nbrOut, uint32_t* ncOut)
 {
     if (!x || !y || !z || !h || ngmax == 0) return SPHGB_ERR_ARG;
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    SPHGB_TRY(validateParticles(c, x, y, z, h, hPrec == SPHGB_MIXED, c->n));
     SPHGB_TRY(prepareLists(c, x, y, z, first, last, ngmax));
     const int64_t nWork = last - first;
     SPHGB_TRY(runSearch(c, x, y, z, h, hPrec == SPHGB_MIXED, first, last, ngmax, nullptr));
