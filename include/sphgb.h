@@ -120,6 +120,17 @@ int sphgb_set_adjoint_tape(sphgb_ctx* ctx, int32_t on);
  * FP32 error bound, with the neighbour shells their values depend on; on = 0 leaves the FP32
  * results.  The counts of the last sweep are in sphgb_stats.refined_gradh / refined_divv. */
 int sphgb_set_mixed_refinement(sphgb_ctx* ctx, int32_t on);
+/* Form of the kernel function W(v) and dW/dv in the FP64 pair passes and the FP64 adjoints (no
+ * reference counterpart).  SPHGB_KERNEL_TABLE (default): the reference's linear interpolant of its
+ * 20000-entry tables (sph/include/sph/table_lookup.hpp:10-26), whose slope jumps at every node
+ * (every 1e-4 in v).  SPHGB_KERNEL_SMOOTH: a cubic Hermite piece on each of the same intervals
+ * through the closed-form values and derivatives of sinc^n (sph_kernel_tables.hpp:77-157) at both
+ * nodes, so W and dW/dv are continuously differentiable and central differences of the forward
+ * passes converge to the adjoint's gradient; results differ from the table form by the table's
+ * interpolation error (within 2e-8 of
+ * the maximum of W and of |dW/dv|).  The mixed passes always use their own cubic pieces. */
+typedef enum { SPHGB_KERNEL_TABLE = 0, SPHGB_KERNEL_SMOOTH = 1 } sphgb_kernel_form;
+int sphgb_set_kernel_form(sphgb_ctx* ctx, int32_t form);
 /* Domain mode.  0 (default): every sphgb_domain_sync stands alone (open dimensions take the
  * particle extrema).  1: the syncs are the steps of one simulation, as cstone::Domain::sync
  * (domain/include/cstone/domain/assignment.hpp:80-82): from the second sync on, the open-dimension

@@ -30,7 +30,7 @@ sys.path[0] = str(HERE.parent)  # import `oracle` as the package at the reposito
 from oracle import oracle as O  # noqa: E402
 from sphexa_gb300 import workloads as W  # noqa: E402
 
-REF = Path(os.environ.get("SPHGB_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("SPHGB_REFERENCE", Path(__file__).resolve().parents[2] / "reference"))
 OJ = dict(xmass=0, gradh=1, iad_std=2, iad_ve=3, divv=4, av=5, me_std=6, me_ve=7)
 OPS = ["add", "mul", "div", "sqrt", "transc", "cmp"]
 

@@ -18,6 +18,8 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+# the reference checkout: $SPHGB_REFERENCE, else a directory "reference" beside the repository
+REFERENCE_DEFAULT = HERE.parent.parent / "reference"
 
 FIELDS = ["x", "y", "z", "h", "m", "u", "vx", "vy", "vz", "alpha",
           "rho", "p", "c", "c11", "c12", "c13", "c22", "c23", "c33",
@@ -56,9 +58,15 @@ def build_port() -> Path:
     return HERE / "liboracle.so"
 
 
+def build_port_timed() -> Path:
+    """Compile liboracle_o3.so: the same restatement with release flags, for the timed CPU baseline."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "liboracle_o3.so"], check=True)
+    return HERE / "liboracle_o3.so"
+
+
 def build_reference() -> bool:
     """Compile the reference-driven oracle if the reference sources are present here."""
-    ref = Path(os.environ.get("SPHGB_REFERENCE", "/root/reference"))
+    ref = Path(os.environ.get("SPHGB_REFERENCE", REFERENCE_DEFAULT))
     if not (ref / "domain" / "include" / "cstone").is_dir():
         return False
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref}"], check=True)
@@ -166,6 +174,14 @@ def port() -> Oracle:
     if not path.exists():
         build_port()
     return Oracle(path, "port")
+
+
+def port_timed() -> Oracle:
+    """the restatement built with release flags (timed CPU baseline only; parity uses port())"""
+    path = HERE / "liboracle_o3.so"
+    if not path.exists():
+        build_port_timed()
+    return Oracle(path, "port-O3")
 
 
 def reference(kind: str = "fp64") -> Oracle | None:

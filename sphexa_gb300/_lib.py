@@ -18,6 +18,7 @@ SPHGB_ERR_TOO_LARGE = 8
 SPHGB_ERR_INPUT = 9
 SPHGB_FP64, SPHGB_MIXED = 0, 1
 SPHGB_STD, SPHGB_VE = 0, 1
+SPHGB_KERNEL_TABLE, SPHGB_KERNEL_SMOOTH = 0, 1
 
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "device allocation failed",
                 4: "call out of order", 5: "octree traversal stack overflow",
@@ -88,6 +89,7 @@ SIGNATURES = {
     "sphgb_set_adjoint_tape": [_P, C.c_int32],
     "sphgb_set_mixed_refinement": [_P, C.c_int32],
     "sphgb_set_domain_mode": [_P, C.c_int32],
+    "sphgb_set_kernel_form": [_P, C.c_int32],
     "sphgb_get_kernel_K": [_P, C.POINTER(C.c_double)],
     "sphgb_domain_sync": [_P, C.POINTER(SphgbParticles), C.POINTER(SphgbBox)],
     "sphgb_get_tree": [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),

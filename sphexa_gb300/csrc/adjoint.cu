@@ -24,25 +24,19 @@ namespace {
 
 constexpr int kAdjBlock = 128;
 
-// interpolant value and slope (dw/dv) of the interval holding v, from the interleaved table
-// {t[k], t[k+1] - t[k]} with the interval taken from the bits of v / dx (as the forward passes)
-__device__ __forceinline__ double lookupSlope(const double2* __restrict__ tabX, double v, double& slope)
+// kernel function value and derivative dw/dv at v, on the interval the forward passes select (from
+// the bits of v / dx): the slope of the linear interpolant, or the derivative of the cubic piece in
+// the smooth form
+__device__ __forceinline__ double lookupSlope(const Tab64& tab, double v, double& slope)
 {
-    const TabSlot s = tabSlot(v * kTabInvDx);
-    if (s.k < 0) {
-        slope = 0.0;
-        return 0.0;
-    }
-    const double2 t = __ldg(tabX + s.k);
-    slope = t.y * kTabInvDx;
-    return fma(t.y, s.frac, t.x);
+    return lookupVSlope(tab, v, slope);
 }
 
 struct AdjArgs {
     // forward state
     const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *rho, *p, *c;
     const double *c11, *c12, *c13, *c22, *c23, *c33;
-    const double2* wh;  // interleaved {t[k], t[k+1] - t[k]}
+    Tab64 wh;  // W in the context's form
     double K, gamma;
     DevBox box;
     // lists: own (transposed layout) and incoming (CSR by neighbour)
@@ -141,7 +135,7 @@ struct PairGrad {
 };
 
 template<bool WantI, bool WantJ>
-__device__ __forceinline__ void mePairAdj(const DevBox& b, const double2* tab, const Side& I, const Side& J,
+__device__ __forceinline__ void mePairAdj(const DevBox& b, const Tab64& tab, const Side& I, const Side& J,
                                           const double gA[3], double gE, PairGrad& g)
 {
     double r[3];
@@ -448,14 +442,14 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
 // of the mixed forward); every accumulation is FP64.
 template<class T>
 struct TabOf {
-    using type = double2;
+    using type = Tab64;
 };
 template<>
 struct TabOf<float> {
-    using type = float2;
+    using type = const float2*;
 };
 
-__device__ __forceinline__ double lookupSlopeT(const double2* __restrict__ tab, double v, double& slope)
+__device__ __forceinline__ double lookupSlopeT(const Tab64& tab, double v, double& slope)
 {
     return lookupSlope(tab, v, slope);
 }
@@ -481,7 +475,7 @@ struct StdScatterArgs {
     const double *x, *y, *z, *u;
     const T *vx, *vy, *vz, *h, *m, *rho, *p, *c;
     const T* C[6];
-    const typename TabOf<T>::type* wh;
+    typename TabOf<T>::type wh;  // FP64: W in the context's form; FP32: the linear table
     double K, gamma;
     DevBox box;
     ListView lv;
@@ -989,7 +983,7 @@ static int adjointStdScatter(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds
     a.c = f(p->c);
     const void* Cs[6] = {p->c11, p->c12, p->c13, p->c22, p->c23, p->c33};
     for (int q = 0; q < 6; ++q) a.C[q] = f(Cs[q]);
-    if constexpr (std::is_same_v<T, double>) a.wh = c->whx64.as<double2>();
+    if constexpr (std::is_same_v<T, double>) a.wh = tabW64(c);
     else a.wh = c->whx32.as<float2>();
     a.K = c->K;
     a.gamma = c->prm.gamma;
@@ -1100,7 +1094,7 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     a.c22 = static_cast<const double*>(p->c22);
     a.c23 = static_cast<const double*>(p->c23);
     a.c33 = static_cast<const double*>(p->c33);
-    a.wh = c->whx64.as<double2>();
+    a.wh = tabW64(c);
     a.K = c->K;
     a.gamma = c->prm.gamma;
     a.box = c->box;

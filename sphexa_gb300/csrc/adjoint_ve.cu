@@ -32,7 +32,7 @@ struct VeAdjArgs {
     const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *alpha0, *alpha, *xm, *kx, *gradh, *prho, *c, *divv;
     const double* C[6];
     const double* dV[6];
-    const double2 *wh, *whd;  // interleaved {t[k], t[k+1] - t[k]}
+    Tab64 wh, whd;  // W and dW/dv in the context's form
     double K, gamma;
     AvPrm av;
     DevBox box;
@@ -64,16 +64,9 @@ struct VeAdjArgs {
 constexpr uint32_t kNoPair = 0xffffffffu;
 
 // interpolant value and slope (dw/dv) on the interval holding v (as the forward passes select it)
-__device__ __forceinline__ double lookupVS(const double2* __restrict__ tab, double v, double& slope)
+__device__ __forceinline__ double lookupVS(const Tab64& tab, double v, double& slope)
 {
-    const TabSlot s = tabSlot(v * kTabInvDx);
-    if (s.k < 0) {
-        slope = 0.0;
-        return 0.0;
-    }
-    const double2 t = __ldg(tab + s.k);
-    slope = t.y * kTabInvDx;
-    return fma(t.y, s.frac, t.x);
+    return lookupVSlope(tab, v, slope);
 }
 
 // r = x_i - x_j with the legacy periodic fold at 2 h_i (box.hpp:216-238), d = |r|
@@ -1181,8 +1174,8 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
         a.C[q] = d(Cs[q]);
         a.dV[q] = avClean ? d(dVs[q]) : nullptr;
     }
-    a.wh = c->whx64.as<double2>();
-    a.whd = c->whdx64.as<double2>();
+    a.wh = tabW64(c);
+    a.whd = tabDW64(c);
     a.K = c->K;
     a.gamma = c->prm.gamma;
     a.av = AvPrm{c->K, c->prm.minDt, c->prm.alphamin, c->prm.alphamax, c->prm.decay_constant};

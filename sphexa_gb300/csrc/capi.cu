@@ -143,7 +143,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pack,       &c->whx32,     &c->whH32, &c->whdH32,    &c->refMask,
                     &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape,
-                    &c->checkWord};
+                    &c->checkWord,  &c->whS64,      &c->whdS64};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -192,6 +192,13 @@ int sphgb_set_domain_mode(sphgb_ctx* c, int32_t mode)
     if (!c || (mode != 0 && mode != 1)) return SPHGB_ERR_ARG;
     c->domainMode = mode;
     c->domainFirst = true;
+    return SPHGB_OK;
+}
+
+int sphgb_set_kernel_form(sphgb_ctx* c, int32_t form)
+{
+    if (!c || (form != SPHGB_KERNEL_TABLE && form != SPHGB_KERNEL_SMOOTH)) return SPHGB_ERR_ARG;
+    c->smoothKernel = form == SPHGB_KERNEL_SMOOTH;
     return SPHGB_OK;
 }
 

@@ -136,6 +136,10 @@ struct sphgb_ctx {
 
     // kernel tables W and dW/dv, FP64 and FP32, interleaved {t[k], t[k+1] - t[k]}
     sphgb::DBuf whx64, whdx64;
+    // smooth form of the FP64 kernel function (sphgb_set_kernel_form): cubic Hermite pieces of W and
+    // dW/dv on the table's intervals, {c0 c1} {c2 c3} per interval; used when smoothKernel is set
+    sphgb::DBuf whS64, whdS64;
+    bool smoothKernel = false;
     sphgb::DBuf whx32;  // FP32 linear table (the mixed adjoint)
     sphgb::DBuf whH32, whdH32;  // mixed passes: cubic pieces of W and dW/dv (kHermIntervals float4)
 

@@ -20,14 +20,15 @@ namespace {
 // ---------------------------------------------------------------- density / xmass
 template<class P, bool StoreRho>
 __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
-                                                          const void* m, const void* wh, double K, void* out)
+                                                          const void* m, const void* wh, Tab64 w64, double K,
+                                                          void* out)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double2* tab = static_cast<const double2*>(wh);
+        const Tab64 tab = w64;
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
 // FP64 xmass / density with one evaluation per mutual pair over the owned lists: i adds
 // W(d / h_i) m_j, and for a mutual pair j receives W(d / h_j) m_i by an FP64 atomic
 __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
-                                                               const double* h, const double* m, const double2* tab,
+                                                               const double* h, const double* m, Tab64 tab,
                                                                const double* hInvDx, double* acc)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -149,14 +150,15 @@ struct IadOut {
 // vol[j] = m[j] / rho[j], formed once per particle (the reference divides per pair)
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
-                                                        const void* vol, const void* wh, double K, IadOut o)
+                                                        const void* vol, const void* wh, Tab64 w64, double K,
+                                                        IadOut o)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double2* tab = static_cast<const double2*>(wh);
+        const Tab64 tab = w64;
         auto t = cf.target(i);
         double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
@@ -217,7 +219,8 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
 struct MeStdArgs {
     const void *vx, *vy, *vz, *h, *m, *rho, *p, *c;
     const void *c11, *c12, *c13, *c22, *c23, *c33;
-    const void* wh;
+    const void* wh;        // mixed: cubic pieces of W
+    Tab64 w64;             // FP64: W in the context's form
     const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
     const void* aux;       // m/rho, p/rho, p/rho^2
     int64_t n;
@@ -251,7 +254,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+        const Tab64 tabX = a.w64;
         const double* hInv3 = a.hInv64 + a.n;
         const double* hInvDx = a.hInv64 + 2 * a.n;
         T hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
@@ -375,7 +378,7 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * size_t(n), c->stream));
         xmassOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
             lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-            c->whx64.as<double2>(), c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
+            tabW64(c), c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
         SPHGB_TRY(launched(c, "xmassOnceKernel"));
         const unsigned eb = gridFor(last - first, 256);
         if (storeRho)
@@ -389,9 +392,11 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
         return launched(c, "xmassOnceFinish");
     }
     if (storeRho)
-        xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
+        xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c), c->K,
+                                                                    out);
     else
-        xmassKernel<P, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, c->K, out);
+        xmassKernel<P, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c), c->K,
+                                                                     out);
     return launched(c, "xmassKernel");
 }
 
@@ -404,7 +409,7 @@ int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     lv.last = last;
     const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
     iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
-        lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, c->K,
+        lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, tabW64(c), c->K,
         IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
     return launched(c, "iadKernel");
 }
@@ -432,6 +437,7 @@ int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, d
     a.c23 = p->c23;
     a.c33 = p->c33;
     a.wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
+    a.w64 = tabW64(c);
     a.hInv64 = c->hInv64.as<double>();
     a.aux = c->aux.p;
     a.n = p->n;

@@ -87,7 +87,8 @@ __global__ void packGradhKernel(int64_t n, const void* xm, const void* m, float2
 template<class P>
 __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
                                                           const void* m, const void* xm, const void* wh,
-                                                          const void* whd, double K, void* kxOut, void* gradhOut,
+                                                          const void* whd, Tab64 w64, Tab64 dw64, double K,
+                                                          void* kxOut, void* gradhOut,
                                                           double* tapeWom = nullptr, double* tapeWr0 = nullptr,
                                                           const float2* rec = nullptr)
 {
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const double2 *tw = static_cast<const double2*>(wh), *tdw = static_cast<const double2*>(whd);
+        const Tab64 tw = w64, tdw = dw64;
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i), xmi = ld<double>(xm, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
@@ -207,6 +208,7 @@ __global__ void eosAuxVeKernel(int64_t n, const double* u, const void* m, const 
 // ---------------------------------------------------------------- IAD + divv/curlv
 struct IadDivvArgs {
     const void *h, *vx, *vy, *vz, *xm, *kx, *wh;
+    Tab64 w64;          // FP64: W in the context's form (wh: the mixed pieces)
     const void* vol;    // aux: xm/kx per particle
     float* divvBound;   // mixed: error bound of divv per particle (refinement flag), may be null
     double K;
@@ -281,7 +283,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         using T = double;
-        const double2* tab = static_cast<const double2*>(a.wh);
+        const Tab64 tab = a.w64;
         auto t = cf.target(i);
         T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
         const T hInvDx = hiInv * kTabInvDx;
@@ -414,6 +416,7 @@ struct AvArgs {
     int64_t tapeN;
     const float4* rec;   // mixed: neighbour records {vx vy vz c} and {vol divv} (packAvKernel)
     const float2* rec2;
+    Tab64 w64;  // FP64: W in the context's form (wh: the mixed pieces)
 };
 
 // neighbour-side fields of the mixed AV-switch pass as a 16-byte and an 8-byte record per particle
@@ -458,7 +461,7 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
     T gx, gy, gz;
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+        const Tab64 tabX = a.w64;
         T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         const T kh3 = a.K * hiInv3;
@@ -526,7 +529,8 @@ struct MeVeArgs {
     const void *vx, *vy, *vz, *h, *m, *prho, *c, *kx, *xm, *alpha;
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
-    const void* wh;
+    const void* wh;        // mixed: cubic pieces of W
+    Tab64 w64;             // FP64: W in the context's form
     const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
     const void* aux;       // rho, m/rho, xm/kx, m*prho, ln xm, 1/rho (6 x n)
     int64_t n;
@@ -621,7 +625,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+        const Tab64 tabX = a.w64;
         const double* hInv = a.hInv64;
         const double* hInv3 = a.hInv64 + a.n;
         const double* hInvDx = a.hInv64 + 2 * a.n;
@@ -795,7 +799,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
 // epilogue (ve_def_gradh_kern.hpp:60-62, 80-88) run in gradhOnceFinish.
 __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, const double* xm,
-                                                               const double2* tw, const double2* tdw,
+                                                               Tab64 tw, Tab64 tdw,
                                                                const double* hInv64, int64_t n, double* acc)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -902,7 +906,7 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned no = ov.size(ii);
-    const double2* tab = static_cast<const double2*>(a.wh);
+    const Tab64 tab = a.w64;
     const double* hInvDx = hInv64 + 2 * n;
     const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
                  *vz = static_cast<const double*>(a.vz), *xm = static_cast<const double*>(a.xm),
@@ -992,7 +996,7 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned no = ov.size(ii);
-    const double2* tabX = static_cast<const double2*>(a.wh);
+    const Tab64 tabX = a.w64;
     const double* hInvDx = hInv64 + 2 * n;
     const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
                  *vz = static_cast<const double*>(a.vz), *c = static_cast<const double*>(a.c),
@@ -1076,7 +1080,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nOwned = __ldg(a.ownedCount + ii);
-    const double2* tabX = reinterpret_cast<const double2*>(a.wh);
+    const Tab64 tabX = a.w64;
     const T* aux = static_cast<const T*>(a.aux);
     const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n,
             *auxRhoInv = aux + 5 * a.n;
@@ -1224,7 +1228,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 3 * size_t(n), c->stream));
         gradhOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
             lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-            static_cast<const double*>(p->xm), c->whx64.as<double2>(), c->whdx64.as<double2>(),
+            static_cast<const double*>(p->xm), tabW64(c), tabDW64(c),
             c->hInv64.as<double>(), n, c->pairAcc.as<double>());
         SPHGB_TRY(launched(c, "gradhOnceKernel"));
         if (c->inSweep && p->u && p->prho && p->c) {  // EOS and quotients fused into the epilogue
@@ -1248,15 +1252,17 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         packGradhKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->xm, p->m, rec);
         SPHGB_TRY(launched(c, "packGradhKernel"));
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                    p->xm, c->whH32.p, c->whdH32.p, c->K, p->kx,
-                                                                    p->gradh, nullptr, nullptr, rec);
+                                                                    p->xm, c->whH32.p, c->whdH32.p, Tab64{},
+                                                                    Tab64{}, c->K, p->kx, p->gradh, nullptr, nullptr,
+                                                                    rec);
         SPHGB_TRY(launched(c, "gradhKernel"));
         if (first == 0 && last == p->n) return refineMixedGradh(c, p);
         c->stats_refinedGradh = 0;
         return SPHGB_OK;
     } else
         gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                   p->xm, c->whx64.p, c->whdx64.p, c->K, p->kx,
+                                                                   p->xm, c->whx64.p, c->whdx64.p, tabW64(c),
+                                                                   tabDW64(c), c->K, p->kx,
                                                                    p->gradh, tWom, tWr0);
     return launched(c, "gradhKernel");
 }
@@ -1347,6 +1353,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
         return refineMixedDivv(c, p, refine ? a.divvBound : nullptr);
     } else {
         a.wh = c->whx64.p;
+        a.w64 = tabW64(c);
         SPHGB_TRY(tapeFor(c, p, first, last, kTapeIad, &a.tapeP));
         if (a.tapeP) a.tapeP += int64_t(kTapeP) * p->n;
         a.tapeN = p->n;
@@ -1397,6 +1404,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
     } else if (pairOnce(c, p, first, last)) {
         const int64_t n = p->n;
         a.wh = c->whx64.p;
+        a.w64 = tabW64(c);
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 4 * size_t(n)));
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 4 * size_t(n), c->stream));
         avOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, ownedView(c), coordFp64(c, p), a,
@@ -1406,6 +1414,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         return launched(c, "avOnceFinish");
     } else {
         a.wh = c->whx64.p;
+        a.w64 = tabW64(c);
         avKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     }
     return launched(c, "avKernel");
@@ -1471,6 +1480,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {
         a.wh = c->whx64.p;
+        a.w64 = tabW64(c);
         double* tape;
         SPHGB_TRY(tapeFor(c, p, first, last, kTapeMe, &tape));
         if (tape) {

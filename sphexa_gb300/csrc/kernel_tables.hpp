@@ -43,18 +43,20 @@ inline void sincDerivs(double v, double& s, double& s1, double& s2)
     s2 = a * a * (-x * x * sn - 2.0 * x * cs + 2.0 * sn) / (x * x * x);
 }
 
-// the mixed passes' kernel function: per interval of [0, 2] the cubic Hermite piece through f and
-// f' at both ends, as FP32 coefficients {c0 c1 c2 c3} of c0 + t (c1 + t (c2 + t c3)), t in [0, 1)
-inline void hermiteTable(const std::vector<double>& f, const std::vector<double>& d, double dv, std::vector<float>& out)
+// per interval of [0, 2] the cubic Hermite piece through f and f' at both ends, as coefficients
+// {c0 c1 c2 c3} of c0 + t (c1 + t (c2 + t c3)), t in [0, 1) (FP32 for the mixed passes, FP64 for the
+// smooth form of the FP64 passes)
+template<class R>
+inline void hermiteTable(const std::vector<double>& f, const std::vector<double>& d, double dv, std::vector<R>& out)
 {
     const int m = int(f.size()) - 1;
     out.resize(4 * size_t(m));
     for (int k = 0; k < m; ++k) {
         const double f0 = f[k], f1 = f[k + 1], d0 = dv * d[k], d1 = dv * d[k + 1];
-        out[4 * k] = float(f0);
-        out[4 * k + 1] = float(d0);
-        out[4 * k + 2] = float(3.0 * (f1 - f0) - 2.0 * d0 - d1);
-        out[4 * k + 3] = float(2.0 * (f0 - f1) + d0 + d1);
+        out[4 * k] = R(f0);
+        out[4 * k + 1] = R(d0);
+        out[4 * k + 2] = R(3.0 * (f1 - f0) - 2.0 * d0 - d1);
+        out[4 * k + 3] = R(2.0 * (f0 - f1) + d0 + d1);
     }
 }
 
@@ -78,7 +80,8 @@ inline double kernelNormalisation(double n)
 
 // W = sinc^n and dW/dv as cubic pieces on `intervals` equal intervals of [0, 2] (node values and
 // first derivatives from the closed form; W'' at the nodes for the pieces of dW/dv)
-inline void hermitePieces(double n, int intervals, std::vector<float>& w32, std::vector<float>& dw32)
+template<class R>
+inline void hermitePieces(double n, int intervals, std::vector<R>& w32, std::vector<R>& dw32)
 {
     const double dv = 2.0 / intervals;
     std::vector<double> w(intervals + 1), w1(intervals + 1), w2(intervals + 1);

@@ -243,6 +243,61 @@ __device__ __forceinline__ double lookupX(const double2* __restrict__ tabX, doub
     return lookupX(tabX, tabSlot(x));
 }
 
+// ---- the FP64 passes' kernel function, W or dW/dv, in one of two forms ----
+// table (default): the reference's linear interpolant, t[k] = {t[k], t[k+1] - t[k]};
+// smooth (sphgb_set_kernel_form): a cubic Hermite piece on each of the same 19999 intervals, through
+//   the closed-form values and derivatives at both nodes, t[2k] = {c0, c1}, t[2k+1] = {c2, c3} of
+//   c0 + f (c1 + f (c2 + f c3)), f = x - k.  The function is then continuously differentiable, so
+//   central differences of the forward passes agree with the adjoint (which differentiates the same
+//   pieces); it differs from the table form by the table's interpolation error (within 2e-8 of the
+//   function's maximum).
+// The form is uniform over a launch, so the branch costs no divergence.
+struct Tab64 {
+    const double2* t;
+    int smooth;
+};
+
+__device__ __forceinline__ double lookupX(const Tab64& tb, const TabSlot& s)
+{
+    if (s.k < 0) return 0.0;
+    if (tb.smooth) {
+        const double2 a = __ldg(tb.t + 2 * s.k), b = __ldg(tb.t + 2 * s.k + 1);
+        return fma(fma(fma(b.y, s.frac, b.x), s.frac, a.y), s.frac, a.x);
+    }
+    const double2 t = __ldg(tb.t + s.k);
+    return fma(t.y, s.frac, t.x);
+}
+
+__device__ __forceinline__ double lookupX(const Tab64& tb, double x) { return lookupX(tb, tabSlot(x)); }
+
+// value at v and its derivative d/dv (the slope of the interval in the table form)
+__device__ __forceinline__ double lookupVSlope(const Tab64& tb, double v, double& slope)
+{
+    const TabSlot s = tabSlot(v * kTabInvDx);
+    if (s.k < 0) {
+        slope = 0.0;
+        return 0.0;
+    }
+    if (tb.smooth) {
+        const double2 a = __ldg(tb.t + 2 * s.k), b = __ldg(tb.t + 2 * s.k + 1);
+        const double f = s.frac;
+        slope = fma(fma(3.0 * b.y, f, 2.0 * b.x), f, a.y) * kTabInvDx;
+        return fma(fma(fma(b.y, f, b.x), f, a.y), f, a.x);
+    }
+    const double2 t = __ldg(tb.t + s.k);
+    slope = t.y * kTabInvDx;
+    return fma(t.y, s.frac, t.x);
+}
+
+inline Tab64 tabW64(const sphgb_ctx* c)
+{
+    return c->smoothKernel ? Tab64{c->whS64.as<double2>(), 1} : Tab64{c->whx64.as<double2>(), 0};
+}
+inline Tab64 tabDW64(const sphgb_ctx* c)
+{
+    return c->smoothKernel ? Tab64{c->whdS64.as<double2>(), 1} : Tab64{c->whdx64.as<double2>(), 0};
+}
+
 // ---- the mixed passes' kernel function: a cubic Hermite piece per interval of [0, 2] ----
 // The pieces interpolate W and dW/dv at kHermIntervals + 1 nodes with their derivatives (error
 // ~1e-11, below FP32 rounding), so the FP32 result is the kernel function itself, within 1e-8 of

@@ -98,6 +98,14 @@ int buildTables(sphgb_ctx* c)
         SPHGB_CUDA(cudaMemcpy(c->whH32.p, hw.data(), sizeof(float) * hw.size(), cudaMemcpyHostToDevice));
         SPHGB_CUDA(cudaMemcpy(c->whdH32.p, hd.data(), sizeof(float) * hd.size(), cudaMemcpyHostToDevice));
     }
+    {  // smooth form of the FP64 kernel function: cubic pieces on the linear table's intervals
+        std::vector<double> sw, sd;
+        tables::hermitePieces(n, kTableSize - 1, sw, sd);
+        SPHGB_TRY(c->whS64.ensure(sizeof(double) * sw.size()));
+        SPHGB_TRY(c->whdS64.ensure(sizeof(double) * sd.size()));
+        SPHGB_CUDA(cudaMemcpy(c->whS64.p, sw.data(), sizeof(double) * sw.size(), cudaMemcpyHostToDevice));
+        SPHGB_CUDA(cudaMemcpy(c->whdS64.p, sd.data(), sizeof(double) * sd.size(), cudaMemcpyHostToDevice));
+    }
     SPHGB_TRY(c->whx64.ensure(sizeof(double) * 2 * kTableSize));
     SPHGB_TRY(c->whdx64.ensure(sizeof(double) * 2 * kTableSize));
     SPHGB_CUDA(cudaMemcpy(c->whx64.p, wx.data(), sizeof(double) * 2 * kTableSize, cudaMemcpyHostToDevice));

@@ -90,6 +90,11 @@ class Context:
         error) in FP64 from the exact inputs (default True)."""
         check(self.lib.sphgb_set_mixed_refinement(self.h, int(bool(on))), "sphgb_set_mixed_refinement")
 
+    def set_kernel_form(self, smooth: bool) -> None:
+        """Kernel function of the FP64 passes and adjoints: the reference's linear table interpolant
+        (False, default) or C1 cubic pieces through the closed form (True, sphgb_set_kernel_form)."""
+        check(self.lib.sphgb_set_kernel_form(self.h, int(bool(smooth))), "sphgb_set_kernel_form")
+
     def set_domain_mode(self, mode: int) -> None:
         """0: every sync stands alone; 1: syncs are the steps of one simulation (box shrink limit)."""
         check(self.lib.sphgb_set_domain_mode(self.h, int(mode)), "sphgb_set_domain_mode")

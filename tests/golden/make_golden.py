@@ -32,7 +32,7 @@ sys.path.insert(0, str(ROOT))
 from oracle import oracle as O  # noqa: E402
 from sphexa_gb300 import workloads as W  # noqa: E402
 
-REF = Path(os.environ.get("SPHGB_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("SPHGB_REFERENCE", Path(__file__).resolve().parents[3] / "reference"))
 
 OJ = dict(xmass=0, gradh=1, iad_std=2, iad_ve=3, divv=4, av=5, me_std=6, me_ve=7)
 

@@ -36,7 +36,7 @@ def test_bench_constants_are_the_counted_table():
 
 
 def test_flop_table_reproduces_from_the_reference(tmp_path):
-    ref = Path(os.environ.get("SPHGB_REFERENCE", "/root/reference"))
+    ref = Path(os.environ.get("SPHGB_REFERENCE", ROOT.parent / "reference"))
     if not (ref / "sph" / "include" / "sph" / "hydro_ve" / "momentum_energy_kern.hpp").exists():
         pytest.skip("reference sources not present")
     import ctypes as C

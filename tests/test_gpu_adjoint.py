@@ -1,12 +1,17 @@
-"""The hand-written adjoint of the std chain against FP64 central differences.
+"""The hand-written adjoint of the std chain against an FP64 reference gradient and FP64 central
+differences.
 
 Workload: the adjoint configuration's generator (jittered periodic lattice, Fourier density
-field, Gaussian velocities, an independent target density field) at 12^3 particles.  Loss
-L = sum (rho - rho_target)^2 + sum |a|^2 on the frozen neighbour lists; gradients by the adjoint
-through torch.autograd; central differences with eps = 1e-6 (relative to h for h) on 64 seeded
-coordinates.  Bar: relative agreement <= 1e-6 for coordinates whose +-eps evaluations stay on one
-smooth piece (no pair distance crossing a node of the kernel table's linear interpolant and no
-viscosity switch flip); the count of those is reported.
+field, Gaussian velocities, an independent target density field) at 10^3 to 12^3 particles.  Loss
+L = sum (rho - rho_target)^2 + sum |a|^2 on the frozen neighbour lists.
+
+* Reference gradient: torch autograd through the FP64 torch restatement of the same chain on the
+  same edges (tests/torch_reference.py), in both kernel forms (the reference's linear table and the
+  smooth cubic pieces); bar normwise 1e-9 per field.
+* Central differences: smooth kernel form, eps = 1e-6 absolute for every field, 64 coordinates from
+  PCG64(55555); a coordinate whose stencil straddles a kink of the forward (the viscosity branch) is
+  reported and replaced by the next draw (tests/fd_check.py).  Bar: relative agreement <= 1e-6 on
+  every checked coordinate.  The full-size version (1M particles) is tests/test_gpu_adjoint_fd.py.
 """
 
 import numpy as np
@@ -17,11 +22,12 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
 
 
-def setup(side=12, seed=5, deterministic=False, ordered_forward=False, precision="fp64"):
+def setup(side=12, seed=5, deterministic=False, ordered_forward=False, precision="fp64", smooth=False):
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
     ctx = sph.Context(0)
+    ctx.set_kernel_form(smooth)
     if ordered_forward:  # the scatter adjoint then walks the full lists (no owned lists in use)
         ctx.set_deterministic(True)
     d = sph.ParticlesData.from_workload(wl, precision, "cuda:0")
@@ -39,8 +45,9 @@ def loss_of(sw, rho_t, vals):
     return float(AG.loss_rho_a(rho, ax, ay, az, rho_t).item())
 
 
+@pytest.mark.parametrize("smooth", [False, True])
 @pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided"])
-def test_adjoint_matches_fp64_reference_gradient(port, form):
+def test_adjoint_matches_fp64_reference_gradient(port, form, smooth):
     """Every gradient component of every particle against torch autograd through the FP64 torch
     restatement of the same chain on the same frozen edges (tests/torch_reference.py).  pair-once:
     one evaluation per mutual pair of the owned lists; scatter: every list entry once with atomics;
@@ -48,7 +55,8 @@ def test_adjoint_matches_fp64_reference_gradient(port, form):
     import torch
     from sphexa_gb300 import autograd as AG, sph
     from torch_reference import std_chain
-    wl, ctx, sw, rho_t = setup(side=10, seed=7, deterministic=form == "two-sided", ordered_forward=form == "scatter")
+    wl, ctx, sw, rho_t = setup(side=10, seed=7, deterministic=form == "two-sided", ordered_forward=form == "scatter",
+                               smooth=smooth)
     n = wl.n
     ng = int(ctx.params.ngmax)
     nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
@@ -57,7 +65,11 @@ def test_adjoint_matches_fp64_reference_gradient(port, form):
     ej = np.concatenate([nb[k, :cnt[k]] for k in range(n)])
     dev = "cuda:0"
     ei_t, ej_t = torch.tensor(ei, device=dev), torch.tensor(ej, device=dev)
-    wh, _ = port.tables(6.0)
+    if smooth:
+        from torch_reference import hermite_tables
+        wh, _ = hermite_tables(6.0)
+    else:
+        wh, _ = port.tables(6.0)
     tab = torch.tensor(wh, dtype=torch.float64, device=dev)
     inp = [t.clone().requires_grad_(True) for t in sw.inputs()]
     m = sw.d.m.clone()
@@ -96,39 +108,15 @@ def test_deterministic_adjoint_is_bit_reproducible():
 
 
 def test_adjoint_matches_central_differences():
-    import torch
-    from sphexa_gb300 import autograd as AG
-    wl, ctx, sw, rho_t = setup()
-    base = [t.clone().requires_grad_(True) for t in sw.inputs()]
-    rho, ax, ay, az, du = AG.StdSweepFunction.apply(sw, *base)
-    L = AG.loss_rho_a(rho, ax, ay, az, rho_t)
-    L.backward()
-    grads = {f: base[k].grad.detach().cpu().numpy() for k, f in enumerate(FIELDS)}
-    rng = np.random.Generator(np.random.PCG64(55555))
-    picks = [(FIELDS[rng.integers(0, 8)], int(rng.integers(0, wl.n))) for _ in range(64)]
-    rows = []
-    for field, i in picks:
-        k = FIELDS.index(field)
-        vals = [t.detach().clone() for t in base]
-        x0 = float(vals[k][i])
-        eps = 1e-6 * (x0 if field == "h" else 1.0)
-        vals[k][i] = x0 + eps
-        lp = loss_of(sw, rho_t, vals)
-        vals[k][i] = x0 - eps
-        lm = loss_of(sw, rho_t, vals)
-        fd = (lp - lm) / (2 * eps)
-        ad = float(grads[field][i])
-        scale = max(abs(fd), 1e-3 * float(np.max(np.abs(grads[field]))), 1e-300)
-        rows.append((field, i, ad, fd, abs(ad - fd) / scale))
-    errs = {f: [r[4] for r in rows if r[0] == f] for f in FIELDS}
-    for f in FIELDS:
-        if errs[f]:
-            print(f"{f:3s} n={len(errs[f]):2d} max rel {max(errs[f]):.3e} median {np.median(errs[f]):.3e}")
-    # velocities and internal energy do not move any pair distance: smooth pieces everywhere
-    smooth = [r[4] for r in rows if r[0] in ("vx", "vy", "vz", "u")]
-    assert smooth and max(smooth) <= 1e-6
-    allrel = [r[4] for r in rows]
-    assert np.median(allrel) <= 1e-4
+    from fd_check import adjoint_gradient, fd_check, report
+    wl, ctx, sw, rho_t = setup(smooth=True)
+    grads = adjoint_gradient(sw, rho_t, [t.detach().clone() for t in sw.inputs()])
+    ctx.set_deterministic(True)  # bitwise reproducible forward for the differences
+    rows, straddles = fd_check(sw, rho_t, wl.n, grads)
+    report(rows, straddles, "std chain, 12^3")
+    assert len(rows) == 64
+    worst = max(rows, key=lambda r: r[4])
+    assert worst[4] <= 1e-6, worst
     ctx.close()
 
 

@@ -7,6 +7,14 @@ field, Gaussian velocities) at 10^3 to 12^3 particles, with u, h and the alpha b
 varied per particle (so that the AV switch takes both of its branches, the Atwood weights all three
 of theirs and no two h coincide) and an AV time step of 1e-2.  Loss L = sum (rho - rho_target)^2 +
 sum |a|^2 (+ a seed on du for the reference-gradient test) on the frozen neighbour lists.
+
+* Reference gradient: every form of the adjoint, avClean on and off, in both kernel forms (the
+  reference's linear table, the smooth cubic pieces); bar normwise 1e-9 per field.
+* Central differences: smooth kernel form, eps = 1e-6 absolute for every field, 64 coordinates from
+  PCG64(55555); a coordinate whose stencil straddles a kink of the forward (AV switch, Atwood ramp,
+  signal-velocity maximum, max(0, .), avClean clamp) is reported and replaced by the next draw
+  (tests/fd_check.py).  Bar: relative agreement <= 1e-6 on every checked coordinate.  The full-size
+  version (1M particles) is tests/test_gpu_adjoint_fd.py.
 """
 
 import numpy as np
@@ -17,7 +25,7 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "h", "u")
 
 
-def setup(side=10, seed=7, av_clean=False, deterministic=False, ordered_forward=False):
+def setup(side=10, seed=7, av_clean=False, deterministic=False, ordered_forward=False, smooth=False):
     import torch
     from sphexa_gb300 import autograd as AG, sph, workloads as W
     wl = W.fourier(side, seed=seed, rho_seed=55, v_seed=555, target_seed=5555)
@@ -27,6 +35,7 @@ def setup(side=10, seed=7, av_clean=False, deterministic=False, ordered_forward=
     wl.fields["alpha"] = rng.uniform(0.05, 0.5, wl.n)
     ctx = sph.Context(0)
     ctx.set_params(minDt=1e-2)
+    ctx.set_kernel_form(smooth)
     if ordered_forward:  # forward passes in list order; the scatter adjoint then walks the full lists
         ctx.set_deterministic(True)
     d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0", av_clean=av_clean)
@@ -38,16 +47,17 @@ def setup(side=10, seed=7, av_clean=False, deterministic=False, ordered_forward=
     return wl, ctx, sw, rho_t
 
 
+@pytest.mark.parametrize("smooth", [False, True])
 @pytest.mark.parametrize("av_clean", [False, True])
 @pytest.mark.parametrize("form", ["pair-once", "scatter", "two-sided"])
-def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, form):
+def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, form, smooth):
     """pair-once: one evaluation per mutual pair of the owned lists; scatter: every list entry
     once with atomics (context in deterministic mode); two-sided: bit-reproducible form"""
     import torch
     from sphexa_gb300 import autograd as AG, sph
     from torch_reference import ve_chain
     wl, ctx, sw, rho_t = setup(side=10, seed=7, av_clean=av_clean, deterministic=form == "two-sided",
-                               ordered_forward=form == "scatter")
+                               ordered_forward=form == "scatter", smooth=smooth)
     n = wl.n
     ng = int(ctx.params.ngmax)
     nb = sph.export_neighbors(ctx, n, ng).cpu().numpy().reshape(n, ng).astype(np.int64)
@@ -55,7 +65,11 @@ def test_ve_adjoint_matches_fp64_reference_gradient(port, av_clean, form):
     ei = np.repeat(np.arange(n), cnt)
     ej = np.concatenate([nb[k, :cnt[k]] for k in range(n)])
     dev = "cuda:0"
-    wh, whd = port.tables(6.0)
+    if smooth:
+        from torch_reference import hermite_tables
+        wh, whd = hermite_tables(6.0)
+    else:
+        wh, whd = port.tables(6.0)
     tab = torch.tensor(wh, dtype=torch.float64, device=dev)
     tabd = torch.tensor(whd, dtype=torch.float64, device=dev)
     p = ctx.params
@@ -111,37 +125,15 @@ def test_ve_adjoint_requires_alpha_before_the_switch():
 
 @pytest.mark.parametrize("av_clean", [False, True])
 def test_ve_adjoint_matches_central_differences(av_clean):
-    from sphexa_gb300 import autograd as AG
-    wl, ctx, sw, rho_t = setup(side=12, seed=5, av_clean=av_clean)
-    base = [t.clone().requires_grad_(True) for t in sw.inputs()]
-    rho, ax, ay, az, du = AG.VeSweepFunction.apply(sw, *base)
-    L = AG.loss_rho_a(rho, ax, ay, az, rho_t)
-    L.backward()
-    grads = {f: base[k].grad.detach().cpu().numpy() for k, f in enumerate(FIELDS)}
-    rng = np.random.Generator(np.random.PCG64(55555))
-    picks = [(FIELDS[rng.integers(0, 8)], int(rng.integers(0, wl.n))) for _ in range(64)]
-    rows = []
-    for field, i in picks:
-        k = FIELDS.index(field)
-        vals = [t.detach().clone() for t in base]
-        x0 = float(vals[k][i])
-        eps = 1e-6 * (x0 if field == "h" else 1.0)
-        vals[k][i] = x0 + eps
-        lp = float(AG.loss_rho_a(*sw.forward(*vals)[:4], rho_t).item())
-        vals[k][i] = x0 - eps
-        lm = float(AG.loss_rho_a(*sw.forward(*vals)[:4], rho_t).item())
-        fd = (lp - lm) / (2 * eps)
-        ad = float(grads[field][i])
-        scale = max(abs(fd), 1e-3 * float(np.max(np.abs(grads[field]))), 1e-300)
-        rows.append((field, i, ad, fd, abs(ad - fd) / scale))
-    for f in FIELDS:
-        e = [r[4] for r in rows if r[0] == f]
-        if e:
-            print(f"{f:3s} n={len(e):2d} max rel {max(e):.3e} median {np.median(e):.3e}")
-    # u moves no pair distance and no branch of the AV switch or the Atwood weights: smooth
-    smooth = [r[4] for r in rows if r[0] == "u"]
-    assert smooth and max(smooth) <= 1e-6
-    assert np.median([r[4] for r in rows]) <= 1e-4
+    from fd_check import adjoint_gradient, fd_check, report
+    wl, ctx, sw, rho_t = setup(side=12, seed=5, av_clean=av_clean, smooth=True)
+    grads = adjoint_gradient(sw, rho_t, [t.detach().clone() for t in sw.inputs()])
+    ctx.set_deterministic(True)  # bitwise reproducible forward for the differences
+    rows, straddles = fd_check(sw, rho_t, wl.n, grads)
+    report(rows, straddles, f"VE chain{' avClean' if av_clean else ''}, 12^3")
+    assert len(rows) == 64
+    worst = max(rows, key=lambda r: r[4])
+    assert worst[4] <= 1e-6, worst
     ctx.close()
 
 

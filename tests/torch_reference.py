@@ -12,7 +12,48 @@ from __future__ import annotations
 import torch
 
 
+def hermite_tables(n: float, intervals: int = 19999):
+    """W = sinc^n and dW/dv as cubic Hermite pieces on `intervals` equal intervals of [0, 2], rows
+    {c0 c1 c2 c3} of c0 + f (c1 + f (c2 + f c3)): the smooth kernel form of the FP64 passes
+    (sphgb_set_kernel_form), node values and derivatives from the closed form of
+    sph/include/sph/kernels.hpp:35-61 (series below pi v / 2 = 1e-2)."""
+    import numpy as np
+    a = np.pi / 2
+    v = np.arange(intervals + 1) * (2.0 / intervals)
+    x = a * v
+    small = x < 1e-2
+    xs = np.where(small, 1.0, x)
+    sn, cs = np.sin(xs), np.cos(xs)
+    x2 = x * x
+    s0 = np.where(small, 1 - x2 / 6 + x2 * x2 / 120 - x2 ** 3 / 5040, sn / xs)
+    s1 = np.where(small, a * x * (-1 / 3 + x2 / 30 - x2 * x2 / 840), a * (xs * cs - sn) / (xs * xs))
+    s2 = np.where(small, a * a * (-1 / 3 + x2 / 10 - x2 * x2 / 168),
+                  a * a * (-xs * xs * sn - 2 * xs * cs + 2 * sn) / xs ** 3)
+    s0 = np.maximum(s0, 0.0)
+    w = s0 ** n
+    w1 = n * s0 ** (n - 1) * s1
+    w2 = np.where(s0 > 0, n * (n - 1) * s0 ** (n - 2) * s1 * s1 + n * s0 ** (n - 1) * s2, 0.0)
+    dv = 2.0 / intervals
+
+    def pieces(f, d):
+        f0, f1, d0, d1 = f[:-1], f[1:], dv * d[:-1], dv * d[1:]
+        return np.stack([f0, d0, 3 * (f1 - f0) - 2 * d0 - d1, 2 * (f0 - f1) + d0 + d1], 1)
+
+    return pieces(w, w1), pieces(w1, w2)
+
+
 def lookup(tab: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+    """kernel function at v: the linear interpolant of a 1-D table, or the cubic pieces of a
+    (intervals, 4) coefficient table (the smooth form)"""
+    if tab.dim() == 2:
+        n_int = tab.shape[0]
+        inv_dx = n_int / 2.0
+        xv = v * inv_dx
+        idx = torch.clamp(xv.detach().to(torch.int64), max=n_int)
+        c = tab[torch.clamp(idx, max=n_int - 1)]
+        f = xv - idx.to(v.dtype)
+        val = c[:, 0] + f * (c[:, 1] + f * (c[:, 2] + f * c[:, 3]))
+        return torch.where(idx >= n_int, torch.zeros_like(v), val)
     n_int = tab.numel() - 1
     dx = 2.0 / n_int
     inv_dx = 1.0 / dx
