@@ -45,6 +45,15 @@ STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # "me" and "av" are the pair-once kernels of the default (non-deterministic) FP64 mode.
 NCU_DRAM_BYTES_PER_PARTICLE = {"me": 584.7, "iad_divv": 564.3, "av": 381.7}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
+STAGES_STD = ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
+# FP32 distance test of one search candidate against the target's radius: 3 coordinate differences,
+# one multiply and two FMAs (an FMA counts 2)
+SEARCH_FLOPS_PER_TEST = 8
+# fields compared between the mixed and the FP64 form
+CMP_FIELDS = ("xm", "kx", "rho", "ax", "ay", "az", "du", "c11", "c12", "c13", "c22", "c23", "c33", "divv", "curlv",
+              "alpha")
+# the other configurations measured beside the headline: (timed sweeps, warm-up sweeps)
+EXTRA_CONFIGS = {"fourier300": (5, 2), "sphere10M": (5, 2)}
 
 
 def env_rank():
@@ -108,6 +117,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
 
 
+def host_cpu() -> dict:
+    """The host cores the CPU baseline runs on: count, model and the OpenMP settings in force."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model, "OMP_NUM_THREADS": os.environ.get("OMP_NUM_THREADS"),
+            "OMP_PROC_BIND": os.environ.get("OMP_PROC_BIND"),
+            "build": "oracle/liboracle_o3.so: g++ -std=c++20 -O3 -fopenmp (no -march/-mcpu=native)"}
+
+
+def set_cpu_threads() -> None:
+    """every host core for the OpenMP CPU baseline, threads bound close (set before any OpenMP
+    runtime starts)"""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -164,28 +196,22 @@ def structure_report(ctx, d, stats: dict, ngmax: int) -> dict:
                             "max_over_mean": float(g.max() / g.mean())}}
 
 
-# bounded CPU sample of each workload: the same generator at side^3 particles
-SAMPLES = {"sedov200_jit": lambda W, s: W.sedov(s, jitter=0.25, seed=2),
-           "sedov100_jit": lambda W, s: W.sedov(s, jitter=0.25, seed=2),
-           "fourier300": lambda W, s: W.fourier(s),
-           "sphere10M": lambda W, s: W.sphere(s ** 3)}
-
-
-def cpu_baseline(side: int, threads: int = 0, workload: str = "sedov200_jit", variant: str = "ve") -> dict:
-    """The oracle (my CPU restatement of the reference's OpenMP path) on a bounded sample of the
-    workload: the same generator at side^3 particles, one full sweep."""
+def cpu_baseline(wl, workload: str, variant: str = "ve", sweeps: int = 1) -> dict:
+    """The oracle (my CPU restatement of the reference's OpenMP path, release flags) on the same
+    workload as the GPU arm: `sweeps` full sweeps, all host cores."""
     from oracle import oracle as O
-    from sphexa_gb300 import workloads as W
-    O.build_port()
-    port = O.port()
-    wl = SAMPLES[workload](W, side)
-    t0 = time.perf_counter()
-    r = port.sweep(wl, variant, False, want_nbr=False, want_tree=False, nthreads=threads)
-    dt = time.perf_counter() - t0
+    port = O.port_timed()
+    times, r = [], None
+    for _ in range(sweeps):
+        t0 = time.perf_counter()
+        r = port.sweep(wl, variant, False, want_nbr=False, want_tree=False)
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
     return {"value": wl.n / dt, "unit": UNIT, "cores": int(r["threads"]), "kind": "port",
-            "sample": f"one {variant.upper()} sweep of the same generator ({workload}) at {wl.n} particles "
-                      f"({dt:.1f} s; stages keys {r['times']['keys']:.2f} tree {r['times']['tree']:.2f} "
-                      f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)"}
+            "sample": f"{sweeps} full {variant.upper()} sweep(s) of the {workload} workload ({wl.n} particles, "
+                      f"median {dt:.2f} s; stages keys {r['times']['keys']:.2f} tree {r['times']['tree']:.2f} "
+                      f"nbr {r['times']['nbr']:.2f} hydro {r['times']['hydro']:.2f} s)",
+            "host": host_cpu()}
 
 
 def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str = "std",
@@ -236,29 +262,87 @@ def adjoint_timing(ctx, dev: str, side: int, steps: int, warmup: int, chain: str
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference's CPU OpenMP path for this sweep (restated in oracle/, built
+    with release flags) on the GPU arm's workload, one full sweep per step, all host cores."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    side = args.cpu_side
-    vals = []
-    for _ in range(args.warmup):  # untimed, the same bounded sample as a timed step
-        cpu_baseline(side, workload=args.workload, variant=args.variant)
+    set_cpu_threads()
+    from oracle import oracle as O
+    wl = make_workload(args.workload)
+    port = O.port_timed()
+    for _ in range(args.warmup):  # untimed, the same work as a timed step
+        port.sweep(wl, args.variant, False, want_nbr=False, want_tree=False)
+    times, r = [], None
     t_all = time.perf_counter()
-    last = None
     for _ in range(args.steps):
-        last = cpu_baseline(side, workload=args.workload, variant=args.variant)
-        vals.append(last["value"])
+        t0 = time.perf_counter()
+        r = port.sweep(wl, args.variant, False, want_nbr=False, want_tree=False)
+        times.append(time.perf_counter() - t0)
     wall = time.perf_counter() - t_all
-    v = statistics.median(vals)
+    v = wl.n * args.steps / wall
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded generator of the named configuration (no dataset)", "impl": "reference",
             "config": bench_config(args, world),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
-                             "sample": last["sample"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": int(r["threads"]), "kind": "port",
+                             "sample": f"every step one full {args.variant.upper()} sweep of the workload "
+                                       f"({wl.n} particles; step median {statistics.median(times):.2f} s, "
+                                       f"min {min(times):.2f} s)",
+                             "host": host_cpu()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def pair_roofline(stages: np.ndarray, names: list, pairs: int, flops: dict, peak: float, bound: str) -> dict:
+    """the pair pass with the largest share of the sweep against a pipe peak: counted reference flops
+    of its j-loop per neighbour pair x pairs, over its CUDA-event time"""
+    cand = [k for k in range(len(names)) if names[k] in flops]
+    k = max(cand, key=lambda q: stages[q])
+    achieved = pairs * flops[names[k]] / (stages[k] * 1e-3)
+    return {"bound": bound, "kernel": names[k], "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": achieved / peak, "ms": float(stages[k]),
+            "algorithmic": f"{pairs} pairs x {flops[names[k]]} flop/pair per launch",
+            "peak_source": f"{bound.upper()} FMA probe measured in this run (MEASURED_PEAKS.json has no "
+                           f"{bound.upper()} figure)"}
+
+
+def search_roofline(stats: dict, ms: float, n: int, fp32_peak: float, hbm_gbs: float) -> dict:
+    """the neighbour search: FP32 distance tests against the FP32 pipe, list bytes against HBM"""
+    tests = int(stats["candidates"])
+    list_bytes = 4 * int(stats["nc_sum"]) + 4 * n  # transposed list entries + counts
+    tf = tests * SEARCH_FLOPS_PER_TEST / (ms * 1e-3)
+    gbs = list_bytes / (ms * 1e-3) / 1e9
+    return {"bound": "issue (instructions per candidate test; profiles/nbrGroupKernel_*: sm__inst_issued, "
+                     "ALU pipe busiest)",
+            "ms": ms, "candidate_tests": tests, "tests_per_particle": tests / n,
+            "flop_per_test": SEARCH_FLOPS_PER_TEST, "fp32_tflops": tf / 1e12, "fp32_frac": tf / fp32_peak,
+            "list_bytes": list_bytes, "list_gbs": gbs, "hbm_frac": gbs / hbm_gbs if hbm_gbs else None}
+
+
+def mixed_errors(ref64: dict, r32: dict) -> dict:
+    """errors of the mixed form against the FP64 form of the same run, per output field (device
+    tensors; rho and xm max relative per particle, the rest max abs over the field's max or normwise)"""
+    import torch
+
+    def mx(t):
+        return float(t.abs().max().item())
+
+    a64 = torch.stack([ref64["ax"], ref64["ay"], ref64["az"]], 1)
+    a32 = torch.stack([r32["ax"], r32["ay"], r32["az"]], 1)
+    err = {"rho_max_rel": mx((r32["rho"] - ref64["rho"]) / ref64["rho"]),
+           "xm_max_rel": mx((r32["xm"] - ref64["xm"]) / ref64["xm"]),
+           "a_normwise": float((torch.linalg.norm(a32 - a64) / torch.linalg.norm(a64).clamp_min(1e-300)).item()),
+           "du_normwise": float((torch.linalg.norm(r32["du"] - ref64["du"]) /
+                                 torch.linalg.norm(ref64["du"]).clamp_min(1e-300)).item())}
+    cij = [f"c{a}{b}" for a, b in ("11", "12", "13", "22", "23", "33")]
+    cmag = max(mx(ref64[k]) for k in cij)
+    err["cij_max_over_tensor_max"] = max(mx(r32[k] - ref64[k]) for k in cij) / cmag
+    for k in ("divv", "curlv", "alpha", "du"):
+        scale = mx(ref64[k])
+        err[f"{k}_max_over_field_max"] = mx(r32[k] - ref64[k]) / scale if scale > 0 else mx(r32[k] - ref64[k])
+    return err
 
 
 def main() -> None:
@@ -269,7 +353,7 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sedov200_jit")
     ap.add_argument("--variant", default="ve", choices=["ve", "std"])
-    ap.add_argument("--cpu-side", type=int, default=100)
+    ap.add_argument("--no-configs", action="store_true", help="skip the Fourier 27M and sphere 10M blocks")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -277,6 +361,7 @@ def main() -> None:
     ap.add_argument("--no-integration", action="store_true")
     ap.add_argument("--adjoint-side", type=int, default=100)
     args = ap.parse_args()
+    set_cpu_threads()
 
     if args.impl == "reference":
         run_reference(args)
@@ -327,35 +412,53 @@ def main() -> None:
         ms = R.max_over_ranks(e0.elapsed_time(e1), world, dev)
         return ms, stage_sum / steps, ctx.launches() - l0, ck
 
-    # ---------------- FP64 form (headline)
-    d64 = sph.ParticlesData.from_workload(wl, "fp64", dev)
-    box = sph.Box(wl.box.copy(), wl.bc.copy())
-    ms64, st64, launches, clocks = timed_sweeps(d64, box, args.steps, args.warmup)
-    stats = ctx.stats()
-    pairs = stats["nc_sum"]
-    value = R.job_throughput(n, args.steps, world, ms64)
+    names = STAGES_VE if args.variant == "ve" else STAGES_STD
+    flops = VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR
 
-    # dominant kernel: largest per-stage time of the FP64 sweep
-    names = STAGES_VE if args.variant == "ve" else ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
-    dom = int(np.argmax(st64))
-    flops_pp = (VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR).get(names[dom])
-    if flops_pp:
-        achieved = pairs * flops_pp / (st64[dom] * 1e-3)
-        traffic = NCU_DRAM_BYTES_PER_PARTICLE.get(names[dom])
-        roofline = {"bound": "fp64", "kernel": names[dom], "achieved": achieved / 1e12, "peak": fp64_peak / 1e12,
-                    "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                    "traffic": traffic * n if traffic else None,
-                    "traffic_source": "ncu dram bytes of the same kernel at 1M particles, scaled by particles",
-                    "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                    "algorithmic": f"{pairs} pairs x {flops_pp} flop/pair per launch",
-                    "hbm_peak_gbs": peaks.get("hbm_gbs")}
-        if traffic and peaks.get("hbm_gbs"):  # the same kernel against HBM: DRAM bytes over its time
-            gbs = float(traffic * n / (st64[dom] * 1e-3) / 1e9)
-            roofline["hbm_achieved_gbs"] = gbs
-            roofline["hbm_frac"] = gbs / peaks["hbm_gbs"]
-    else:
-        roofline = {"bound": "hbm", "kernel": names[dom], "achieved": None, "peak": peaks.get("hbm_gbs"),
-                    "unit": "GB/s", "frac": None, "traffic": None}
+    def run_form(w, precision, steps, warmup):
+        """timed sweeps of one form on workload w; returns the record, the particle set and stats"""
+        d = sph.ParticlesData.from_workload(w, precision, dev)
+        b = sph.Box(w.box.copy(), w.bc.copy())
+        ms, st, nl, ck = timed_sweeps(d, b, steps, warmup)
+        stats = ctx.stats()
+        rec = {"value": R.job_throughput(w.n, steps, world, ms), "unit": UNIT, "ms_per_step": ms / steps,
+               "stages_ms": {names[k]: round(float(st[k]), 3) for k in range(len(names)) if names[k] != "-"}}
+        return rec, d, stats, st, nl, ck
+
+    def mixed_vs_fp64(w, rec64, d64, steps, warmup):
+        """the mixed form on workload w against the FP64 results of this run (d64 is released)"""
+        ref64 = {k: d64.f[k].double().clone() for k in CMP_FIELDS}
+        d64 = None
+        torch.cuda.empty_cache()
+        rec32, d32, stats32, st32, _, _ = run_form(w, "mixed", steps, warmup)
+        r32 = {k: d32.f[k].double() for k in CMP_FIELDS}
+        rec32["speedup_vs_fp64"] = rec32["value"] / rec64["value"]
+        rec32["errors_vs_fp64"] = mixed_errors(ref64, r32)
+        rec32["roofline"] = pair_roofline(st32, names, int(stats32["nc_sum"]), flops, fp32_peak, "fp32")
+        rec32["neighbors_roofline"] = search_roofline(stats32, float(st32[1]), w.n, fp32_peak,
+                                                      peaks.get("hbm_gbs"))
+        rec32["dominant_stage"] = names[int(np.argmax(st32))]
+        rec32["dominant_fp32_frac"] = rec32["roofline"]["frac"]
+        del ref64, r32, d32
+        torch.cuda.empty_cache()
+        return rec32
+
+    # ---------------- FP64 form (headline)
+    rec64, d64, stats, st64, launches, clocks = run_form(wl, "fp64", args.steps, args.warmup)
+    ms64 = rec64["ms_per_step"] * args.steps
+    pairs = stats["nc_sum"]
+    value = rec64["value"]
+
+    # dominant kernel: the pair pass with the largest share of the FP64 sweep (the FP64 pipe bounds it)
+    roofline = pair_roofline(st64, names, pairs, flops, fp64_peak, "fp64")
+    traffic = NCU_DRAM_BYTES_PER_PARTICLE.get(roofline["kernel"])
+    roofline["traffic"] = traffic * n if traffic else None
+    roofline["traffic_source"] = "ncu dram bytes of the same kernel at 1M particles, scaled by particles"
+    roofline["hbm_peak_gbs"] = peaks.get("hbm_gbs")
+    if traffic and peaks.get("hbm_gbs"):  # the same kernel against HBM: DRAM bytes over its time
+        gbs = float(traffic * n / (roofline["ms"] * 1e-3) / 1e9)
+        roofline["hbm_achieved_gbs"] = gbs
+        roofline["hbm_frac"] = gbs / peaks["hbm_gbs"]
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -364,51 +467,35 @@ def main() -> None:
            "config": bench_config(args, world), "n_particles": n,
            "roofline": roofline, "gpu_launches": launches // max(1, args.steps) * args.steps,
            "clocks": clocks,
-           "stages_ms": {names[k]: round(float(st64[k]), 3) for k in range(len(names)) if names[k] != "-"},
+           "stages_ms": rec64["stages_ms"],
            "neighbors": {"pairs": pairs, "mean": pairs / n, "max_nc": stats["nc_max"], "capped": stats["capped"],
-                         "candidates": stats["candidates"], "fp64_rechecks": stats["fp64_rechecks"]},
-           "fp32_peak_tflops": fp32_peak / 1e12}
+                         "candidates": stats["candidates"], "fp64_rechecks": stats["fp64_rechecks"],
+                         "roofline": search_roofline(stats, float(st64[1]), n, fp32_peak, peaks.get("hbm_gbs"))},
+           "fp32_peak_tflops": fp32_peak / 1e12, "fp64_peak_tflops": fp64_peak / 1e12}
     if args.workload in ("fourier300", "sphere10M"):
         out["structure"] = structure_report(ctx, d64, stats, int(wl.params["ngmax"]))
 
     # ---------------- mixed form on the same workload, errors against this run's FP64 results
     if not args.no_mixed:
-        ref64 = {k: d64.f[k].double().cpu().numpy()
-                 for k in ("xm", "kx", "rho", "ax", "ay", "az", "du", "c11", "c12", "c13", "c22", "c23", "c33",
-                           "divv", "curlv", "alpha")}
-        del d64
-        torch.cuda.empty_cache()
-        d32 = sph.ParticlesData.from_workload(wl, "mixed", dev)
-        box32 = sph.Box(wl.box.copy(), wl.bc.copy())
-        ms32, st32, _, _ = timed_sweeps(d32, box32, args.steps, args.warmup)
-        v32 = R.job_throughput(n, args.steps, world, ms32)
-        r32 = {k: d32.f[k].double().cpu().numpy() for k in ref64}
-        a64 = np.stack([ref64["ax"], ref64["ay"], ref64["az"]], 1)
-        a32 = np.stack([r32["ax"], r32["ay"], r32["az"]], 1)
-        err = {"rho_max_rel": float(np.max(np.abs(r32["rho"] - ref64["rho"]) / np.abs(ref64["rho"]))),
-               "xm_max_rel": float(np.max(np.abs(r32["xm"] - ref64["xm"]) / np.abs(ref64["xm"]))),
-               "a_normwise": float(np.linalg.norm(a32 - a64) / max(np.linalg.norm(a64), 1e-300)),
-               "du_normwise": float(np.linalg.norm(r32["du"] - ref64["du"]) / max(np.linalg.norm(ref64["du"]),
-                                                                                   1e-300)),
-               "c11_max_rel": float(np.max(np.abs(r32["c11"] - ref64["c11"])) / np.max(np.abs(ref64["c11"])))}
-        cij = [f"c{a}{b}" for a, b in ("11", "12", "13", "22", "23", "33")]
-        cmag = max(float(np.max(np.abs(ref64[k]))) for k in cij)
-        err["cij_max_over_tensor_max"] = max(float(np.max(np.abs(r32[k] - ref64[k]))) for k in cij) / cmag
-        for k in ("divv", "curlv", "alpha"):
-            scale = float(np.max(np.abs(ref64[k])))
-            err[f"{k}_max_over_field_max"] = (float(np.max(np.abs(r32[k] - ref64[k]))) / scale) if scale > 0 else \
-                float(np.max(np.abs(r32[k] - ref64[k])))
-        dom32 = int(np.argmax(st32))
-        fpp32 = (VE_FLOPS_PER_PAIR if args.variant == "ve" else STD_FLOPS_PER_PAIR).get(names[dom32])
-        out["mixed"] = {"value": v32, "unit": UNIT, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
-                        "errors_vs_fp64": err,
-                        "stages_ms": {names[k]: round(float(st32[k]), 3) for k in range(len(names))
-                                      if names[k] != "-"},
-                        "dominant": names[dom32],
-                        "dominant_fp32_frac": (pairs * fpp32 / (st32[dom32] * 1e-3) / fp32_peak) if fpp32 else None}
-        d64 = None
-        del d32
-        torch.cuda.empty_cache()
+        out["mixed"] = mixed_vs_fp64(wl, rec64, d64, args.steps, args.warmup)
+    d64 = None
+    torch.cuda.empty_cache()
+
+    # ---------------- the other configurations: Fourier 27M (the mixed form's own, v != 0) and the
+    # clustered 10M sphere, FP64 and mixed, with structure and per-field errors
+    if not args.no_configs and args.workload == "sedov200_jit":
+        out["configs"] = {}
+        for cname, (csteps, cwarm) in EXTRA_CONFIGS.items():
+            cw = make_workload(cname)
+            c64, cd, cstats, cst, _, _ = run_form(cw, "fp64", csteps, cwarm)
+            c64["roofline"] = pair_roofline(cst, names, int(cstats["nc_sum"]), flops, fp64_peak, "fp64")
+            blk = {"workload": WORKLOADS[cname][0], "n_particles": cw.n, "steps": csteps, "warmup": cwarm,
+                   "fp64": c64, "structure": structure_report(ctx, cd, cstats, int(cw.params["ngmax"]))}
+            blk["mixed"] = mixed_vs_fp64(cw, c64, cd, csteps, cwarm)
+            cd = None
+            out["configs"][cname] = blk
+            del cw
+            torch.cuda.empty_cache()
 
     # ---------------- end to end through the C ABI with host buffers (pinned), FP64 form
     if not args.no_e2e:
@@ -496,7 +583,7 @@ def main() -> None:
         out["adjoint"]["mixed"] = mixed
 
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_side, workload=args.workload, variant=args.variant)
+        out["cpu_baseline"] = cpu_baseline(wl, args.workload, variant=args.variant)
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

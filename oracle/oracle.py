@@ -49,7 +49,8 @@ class OracleOut(C.Structure):
                 ("box", C.c_double * 6), ("num_leaves", C.c_int64), ("num_nodes", C.c_int64),
                 ("num_internal", C.c_int64), ("level_range", C.c_int32 * 23), ("h_iter_fails", C.c_int64),
                 ("minDtCourant", C.c_double), ("t_keys", C.c_double), ("t_tree", C.c_double),
-                ("t_nbr", C.c_double), ("t_hydro", C.c_double), ("threads_used", C.c_int32)]
+                ("t_nbr", C.c_double), ("t_hydro", C.c_double), ("threads_used", C.c_int32),
+                ("centers", C.c_void_p), ("sizes", C.c_void_p)]
 
 
 def build_port() -> Path:
@@ -132,6 +133,10 @@ class Oracle:
             res["prefixes"] = np.zeros(ncap, np.uint64)
             res["child_offsets"] = np.zeros(ncap, np.int32)
             res["internal_to_leaf"] = np.zeros(ncap, np.int32)
+            res["centers"] = np.zeros(3 * ncap)
+            res["sizes"] = np.zeros(3 * ncap)
+            out.centers = res["centers"].ctypes.data
+            out.sizes = res["sizes"].ctypes.data
             out.leaves_cap = cap
             out.nodes_cap = ncap
             out.leaves = res["leaves"].ctypes.data
@@ -157,6 +162,8 @@ class Oracle:
             nn = out.num_nodes
             for k in ("prefixes", "child_offsets", "internal_to_leaf"):
                 res[k] = res[k][:nn]
+            for k in ("centers", "sizes"):
+                res[k] = res[k][:3 * nn].reshape(nn, 3)
         res["num_leaves"] = L
         res["num_nodes"] = out.num_nodes
         res["num_internal"] = out.num_internal

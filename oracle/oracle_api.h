@@ -75,6 +75,8 @@ typedef struct {
     double minDtCourant;
     double t_keys, t_tree, t_nbr, t_hydro;   /* wall seconds per stage */
     int32_t threads_used;
+    double* centers;             /* [3 * nodes_cap] geometric node centers (nodeFpCenters), x y z per node */
+    double* sizes;               /* [3 * nodes_cap] geometric node half sizes */
 } oracle_out;
 
 int oracle_sweep(const oracle_in* in, oracle_out* out);

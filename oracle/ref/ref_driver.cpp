@@ -160,6 +160,8 @@ extern "C" int oracle_sweep(const oracle_in* in, oracle_out* out)
             std::memcpy(out->child_offsets, octree.childOffsets.data(), sizeof(int32_t) * octree.numNodes);
         if (out->internal_to_leaf)
             std::memcpy(out->internal_to_leaf, octree.internalToLeaf.data(), sizeof(int32_t) * octree.numNodes);
+        if (out->centers) std::memcpy(out->centers, centers.data(), sizeof(double) * 3 * octree.numNodes);
+        if (out->sizes) std::memcpy(out->sizes, sizes.data(), sizeof(double) * 3 * octree.numNodes);
     }
     double t2   = omp_get_wtime();
     out->t_tree = t2 - t1;

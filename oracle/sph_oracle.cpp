@@ -838,6 +838,8 @@ extern "C" int oracle_sweep(const oracle_in* in, oracle_out* out)
                 std::memcpy(out->child_offsets, oct.childOffsets.data(), sizeof(int32_t) * oct.numNodes);
             if (out->internal_to_leaf)
                 std::memcpy(out->internal_to_leaf, oct.internalToLeaf.data(), sizeof(int32_t) * oct.numNodes);
+            if (out->centers) std::memcpy(out->centers, oct.center.data(), sizeof(double) * 3 * oct.numNodes);
+            if (out->sizes) std::memcpy(out->sizes, oct.size.data(), sizeof(double) * 3 * oct.numNodes);
         }
     }
     double t2 = omp_get_wtime();

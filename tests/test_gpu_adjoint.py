@@ -8,7 +8,7 @@ L = sum (rho - rho_target)^2 + sum |a|^2 on the frozen neighbour lists.
 * Reference gradient: torch autograd through the FP64 torch restatement of the same chain on the
   same edges (tests/torch_reference.py), in both kernel forms (the reference's linear table and the
   smooth cubic pieces); bar normwise 1e-9 per field.
-* Central differences: smooth kernel form, eps = 1e-6 absolute for every field, 64 coordinates from
+* Central differences: smooth kernel form, eps = 1e-6 (times h for h), 64 coordinates from
   PCG64(55555); a coordinate whose stencil straddles a kink of the forward (the viscosity branch) is
   reported and replaced by the next draw (tests/fd_check.py).  Bar: relative agreement <= 1e-6 on
   every checked coordinate.  The full-size version (1M particles) is tests/test_gpu_adjoint_fd.py.

@@ -10,7 +10,7 @@ differentiable), so the only kinks left are the branches of the physics (artific
 switch, Atwood ramp, max(0, .), signal-velocity maxima, the avClean clamp).  The adjoint's gradient
 comes from the default forms (one evaluation per mutual pair, forward tape); the central differences
 from the deterministic forward (bitwise reproducible sums).  64 coordinates are drawn from
-PCG64(55555) over (x y z vx vy vz h u) x particles, eps = 1e-6 absolute for every field; each
+PCG64(55555) over (x y z vx vy vz h u) x particles, eps = 1e-6 (times h for h); each
 coordinate whose +-eps / +-2 eps stencil straddles a kink of the forward is reported and replaced by
 the next draw (tests/fd_check.py).  Bar: |adjoint - central difference| <= 1e-6 |central difference|
 on every one of the 64 checked coordinates, positions and smoothing lengths included.

@@ -10,7 +10,7 @@ sum |a|^2 (+ a seed on du for the reference-gradient test) on the frozen neighbo
 
 * Reference gradient: every form of the adjoint, avClean on and off, in both kernel forms (the
   reference's linear table, the smooth cubic pieces); bar normwise 1e-9 per field.
-* Central differences: smooth kernel form, eps = 1e-6 absolute for every field, 64 coordinates from
+* Central differences: smooth kernel form, eps = 1e-6 (times h for h), 64 coordinates from
   PCG64(55555); a coordinate whose stencil straddles a kink of the forward (AV switch, Atwood ramp,
   signal-velocity maximum, max(0, .), avClean clamp) is reported and replaced by the next draw
   (tests/fd_check.py).  Bar: relative agreement <= 1e-6 on every checked coordinate.  The full-size
