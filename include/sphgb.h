@@ -155,6 +155,33 @@ int sphgb_domain_sync(sphgb_ctx* ctx, sphgb_particles* p, sphgb_box* box);
 int sphgb_get_tree(sphgb_ctx* ctx, const uint64_t** leaves, const uint32_t** layout,
                    const uint64_t** prefixes, const int32_t** child_offsets,
                    const int32_t** internal_to_leaf, sphgb_stats* stats);
+/* cstone::OctreeNsView (domain/include/cstone/tree/octree.hpp:279-300) of the tree built by the
+ * last sync, as cstone::Domain::octreeProperties returns it (domain/include/cstone/domain/domain.hpp:
+ * 416-428): device pointers, valid until the next sync */
+typedef struct {
+    int64_t num_leaf_nodes, num_nodes, num_internal;
+    const uint64_t* prefixes;        /* node keys with the placeholder bit, level-major order */
+    const int32_t* child_offsets;    /* first child of each node, 0 for a leaf */
+    const int32_t* internal_to_leaf; /* leaf index of each leaf node (the reference's labels otherwise) */
+    const int32_t* level_range;      /* 23 entries: first node of each level */
+    const uint64_t* leaves;          /* cornerstone leaf keys, num_leaf_nodes + 1 entries */
+    const uint32_t* layout;          /* first particle of each leaf, num_leaf_nodes + 1 entries */
+    const double* centers;           /* geometric node centers x y z (focus/source_center.hpp:129-141) */
+    const double* sizes;             /* geometric node half sizes x y z (sfc/box.hpp:317-334) */
+    int32_t max_depth;               /* deepest level that holds a node */
+} sphgb_octree_view;
+int sphgb_get_octree_view(sphgb_ctx* ctx, sphgb_octree_view* view);
+/* the parameters in force (the values sphgb_set_params stored) */
+int sphgb_get_params(sphgb_ctx* ctx, sphgb_params* params);
+/* sph::computeGroups / computeSpatialGroups on the GPU (sph/include/sph/groups.hpp:41-56,
+ * domain/include/cstone/traversal/groups_gpu.cu:58-135): the target groups of this library's pair
+ * passes are the runs of 32 SFC-consecutive particles of [first, last), one warp each.  Writes
+ * *num_groups = ceil((last - first) / 32) and, when `splits` is non-null, the num_groups + 1 group
+ * boundaries first, first + 32, ..., last into splits (device, `capacity` entries), so that
+ * groupStart = splits and groupEnd = splits + 1 as in cstone::GroupData (traversal/groups.hpp:37-52).
+ * groupDt of sphgb_compute_momentum_energy is indexed by these groups. */
+int sphgb_target_groups(sphgb_ctx* ctx, int64_t first, int64_t last, uint32_t* splits, int64_t capacity,
+                        int64_t* num_groups);
 /* sorted order of the last sync: order[i] = pre-sync index of sorted particle i (device) */
 int sphgb_get_order(sphgb_ctx* ctx, const uint32_t** order);
 /* permute one more per-particle field (device, n elements of elem_bytes = 1, 2, 4 or 8) into the

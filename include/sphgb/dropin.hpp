@@ -73,6 +73,12 @@ template<class Dataset>
 sphgb_particles particles(Dataset& d)
 {
     auto& dv = d.devData;
+    // momentumAndEnergyJLoop takes the energy coefficient from tdpdTrho when that field is active
+    // (hydro_ve/momentum_energy_kern.hpp:213-214); this library always uses prho, so an active
+    // tdpdTrho (a non-ideal equation of state) is refused instead of giving a different du
+    if (dv.tdpdTrho.size() != 0)
+        throw std::runtime_error("sphgb: the tdpdTrho field is active; only the ideal-gas energy coefficient "
+                                 "prho is supported");
     sphgb_particles p{};
     p.n = int64_t(dv.x.size());
     p.precision = precisionOf<Dataset>();
@@ -154,85 +160,155 @@ sphgb_box toBox(const Box& box)
     return b;
 }
 
-/*! cstone::Domain at one rank (domain/include/cstone/domain/domain.hpp:181-234, 416-428):
- *  sync() fits the box, sorts by Hilbert key, permutes x y z h and every property field, and
- *  builds the cornerstone tree with the bucket size; exchangeHalos is a no-op at one rank. */
+//! the tree summary the propagators print (ipropagator.hpp:108,124-125): leaf count and depth
+struct TreeSummary {
+    struct View {
+        int64_t numLeafNodes;
+    };
+    int64_t leaves = 0;
+    int maxDepth = 0;
+    int64_t numLeafNodes() const { return leaves; }
+    View octreeViewAcc() const { return {leaves}; }
+    int depth() const { return maxDepth; }
+};
+
+/*! Domain::octreeProperties at one rank: converts to the caller's cstone::OctreeNsView<T, KeyType>
+ *  (tree/octree.hpp:279-300) member by member; every pointer is device memory of the context, valid
+ *  until the next sync.  searchExtFactor keeps its default 1 (the tree is converged at every sync
+ *  of domain mode 1 that rebuilds it, and the search does not read it). */
+struct OctreeNsViewProxy {
+    sphgb_octree_view v;
+    template<class View>
+    operator View() const
+    {
+        View o{};
+        static_assert(sizeof(*o.prefixes) == sizeof(uint64_t), "the tree is built on 64-bit SFC keys");
+        static_assert(sizeof(*o.centers) == 3 * sizeof(double), "node centers are FP64 Vec3");
+        o.numLeafNodes = decltype(o.numLeafNodes)(v.num_leaf_nodes);
+        o.prefixes = reinterpret_cast<decltype(o.prefixes)>(v.prefixes);
+        o.childOffsets = reinterpret_cast<decltype(o.childOffsets)>(v.child_offsets);
+        o.internalToLeaf = reinterpret_cast<decltype(o.internalToLeaf)>(v.internal_to_leaf);
+        o.levelRange = reinterpret_cast<decltype(o.levelRange)>(v.level_range);
+        o.leaves = reinterpret_cast<decltype(o.leaves)>(v.leaves);
+        o.layout = reinterpret_cast<decltype(o.layout)>(v.layout);
+        o.centers = reinterpret_cast<decltype(o.centers)>(v.centers);
+        o.sizes = reinterpret_cast<decltype(o.sizes)>(v.sizes);
+        return o;
+    }
+};
+
+/*! cstone::Domain at one rank (domain/include/cstone/domain/domain.hpp:181-234, 372-428) with the
+ *  surface HydroVeProp / HydroProp use (main/src/propagator/ve_hydro.hpp:119-217,
+ *  std_hydro.hpp:110-170, ipropagator.hpp:104-130):
+ *   sync(keys, x, y, z, h, tuple<properties...>, tuple<scratch...>) fits the box, sorts by Hilbert
+ *     key, permutes x y z h and every property, writes the sorted keys and builds the cornerstone
+ *     tree with bucketSizeFocus; the syncs of one domain are the steps of one simulation (box shrink
+ *     limit and focus-tree update, domain mode 1).  Scratch buffers are not needed (the context
+ *     owns its scratch) and keep their contents.
+ *   startIndex() = 0, endIndex() = nParticles() = nParticlesWithHalos() = particles of the last sync;
+ *   octreeProperties(), box(), globalTree(), focusTree(); exchangeHalos is a no-op (no halos). */
 template<class KeyType, class T, class Box>
 class SingleRankDomain
 {
 public:
     // the tree the reference's octreeProperties() exposes is its focus tree, refined to
     // bucketSizeFocus (domain/domain.hpp:416-428); the coarser global tree (bucketSize) only assigns
-    // ranks, which has no counterpart at one rank
+    // ranks, which has no counterpart at one rank, so globalTree() reports the focus tree too
     SingleRankDomain(int /*rank*/, int /*numRanks*/, unsigned /*bucketSize*/, unsigned bucketSizeFocus,
                      float /*theta*/, const Box& box, int device = 0)
         : box_(box)
         , bucket_(bucketSizeFocus)
         , device_(device)
     {
+        static_assert(sizeof(KeyType) == sizeof(uint64_t), "the tree is built on 64-bit SFC keys");
     }
 
-    template<class Dataset, class... Props>
-    void sync(Dataset& d, Props&... extraProperties)
+    //! Domain::sync (domain.hpp:181-234) at one rank
+    template<class KeyVec, class VectorX, class VectorH, class... Props, class... Scratch>
+    void sync(KeyVec& keys, VectorX& x, VectorX& y, VectorX& z, VectorH& h, std::tuple<Props&...> properties,
+              std::tuple<Scratch&...> /*scratchBuffers*/)
     {
-        sphgb_ctx* c = bind(d, device_);
-        if (!started_) {  // this domain's syncs are the steps of one simulation (box shrink limit)
-            check(sphgb_set_domain_mode(c, 1), "sphgb_set_domain_mode");
-            started_ = true;
-        }
-        sphgb_params prm{};
-        sphgb_default_params(&prm);
-        prm.ng0 = d.ng0;
-        prm.ngmax = d.ngmax;
-        prm.bucket = bucket_;
-        prm.gamma = double(d.gamma);
-        prm.Kcour = double(d.Kcour);
-        prm.sincIndex = double(d.sincIndex);
-        prm.alphamin = double(d.alphamin);
-        prm.alphamax = double(d.alphamax);
-        prm.decay_constant = double(d.decay_constant);
-        prm.minDt = double(d.minDt);
-        check(sphgb_set_params(c, &prm), "sphgb_set_params");
-        sphgb_particles p = particles(d);
-        // dependent fields are recomputed by the passes; only conserved ones move with the sort
+        static_assert(sizeof(*rawPtr(x)) == sizeof(double), "coordinates are FP64 (SphTypes::CoordinateType)");
+        sphgb_ctx* c = context(device_);
+        begin(c);
+        const std::size_t n = x.size();
+        if (y.size() != n || z.size() != n || h.size() != n) throw std::runtime_error("Domain::sync: field sizes differ");
+        if (keys.size() < n) keys.resize(n);
         sphgb_particles q{};
-        q.n = p.n;
-        q.precision = p.precision;
-        q.keys = p.keys;
-        q.x = p.x;
-        q.y = p.y;
-        q.z = p.z;
-        q.u = p.u;
-        q.h = p.h;
-        q.m = p.m;
-        q.vx = p.vx;
-        q.vy = p.vy;
-        q.vz = p.vz;
-        q.alpha = p.alpha;
+        q.n = int64_t(n);
+        q.precision = sizeof(*rawPtr(h)) == sizeof(double) ? SPHGB_FP64 : SPHGB_MIXED;
+        q.keys = reinterpret_cast<uint64_t*>(ptr(keys));
+        q.x = static_cast<double*>(ptr(x));
+        q.y = static_cast<double*>(ptr(y));
+        q.z = static_cast<double*>(ptr(z));
+        q.h = ptr(h);
         sphgb_box b = toBox(box_);
         check(sphgb_domain_sync(c, &q, &b), "Domain::sync");
-        (applyOrder(c, extraProperties), ...);
-        box_ = Box(b.lim[0], b.lim[1], b.lim[2], b.lim[3], b.lim[4], b.lim[5], box_.boundaryX(), box_.boundaryY(),
-                   box_.boundaryZ());
+        std::apply([&](auto&... v) { (applyOrder(c, v, n), ...); }, properties);
+        finish(c, b, n);
+    }
+
+    /*! the same sync over the conserved fields of a dataset (x y z h m u vx vy vz alpha and keys of
+     *  its devData) plus any further device vectors to permute alike */
+    template<class Dataset, class... Props>
+    void syncDataset(Dataset& d, Props&... extraProperties)
+    {
+        auto& dv = d.devData;
+        sync(dv.keys, dv.x, dv.y, dv.z, dv.h, std::tie(dv.m, dv.u, dv.vx, dv.vy, dv.vz, dv.alpha, extraProperties...),
+             std::tuple<>{});
     }
 
     const Box& box() const { return box_; }
-    std::size_t startIndex() const { return 0; }
-    template<class Dataset>
-    std::size_t endIndex(Dataset& d) const
+    uint32_t startIndex() const { return 0; }
+    uint32_t endIndex() const { return uint32_t(n_); }
+    uint32_t nParticles() const { return uint32_t(n_); }
+    uint32_t nParticlesWithHalos() const { return uint32_t(n_); }
+    const TreeSummary& globalTree() const { return tree_; }
+    const TreeSummary& focusTree() const { return tree_; }
+
+    OctreeNsViewProxy octreeProperties() const
     {
-        return d.devData.x.size();
+        OctreeNsViewProxy p{};
+        check(sphgb_get_octree_view(context(device_), &p.v), "Domain::octreeProperties");
+        return p;
     }
+
     template<class... Fields>
     void exchangeHalos(Fields&&...) const
     {
     }
 
 private:
-    template<class V>
-    static void applyOrder(sphgb_ctx* c, V& v)
+    void begin(sphgb_ctx* c)
     {
-        if (v.size() == 0) return;
+        if (!started_) {  // this domain's syncs are the steps of one simulation (box shrink limit)
+            check(sphgb_set_domain_mode(c, 1), "sphgb_set_domain_mode");
+            started_ = true;
+        }
+        sphgb_params prm{};
+        check(sphgb_get_params(c, &prm), "sphgb_get_params");
+        if (prm.bucket != bucket_) {
+            prm.bucket = bucket_;
+            check(sphgb_set_params(c, &prm), "sphgb_set_params");
+        }
+    }
+
+    void finish(sphgb_ctx* c, const sphgb_box& b, std::size_t n)
+    {
+        box_ = Box(b.lim[0], b.lim[1], b.lim[2], b.lim[3], b.lim[4], b.lim[5], box_.boundaryX(), box_.boundaryY(),
+                   box_.boundaryZ());
+        n_ = n;
+        sphgb_octree_view v{};
+        check(sphgb_get_octree_view(c, &v), "Domain::octreeProperties");
+        tree_.leaves = v.num_leaf_nodes;
+        tree_.maxDepth = v.max_depth;
+    }
+
+    template<class V>
+    static void applyOrder(sphgb_ctx* c, V& v, std::size_t n)
+    {
+        if (v.size() == 0) return;  // an inactive field
+        if (v.size() != n) throw std::runtime_error("Domain::sync: a property's size differs from x");
         check(sphgb_apply_order(c, ptr(v), int32_t(sizeof(*rawPtr(v)))), "sphgb_apply_order");
     }
 
@@ -240,6 +316,8 @@ private:
     unsigned bucket_;
     int device_;
     bool started_ = false;
+    std::size_t n_ = 0;
+    TreeSummary tree_;
 };
 
 /*! cstone::findNeighbors (domain/include/cstone/findneighbors.hpp:149-170) on the tree of the last
@@ -276,12 +354,27 @@ void findNeighborsSfc(std::size_t startIndex, std::size_t endIndex, Dataset& d, 
     check(s, "findNeighborsSfc");
 }
 
-//! sph::computeGroups: groups are the 32 SFC-consecutive targets of each warp; nothing to build
+/*! sph::computeGroups on the GPU (sph/include/sph/groups.hpp:41-56): the target groups of the pair
+ *  passes are the runs of 32 SFC-consecutive particles of [startIndex, endIndex) (one warp each);
+ *  groups.data (a device vector) receives their numGroups + 1 boundaries and the view members point
+ *  into it as in computeSpatialGroups, so groupDt and the rung logic of the propagators
+ *  (ve_hydro_bdt.hpp) see numGroups groups */
 template<class Dataset, class Box, class GroupData>
-void computeGroups(std::size_t startIndex, std::size_t endIndex, Dataset&, const Box&, GroupData& groups)
+void computeGroups(std::size_t startIndex, std::size_t endIndex, Dataset& d, const Box&, GroupData& groups)
 {
+    sphgb_ctx* c = bind(d);
+    int64_t ng = 0;
+    check(sphgb_target_groups(c, int64_t(startIndex), int64_t(endIndex), nullptr, 0, &ng), "computeGroups");
+    groups.data.resize(std::size_t(ng + 1));
+    static_assert(sizeof(*rawPtr(groups.data)) == sizeof(uint32_t), "cstone::LocalIndex is 32-bit");
+    check(sphgb_target_groups(c, int64_t(startIndex), int64_t(endIndex), reinterpret_cast<uint32_t*>(rawPtr(groups.data)),
+                              ng + 1, &ng),
+          "computeGroups");
     groups.firstBody = decltype(groups.firstBody)(startIndex);
     groups.lastBody = decltype(groups.lastBody)(endIndex);
+    groups.numGroups = decltype(groups.numGroups)(ng);
+    groups.groupStart = rawPtr(groups.data);
+    groups.groupEnd = rawPtr(groups.data) + 1;
 }
 
 #define SPHGB_DROPIN_PASS(NAME, CALL)                                                    \
@@ -377,6 +470,27 @@ void computePositions(const GroupView& grp, Dataset& d, const Box& box)
     auto& dv = d.devData;
     const sphgb_box b = toBox(box);
     const sphgb_timestep ts = timestepOf(d);
+    check(sphgb_compute_positions(c, &p, &b, ptr(dv.x_m1), ptr(dv.y_m1), ptr(dv.z_m1), ptr(dv.du_m1), &ts,
+                                  int64_t(grp.firstBody), int64_t(grp.lastBody)),
+          "computePositions");
+}
+
+/*! sph::computePositions with the reference's argument list (positions.hpp:177-200): every particle
+ *  on the step dt_forward after dt_m1[0] (the propagator passes d.minDt and {float(d.minDt_m1)}; a
+ *  braced list becomes the reference's Timestep::maxNumRungs = 4 entries, sph/timestep.h:19);
+ *  per-particle rungs are refused */
+template<class GroupView, class Dataset, class Box, class DtM1 = std::array<float, 4>>
+void computePositions(const GroupView& grp, Dataset& d, const Box& box, float dt_forward, const DtM1& dt_m1,
+                      const uint8_t* rung = nullptr)
+{
+    if (rung) throw std::runtime_error("computePositions: per-particle time-step rungs are not supported");
+    sphgb_ctx* c = bind(d);
+    sphgb_particles p = particles(d);
+    auto& dv = d.devData;
+    const sphgb_box b = toBox(box);
+    sphgb_timestep ts = timestepOf(d);
+    ts.minDt = double(dt_forward);
+    ts.minDt_m1 = double(dt_m1[0]);
     check(sphgb_compute_positions(c, &p, &b, ptr(dv.x_m1), ptr(dv.y_m1), ptr(dv.z_m1), ptr(dv.du_m1), &ts,
                                   int64_t(grp.firstBody), int64_t(grp.lastBody)),
           "computePositions");

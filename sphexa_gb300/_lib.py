@@ -52,6 +52,13 @@ class SphgbParticles(C.Structure):
                 + [("nc", C.c_void_p)])
 
 
+class SphgbOctreeView(C.Structure):
+    _fields_ = [("num_leaf_nodes", C.c_int64), ("num_nodes", C.c_int64), ("num_internal", C.c_int64),
+                ("prefixes", C.c_void_p), ("child_offsets", C.c_void_p), ("internal_to_leaf", C.c_void_p),
+                ("level_range", C.c_void_p), ("leaves", C.c_void_p), ("layout", C.c_void_p),
+                ("centers", C.c_void_p), ("sizes", C.c_void_p), ("max_depth", C.c_int32)]
+
+
 class SphgbStats(C.Structure):
     _fields_ = [("num_leaves", C.c_int64), ("num_nodes", C.c_int64), ("num_internal", C.c_int64),
                 ("level_range", C.c_int32 * 23), ("nc_sum", C.c_int64), ("nc_max", C.c_uint32),
@@ -95,6 +102,9 @@ SIGNATURES = {
     "sphgb_get_tree": [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                        C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(SphgbStats)],
     "sphgb_get_order": [_P, C.POINTER(C.c_void_p)],
+    "sphgb_get_octree_view": [_P, C.POINTER(SphgbOctreeView)],
+    "sphgb_get_params": [_P, C.POINTER(SphgbParams)],
+    "sphgb_target_groups": [_P, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)],
     "sphgb_apply_order": [_P, _P, C.c_int32],
     "sphgb_find_neighbors": [_P, _P, _P, _P, _P, C.c_int32, _I64, _I64, C.c_uint32, _P, _P],
     "sphgb_find_neighbors_sph": [_P, C.POINTER(SphgbParticles), _I64, _I64],

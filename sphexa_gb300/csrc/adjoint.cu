@@ -27,16 +27,29 @@ constexpr int kAdjBlock = 128;
 // kernel function value and derivative dw/dv at v, on the interval the forward passes select (from
 // the bits of v / dx): the slope of the linear interpolant, or the derivative of the cubic piece in
 // the smooth form
-__device__ __forceinline__ double lookupSlope(const Tab64& tab, double v, double& slope)
+template<bool Smooth>
+__device__ __forceinline__ double lookupSlope(const KTab<Smooth>& tab, double v, double& slope)
 {
     return lookupVSlope(tab, v, slope);
+}
+
+// the table a kernel reads, with the kernel form of its instantiation (FP64) or as it is (FP32)
+template<bool Smooth>
+__device__ __forceinline__ KTab<Smooth> kernelTab(const double2* t)
+{
+    return {t};
+}
+template<bool Smooth>
+__device__ __forceinline__ const float2* kernelTab(const float2* t)
+{
+    return t;
 }
 
 struct AdjArgs {
     // forward state
     const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *rho, *p, *c;
     const double *c11, *c12, *c13, *c22, *c23, *c33;
-    Tab64 wh;  // W in the context's form
+    const double2* wh;  // W in the context's form (the kernels' Smooth argument tells which)
     double K, gamma;
     DevBox box;
     // lists: own (transposed layout) and incoming (CSR by neighbour)
@@ -134,8 +147,8 @@ struct PairGrad {
     double hJ, rhoJ, pJ, CJ[6];           // partials of j's fields (WantJ)
 };
 
-template<bool WantI, bool WantJ>
-__device__ __forceinline__ void mePairAdj(const DevBox& b, const Tab64& tab, const Side& I, const Side& J,
+template<bool WantI, bool WantJ, bool Smooth>
+__device__ __forceinline__ void mePairAdj(const DevBox& b, const KTab<Smooth>& tab, const Side& I, const Side& J,
                                           const double gA[3], double gE, PairGrad& g)
 {
     double r[3];
@@ -227,8 +240,10 @@ __device__ __forceinline__ bool seedsOf(const AdjArgs& a, int64_t i, double gA[3
     return gA[0] != 0.0 || gA[1] != 0.0 || gA[2] != 0.0 || gE != 0.0;
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const Side S = loadSide(a, k);
@@ -241,7 +256,7 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
             for (unsigned q = 0; q < nc; ++q) {
                 const Side J = loadSide(a, a.lv.at(k, q));
                 PairGrad g;
-                mePairAdj<true, false>(a.box, a.wh, S, J, gA, gE, g);
+                mePairAdj<true, false>(a.box, tab, S, J, gA, gE, g);
                 for (int t = 0; t < 3; ++t) {
                     bx[t] += g.r[t];
                     bv[t] += g.v[t];
@@ -261,7 +276,7 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjKernel(AdjArgs a)
         if (!seedsOf(a, i, gA, gE)) continue;
         const Side I = loadSide(a, i);
         PairGrad g;
-        mePairAdj<false, true>(a.box, a.wh, I, S, gA, gE, g);
+        mePairAdj<false, true>(a.box, tab, I, S, gA, gE, g);
         for (int t = 0; t < 3; ++t) {
             bx[t] -= g.r[t];
             bv[t] -= g.v[t];
@@ -332,8 +347,10 @@ __device__ __forceinline__ double quadTau(const AdjArgs& a, int64_t i, const dou
 }
 
 // tau_i += V_j w(d/h_i) r r^T, V_j = m_j / rho_j
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const Side S = loadPos(a, k);
@@ -348,7 +365,7 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
             const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
             const double rinv = rsqrt(r2), d = r2 * rinv;
             double dw;
-            const double w = lookupSlope(a.wh, d * S.hInv, dw);
+            const double w = lookupSlope(tab, d * S.hInv, dw);
             const double Q = quadTau(a, k, r, Tr);
             const double V = J.moR;
             for (int t = 0; t < 3; ++t) bx[t] += V * (2.0 * w * Tr[t] + Q * dw * S.hInv * r[t] * rinv);
@@ -363,7 +380,7 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjKernel(AdjArgs a)
         const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
         const double rinv = rsqrt(r2), d = r2 * rinv;
         double dw;
-        const double w = lookupSlope(a.wh, d * I.hInv, dw);
+        const double w = lookupSlope(tab, d * I.hInv, dw);
         const double Q = quadTau(a, i, r, Tr);
         const double V = S.moR;
         for (int t = 0; t < 3; ++t) bx[t] -= V * (2.0 * w * Tr[t] + Q * dw * I.hInv * r[t] * rinv);
@@ -388,8 +405,10 @@ __global__ void eosAdjKernel(AdjArgs a)
 }
 
 // rho_i = K h_i^-3 (m_i + sum_j m_j w(d/h_i))
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const Side S = loadPos(a, k);
@@ -408,7 +427,7 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
             const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
             const double rinv = rsqrt(r2), d = r2 * rinv;
             double dw;
-            lookupSlope(a.wh, d * S.hInv, dw);
+            lookupSlope(tab, d * S.hInv, dw);
             const double f = brk * a.K * hi3 * J.m * dw * S.hInv * rinv;
             for (int t = 0; t < 3; ++t) bx[t] += f * r[t];
             sdw += J.m * dw * d;
@@ -423,7 +442,7 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
         const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
         const double rinv = rsqrt(r2), d = r2 * rinv;
         double dw;
-        lookupSlope(a.wh, d * I.hInv, dw);
+        lookupSlope(tab, d * I.hInv, dw);
         const double hI3 = I.hInv * I.hInv * I.hInv;
         const double f = a.bRho[i] * a.K * hI3 * S.m * dw * I.hInv * rinv;
         (void)d;
@@ -442,14 +461,15 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjKernel(AdjArgs a)
 // of the mixed forward); every accumulation is FP64.
 template<class T>
 struct TabOf {
-    using type = Tab64;
+    using type = const double2*;
 };
 template<>
 struct TabOf<float> {
     using type = const float2*;
 };
 
-__device__ __forceinline__ double lookupSlopeT(const Tab64& tab, double v, double& slope)
+template<bool Smooth>
+__device__ __forceinline__ double lookupSlopeT(const KTab<Smooth>& tab, double v, double& slope)
 {
     return lookupSlope(tab, v, slope);
 }
@@ -541,9 +561,10 @@ __device__ __forceinline__ void geomT(const StdScatterArgs<T>& a, int64_t i, int
     }
 }
 
-template<class T>
+template<class T, bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) meAdjScatterT(StdScatterArgs<T> a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const T gA[3] = {a.sAx ? T(a.K * double(a.sAx[k])) : T(0), a.sAy ? T(a.K * double(a.sAy[k])) : T(0),
@@ -561,7 +582,7 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjScatterT(StdScatterArgs<T> a)
             geomT(a, k, j, r, d, rinv);
             const T v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
             T dwi, dwj;
-            const T wi = lookupSlopeT(a.wh, d * S.hInv, dwi), wj = lookupSlopeT(a.wh, d * J.hInv, dwj);
+            const T wi = lookupSlopeT(tab, d * S.hInv, dwi), wj = lookupSlopeT(tab, d * J.hInv, dwj);
             stdad::MeGrad<T> o;
             stdad::meStdAdjPair<T>(r, d, rinv, v, S, J, wi, dwi, wj, dwj, gA, gE, zero, T(0), o);
             for (int t = 0; t < 3; ++t) {
@@ -616,9 +637,10 @@ __global__ void iadPrepT(StdScatterArgs<T> a)
     for (int q = 0; q < 6; ++q) a.tauBar[q * a.n + k] = T(tauB[q]);
 }
 
-template<class T>
+template<class T, bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) iadAdjScatterT(StdScatterArgs<T> a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     T tauB[6];
@@ -631,7 +653,7 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjScatterT(StdScatterArgs<T> a)
         const int64_t j = a.lv.at(k, q);
         T r[3], d, rinv, dw;
         geomT(a, k, j, r, d, rinv);
-        const T w = lookupSlopeT(a.wh, d * hInv, dw);
+        const T w = lookupSlopeT(tab, d * hInv, dw);
         T rb[3], hIb, rhoJb;
         stdad::iadAdjTerm<T>(r, d, rinv, hInv, w, dw, a.moR[j], a.rhoInv[j], tauB, rb, hIb, rhoJb);
         for (int t = 0; t < 3; ++t) bx[t] += rb[t];
@@ -670,9 +692,10 @@ __global__ void gradsToDouble(int64_t n, const float* __restrict__ src, double* 
     for (int k = 0; k < 8; ++k) dst[k][i] = double(src[k * n + i]);
 }
 
-template<class T>
+template<class T, bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) densityAdjScatterT(StdScatterArgs<T> a)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const T rhob = a.bRho[k];
@@ -683,7 +706,7 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjScatterT(StdScatterArgs<T
         const int64_t j = a.lv.at(k, q);
         T r[3], d, rinv, dw;
         geomT(a, k, j, r, d, rinv);
-        lookupSlopeT(a.wh, d * hInv, dw);
+        lookupSlopeT(tab, d * hInv, dw);
         T rb[3], hIb;
         stdad::densityAdjTerm<T>(r, d, rinv, hInv, dw, a.m[j], T(a.K), rhob, rb, hIb);
         for (int t = 0; t < 3; ++t) bx[t] += rb[t];
@@ -729,8 +752,10 @@ __device__ __forceinline__ void pairGeom(const AdjArgs& a, int64_t i, int64_t j,
     d = r2 * rinv;
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) meAdjOnceKernel(AdjArgs a, OwnedView ov)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double gA[3], gE;
@@ -749,7 +774,7 @@ __global__ void __launch_bounds__(kAdjBlock) meAdjOnceKernel(AdjArgs a, OwnedVie
         pairGeom(a, k, j, r, d, rinv);
         const double v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
         double dwi, dwj;
-        const double wi = lookupSlope(a.wh, d * S.hInv, dwi), wj = lookupSlope(a.wh, d * J.hInv, dwj);
+        const double wi = lookupSlope(tab, d * S.hInv, dwi), wj = lookupSlope(tab, d * J.hInv, dwj);
         const double zero[3] = {0.0, 0.0, 0.0};
         stdad::MeGrad<> o;
         stdad::meStdAdjPair(r, d, rinv, v, S, J, wi, dwi, wj, dwj, anyK ? gA : zero, anyK ? gE : 0.0, gAj, gEj, o);
@@ -793,8 +818,10 @@ __device__ __forceinline__ void tauOf(const AdjArgs& a, int64_t i, double t[6])
     for (int q = 0; q < 6; ++q) t[q] = a.tauBar[q * a.n + i];
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) iadAdjOnceKernel(AdjArgs a, OwnedView ov)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double bx[3] = {0, 0, 0}, bh = 0, brho = 0, tauK[6];
@@ -806,7 +833,7 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjOnceKernel(AdjArgs a, OwnedVi
         const uint32_t j = ov.at(k, q, mutual);
         double r[3], d, rinv, dw;
         pairGeom(a, k, j, r, d, rinv);
-        double w = lookupSlope(a.wh, d * hInvK, dw);
+        double w = lookupSlope(tab, d * hInvK, dw);
         double rb[3], hIb, rhoJb;
         stdad::iadAdjTerm(r, d, rinv, hInvK, w, dw, a.mOverRho[j], a.rhoInv[j], tauK, rb, hIb, rhoJb);
         bh += hIb;
@@ -815,7 +842,7 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjOnceKernel(AdjArgs a, OwnedVi
             tauOf(a, j, tauJ);
             const double hInvJ = a.hInv[j];
             const double rm[3] = {-r[0], -r[1], -r[2]};
-            w = lookupSlope(a.wh, d * hInvJ, dw);
+            w = lookupSlope(tab, d * hInvJ, dw);
             double pb[3], hJb, rhoKb;
             stdad::iadAdjTerm(rm, d, rinv, hInvJ, w, dw, volK, rhoInvK, tauJ, pb, hJb, rhoKb);
             for (int t = 0; t < 3; ++t) rb[t] -= pb[t];
@@ -835,8 +862,10 @@ __global__ void __launch_bounds__(kAdjBlock) iadAdjOnceKernel(AdjArgs a, OwnedVi
     atomicAdd(a.bRho + k, brho);
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kAdjBlock) densityAdjOnceKernel(AdjArgs a, OwnedView ov)
 {
+    const auto tab = kernelTab<Smooth>(a.wh);
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     const double rhobK = a.bRho[k], hInvK = a.hInv[k], mK = a.m[k];
@@ -847,14 +876,14 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjOnceKernel(AdjArgs a, Own
         const uint32_t j = ov.at(k, q, mutual);
         double r[3], d, rinv, dw;
         pairGeom(a, k, j, r, d, rinv);
-        lookupSlope(a.wh, d * hInvK, dw);
+        lookupSlope(tab, d * hInvK, dw);
         double rb[3], hIb;
         stdad::densityAdjTerm(r, d, rinv, hInvK, dw, a.m[j], a.K, rhobK, rb, hIb);
         bh += hIb;
         if (mutual) {
             const double hInvJ = a.hInv[j];
             const double rm[3] = {-r[0], -r[1], -r[2]};
-            lookupSlope(a.wh, d * hInvJ, dw);
+            lookupSlope(tab, d * hInvJ, dw);
             double pb[3], hJb;
             stdad::densityAdjTerm(rm, d, rinv, hInvJ, dw, mK, a.K, a.bRho[j], pb, hJb);
             for (int t = 0; t < 3; ++t) rb[t] -= pb[t];
@@ -1034,18 +1063,21 @@ static int adjointStdScatter(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds
     }
     SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(T) * 9 * n, c->stream));
     const unsigned blocks = gridFor(n, kAdjBlock), eb = gridFor(n, 256);
-    stdQuotKernel<T><<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "stdQuotKernel"));
-    meAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "meAdjScatterT"));
-    iadPrepT<T><<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "iadPrepT"));
-    iadAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "iadAdjScatterT"));
-    eosAdjT<T><<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "eosAdjT"));
-    densityAdjScatterT<T><<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "densityAdjScatterT"));
+    SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+        constexpr bool S = !fp32 && decltype(smooth)::value;  // the FP32 form has one (linear) table
+        stdQuotKernel<T><<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "stdQuotKernel"));
+        meAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "meAdjScatterT"));
+        iadPrepT<T><<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "iadPrepT"));
+        iadAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "iadAdjScatterT"));
+        eosAdjT<T><<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "eosAdjT"));
+        densityAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        return launched(c, "densityAdjScatterT");
+    }));
     if constexpr (fp32) {
         gradsToDouble<<<eb, 256, 0, c->stream>>>(n, st + 20 * n, g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h, g->u);
         SPHGB_TRY(launched(c, "gradsToDouble"));
@@ -1132,27 +1164,28 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
     const unsigned blocks = gridFor(n, kAdjBlock);
     adjQuotientsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a, quot);
     SPHGB_TRY(launched(c, "adjQuotientsKernel"));
-    if (deterministic) {
-        meAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "meAdjKernel"));
-    } else {
+    if (!deterministic) {
         // accumulators start at zero; every contribution arrives by atomic add
         for (double* q : {g->x, g->y, g->z, g->vx, g->vy, g->vz, g->h})
             SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
         SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(double) * 9 * n, c->stream));
-        meAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-        SPHGB_TRY(launched(c, "meAdjOnceKernel"));
     }
-    iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "iadPrepKernel"));
-    if (deterministic) iadAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    else iadAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    SPHGB_TRY(launched(c, "iadAdjKernel"));
-    eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "eosAdjKernel"));
-    if (deterministic) densityAdjKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a);
-    else densityAdjOnceKernel<<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    SPHGB_TRY(launched(c, "densityAdjKernel"));
+    SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+        constexpr bool S = decltype(smooth)::value;
+        if (deterministic) meAdjKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        else meAdjOnceKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        SPHGB_TRY(launched(c, "meAdjKernel"));
+        iadPrepKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "iadPrepKernel"));
+        if (deterministic) iadAdjKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        else iadAdjOnceKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        SPHGB_TRY(launched(c, "iadAdjKernel"));
+        eosAdjKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "eosAdjKernel"));
+        if (deterministic) densityAdjKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+        else densityAdjOnceKernel<S><<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        return launched(c, "densityAdjKernel");
+    }));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;
 }

@@ -32,7 +32,7 @@ struct VeAdjArgs {
     const double *x, *y, *z, *vx, *vy, *vz, *h, *m, *u, *alpha0, *alpha, *xm, *kx, *gradh, *prho, *c, *divv;
     const double* C[6];
     const double* dV[6];
-    Tab64 wh, whd;  // W and dW/dv in the context's form
+    const double2 *wh, *whd;  // W and dW/dv in the context's form (the kernels' Smooth argument tells which)
     double K, gamma;
     AvPrm av;
     DevBox box;
@@ -64,7 +64,8 @@ struct VeAdjArgs {
 constexpr uint32_t kNoPair = 0xffffffffu;
 
 // interpolant value and slope (dw/dv) on the interval holding v (as the forward passes select it)
-__device__ __forceinline__ double lookupVS(const Tab64& tab, double v, double& slope)
+template<bool Smooth>
+__device__ __forceinline__ double lookupVS(const KTab<Smooth>& tab, double v, double& slope)
 {
     return lookupVSlope(tab, v, slope);
 }
@@ -142,8 +143,10 @@ __global__ void veQuotKernel(VeAdjArgs a)
 }
 
 // forward sums of the momentum-energy pass: en_i, avE_i (before max(0, .))
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) vePreMeKernel(VeAdjArgs a)
 {
+    const KTab<Smooth> tw{a.wh};
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= a.n) return;
     const MeSide I = meSide(a, i);
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreMeKernel(VeAdjArgs a)
         vdiff(a, i, j, v);
         const MeSide J = meSide(a, j);
         double s;
-        const double wi = lookupVS(a.wh, d * I.hInv, s), wj = lookupVS(a.wh, d * J.hInv, s);
+        const double wi = lookupVS(tw, d * I.hInv, s), wj = lookupVS(tw, d * J.hInv, s);
         MeFwd f;
         meFwd(r, d, rinv, v, I, J, wi, wj, a.avClean != 0, etaCrit, f);
         meSums(v, J, f, en, avE);
@@ -242,8 +245,11 @@ __global__ void __launch_bounds__(kVeAdjBlock) veArgKernel(VeAdjArgs a)
 
 // forward sums of the AV switch (G_i, vsig_i and the pair that set it), of divv (P_i) and of
 // gradh (whomega0 = K h^-4 S_om, wrho0 = K h^-4 S_r0)
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
 {
+    const KTab<Smooth> tw{a.wh};
+    const KTab<Smooth> tdw{a.whd};
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= a.n) return;
     double Ci[6];
@@ -261,8 +267,8 @@ __global__ void __launch_bounds__(kVeAdjBlock) vePreKernel(VeAdjArgs a)
         vdiff(a, i, j, v);
         const double v1 = d * hInv;
         double dw, dwd;
-        const double w = lookupVS(a.wh, v1, dw);
-        const double wd = lookupVS(a.whd, v1, dwd);
+        const double w = lookupVS(tw, v1, dw);
+        const double wd = lookupVS(tdw, v1, dwd);
         vsigStep(a, j, r, rinv, v, ci, vsig, arg);
         const double fac = a.vol[j] * (divvi - a.divv[j]) * w;
         const double xw = a.xm[j] * w;
@@ -380,20 +386,21 @@ __device__ __forceinline__ void meFlush(const VeAdjArgs& a, int64_t k, const MeA
         for (int q = 0; q < 6; ++q) put(a.gB + q * a.n, k, s.g[q], atomic);
 }
 
-template<bool AvClean, bool WithDu>
+template<bool AvClean, bool WithDu, bool Smooth>
 __device__ __forceinline__ void mePair(const VeAdjArgs& a, int64_t i, int64_t j, const MeSide& I, const MeSide& J,
                                        double etaCrit, const MeSeed& sd, MeGrad& o)
 {
+    const KTab<Smooth> tw{a.wh};
     double r[3], d, rinv, v[3];
     geom(a, i, j, r, d, rinv);
     vdiff(a, i, j, v);
     double dwi, dwj;
-    const double wi = lookupVS(a.wh, d * I.hInv, dwi), wj = lookupVS(a.wh, d * J.hInv, dwj);
+    const double wi = lookupVS(tw, d * I.hInv, dwi), wj = lookupVS(tw, d * J.hInv, dwj);
     meAdj<AvClean, WithDu>(r, d, rinv, v, I, J, wi, dwi, wj, dwj, etaCrit, sd.mb, sd.enb, sd.avEb, o);
 }
 
 // WithDu: a du seed is given (the energy sums en, avE of the forward are then needed)
-template<bool TwoSided, bool AvClean, bool WithDu>
+template<bool TwoSided, bool AvClean, bool WithDu, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
             const int64_t j = a.lv.at(k, q);
             const MeSide J = meSide(a, j);
             MeGrad o;
-            mePair<AvClean, WithDu>(a, k, j, S, J, etaCrit, sd, o);
+            mePair<AvClean, WithDu, Smooth>(a, k, j, S, J, etaCrit, sd, o);
             meAddI(s, o);
             if (!TwoSided) {
                 atomicAdd(a.bx + j, -o.r[0]);
@@ -441,7 +448,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
             if (!si.any) continue;
             const MeSide I = meSide(a, i);
             MeGrad o;
-            mePair<AvClean, WithDu>(a, i, k, I, S, etaCritOf(a.lv.capped(i)), si, o);
+            mePair<AvClean, WithDu, Smooth>(a, i, k, I, S, etaCritOf(a.lv.capped(i)), si, o);
             meAddJ(s, o);
         }
     }
@@ -451,9 +458,10 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjKernel(VeAdjArgs a)
 // one evaluation per owned entry of the owned lists built with the neighbour lists: a mutual pair
 // gives both particles' terms (meAdjMutual), a one-sided entry its owner's (the same function with
 // the neighbour's seeds zero); the neighbour's partials are added with FP64 atomics.  No avClean.
-template<bool WithDu>
+template<bool WithDu, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjOnceKernel(VeAdjArgs a, OwnedView ov)
 {
+    const KTab<Smooth> tw{a.wh};
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     MeAcc s{};
@@ -473,7 +481,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) meVeAdjOnceKernel(VeAdjArgs a, Ow
         geom(a, k, j, r, d, rinv);
         vdiff(a, k, j, v);
         double dwi, dwj;
-        const double wi = lookupVS(a.wh, d * S.hInv, dwi), wj = lookupVS(a.wh, d * J.hInv, dwj);
+        const double wi = lookupVS(tw, d * S.hInv, dwi), wj = lookupVS(tw, d * J.hInv, dwj);
         MeGrad o;
         meAdjMutual<WithDu>(r, d, rinv, v, S, J, wi, dwi, wj, dwj, sd.mb, sd.enb, sd.avEb, sj.mb, sj.enb, sj.avEb, o);
         meAddI(s, o);
@@ -539,19 +547,21 @@ __device__ __forceinline__ AvSeedV avSeedOf(const VeAdjArgs& a, int64_t i)
     return s;
 }
 
+template<bool Smooth>
 __device__ __forceinline__ void avPair(const VeAdjArgs& a, int64_t i, int64_t j, const AvSeedV& sd, AvGrad& o)
 {
+    const KTab<Smooth> tw{a.wh};
     double r[3], d, rinv, v[3];
     geom(a, i, j, r, d, rinv);
     vdiff(a, i, j, v);
     const double hInv = a.hInv[i];
     double dw;
-    const double w = lookupVS(a.wh, d * hInv, dw);
+    const double w = lookupVS(tw, d * hInv, dw);
     avAdj(r, d, rinv, v, hInv, w, dw, a.K, a.vol[j], a.kxInv[j], a.divv[i], a.divv[j], sd.CGb, sd.vsigb,
           uint32_t(j) == sd.arg, o);
 }
 
-template<bool TwoSided>
+template<bool TwoSided, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -565,7 +575,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
             const int64_t j = a.lv.at(k, q);
             if (!sd.gAny && uint32_t(j) != sd.arg) continue;
             AvGrad o;
-            avPair(a, k, j, sd, o);
+            avPair<Smooth>(a, k, j, sd, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] += o.r[t];
@@ -599,7 +609,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
             const AvSeedV si = avSeedOf(a, i);
             if (!si.any || (!si.gAny && uint32_t(k) != si.arg)) continue;
             AvGrad o;
-            avPair(a, i, k, si, o);
+            avPair<Smooth>(a, i, k, si, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] -= o.r[t];
@@ -626,8 +636,10 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjKernel(VeAdjArgs a)
 }
 
 // scatter form over the owned lists: a mutual pair gives both directed terms from one geometry
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjOnceKernel(VeAdjArgs a, OwnedView ov)
 {
+    const KTab<Smooth> tw{a.wh};
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, R[3] = {0, 0, 0}, c = 0, h = 0, divv = 0, xm = 0, kx = 0;
@@ -652,7 +664,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjOnceKernel(VeAdjArgs a, Ow
         const double divvJ = a.divv[j];
         if (wantK) {
             double dw;
-            const double w = lookupVS(a.wh, d * hInvK, dw);
+            const double w = lookupVS(tw, d * hInvK, dw);
             AvGrad o;
             avAdj(r, d, rinv, vv, hInvK, w, dw, a.K, a.vol[j], a.kxInv[j], divvK, divvJ, sk.CGb, sk.vsigb,
                   j == sk.arg, o);
@@ -675,7 +687,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veAvAdjOnceKernel(VeAdjArgs a, Ow
         if (wantJ) {
             const double hInvJ = a.hInv[j];
             double dw;
-            const double w = lookupVS(a.wh, d * hInvJ, dw);
+            const double w = lookupVS(tw, d * hInvJ, dw);
             const double rm[3] = {-r[0], -r[1], -r[2]}, vm[3] = {-vv[0], -vv[1], -vv[2]};
             AvGrad p;
             avAdj(rm, d, rinv, vm, hInvJ, w, dw, a.K, volK, kxInvK, divvJ, divvK, sj.CGb, sj.vsigb,
@@ -754,15 +766,17 @@ __global__ void veIadSeedKernel(VeAdjArgs a)
     a.kxB[k] += kxb;
 }
 
+template<bool Smooth>
 __device__ __forceinline__ void iadPair(const VeAdjArgs& a, int64_t i, int64_t j, const double tauB[6],
                                         const double PB[9], IadGrad& o)
 {
+    const KTab<Smooth> tw{a.wh};
     double r[3], d, rinv, v[3];
     geom(a, i, j, r, d, rinv);
     vdiff(a, i, j, v);
     const double hInv = a.hInv[i];
     double dw;
-    const double w = lookupVS(a.wh, d * hInv, dw);
+    const double w = lookupVS(tw, d * hInv, dw);
     iadDivvAdj(r, d, rinv, v, hInv, w, dw, a.vol[j], a.kxInv[j], a.xm[j], tauB, PB, o);
 }
 
@@ -774,7 +788,7 @@ __device__ __forceinline__ void iadSeedOf(const VeAdjArgs& a, int64_t i, double 
     for (int t = 0; t < 9; ++t) PB[t] = a.PB[t * a.n + i];
 }
 
-template<bool TwoSided>
+template<bool TwoSided, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -787,7 +801,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjKernel(VeAdjArgs a)
         for (unsigned q = 0; q < nc; ++q) {
             const int64_t j = a.lv.at(k, q);
             IadGrad o;
-            iadPair(a, k, j, tauB, PB, o);
+            iadPair<Smooth>(a, k, j, tauB, PB, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] += o.r[t];
@@ -812,7 +826,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjKernel(VeAdjArgs a)
             double tauB[6], PB[9];
             iadSeedOf(a, i, tauB, PB);
             IadGrad o;
-            iadPair(a, i, k, tauB, PB, o);
+            iadPair<Smooth>(a, i, k, tauB, PB, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) {
                 x[t] -= o.r[t];
@@ -836,8 +850,10 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjKernel(VeAdjArgs a)
 
 // scatter form over the owned lists: a mutual pair gives both directed terms from one geometry
 // (the neighbour's term with r -> -r, v -> -v and the roles swapped), a one-sided entry its owner's
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjOnceKernel(VeAdjArgs a, OwnedView ov)
 {
+    const KTab<Smooth> tw{a.wh};
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, h = 0, xm = 0, kx = 0;
@@ -852,7 +868,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjOnceKernel(VeAdjArgs a, O
         geom(a, k, j, r, d, rinv);
         vdiff(a, k, j, vv);
         double dw;
-        double w = lookupVS(a.wh, d * hInvK, dw);
+        double w = lookupVS(tw, d * hInvK, dw);
         IadGrad o;
         iadDivvAdj(r, d, rinv, vv, hInvK, w, dw, a.vol[j], a.kxInv[j], a.xm[j], tauK, PK, o);
         double rj[3], vj[3], hj = 0.0;
@@ -869,7 +885,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veIadAdjOnceKernel(VeAdjArgs a, O
             iadSeedOf(a, j, tauJ, PJ);
             const double hInvJ = a.hInv[j];
             const double rm[3] = {-r[0], -r[1], -r[2]}, vm[3] = {-vv[0], -vv[1], -vv[2]};
-            w = lookupVS(a.wh, d * hInvJ, dw);
+            w = lookupVS(tw, d * hInvJ, dw);
             IadGrad p;
             iadDivvAdj(rm, d, rinv, vm, hInvJ, w, dw, a.vol[k], a.kxInv[k], a.xm[k], tauJ, PJ, p);
 #pragma unroll
@@ -931,18 +947,21 @@ __global__ void veGradhSeedKernel(VeAdjArgs a)
     a.xmB[k] += xmb;
 }
 
+template<bool Smooth>
 __device__ __forceinline__ void gradhPair(const VeAdjArgs& a, int64_t i, int64_t j, GradhGrad& o)
 {
+    const KTab<Smooth> tw{a.wh};
+    const KTab<Smooth> tdw{a.whd};
     double r[3], d, rinv;
     geom(a, i, j, r, d, rinv);
     const double hInv = a.hInv[i];
     double dw, dwd;
-    const double w = lookupVS(a.wh, d * hInv, dw);
-    const double wd = lookupVS(a.whd, d * hInv, dwd);
+    const double w = lookupVS(tw, d * hInv, dw);
+    const double wd = lookupVS(tdw, d * hInv, dwd);
     gradhAdj(r, d, rinv, hInv, w, dw, wd, dwd, a.xm[j], a.m[j], a.Skx[i], a.Som[i], a.Sr0[i], o);
 }
 
-template<bool TwoSided>
+template<bool TwoSided, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -952,7 +971,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjKernel(VeAdjArgs a)
     for (unsigned q = 0; q < nc; ++q) {
         const int64_t j = a.lv.at(k, q);
         GradhGrad o;
-        gradhPair(a, k, j, o);
+        gradhPair<Smooth>(a, k, j, o);
 #pragma unroll
         for (int t = 0; t < 3; ++t) x[t] += o.r[t];
         h += o.hI;
@@ -967,7 +986,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjKernel(VeAdjArgs a)
         for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
             const int64_t i = a.tIdx[e];
             GradhGrad o;
-            gradhPair(a, i, k, o);
+            gradhPair<Smooth>(a, i, k, o);
 #pragma unroll
             for (int t = 0; t < 3; ++t) x[t] -= o.r[t];
             xm += o.xmJ;
@@ -981,8 +1000,11 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjKernel(VeAdjArgs a)
     put(a.xmB, k, xm, at);
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjOnceKernel(VeAdjArgs a, OwnedView ov)
 {
+    const KTab<Smooth> tw{a.wh};
+    const KTab<Smooth> tdw{a.whd};
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double x[3] = {0, 0, 0}, h = 0, xm = 0;
@@ -995,7 +1017,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjOnceKernel(VeAdjArgs a,
         double r[3], d, rinv;
         geom(a, k, j, r, d, rinv);
         double dw, dwd;
-        double w = lookupVS(a.wh, d * hInvK, dw), wd = lookupVS(a.whd, d * hInvK, dwd);
+        double w = lookupVS(tw, d * hInvK, dw), wd = lookupVS(tdw, d * hInvK, dwd);
         GradhGrad o;
         gradhAdj(r, d, rinv, hInvK, w, dw, wd, dwd, a.xm[j], a.m[j], skx, som, sr0, o);
         double rj[3];
@@ -1008,8 +1030,8 @@ __global__ void __launch_bounds__(kVeAdjBlock) veGradhAdjOnceKernel(VeAdjArgs a,
         if (mutual) {
             const double hInvJ = a.hInv[j];
             const double rm[3] = {-r[0], -r[1], -r[2]};
-            w = lookupVS(a.wh, d * hInvJ, dw);
-            wd = lookupVS(a.whd, d * hInvJ, dwd);
+            w = lookupVS(tw, d * hInvJ, dw);
+            wd = lookupVS(tdw, d * hInvJ, dwd);
             GradhGrad p;
             gradhAdj(rm, d, rinv, hInvJ, w, dw, wd, dwd, xmK, mK, a.Skx[j], a.Som[j], a.Sr0[j], p);
 #pragma unroll
@@ -1042,17 +1064,19 @@ __global__ void veXmassSeedKernel(VeAdjArgs a)
     a.bh[k] += hb;
 }
 
+template<bool Smooth>
 __device__ __forceinline__ void xmassPair(const VeAdjArgs& a, int64_t i, int64_t j, double rb[3], double& hIb)
 {
+    const KTab<Smooth> tw{a.wh};
     double r[3], d, rinv;
     geom(a, i, j, r, d, rinv);
     const double hInv = a.hInv[i];
     double dw;
-    lookupVS(a.wh, d * hInv, dw);
+    lookupVS(tw, d * hInv, dw);
     xmassAdj(r, d, rinv, hInv, dw, a.m[j], a.R0b[i], rb, hIb);
 }
 
-template<bool TwoSided>
+template<bool TwoSided, bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjKernel(VeAdjArgs a)
 {
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -1062,7 +1086,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjKernel(VeAdjArgs a)
     for (unsigned q = 0; q < nc; ++q) {
         const int64_t j = a.lv.at(k, q);
         double rb[3], hIb;
-        xmassPair(a, k, j, rb, hIb);
+        xmassPair<Smooth>(a, k, j, rb, hIb);
 #pragma unroll
         for (int t = 0; t < 3; ++t) x[t] += rb[t];
         h += hIb;
@@ -1076,7 +1100,7 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjKernel(VeAdjArgs a)
         for (uint32_t e = a.tOff[k]; e < a.tOff[k + 1]; ++e) {
             const int64_t i = a.tIdx[e];
             double rb[3], hIb;
-            xmassPair(a, i, k, rb, hIb);
+            xmassPair<Smooth>(a, i, k, rb, hIb);
 #pragma unroll
             for (int t = 0; t < 3; ++t) x[t] -= rb[t];
         }
@@ -1088,8 +1112,10 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjKernel(VeAdjArgs a)
     put(a.bh, k, h, at);
 }
 
+template<bool Smooth>
 __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjOnceKernel(VeAdjArgs a, OwnedView ov)
 {
+    const KTab<Smooth> tw{a.wh};
     const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= a.n) return;
     double x[3] = {0, 0, 0}, h = 0;
@@ -1101,14 +1127,14 @@ __global__ void __launch_bounds__(kVeAdjBlock) veXmassAdjOnceKernel(VeAdjArgs a,
         double r[3], d, rinv;
         geom(a, k, j, r, d, rinv);
         double dw;
-        lookupVS(a.wh, d * hInvK, dw);
+        lookupVS(tw, d * hInvK, dw);
         double rb[3], hIb;
         xmassAdj(r, d, rinv, hInvK, dw, a.m[j], r0b, rb, hIb);
         h += hIb;
         if (mutual) {
             const double hInvJ = a.hInv[j];
             const double rm[3] = {-r[0], -r[1], -r[2]};
-            lookupVS(a.wh, d * hInvJ, dw);
+            lookupVS(tw, d * hInvJ, dw);
             double pb[3], hJb;
             xmassAdj(rm, d, rinv, hInvJ, dw, mK, a.R0b[j], pb, hJb);
 #pragma unroll
@@ -1281,61 +1307,64 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
             a.avE = tp + int64_t(kTapeAvE) * n;
         }
     }
-    if (withDu && !tapedMe) {  // en and avE enter only through the du seed
-        vePreMeKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "vePreMeKernel"));
-    }
-    if (taped) {
-        veArgKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "veArgKernel"));
-    } else {
-        vePreKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "vePreKernel"));
-    }
-    {
-        using K = void (*)(VeAdjArgs);
-        // [two-sided][avClean][du seed]
-        const K me[2][2][2] = {{{meVeAdjKernel<false, false, false>, meVeAdjKernel<false, false, true>},
-                                {meVeAdjKernel<false, true, false>, meVeAdjKernel<false, true, true>}},
-                               {{meVeAdjKernel<true, false, false>, meVeAdjKernel<true, false, true>},
-                                {meVeAdjKernel<true, true, false>, meVeAdjKernel<true, true, true>}}};
-        // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
-        if (!two && !c->deterministic && !a.avClean && c->ownedEpoch == c->nbrEpoch) {
-            if (withDu) meVeAdjOnceKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-            else meVeAdjOnceKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-        } else
-            me[two][a.avClean][withDu]<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "meVeAdjKernel"));
-    }
-    veAvSeedKernel<<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veAvSeedKernel"));
-    const bool once = !two && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
-    if (two) veAvAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    else if (once) veAvAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else veAvAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veAvAdjKernel"));
-    veIadSeedKernel<<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veIadSeedKernel"));
-    if (two) veIadAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    else if (once) veIadAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else veIadAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veIadAdjKernel"));
-    veEosAdjKernel<<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veEosAdjKernel"));
-    veGradhSeedKernel<<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veGradhSeedKernel"));
-    if (two) veGradhAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    else if (once) veGradhAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else veGradhAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veGradhAdjKernel"));
-    veXmassSeedKernel<<<eb, 256, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veXmassSeedKernel"));
-    if (two) veXmassAdjKernel<true><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    else if (once) veXmassAdjOnceKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
-    else veXmassAdjKernel<false><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
-    SPHGB_TRY(launched(c, "veXmassAdjKernel"));
-    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
-    return SPHGB_OK;
+    return withKernelForm(c, [&](auto smooth) -> int {
+        constexpr bool S = decltype(smooth)::value;
+        if (withDu && !tapedMe) {  // en and avE enter only through the du seed
+            vePreMeKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+            SPHGB_TRY(launched(c, "vePreMeKernel"));
+        }
+        if (taped) {
+            veArgKernel<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+            SPHGB_TRY(launched(c, "veArgKernel"));
+        } else {
+            vePreKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+            SPHGB_TRY(launched(c, "vePreKernel"));
+        }
+        {
+            using K = void (*)(VeAdjArgs);
+            // [two-sided][avClean][du seed]
+            const K me[2][2][2] = {{{meVeAdjKernel<false, false, false, S>, meVeAdjKernel<false, false, true, S>},
+                                    {meVeAdjKernel<false, true, false, S>, meVeAdjKernel<false, true, true, S>}},
+                                   {{meVeAdjKernel<true, false, false, S>, meVeAdjKernel<true, false, true, S>},
+                                    {meVeAdjKernel<true, true, false, S>, meVeAdjKernel<true, true, true, S>}}};
+            // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
+            if (!two && !c->deterministic && !a.avClean && c->ownedEpoch == c->nbrEpoch) {
+                if (withDu) meVeAdjOnceKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+                else meVeAdjOnceKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+            } else
+                me[two][a.avClean][withDu]<<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+            SPHGB_TRY(launched(c, "meVeAdjKernel"));
+        }
+        veAvSeedKernel<<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veAvSeedKernel"));
+        const bool once = !two && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
+        if (two) veAvAdjKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        else if (once) veAvAdjOnceKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        else veAvAdjKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veAvAdjKernel"));
+        veIadSeedKernel<<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veIadSeedKernel"));
+        if (two) veIadAdjKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        else if (once) veIadAdjOnceKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        else veIadAdjKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veIadAdjKernel"));
+        veEosAdjKernel<<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veEosAdjKernel"));
+        veGradhSeedKernel<<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veGradhSeedKernel"));
+        if (two) veGradhAdjKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        else if (once) veGradhAdjOnceKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        else veGradhAdjKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veGradhAdjKernel"));
+        veXmassSeedKernel<<<eb, 256, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veXmassSeedKernel"));
+        if (two) veXmassAdjKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        else if (once) veXmassAdjOnceKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
+        else veXmassAdjKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
+        SPHGB_TRY(launched(c, "veXmassAdjKernel"));
+        SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+        return SPHGB_OK;
+    });
 }
 
 }  // namespace sphgb

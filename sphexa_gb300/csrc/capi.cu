@@ -46,6 +46,14 @@ void collectTimings(sphgb_ctx* c, int upto)
     }
 }
 
+// boundaries of the 32-particle target groups of [first, last): splits[g] = first + 32 g, splits[G] = last
+__global__ void targetGroupsKernel(int64_t first, int64_t last, int64_t groups, uint32_t* __restrict__ splits)
+{
+    const int64_t g = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (g > groups) return;
+    splits[g] = uint32_t(g == groups ? last : first + int64_t(kWarp) * g);
+}
+
 int checkRange(const sphgb_particles* p, int64_t first, int64_t last)
 {
     if (!p || first < 0 || last > p->n || first >= last) return SPHGB_ERR_ARG;
@@ -242,6 +250,51 @@ int sphgb_get_tree(sphgb_ctx* c, const uint64_t** leaves, const uint32_t** layou
     if (childOffsets) *childOffsets = c->childOffsets.as<int32_t>();
     if (internalToLeaf) *internalToLeaf = c->internalToLeaf.as<int32_t>();
     if (stats) *stats = c->stats;
+    return SPHGB_OK;
+}
+
+int sphgb_get_octree_view(sphgb_ctx* c, sphgb_octree_view* v)
+{
+    if (!c || !v) return SPHGB_ERR_ARG;
+    if (!c->haveTree) return SPHGB_ERR_STATE;
+    v->num_leaf_nodes = c->numLeaves;
+    v->num_nodes = c->numNodes;
+    v->num_internal = c->numInternal;
+    v->prefixes = reinterpret_cast<const uint64_t*>(c->prefixes.p);
+    v->child_offsets = c->childOffsets.as<int32_t>();
+    v->internal_to_leaf = c->internalToLeaf.as<int32_t>();
+    // levelRangeDev holds the internal nodes' level starts, then the level ranges of all nodes
+    v->level_range = c->levelRangeDev.as<int32_t>() + (kMaxLevel + 2);
+    v->leaves = reinterpret_cast<const uint64_t*>(c->leaves.p);
+    v->layout = c->layout.as<uint32_t>();
+    v->centers = c->nodeCenter.as<double>();
+    v->sizes = c->nodeSize.as<double>();
+    int depth = 0;
+    for (int l = 0; l <= kMaxLevel; ++l)
+        if (c->levelRange[l + 1] > c->levelRange[l]) depth = l;
+    v->max_depth = depth;
+    return SPHGB_OK;
+}
+
+int sphgb_get_params(sphgb_ctx* c, sphgb_params* p)
+{
+    if (!c || !p) return SPHGB_ERR_ARG;
+    *p = c->prm;
+    return SPHGB_OK;
+}
+
+int sphgb_target_groups(sphgb_ctx* c, int64_t first, int64_t last, uint32_t* splits, int64_t capacity,
+                        int64_t* numGroups)
+{
+    SPHGB_TRY(useDevice(c));
+    if (!numGroups || first < 0 || last < first || last > int64_t(UINT32_MAX)) return SPHGB_ERR_ARG;
+    const int64_t groups = (last - first + kWarp - 1) / kWarp;
+    *numGroups = groups;
+    if (!splits) return SPHGB_OK;
+    if (capacity < groups + 1) return SPHGB_ERR_ARG;
+    targetGroupsKernel<<<gridFor(groups + 1, 256), 256, 0, c->stream>>>(first, last, groups, splits);
+    SPHGB_TRY(launched(c, "targetGroupsKernel"));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
     return SPHGB_OK;
 }
 

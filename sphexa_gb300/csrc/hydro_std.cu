@@ -18,17 +18,17 @@ namespace sphgb {
 namespace {
 
 // ---------------------------------------------------------------- density / xmass
-template<class P, bool StoreRho>
+template<class P, bool StoreRho, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
-                                                          const void* m, const void* wh, Tab64 w64, double K,
-                                                          void* out)
+                                                          const void* m, const void* wh, const double2* w64,
+                                                          double K, void* out)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const Tab64 tab = w64;
+        const KTab<Smooth> tab{w64};
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
 
 // FP64 xmass / density with one evaluation per mutual pair over the owned lists: i adds
 // W(d / h_i) m_j, and for a mutual pair j receives W(d / h_j) m_i by an FP64 atomic
+template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
-                                                               const double* h, const double* m, Tab64 tab,
+                                                               const double* h, const double* m, KTab<Smooth> tab,
                                                                const double* hInvDx, double* acc)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -148,17 +149,17 @@ struct IadOut {
 };
 
 // vol[j] = m[j] / rho[j], formed once per particle (the reference divides per pair)
-template<class P>
+template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
-                                                        const void* vol, const void* wh, Tab64 w64, double K,
-                                                        IadOut o)
+                                                        const void* vol, const void* wh, const double2* w64,
+                                                        double K, IadOut o)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const Tab64 tab = w64;
+        const KTab<Smooth> tab{w64};
         auto t = cf.target(i);
         double hi = ld<double>(h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
@@ -220,7 +221,7 @@ struct MeStdArgs {
     const void *vx, *vy, *vz, *h, *m, *rho, *p, *c;
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void* wh;        // mixed: cubic pieces of W
-    Tab64 w64;             // FP64: W in the context's form
+    const double2* w64;    // FP64: W in the context's form
     const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
     const void* aux;       // m/rho, p/rho, p/rho^2
     int64_t n;
@@ -231,7 +232,7 @@ struct MeStdArgs {
     unsigned long long* minDt;
 };
 
-template<class P>
+template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64 cf, CoordMixed cm, MeStdArgs a)
 {
     using T = typename P::T;
@@ -240,7 +241,6 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
     const int64_t i = valid ? i0 : lv.first;
     const int64_t ii = i - lv.first;
     const unsigned nc = valid ? lv.capped(ii) : 0u;
-    const T* tab = static_cast<const T*>(a.wh);
     const T* aux = static_cast<const T*>(a.aux);
     const T *auxMoR = aux, *auxPoR = aux + a.n, *auxPoR2 = aux + 2 * a.n;
     double dt = INFINITY;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const Tab64 tabX = a.w64;
+        const KTab<Smooth> tabX{a.w64};
         const double* hInv3 = a.hInv64 + a.n;
         const double* hInvDx = a.hInv64 + 2 * a.n;
         T hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
@@ -376,10 +376,13 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
         const int64_t n = p->n;
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * size_t(n)));
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * size_t(n), c->stream));
-        xmassOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
-            lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-            tabW64(c), c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
-        SPHGB_TRY(launched(c, "xmassOnceKernel"));
+        SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+            constexpr bool S = decltype(smooth)::value;
+            xmassOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
+                lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
+                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
+            return launched(c, "xmassOnceKernel");
+        }));
         const unsigned eb = gridFor(last - first, 256);
         if (storeRho)
             xmassOnceFinish<true><<<eb, 256, 0, c->stream>>>(first, last, static_cast<const double*>(p->h),
@@ -391,13 +394,16 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
                                                                c->pairAcc.as<double>(), static_cast<double*>(out));
         return launched(c, "xmassOnceFinish");
     }
-    if (storeRho)
-        xmassKernel<P, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c), c->K,
-                                                                    out);
-    else
-        xmassKernel<P, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c), c->K,
-                                                                     out);
-    return launched(c, "xmassKernel");
+    return withKernelForm(c, [&](auto smooth) {
+        constexpr bool S = std::is_same_v<P, Fp64Tag> && decltype(smooth)::value;
+        if (storeRho)
+            xmassKernel<P, true, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c),
+                                                                           c->K, out);
+        else
+            xmassKernel<P, false, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c),
+                                                                            c->K, out);
+        return launched(c, "xmassKernel");
+    });
 }
 
 template<class P>
@@ -408,10 +414,13 @@ int launchIad(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
     lv.first = first;
     lv.last = last;
     const void* wh = std::is_same_v<P, Fp64Tag> ? c->whx64.p : c->whH32.p;
-    iadKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
-        lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, tabW64(c), c->K,
-        IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
-    return launched(c, "iadKernel");
+    return withKernelForm(c, [&](auto smooth) {
+        constexpr bool S = std::is_same_v<P, Fp64Tag> && decltype(smooth)::value;
+        iadKernel<P, S><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(
+            lv, coordFp64(c, p), coordMixed(c), p->h, c->aux.p, wh, tabW64(c), c->K,
+            IadOut{p->c11, p->c12, p->c13, p->c22, p->c23, p->c33});
+        return launched(c, "iadKernel");
+    });
 }
 
 template<class P>
@@ -448,9 +457,12 @@ int launchMeStd(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, d
     a.az = p->az;
     a.du = p->du;
     SPHGB_TRY(beginDtReduction(c, &a.minDt));
-    meStdKernel<P><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p),
-                                                                                     coordMixed(c), a);
-    SPHGB_TRY(launched(c, "meStdKernel"));
+    SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+        constexpr bool S = std::is_same_v<P, Fp64Tag> && decltype(smooth)::value;
+        meStdKernel<P, S><<<gridFor(last - first, kPairBlock), kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p),
+                                                                                            coordMixed(c), a);
+        return launched(c, "meStdKernel");
+    }));
     return endDtReduction(c, a.minDt, minDt);
 }
 

@@ -84,10 +84,11 @@ __global__ void packGradhKernel(int64_t n, const void* xm, const void* m, float2
     rec[j] = make_float2(ld<float>(xm, j), ld<float>(m, j));
 }
 
-template<class P>
+template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
                                                           const void* m, const void* xm, const void* wh,
-                                                          const void* whd, Tab64 w64, Tab64 dw64, double K,
+                                                          const void* whd, const double2* w64, const double2* dw64,
+                                                          double K,
                                                           void* kxOut, void* gradhOut,
                                                           double* tapeWom = nullptr, double* tapeWr0 = nullptr,
                                                           const float2* rec = nullptr)
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
     const int64_t ii = i - lv.first;
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
-        const Tab64 tw = w64, tdw = dw64;
+        const KTab<Smooth> tw{w64}, tdw{dw64};
         auto t = cf.target(i);
         double hi = ld<double>(h, i), mi = ld<double>(m, i), xmi = ld<double>(xm, i);
         double hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv, twoH = 2.0 * hi, hInvDx = hInv * kTabInvDx;
@@ -208,7 +209,7 @@ __global__ void eosAuxVeKernel(int64_t n, const double* u, const void* m, const 
 // ---------------------------------------------------------------- IAD + divv/curlv
 struct IadDivvArgs {
     const void *h, *vx, *vy, *vz, *xm, *kx, *wh;
-    Tab64 w64;          // FP64: W in the context's form (wh: the mixed pieces)
+    const double2* w64;  // FP64: W in the context's form (wh: the mixed pieces)
     const void* vol;    // aux: xm/kx per particle
     float* divvBound;   // mixed: error bound of divv per particle (refinement flag), may be null
     double K;
@@ -273,7 +274,7 @@ __device__ __forceinline__ void iadEpilogue64(const IadDivvArgs& a, int64_t i, d
     }
 }
 
-template<class P>
+template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
 iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
 {
@@ -283,7 +284,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
     const unsigned nc = lv.capped(ii);
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         using T = double;
-        const Tab64 tab = a.w64;
+        const KTab<Smooth> tab{a.w64};
         auto t = cf.target(i);
         T hi = ld<T>(a.h, i), hiInv = 1.0 / hi, twoH = 2.0 * hi;
         const T hInvDx = hiInv * kTabInvDx;
@@ -416,7 +417,7 @@ struct AvArgs {
     int64_t tapeN;
     const float4* rec;   // mixed: neighbour records {vx vy vz c} and {vol divv} (packAvKernel)
     const float2* rec2;
-    Tab64 w64;  // FP64: W in the context's form (wh: the mixed pieces)
+    const double2* w64;  // FP64: W in the context's form (wh: the mixed pieces)
 };
 
 // neighbour-side fields of the mixed AV-switch pass as a 16-byte and an 8-byte record per particle
@@ -444,7 +445,7 @@ __device__ __forceinline__ T avAlpha(const AvArgs& a, T alpha_i, T hi, T ci, T d
     return alpha_i + adot * T(a.dt);
 }
 
-template<class P>
+template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf, CoordMixed cm, AvArgs a)
 {
     using T = typename P::T;
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
     T gx, gy, gz;
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const Tab64 tabX = a.w64;
+        const KTab<Smooth> tabX{a.w64};
         T hiInv = 1.0 / hi, hiInv3 = hiInv * hiInv * hiInv, twoH = 2.0 * hi, hInvDx = hiInv * kTabInvDx;
         const bool wrap = cf.needsWrap(t, twoH);
         const T kh3 = a.K * hiInv3;
@@ -530,7 +531,7 @@ struct MeVeArgs {
     const void *c11, *c12, *c13, *c22, *c23, *c33;
     const void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
     const void* wh;        // mixed: cubic pieces of W
-    Tab64 w64;             // FP64: W in the context's form
+    const double2* w64;    // FP64: W in the context's form
     const double* hInv64;  // [0,n) 1/h, [n,2n) 1/h^3, [2n,3n) 1/(h dx)
     const void* aux;       // rho, m/rho, xm/kx, m*prho, ln xm, 1/rho (6 x n)
     int64_t n;
@@ -589,7 +590,7 @@ __global__ void meVePackKernel(int64_t n, MeVeArgs a, float4* __restrict__ pack)
     pack[4 * j + 3] = make_float4(ld<float>(a.alpha, j), rho, m / rho, m * ld<float>(a.prho, j));
 }
 
-template<class P, bool AvClean>
+template<class P, bool AvClean, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 cf, CoordMixed cm, MeVeArgs a)
 {
     using T = typename P::T;
@@ -625,7 +626,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
 
     if constexpr (std::is_same_v<P, Fp64Tag>) {
         auto t = cf.target(i);
-        const Tab64 tabX = a.w64;
+        const KTab<Smooth> tabX{a.w64};
         const double* hInv = a.hInv64;
         const double* hInv3 = a.hInv64 + a.n;
         const double* hInvDx = a.hInv64 + 2 * a.n;
@@ -797,9 +798,10 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
 // dterh_i xm_j and dterh_i m_j (veDefGradhJLoop, ve_def_gradh_kern.hpp:64-78); a mutual pair also
 // gives j its terms at v_j = d / h_j with xm_i and m_i, by FP64 atomics.  The self terms and the
 // epilogue (ve_def_gradh_kern.hpp:60-62, 80-88) run in gradhOnceFinish.
+template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, const double* xm,
-                                                               Tab64 tw, Tab64 tdw,
+                                                               KTab<Smooth> tw, KTab<Smooth> tdw,
                                                                const double* hInv64, int64_t n, double* acc)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -899,6 +901,7 @@ __global__ void gradhEosFinish(int64_t n, const double* h, const double* m, cons
 // vol_j W_i r r^T and xm_j W_i (v_j - v_i) r^T (r = x_i - x_j); a mutual pair also gives j
 // vol_i W_j r r^T and xm_i W_j (v_j - v_i) r^T (r and the velocity difference both change sign) by
 // FP64 atomics.  The inversion and divv/curlv follow per particle in iadOnceFinish.
+template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, IadDivvArgs a,
                                                              const double* hInv64, int64_t n, double* acc)
 {
@@ -906,7 +909,7 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned no = ov.size(ii);
-    const Tab64 tab = a.w64;
+    const KTab<Smooth> tab{a.w64};
     const double* hInvDx = hInv64 + 2 * n;
     const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
                  *vz = static_cast<const double*>(a.vz), *xm = static_cast<const double*>(a.xm),
@@ -989,6 +992,7 @@ __global__ void iadOnceFinish(int64_t first, int64_t last, int64_t n, IadDivvArg
 // S_i = sum vol_j (divv_i - divv_j) W_i r (r = x_i - x_j; c_i is applied after the walk), j's term of
 // the same pair is vol_i (divv_i - divv_j) W_j r (r and the divv difference both change sign);
 // the signal-velocity candidate c_i + c_j - 3 (r.v) / |r| of approaching pairs is symmetric.
+template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, AvArgs a,
                                                             const double* hInv64, int64_t n, double* acc)
 {
@@ -996,7 +1000,7 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned no = ov.size(ii);
-    const Tab64 tabX = a.w64;
+    const KTab<Smooth> tabX{a.w64};
     const double* hInvDx = hInv64 + 2 * n;
     const double *vx = static_cast<const double*>(a.vx), *vy = static_cast<const double*>(a.vy),
                  *vz = static_cast<const double*>(a.vz), *c = static_cast<const double*>(a.c),
@@ -1073,6 +1077,7 @@ __global__ void avOnceFinish(int64_t first, int64_t last, int64_t n, AvArgs a, c
 // 1/rho_i and 1/rho_j trade places; the viscosity and the signal velocity are symmetric.  i's terms
 // stay in registers; j's go to its accumulators with FP64 atomics (the signal-velocity maximum as an
 // integer maximum of non-negative bit patterns).
+template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordFp64 cf, MeVeArgs a)
 {
     using T = double;
@@ -1080,7 +1085,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
     const unsigned nOwned = __ldg(a.ownedCount + ii);
-    const Tab64 tabX = a.w64;
+    const KTab<Smooth> tabX{a.w64};
     const T* aux = static_cast<const T*>(a.aux);
     const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n,
             *auxRhoInv = aux + 5 * a.n;
@@ -1226,11 +1231,14 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         const int64_t n = p->n;
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 3 * size_t(n)));
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 3 * size_t(n), c->stream));
-        gradhOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(
-            lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-            static_cast<const double*>(p->xm), tabW64(c), tabDW64(c),
-            c->hInv64.as<double>(), n, c->pairAcc.as<double>());
-        SPHGB_TRY(launched(c, "gradhOnceKernel"));
+        SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+            constexpr bool S = decltype(smooth)::value;
+            gradhOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
+                lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
+                static_cast<const double*>(p->xm), KTab<S>{tabW64(c)}, KTab<S>{tabDW64(c)}, c->hInv64.as<double>(),
+                n, c->pairAcc.as<double>());
+            return launched(c, "gradhOnceKernel");
+        }));
         if (c->inSweep && p->u && p->prho && p->c) {  // EOS and quotients fused into the epilogue
             SPHGB_TRY(c->aux.ensure(sizeof(double) * 6 * n));
             gradhEosFinish<<<gridFor(n, 256), 256, 0, c->stream>>>(
@@ -1252,19 +1260,20 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         packGradhKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->xm, p->m, rec);
         SPHGB_TRY(launched(c, "packGradhKernel"));
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                    p->xm, c->whH32.p, c->whdH32.p, Tab64{},
-                                                                    Tab64{}, c->K, p->kx, p->gradh, nullptr, nullptr,
+                                                                    p->xm, c->whH32.p, c->whdH32.p, nullptr,
+                                                                    nullptr, c->K, p->kx, p->gradh, nullptr, nullptr,
                                                                     rec);
         SPHGB_TRY(launched(c, "gradhKernel"));
         if (first == 0 && last == p->n) return refineMixedGradh(c, p);
         c->stats_refinedGradh = 0;
         return SPHGB_OK;
-    } else
-        gradhKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
-                                                                   p->xm, c->whx64.p, c->whdx64.p, tabW64(c),
-                                                                   tabDW64(c), c->K, p->kx,
-                                                                   p->gradh, tWom, tWr0);
-    return launched(c, "gradhKernel");
+    }
+    return withKernelForm(c, [&](auto smooth) {
+        gradhKernel<Fp64Tag, decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
+            lv, coordFp64(c, p), coordMixed(c), p->h, p->m, p->xm, c->whx64.p, c->whdx64.p, tabW64(c), tabDW64(c),
+            c->K, p->kx, p->gradh, tWom, tWr0);
+        return launched(c, "gradhKernel");
+    });
 }
 
 int passEosVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
@@ -1361,13 +1370,19 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
             const int64_t n = p->n;
             SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 15 * size_t(n)));
             SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 15 * size_t(n), c->stream));
-            iadOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, ownedView(c), coordFp64(c, p), a,
-                                                                 c->hInv64.as<double>(), n, c->pairAcc.as<double>());
-            SPHGB_TRY(launched(c, "iadOnceKernel"));
+            SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+                iadOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
+                    lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+                return launched(c, "iadOnceKernel");
+            }));
             iadOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
             return launched(c, "iadOnceFinish");
         }
-        iadDivvKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+        return withKernelForm(c, [&](auto smooth) {
+            iadDivvKernel<Fp64Tag, decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
+                lv, coordFp64(c, p), coordMixed(c), a);
+            return launched(c, "iadDivvKernel");
+        });
     }
     return launched(c, "iadDivvKernel");
 }
@@ -1407,15 +1422,21 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         a.w64 = tabW64(c);
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * 4 * size_t(n)));
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 4 * size_t(n), c->stream));
-        avOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, ownedView(c), coordFp64(c, p), a,
-                                                            c->hInv64.as<double>(), n, c->pairAcc.as<double>());
-        SPHGB_TRY(launched(c, "avOnceKernel"));
+        SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+            avOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
+                lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+            return launched(c, "avOnceKernel");
+        }));
         avOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
         return launched(c, "avOnceFinish");
     } else {
         a.wh = c->whx64.p;
         a.w64 = tabW64(c);
-        avKernel<Fp64Tag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
+        return withKernelForm(c, [&](auto smooth) {
+            avKernel<Fp64Tag, decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p),
+                                                                                              coordMixed(c), a);
+            return launched(c, "avKernel");
+        });
     }
     return launched(c, "avKernel");
 }
@@ -1495,14 +1516,21 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
             a.owned = c->owned.as<uint32_t>();
             a.ownedCount = c->ownedCount.as<uint32_t>();
             a.acc = c->pairAcc.as<double>();
-            meVeOnceKernel<<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a);
-            SPHGB_TRY(launched(c, "meVeOnceKernel"));
+            SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+                meVeOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a);
+                return launched(c, "meVeOnceKernel");
+            }));
             meVeOnceFinish<<<blocks, kPairBlock, 0, c->stream>>>(lv, a);
             SPHGB_TRY(launched(c, "meVeOnceFinish"));
             return endDtReduction(c, a.minDt, minDt);
         }
-        if (avClean) meVeKernel<Fp64Tag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
-        else meVeKernel<Fp64Tag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+        SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
+            constexpr bool S = decltype(smooth)::value;
+            if (avClean) meVeKernel<Fp64Tag, true, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+            else meVeKernel<Fp64Tag, false, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
+            return launched(c, "meVeKernel");
+        }));
+        return endDtReduction(c, a.minDt, minDt);
     }
     SPHGB_TRY(launched(c, "meVeKernel"));
     return endDtReduction(c, a.minDt, minDt);

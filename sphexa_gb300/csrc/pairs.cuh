@@ -12,6 +12,8 @@
 //           rounding.  Sums that the error budget needs are Kahan-compensated.
 #pragma once
 
+#include <type_traits>
+
 #include "context.cuh"
 
 namespace sphgb {
@@ -251,51 +253,69 @@ __device__ __forceinline__ double lookupX(const double2* __restrict__ tabX, doub
 //   central differences of the forward passes agree with the adjoint (which differentiates the same
 //   pieces); it differs from the table form by the table's interpolation error (within 2e-8 of the
 //   function's maximum).
-// The form is uniform over a launch, so the branch costs no divergence.
-struct Tab64 {
+// The form is a template argument of the kernels (withKernelForm picks the instantiation at launch):
+// a run-time test inside the lookup cost the FP64-bound passes 5-35 % of their time.
+template<bool Smooth>
+struct KTab {
     const double2* t;
-    int smooth;
 };
 
-__device__ __forceinline__ double lookupX(const Tab64& tb, const TabSlot& s)
+template<bool Smooth>
+__device__ __forceinline__ double lookupX(const KTab<Smooth>& tb, const TabSlot& s)
 {
     if (s.k < 0) return 0.0;
-    if (tb.smooth) {
+    if constexpr (Smooth) {
         const double2 a = __ldg(tb.t + 2 * s.k), b = __ldg(tb.t + 2 * s.k + 1);
         return fma(fma(fma(b.y, s.frac, b.x), s.frac, a.y), s.frac, a.x);
+    } else {
+        const double2 t = __ldg(tb.t + s.k);
+        return fma(t.y, s.frac, t.x);
     }
-    const double2 t = __ldg(tb.t + s.k);
-    return fma(t.y, s.frac, t.x);
 }
 
-__device__ __forceinline__ double lookupX(const Tab64& tb, double x) { return lookupX(tb, tabSlot(x)); }
+template<bool Smooth>
+__device__ __forceinline__ double lookupX(const KTab<Smooth>& tb, double x)
+{
+    return lookupX(tb, tabSlot(x));
+}
 
 // value at v and its derivative d/dv (the slope of the interval in the table form)
-__device__ __forceinline__ double lookupVSlope(const Tab64& tb, double v, double& slope)
+template<bool Smooth>
+__device__ __forceinline__ double lookupVSlope(const KTab<Smooth>& tb, double v, double& slope)
 {
     const TabSlot s = tabSlot(v * kTabInvDx);
     if (s.k < 0) {
         slope = 0.0;
         return 0.0;
     }
-    if (tb.smooth) {
+    if constexpr (Smooth) {
         const double2 a = __ldg(tb.t + 2 * s.k), b = __ldg(tb.t + 2 * s.k + 1);
         const double f = s.frac;
         slope = fma(fma(3.0 * b.y, f, 2.0 * b.x), f, a.y) * kTabInvDx;
         return fma(fma(fma(b.y, f, b.x), f, a.y), f, a.x);
+    } else {
+        const double2 t = __ldg(tb.t + s.k);
+        slope = t.y * kTabInvDx;
+        return fma(t.y, s.frac, t.x);
     }
-    const double2 t = __ldg(tb.t + s.k);
-    slope = t.y * kTabInvDx;
-    return fma(t.y, s.frac, t.x);
 }
 
-inline Tab64 tabW64(const sphgb_ctx* c)
+// the context's FP64 tables of W and dW/dv in its kernel form
+inline const double2* tabW64(const sphgb_ctx* c)
 {
-    return c->smoothKernel ? Tab64{c->whS64.as<double2>(), 1} : Tab64{c->whx64.as<double2>(), 0};
+    return c->smoothKernel ? c->whS64.as<double2>() : c->whx64.as<double2>();
 }
-inline Tab64 tabDW64(const sphgb_ctx* c)
+inline const double2* tabDW64(const sphgb_ctx* c)
 {
-    return c->smoothKernel ? Tab64{c->whdS64.as<double2>(), 1} : Tab64{c->whdx64.as<double2>(), 0};
+    return c->smoothKernel ? c->whdS64.as<double2>() : c->whdx64.as<double2>();
+}
+
+// calls launch(std::integral_constant<bool, smooth>) for the context's kernel form
+template<class F>
+inline int withKernelForm(const sphgb_ctx* c, F&& launch)
+{
+    if (c->smoothKernel) return launch(std::true_type{});
+    return launch(std::false_type{});
 }
 
 // ---- the mixed passes' kernel function: a cubic Hermite piece per interval of [0, 2] ----

@@ -245,6 +245,33 @@ class Domain:
                     level_range=np.array(st.level_range[:], dtype=np.int32))
 
 
+    def octree_properties(self) -> dict:
+        """Domain::octreeProperties (domain.hpp:416-428): the OctreeNsView arrays of the last sync
+        (incl. the FP64 node centers and half sizes), copied to the host."""
+        v = _lib.SphgbOctreeView()
+        check(self.ctx.lib.sphgb_get_octree_view(self.ctx.h, C.byref(v)), "sphgb_get_octree_view")
+        L, NN = v.num_leaf_nodes, v.num_nodes
+        return dict(num_leaf_nodes=L, num_nodes=NN, num_internal=v.num_internal, max_depth=v.max_depth,
+                    prefixes=_device_array(v.prefixes, NN, np.uint64),
+                    child_offsets=_device_array(v.child_offsets, NN, np.int32),
+                    internal_to_leaf=_device_array(v.internal_to_leaf, NN, np.int32),
+                    level_range=_device_array(v.level_range, 23, np.int32),
+                    leaves=_device_array(v.leaves, L + 1, np.uint64),
+                    layout=_device_array(v.layout, L + 1, np.uint32),
+                    centers=_device_array(v.centers, 3 * NN, np.float64).reshape(NN, 3),
+                    sizes=_device_array(v.sizes, 3 * NN, np.float64).reshape(NN, 3))
+
+
+def target_groups(ctx: Context, first: int, last: int) -> np.ndarray:
+    """sph::computeGroups: boundaries of the 32-particle target groups of [first, last) (host copy)"""
+    g = C.c_int64()
+    check(ctx.lib.sphgb_target_groups(ctx.h, first, last, None, 0, C.byref(g)), "sphgb_target_groups")
+    out = torch.zeros(g.value + 1, dtype=torch.int32, device=f"cuda:{ctx.device}")
+    check(ctx.lib.sphgb_target_groups(ctx.h, first, last, out.data_ptr(), g.value + 1, C.byref(g)),
+          "sphgb_target_groups")
+    return out.cpu().numpy().view(np.uint32).astype(np.int64)
+
+
 class _DeviceView:
     """borrowed view of library-owned device memory for torch.as_tensor"""
 

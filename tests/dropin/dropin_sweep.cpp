@@ -66,7 +66,7 @@ int run(const char* in, const char* out, bool ve, double lim[6], int bc[3])
     auto bt = [](int b) { return b == 1 ? BoundaryType::periodic : BoundaryType::open; };
     Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
     dr::SingleRankDomain<uint64_t, double, Box<double>> domain(0, 1, 64, 64, 0.5f, box);
-    domain.sync(d);
+    domain.syncDataset(d);
     GroupView grp{0, uint32_t(n), 1, nullptr, nullptr};
     dr::findNeighborsSfc(0, n, d, domain.box());
     if (ve) {
@@ -131,7 +131,7 @@ int runAdjoint(const char* in, const char* out, double lim[6], int bc[3])
     auto bt = [](int b) { return b == 1 ? BoundaryType::periodic : BoundaryType::open; };
     Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
     dr::SingleRankDomain<uint64_t, double, Box<double>> domain(0, 1, 64, 64, 0.5f, box);
-    domain.sync(d);
+    domain.syncDataset(d);
     GroupView grp{0, uint32_t(n), 1, nullptr, nullptr};
     dr::findNeighborsSfc(0, n, d, domain.box());
     DeviceVector<double> alphaPrev(n);
@@ -193,6 +193,101 @@ int runAdjoint(const char* in, const char* out, double lim[6], int bc[3])
     return 0;
 }
 
+// One step of HydroVeProp as the reference propagator writes it (main/src/propagator/ve_hydro.hpp:
+// 100-217): Domain::sync of keys x y z h with the conserved fields as properties and the dependent
+// ones as scratch, d.treeView = domain.octreeProperties(), findNeighborsSfc, computeGroups into a
+// GroupData, the VE passes on groups_.view() with the (no-op) halo exchanges between them,
+// rhoTimestep, then computeTimestep, computePositions with the reference's argument list and
+// updateSmoothingLength.  Writes the forces, the groups, the tree view (leaf count, depth, node
+// centers and sizes) and the integrated fields.
+int runPropagator(const char* in, const char* out, double lim[6], int bc[3])
+{
+    using Th = double;
+    std::FILE* f = std::fopen(in, "rb");
+    if (!f) return 2;
+    long long n = 0;
+    if (std::fread(&n, sizeof(n), 1, f) != 1) return 2;
+    std::vector<double> a(10 * n);
+    if (std::fread(a.data(), sizeof(double), a.size(), f) != a.size()) return 2;
+    std::fclose(f);
+    auto col = [&](int k) { return std::vector<double>(a.begin() + k * n, a.begin() + (k + 1) * n); };
+    ParticlesData<Th, Th> d;
+    auto& dv = d.devData;
+    DeviceVector<double>* inputs[] = {&dv.x, &dv.y, &dv.z, &dv.h, &dv.m, &dv.u, &dv.vx, &dv.vy, &dv.vz, &dv.alpha};
+    for (int k = 0; k < 10; ++k) upload(*inputs[k], col(k));
+    for (auto* v : {&dv.rho, &dv.p, &dv.c, &dv.xm, &dv.kx, &dv.gradh, &dv.prho, &dv.divv, &dv.curlv, &dv.c11, &dv.c12,
+                    &dv.c13, &dv.c22, &dv.c23, &dv.c33, &dv.ax, &dv.ay, &dv.az, &dv.du, &dv.x_m1, &dv.y_m1,
+                    &dv.z_m1, &dv.du_m1})
+        v->resize(n);
+    dv.nc.resize(n);  // keys are sized by the sync
+    auto bt = [](int b) { return b == 1 ? BoundaryType::periodic : BoundaryType::open; };
+    Box<double> box(lim[0], lim[1], lim[2], lim[3], lim[4], lim[5], bt(bc[0]), bt(bc[1]), bt(bc[2]));
+    dr::SingleRankDomain<uint64_t, double, Box<double>> domain(0, 1, 64, 64, 0.5f, box);
+    GroupData groups_;
+
+    // sync(domain, simData) (ve_hydro.hpp:100-117)
+    domain.sync(dv.keys, dv.x, dv.y, dv.z, dv.h,
+                std::tie(dv.m, dv.u, dv.vx, dv.vy, dv.vz, dv.x_m1, dv.y_m1, dv.z_m1, dv.du_m1, dv.alpha),
+                std::tie(dv.rho, dv.p, dv.c, dv.kx));
+    d.treeView = domain.octreeProperties();
+    // computeForces (ve_hydro.hpp:119-190)
+    if (domain.nParticlesWithHalos() != uint32_t(n) || domain.nParticles() != uint32_t(n)) return 4;
+    std::size_t first = domain.startIndex();
+    std::size_t last = domain.endIndex();
+    dr::findNeighborsSfc(first, last, d, domain.box());
+    dr::computeGroups(first, last, d, domain.box(), groups_);
+    dr::computeXMass(groups_.view(), d, domain.box());
+    domain.exchangeHalos(std::tie(dv.xm), dv.ax, dv.keys);
+    dr::computeVeDefGradh(groups_.view(), d, domain.box());
+    dr::computeEOS(first, last, d);
+    domain.exchangeHalos(std::tie(dv.vx, dv.vy, dv.vz, dv.prho, dv.c, dv.kx), dv.ax, dv.keys);
+    dr::computeIadDivvCurlv(groups_.view(), d, domain.box());
+    d.minDtRho = dr::rhoTimestep(first, last, d);
+    domain.exchangeHalos(std::tie(dv.c11, dv.c12, dv.c13, dv.c22, dv.c23, dv.c33, dv.divv), dv.ax, dv.keys);
+    dr::computeAVswitches(groups_.view(), d, domain.box());
+    domain.exchangeHalos(std::tie(dv.alpha), dv.ax, dv.keys);
+    std::vector<float> groupDt(groups_.numGroups);
+    DeviceVector<float> groupDtDev(groups_.numGroups);
+    dr::computeMomentumEnergy<false>(groups_.view(), rawPtr(groupDtDev), d, domain.box());
+
+    std::FILE* o = std::fopen(out, "wb");
+    for (auto* v : {&dv.xm, &dv.kx, &dv.c11, &dv.divv, &dv.alpha, &dv.ax, &dv.ay, &dv.az, &dv.du}) download(*v, o);
+    std::vector<uint32_t> gs(groups_.numGroups + 1);
+    cudaMemcpy(gs.data(), groups_.groupStart, gs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(groupDt.data(), rawPtr(groupDtDev), groupDt.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    const auto& tv = d.treeView;
+    const long long nn = (long long)(domain.focusTree().octreeViewAcc().numLeafNodes);
+    if (domain.globalTree().numLeafNodes() != nn) return 5;
+    int lr[23];
+    cudaMemcpy(lr, tv.levelRange, sizeof(lr), cudaMemcpyDeviceToHost);
+    const long long numNodes = lr[22] > 0 ? lr[22] : 0;  // levelRange[maxTreeLevel + 1] = node count
+    std::vector<double> cen(3 * numNodes), siz(3 * numNodes);
+    cudaMemcpy(cen.data(), tv.centers, cen.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(siz.data(), tv.sizes, siz.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    const double head[6] = {double(groups_.numGroups), double(groups_.firstBody), double(groups_.lastBody),
+                            double(tv.numLeafNodes), double(nn), double(domain.focusTree().depth())};
+    std::fwrite(head, sizeof(double), 6, o);
+    std::vector<double> gsd(gs.begin(), gs.end()), gdt(groupDt.begin(), groupDt.end());
+    std::fwrite(gsd.data(), sizeof(double), gsd.size(), o);
+    std::fwrite(gdt.data(), sizeof(double), gdt.size(), o);
+    const double nnd = double(numNodes);
+    std::fwrite(&nnd, sizeof(double), 1, o);
+    std::fwrite(cen.data(), sizeof(double), cen.size(), o);
+    std::fwrite(siz.data(), sizeof(double), siz.size(), o);
+
+    // integrate (ve_hydro.hpp:192-204)
+    dr::computeTimestep(first, last, d);
+    dr::computePositions(groups_.view(), d, domain.box(), d.minDt, {float(d.minDt_m1)});
+    dr::updateSmoothingLength(groups_.view(), d);
+    download(dv.x, o);
+    download(dv.u, o);
+    download(dv.h, o);
+    const double tail[2] = {d.minDt, d.minDtRho};
+    std::fwrite(tail, sizeof(double), 2, o);
+    std::fclose(o);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 5) return 1;
@@ -203,6 +298,7 @@ int main(int argc, char** argv)
     bool ve = std::string(argv[4]) == "ve";
     try {
         if (std::string(argv[3]) == "adjoint") return runAdjoint(argv[1], argv[2], lim, bc);
+        if (std::string(argv[3]) == "propagator") return runPropagator(argv[1], argv[2], lim, bc);
         if (std::string(argv[3]) == "mixed") return run<float>(argv[1], argv[2], ve, lim, bc);
         return run<double>(argv[1], argv[2], ve, lim, bc);
     } catch (const std::exception& e) {

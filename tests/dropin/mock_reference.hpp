@@ -1,5 +1,6 @@
 // Minimal stand-ins with the member names of the reference types the drop-in adapter reads
-// (cstone::DeviceVector, cstone::Box, cstone::GroupView, sphexa::ParticlesData<GpuTag>), so that
+// (cstone::DeviceVector, cstone::Box, cstone::GroupView, cstone::GroupData, cstone::OctreeNsView,
+// sphexa::ParticlesData<GpuTag>), so that
 // include/sphgb/dropin.hpp can be compiled and linked without the reference sources.
 #pragma once
 
@@ -82,6 +83,39 @@ struct GroupView
     const uint32_t* groupEnd;
 };
 
+// cstone::GroupData<GpuTag> (traversal/groups.hpp:37-52): uninitialised scalars until filled
+struct GroupData
+{
+    GroupView view() const { return {firstBody, lastBody, numGroups, groupStart, groupEnd}; }
+    DeviceVector<uint32_t> data;
+    uint32_t firstBody, lastBody;
+    uint32_t numGroups;
+    uint32_t* groupStart;
+    uint32_t* groupEnd;
+};
+
+template<class T>
+struct Vec3
+{
+    T v[3];
+};
+
+// cstone::OctreeNsView (tree/octree.hpp:279-300)
+template<class T, class KeyType>
+struct OctreeNsView
+{
+    int numLeafNodes;
+    const KeyType* prefixes;
+    const int* childOffsets;
+    const int* internalToLeaf;
+    const int* levelRange;
+    const KeyType* leaves;
+    const uint32_t* layout;
+    const Vec3<T>* centers;
+    const Vec3<T>* sizes;
+    float searchExtFactor{1.0};
+};
+
 template<class Th, class Tm>
 struct DeviceParticlesData
 {
@@ -89,7 +123,7 @@ struct DeviceParticlesData
     DeviceVector<Th> h, vx, vy, vz, alpha, rho, p, c, xm, kx, gradh, prho, divv, curlv, c11, c12, c13, c22, c23, c33,
         ax, ay, az, dV11, dV12, dV13, dV22, dV23, dV33;
     DeviceVector<Tm> m;
-    DeviceVector<Th> x_m1, y_m1, z_m1, du_m1;
+    DeviceVector<Th> x_m1, y_m1, z_m1, du_m1, tdpdTrho;
     DeviceVector<uint64_t> keys;
     DeviceVector<unsigned> nc;
 };
@@ -105,5 +139,6 @@ struct ParticlesData
     constexpr static double maxDtIncrease = 1.1;
     Th alphamin{0.05f}, alphamax{1.0f}, decay_constant{0.2f};
     DeviceParticlesData<Th, Tm> devData;
+    OctreeNsView<double, uint64_t> treeView;
 };
 } // namespace mockref

@@ -1,6 +1,8 @@
 """The C++ drop-in adapter (include/sphgb/dropin.hpp) in a program written like the reference's
-propagators: it compiles and links against libsphgb.so on the CPU; on a GPU it runs a VE and a std
-sweep whose outputs match the oracle."""
+propagators: it compiles and links against libsphgb.so on the CPU (against stand-in types with the
+reference's member names, and, where the reference sources are present, against the reference's
+own ParticlesData / GroupData / Box / OctreeNsView headers); on a GPU it runs a VE and a std sweep
+and the call sequence of HydroVeProp::computeForces + integrate, whose outputs match the oracle."""
 
 import os
 import shutil
@@ -30,6 +32,23 @@ def build_driver(tmp: Path) -> Path:
 def test_dropin_adapter_compiles_and_links(tmp_path):
     exe = build_driver(tmp_path)
     assert exe.exists()
+
+
+def test_dropin_adapter_compiles_against_reference_headers(tmp_path):
+    """every adapter call of the propagators (ve_hydro.hpp, std_hydro.hpp) instantiated over the
+    reference's own sphexa::ParticlesData<GpuTag>, cstone::GroupData<GpuTag>, cstone::Box and
+    cstone::OctreeNsView (tests/dropin/dropin_reference_compile.cu), compiled with nvcc and the
+    reference's USE_CUDA switch; skipped where the reference sources are absent"""
+    ref = Path(os.environ.get("SPHGB_REFERENCE", ROOT.parent / "reference"))
+    if not (ref / "sph" / "include" / "sph" / "particles_data.hpp").exists():
+        pytest.skip("reference sources not present on this machine")
+    nvcc = shutil.which("nvcc") or str(CUDA / "bin" / "nvcc")
+    cmd = [nvcc, "-std=c++20", "-DUSE_CUDA", "-gencode", "arch=compute_103a,code=sm_103a", "-c",
+           "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(ref / "domain" / "include"), "-I",
+           str(ref / "sph" / "include"), "-I", str(ref / "main" / "src"),
+           str(ROOT / "tests" / "dropin" / "dropin_reference_compile.cu"), "-o", str(tmp_path / "dr.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
 
 
 @pytest.mark.gpu
@@ -104,3 +123,84 @@ def test_dropin_ve_adjoint_matches_central_difference(tmp_path):
     assert r.returncode == 0, r.stderr
     ad, fd = np.fromfile(out, dtype=np.float64)
     assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
+
+
+def _write_input(wl, path):
+    cols = ["x", "y", "z", "h", "m", "u", "vx", "vy", "vz", "alpha"]
+    with open(path, "wb") as f:
+        np.array([wl.n], dtype=np.int64).tofile(f)
+        np.concatenate([wl.fields[c] for c in cols]).astype(np.float64).tofile(f)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["fourier", "sphere"])
+def test_dropin_propagator_step_matches_oracle(tmp_path, port, case):
+    """HydroVeProp::computeForces + integrate (main/src/propagator/ve_hydro.hpp:100-217) through the
+    adapter: Domain::sync(keys, x, y, z, h, properties, scratch), octreeProperties into the dataset's
+    treeView, computeGroups into a GroupData, the VE passes on groups_.view(), rhoTimestep,
+    computeTimestep, computePositions(grp, d, box, d.minDt, {float(d.minDt_m1)}), updateH"""
+    from oracle import oracle as O
+    from sphexa_gb300 import workloads as W
+    exe = build_driver(tmp_path)
+    wl = W.fourier(16, seed=81, rho_seed=82, v_seed=83) if case == "fourier" else W.sphere(6000, seed=84)
+    inp = tmp_path / "in.bin"
+    _write_input(wl, inp)
+    out = tmp_path / "prop.bin"
+    args = [str(exe), str(inp), str(out), "propagator", "ve"] + [repr(float(v)) for v in wl.box] + \
+           [str(int(b)) for b in wl.bc]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    res = np.fromfile(out, dtype=np.float64)
+    n = wl.n
+    names = ["xm", "kx", "c11", "divv", "alpha", "ax", "ay", "az", "du"]
+    got = {k: res[i * n:(i + 1) * n] for i, k in enumerate(names)}
+    pos = 9 * n
+    ng, fb, lb, tv_leaves, ft_leaves, depth = res[pos:pos + 6]
+    pos += 6
+    G = (n + 31) // 32
+    assert int(ng) == G and int(fb) == 0 and int(lb) == n
+    np.testing.assert_array_equal(res[pos:pos + G + 1], np.append(np.arange(0, n, 32), n))
+    pos += G + 1
+    group_dt = res[pos:pos + G]
+    pos += G
+    nn = int(res[pos])
+    pos += 1
+    centers = res[pos:pos + 3 * nn].reshape(nn, 3)
+    pos += 3 * nn
+    sizes = res[pos:pos + 3 * nn].reshape(nn, 3)
+    pos += 3 * nn
+    step = {k: res[pos + i * n:pos + (i + 1) * n] for i, k in enumerate(["x", "u", "h"])}
+    pos += 3 * n
+    min_dt, min_dt_rho = res[pos:pos + 2]
+
+    ref = port.sweep(wl, "ve", False)
+    for k in names:
+        scale = np.max(np.abs(ref[k])) + 1e-300
+        if k in ("ax", "ay", "az"):
+            scale = max(np.max(np.abs(ref[q])) for q in ("ax", "ay", "az"))
+        g = np.asarray(ref["gradh"])
+        kappa = float(np.max(np.abs(1.0 - g) / np.maximum(np.abs(g), 1e-300)))
+        tol = 1e-12 * (max(1.0, kappa / 1e3) if k in ("ax", "ay", "az", "du") else 1.0)
+        assert np.max(np.abs(got[k] - ref[k])) <= tol * scale, k
+    assert int(tv_leaves) == ref["num_leaves"] and int(ft_leaves) == ref["num_leaves"]
+    lr = ref["level_range"]
+    assert int(depth) == max(k for k in range(22) if lr[k + 1] > lr[k])
+    assert nn == ref["num_nodes"]
+    np.testing.assert_array_equal(centers, ref["centers"])
+    np.testing.assert_array_equal(sizes, ref["sizes"])
+    # groupDt holds each group's Courant minimum; their minimum is the pass's minDtCourant
+    assert float(group_dt.min()) == pytest.approx(ref["minDtCourant"], rel=1e-6)
+    assert min_dt_rho == pytest.approx(0.06 / abs(float(np.max(ref["divv"]))), rel=1e-10)
+    dt = min(ref["minDtCourant"], min_dt_rho, 1.1 * 1e-6)
+    assert min_dt == pytest.approx(dt, rel=1e-10)
+    f = {k: ref[k].copy() for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "u", "du", "h")}
+    for k in ("xm1", "ym1", "zm1", "dum1"):
+        f[k] = np.zeros(n)
+    # the propagator hands the step to computePositions as float (positions.hpp:179)
+    O.run_positions(port.lib, f, float(np.float32(min_dt)), float(np.float32(1e-6)), ref["box"], wl.bc)
+    for k in ("x", "u"):
+        scale = np.max(np.abs(f[k])) + 1e-300
+        assert np.max(np.abs(step[k] - f[k])) <= 1e-12 * scale, k
+    h = ref["h"].copy()
+    O.run_update_h(port.lib, 100, ref["nc"].astype(np.uint32), h)
+    np.testing.assert_allclose(step["h"], h, rtol=1e-15)

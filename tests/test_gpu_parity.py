@@ -292,3 +292,42 @@ def test_drop_in_find_neighbors_layout(gpu_ctx, port):
     s_ref = __import__("oracle.oracle", fromlist=["x"]).sorted_sets(ref["nbr"], ref["nc"], ng)
     np.testing.assert_array_equal(s_gpu[keep], s_ref[keep])
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("case", ["sedov", "sphere", "mixed_bc"])
+def test_octree_properties_match_oracle(gpu_ctx, port, case):
+    """Domain::octreeProperties: the OctreeNsView arrays of the last sync, including the FP64
+    geometric node centers and half sizes of nodeFpCenters (focus/source_center.hpp:129-141),
+    bit-exact against the oracle (itself equal to the reference's nodeFpCenters,
+    tests/test_oracle_pins.py); the 32-particle target groups of computeGroups"""
+    from oracle import oracle as O
+    from sphexa_gb300 import sph, workloads as W
+    if case == "sedov":
+        wl = W.sedov(20, jitter=0.25, seed=2)
+    elif case == "sphere":
+        wl = W.sphere(20_000, seed=4)
+    else:
+        wl = W.random_cube(30_000, seed=65, periodic=False)
+        wl.bc = np.array([1, 0, 1], dtype=np.uint8)
+    gpu_ctx.set_params(bucket=64)
+    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+    dom = sph.Domain(gpu_ctx, sph.Box(wl.box.copy(), wl.bc.copy()))
+    dom.sync(d)
+    v = dom.octree_properties()
+    ref = port.sweep(wl, "ve", stages=O.OS_KEYS | O.OS_TREE, want_nbr=False)
+    assert v["num_leaf_nodes"] == ref["num_leaves"] and v["num_nodes"] == ref["num_nodes"]
+    np.testing.assert_array_equal(v["leaves"], ref["leaves"])
+    np.testing.assert_array_equal(v["prefixes"], ref["prefixes"])
+    np.testing.assert_array_equal(v["child_offsets"], ref["child_offsets"])
+    np.testing.assert_array_equal(v["internal_to_leaf"], ref["internal_to_leaf"])
+    np.testing.assert_array_equal(v["level_range"], ref["level_range"])
+    np.testing.assert_array_equal(np.diff(v["layout"].astype(np.int64)), ref["counts"].astype(np.int64))
+    np.testing.assert_array_equal(v["centers"], ref["centers"])
+    np.testing.assert_array_equal(v["sizes"], ref["sizes"])
+    lr = ref["level_range"]
+    assert v["max_depth"] == max(k for k in range(22) if lr[k + 1] > lr[k])
+    g = sph.target_groups(gpu_ctx, 0, wl.n)
+    expect = np.append(np.arange(0, wl.n, 32), wl.n)
+    np.testing.assert_array_equal(g, expect)
+    g = sph.target_groups(gpu_ctx, 5, 100)
+    np.testing.assert_array_equal(g, [5, 37, 69, 100])

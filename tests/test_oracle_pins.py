@@ -167,3 +167,16 @@ def test_hilbert_curve_properties(port):
     xs = np.stack([res["x"], res["y"], res["z"]], 1)
     steps = np.abs(np.diff(xs, axis=0)).sum(1)
     np.testing.assert_allclose(steps, 1.0 / side, rtol=1e-12)
+
+
+def test_port_node_centers_equal_reference(port, ref_oracle):
+    """nodeFpCenters (focus/source_center.hpp:129-141) with centerAndSize (sfc/box.hpp:317-334):
+    the port's geometric node centers and half sizes equal the reference's bit for bit"""
+    from oracle import oracle as O
+    from sphexa_gb300 import workloads as W
+    wls = [W.sedov(20, jitter=0.25, seed=2), W.sphere(5000, seed=4), W.random_cube(3000, seed=66, periodic=False)]
+    for wl in wls:
+        a = port.sweep(wl, "ve", stages=O.OS_KEYS | O.OS_TREE, want_nbr=False)
+        b = ref_oracle.sweep(wl, "ve", stages=O.OS_KEYS | O.OS_TREE, want_nbr=False)
+        np.testing.assert_array_equal(a["centers"], b["centers"])
+        np.testing.assert_array_equal(a["sizes"], b["sizes"])
