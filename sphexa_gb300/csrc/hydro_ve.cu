@@ -546,9 +546,9 @@ struct MeVeArgs {
     const uint32_t* owned;
     const uint32_t* ownedCount;
     double* acc;
-    // mixed form: packed neighbour records {vx vy vz c} {c11 c12 c13 c22} {c23 c33 m xm}
-    // {alpha rho m/rho m*prho} per particle
-    const float4* pack;
+    // mixed form: the neighbour side of a pair in three 32-byte blocks per particle (meVePackKernel):
+    // {cell (2 words) xl yl zl 1/h vx vy} {vz c c11 c12 c13 c22 c23 c33} {m xm alpha rho m/rho m*prho}
+    const Rec8* pack;
     // FP64: the energy sums (en, avE before max(0, .)) for the VE adjoint, or null
     double *tapeEn, *tapeAvE;
 };
@@ -577,17 +577,24 @@ __device__ __forceinline__ T avRv(T rx, T ry, T rz, T eta, T etaCrit, const T gi
     return -phi * (d1 + d2);
 }
 
-// neighbour-side fields of the mixed momentum-energy pass as four 16-byte records per particle
-__global__ void meVePackKernel(int64_t n, MeVeArgs a, float4* __restrict__ pack)
+// neighbour-side fields of the mixed momentum-energy pass as three 32-byte blocks per particle,
+// the grid position (cell, in-cell offset, 1/h) included, each block read by one 256-bit load
+__global__ void meVePackKernel(int64_t n, MeVeArgs a, const u64* __restrict__ cell, const float4* __restrict__ loc,
+                               float4* __restrict__ pack)
 {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (j >= n) return;
     const float m = ld<float>(a.m, j), xm = ld<float>(a.xm, j), kx = ld<float>(a.kx, j);
     const float rho = kx * m / xm;
-    pack[4 * j] = make_float4(ld<float>(a.vx, j), ld<float>(a.vy, j), ld<float>(a.vz, j), ld<float>(a.c, j));
-    pack[4 * j + 1] = make_float4(ld<float>(a.c11, j), ld<float>(a.c12, j), ld<float>(a.c13, j), ld<float>(a.c22, j));
-    pack[4 * j + 2] = make_float4(ld<float>(a.c23, j), ld<float>(a.c33, j), m, xm);
-    pack[4 * j + 3] = make_float4(ld<float>(a.alpha, j), rho, m / rho, m * ld<float>(a.prho, j));
+    const u64 cj = cell[j];
+    const float4 l = loc[j];
+    float4* q = pack + 6 * j;
+    q[0] = make_float4(__uint_as_float(unsigned(cj)), __uint_as_float(unsigned(cj >> 32)), l.x, l.y);
+    q[1] = make_float4(l.z, l.w, ld<float>(a.vx, j), ld<float>(a.vy, j));
+    q[2] = make_float4(ld<float>(a.vz, j), ld<float>(a.c, j), ld<float>(a.c11, j), ld<float>(a.c12, j));
+    q[3] = make_float4(ld<float>(a.c13, j), ld<float>(a.c22, j), ld<float>(a.c23, j), ld<float>(a.c33, j));
+    q[4] = make_float4(m, xm, ld<float>(a.alpha, j), rho);
+    q[5] = make_float4(m / rho, m * ld<float>(a.prho, j), 0.f, 0.f);
 }
 
 template<class P, bool AvClean, bool Smooth = false>
@@ -710,35 +717,42 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             dt = courantDt(__longlong_as_double(maxvBits), hi, ci, a.Kcour);
         }
     } else {
-        // neighbour fields from the packed records (4 x 16 B per particle, meVePackKernel): six
-        // gathers per pair (cell, offset, 4 records) instead of seventeen scalar ones
+        // neighbour fields from three 32-byte blocks per particle (meVePackKernel), one 256-bit
+        // load each; the kernel function's cubic pieces from shared memory
+        __shared__ float4 tabW[kHermIntervals];
+        stageHermTable(tabW, static_cast<const float4*>(a.wh));
         auto t = cm.target(i);
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         T rhoiInv = __frcp_rn(rhoi);
         KSum mx, my, mz, en, avE;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
-            T rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
-            const float4 pv = __ldg(a.pack + 4 * int64_t(j));      // vx vy vz c
-            const float4 pc = __ldg(a.pack + 4 * int64_t(j) + 1);  // c11 c12 c13 c22
-            const float4 pd = __ldg(a.pack + 4 * int64_t(j) + 2);  // c23 c33 m xm
-            const float4 pe = __ldg(a.pack + 4 * int64_t(j) + 3);  // alpha rho m/rho m*prho
+            const Rec8 b0 = ldRec8(a.pack + 3 * int64_t(j));      // cell xl yl zl 1/h vx vy
+            const Rec8 b1 = ldRec8(a.pack + 3 * int64_t(j) + 1);  // vz c c11 c12 c13 c22 c23 c33
+            const Rec8 b2 = ldRec8(a.pack + 3 * int64_t(j) + 2);  // m xm alpha rho m/rho m*prho
+            const u64 cj = u64(__float_as_uint(b0.v[0])) | (u64(__float_as_uint(b0.v[1])) << 32);
+            const int ddx = CoordMixed::wrap(t.ix - int(cj & kGridMask), cm.pbc[0]);
+            const int ddy = CoordMixed::wrap(t.iy - int((cj >> kGridBits) & kGridMask), cm.pbc[1]);
+            const int ddz = CoordMixed::wrap(t.iz - int(cj >> (2 * kGridBits)), cm.pbc[2]);
+            const T rx = fmaf(float(ddx), cm.u[0], t.xl - b0.v[2]);
+            const T ry = fmaf(float(ddy), cm.u[1], t.yl - b0.v[3]);
+            const T rz = fmaf(float(ddz), cm.u[2], t.zl - b0.v[4]);
+            const T hjInv = b0.v[5];
             T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
             T rinv = rsqrtf(r2);
             T dist = r2 * rinv;
-            T vxij = vxi - pv.x, vyij = vyi - pv.y, vzij = vzi - pv.z;
+            T vxij = vxi - b0.v[6], vyij = vyi - b0.v[7], vzij = vzi - b1.v[0];
             T v1 = dist * hiInv, v2 = dist * hjInv;
-            T Wi = hiInv3 * lookupH32(reinterpret_cast<const float4*>(a.wh), v1);
-            T Wj = (hjInv * hjInv * hjInv) * lookupH32(reinterpret_cast<const float4*>(a.wh), v2);
+            T Wi = hiInv3 * lookupH32Shared(tabW, v1);
+            T Wj = (hjInv * hjInv * hjInv) * lookupH32Shared(tabW, v2);
             T gix = c11i * rx + c12i * ry + c13i * rz;
             T giy = c12i * rx + c22i * ry + c23i * rz;
             T giz = c13i * rx + c23i * ry + c33i * rz;
-            T gjx = pc.x * rx + pc.y * ry + pc.z * rz;
-            T gjy = pc.y * rx + pc.w * ry + pd.x * rz;
-            T gjz = pc.z * rx + pd.x * ry + pd.y * rz;
-            T mj = pd.z, cj = pv.w, xmj = pd.w;
-            T rhoj = pe.y;
+            T gjx = b1.v[2] * rx + b1.v[3] * ry + b1.v[4] * rz;
+            T gjy = b1.v[3] * rx + b1.v[5] * ry + b1.v[6] * rz;
+            T gjz = b1.v[4] * rx + b1.v[6] * ry + b1.v[7] * rz;
+            T mj = b2.v[0], csj = b1.v[1], xmj = b2.v[1];
+            T rhoj = b2.v[3];
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
@@ -746,8 +760,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
                 rv += avRv<T>(rx, ry, rz, fminf(v1, v2), etaCrit, gi, gj);
             }
             T wij = rv * rinv;
-            T visc = artificialViscosity<T>(ai, pe.x, ci, cj, wij);
-            T vsig = T(0.5) * (ci + cj) - T(2) * wij;
+            T visc = artificialViscosity<T>(ai, b2.v[2], ci, csj, wij);
+            T vsig = T(0.5) * (ci + csj) - T(2) * wij;
             maxv = (vsig > maxv) ? vsig : maxv;
             T dr = fabsf(rhoi - rhoj), sr = rhoi + rhoj;
             T am, bm;
@@ -763,8 +777,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
                 am = xmi2 * q;
                 bm = xmj * xmj * __frcp_rn(q);
             }
-            T av = mj * rhoiInv * visc, bv = pe.z * visc;
-            T momi = mj * prhoi * am, momj = pe.w * bm;
+            T av = mj * rhoiInv * visc, bv = b2.v[4] * visc;
+            T momi = mj * prhoi * am, momj = b2.v[5] * bm;
             T si = vxij * gix + vyij * giy + vzij * giz;
             T sj = vxij * gjx + vyij * gjy + vzij * gjz;
             T avWi = av * Wi, bvWj = bv * Wj;
@@ -1493,10 +1507,11 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
     auto cm = coordMixed(c);
     if (mixed) {
         a.wh = c->whH32.p;
-        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));
-        meVePackKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>());
+        SPHGB_TRY(c->pack.ensure(sizeof(Rec8) * 3 * size_t(p->n)));
+        meVePackKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->gridKey.as<u64>(),
+                                                                 c->gridLoc.as<float4>(), c->pack.as<float4>());
         SPHGB_TRY(launched(c, "meVePackKernel"));
-        a.pack = c->pack.as<float4>();
+        a.pack = c->pack.as<Rec8>();
         if (avClean) meVeKernel<MixedTag, true><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
         else meVeKernel<MixedTag, false><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, a);
     } else {

@@ -334,6 +334,40 @@ __device__ __forceinline__ float lookupH32(const float4* __restrict__ tab, float
     return hermEval(__ldg(tab + k), x - float(k));
 }
 
+// the same from a copy of the table in shared memory: a warp's 32 lookups land on random pieces,
+// which costs one L1 sector per lane from global memory but only a few shared-memory wavefronts
+__device__ __forceinline__ float lookupH32Shared(const float4* tab, float v)
+{
+    const float x = v * (0.5f * kHermIntervals);
+    const int k = int(x);
+    if (k >= kHermIntervals) return 0.f;  // v >= 2
+    return hermEval(tab[k], x - float(k));
+}
+
+// copies a kHermIntervals-piece table into shared memory (every thread of the block takes part)
+__device__ __forceinline__ void stageHermTable(float4* dst, const float4* __restrict__ src)
+{
+    for (int q = threadIdx.x; q < kHermIntervals; q += blockDim.x) dst[q] = __ldg(src + q);
+    __syncthreads();
+}
+
+// ---- 32-byte neighbour records, one 256-bit load each ----
+// A warp's gather of 16-byte records touches about one L1 sector per lane and record; packing a
+// neighbour's fields into 32-byte blocks halves the sector accesses per pair.
+struct alignas(32) Rec8 {
+    float v[8];
+};
+
+__device__ __forceinline__ Rec8 ldRec8(const Rec8* p)
+{
+    Rec8 r;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]), "=f"(r.v[4]), "=f"(r.v[5]), "=f"(r.v[6]),
+          "=f"(r.v[7])
+        : "l"(p));
+    return r;
+}
+
 // W and dW/dv at the same v
 __device__ __forceinline__ void lookupH32Pair(const float4* __restrict__ tw, const float4* __restrict__ tdw, float v,
                                               float& w, float& dw)
