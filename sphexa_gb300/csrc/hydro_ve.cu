@@ -217,16 +217,20 @@ struct IadDivvArgs {
     void *dV11, *dV12, *dV13, *dV22, *dV23, *dV33;
     double* tapeP;  // FP64: P_i = sum xm_j W (v_j - v_i) r^T for the VE adjoint (9 x tapeN), or null
     int64_t tapeN;
-    const float4* rec;  // mixed: neighbour records {vx vy vz vol} (packIadKernel)
+    const Rec8* rec;    // mixed: neighbour blocks {cell xl yl zl vx vy vz} (packIadKernel)
+    const float2* rec2; // mixed: {vol xm}
 };
 
-// neighbour-side fields of the mixed IAD + divv/curlv pass as one 16-byte record per particle
+// neighbour-side fields of the mixed IAD + divv/curlv pass: the grid position and velocity in one
+// 32-byte block (one 256-bit load) and {vol xm} in 8 bytes
 __global__ void packIadKernel(int64_t n, const void* vx, const void* vy, const void* vz, const void* vol,
-                              float4* __restrict__ rec)
+                              const void* xm, const u64* __restrict__ cell, const float4* __restrict__ loc,
+                              float4* __restrict__ rec, float2* __restrict__ rec2)
 {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (j >= n) return;
-    rec[j] = make_float4(ld<float>(vx, j), ld<float>(vy, j), ld<float>(vz, j), ld<float>(vol, j));
+    packGridBlock(rec + 2 * j, cell[j], loc[j], ld<float>(vx, j), ld<float>(vy, j), ld<float>(vz, j));
+    rec2[j] = make_float2(ld<float>(vol, j), ld<float>(xm, j));
 }
 
 // FP64 epilogue of IAD + divv/curlv for particle i from its sums tau = sum vol_j W r r^T and
@@ -278,6 +282,9 @@ template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
 iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
 {
+    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
+    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
+    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(a.wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -325,7 +332,6 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         iadEpilogue64(a, i, hi, tau, M);
     } else {
         using T = float;
-        const float4* tab = static_cast<const float4*>(a.wh);
         auto t = cm.target(i);
         const T vxi = ld<T>(a.vx, i), vyi = ld<T>(a.vy, i), vzi = ld<T>(a.vz, i);
         // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
@@ -334,12 +340,13 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         float Aabs = 0.f;  // sum over pairs of |xm_j W| |v_j - v_i|_1 |r|_1 >= sum |term| of every M entry
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
-            T rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
-            const float4 R = a.rec[j];  // {vx vy vz vol}
+            const Rec8 B = ldRec8(a.rec + j);  // cell xl yl zl vx vy vz
+            const float2 Q = __ldg(a.rec2 + j);  // vol xm
+            T rx, ry, rz;
+            cm.diffBlock(t, B, rx, ry, rz);
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            T w = lookupH32(tab, dist * t.hInv);
-            T vw = R.w * w;
+            T w = lookupH32Shared(hermTab, dist * t.hInv);
+            T vw = Q.x * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             t11.add(rx * rxv);
             t12.add(ry * rxv);
@@ -347,8 +354,8 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             t22.add(ry * ryv);
             t23.add(rz * ryv);
             t33.add(rz * rzv);
-            T xw = ld<T>(a.xm, j) * w;
-            const T dvx = R.x - vxi, dvy = R.y - vyi, dvz = R.z - vzi;
+            T xw = Q.y * w;
+            const T dvx = B.v[5] - vxi, dvy = B.v[6] - vyi, dvz = B.v[7] - vzi;
             T sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
             Aabs = fmaf(fabsf(xw) * (fabsf(dvx) + fabsf(dvy) + fabsf(dvz)), fabsf(rx) + fabsf(ry) + fabsf(rz), Aabs);
             M[0].add(sx * rx);
@@ -415,18 +422,20 @@ struct AvArgs {
     void* alpha;
     double* tapeG;  // FP64: G_i (3 x tapeN) for the VE adjoint, or null
     int64_t tapeN;
-    const float4* rec;   // mixed: neighbour records {vx vy vz c} and {vol divv} (packAvKernel)
-    const float2* rec2;
+    const Rec8* rec;     // mixed: neighbour blocks {cell xl yl zl vx vy vz} and {c vol divv} (packAvKernel)
+    const float4* rec2;
     const double2* w64;  // FP64: W in the context's form (wh: the mixed pieces)
 };
 
-// neighbour-side fields of the mixed AV-switch pass as a 16-byte and an 8-byte record per particle
-__global__ void packAvKernel(int64_t n, AvArgs a, float4* __restrict__ rec, float2* __restrict__ rec2)
+// neighbour-side fields of the mixed AV-switch pass: the grid position and velocity in one 32-byte
+// block (one 256-bit load) and {c vol divv} in 16 bytes
+__global__ void packAvKernel(int64_t n, AvArgs a, const u64* __restrict__ cell, const float4* __restrict__ loc,
+                             float4* __restrict__ rec, float4* __restrict__ rec2)
 {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (j >= n) return;
-    rec[j] = make_float4(ld<float>(a.vx, j), ld<float>(a.vy, j), ld<float>(a.vz, j), ld<float>(a.c, j));
-    rec2[j] = make_float2(ld<float>(a.vol, j), ld<float>(a.divv, j));
+    packGridBlock(rec + 2 * j, cell[j], loc[j], ld<float>(a.vx, j), ld<float>(a.vy, j), ld<float>(a.vz, j));
+    rec2[j] = make_float4(ld<float>(a.c, j), ld<float>(a.vol, j), ld<float>(a.divv, j), 0.f);
 }
 
 // alpha update in the arithmetic of the field type (av_switches_kern.hpp:114-134)
@@ -449,6 +458,9 @@ template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf, CoordMixed cm, AvArgs a)
 {
     using T = typename P::T;
+    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
+    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
+    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(a.wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -495,17 +507,17 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
         KSum sx, sy, sz;
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
-            T rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
+            const Rec8 B = ldRec8(a.rec + j);  // cell xl yl zl vx vy vz
+            const float4 Q = __ldg(a.rec2 + j);  // c vol divv
+            T rx, ry, rz;
+            cm.diffBlock(t, B, rx, ry, rz);
             T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
             T rinv = rsqrtf(r2);
             T dist = r2 * rinv;
-            const float4 R = a.rec[j];   // {vx vy vz c}
-            const float2 Q = a.rec2[j];  // {vol divv}
-            T vxij = vxi - R.x, vyij = vyi - R.y, vzij = vzi - R.z;
+            T vxij = vxi - B.v[5], vyij = vyi - B.v[6], vzij = vzi - B.v[7];
             T rv = rx * vxij + ry * vyij + rz * vzij;
-            if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + R.w - 3.f * rv * rinv);
-            T fw = Q.x * (divvi - Q.y) * lookupH32(reinterpret_cast<const float4*>(a.wh), dist * t.hInv);
+            if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + Q.x - 3.f * rv * rinv);
+            T fw = Q.y * (divvi - Q.z) * lookupH32Shared(hermTab, dist * t.hInv);
             sx.add(fw * rx);
             sy.add(fw * ry);
             sz.add(fw * rz);
@@ -1366,10 +1378,12 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
             SPHGB_TRY(c->divvBound.ensure(sizeof(float) * size_t(p->n)));
             a.divvBound = c->divvBound.as<float>();
         }
-        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
-        a.rec = c->pack.as<float4>();
-        packIadKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->vx, p->vy, p->vz, a.vol,
-                                                                  c->pack.as<float4>());
+        SPHGB_TRY(c->pack.ensure(sizeof(Rec8) * 3 * size_t(p->n)));  // the ME blocks' space, free here
+        a.rec = c->pack.as<Rec8>();
+        a.rec2 = reinterpret_cast<const float2*>(c->pack.as<Rec8>() + p->n);
+        packIadKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(
+            p->n, p->vx, p->vy, p->vz, a.vol, p->xm, c->gridKey.as<u64>(), c->gridLoc.as<float4>(),
+            c->pack.as<float4>(), reinterpret_cast<float2*>(c->pack.as<Rec8>() + p->n));
         SPHGB_TRY(launched(c, "packIadKernel"));
         iadDivvKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
         SPHGB_TRY(launched(c, "iadDivvKernel"));
@@ -1423,11 +1437,12 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
     }
     if (mixed) {
         a.wh = c->whH32.p;
-        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
-        a.rec = c->pack.as<float4>();
-        a.rec2 = reinterpret_cast<const float2*>(c->pack.as<float4>() + p->n);
-        packAvKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, a, c->pack.as<float4>(),
-                                                                 reinterpret_cast<float2*>(c->pack.as<float4>() + p->n));
+        SPHGB_TRY(c->pack.ensure(sizeof(Rec8) * 3 * size_t(p->n)));  // the ME blocks' space, free here
+        a.rec = c->pack.as<Rec8>();
+        a.rec2 = reinterpret_cast<const float4*>(c->pack.as<Rec8>() + p->n);
+        packAvKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(
+            p->n, a, c->gridKey.as<u64>(), c->gridLoc.as<float4>(), c->pack.as<float4>(),
+            reinterpret_cast<float4*>(c->pack.as<Rec8>() + p->n));
         SPHGB_TRY(launched(c, "packAvKernel"));
         avKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), a);
     } else if (pairOnce(c, p, first, last)) {

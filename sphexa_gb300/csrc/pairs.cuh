@@ -368,6 +368,28 @@ __device__ __forceinline__ Rec8 ldRec8(const Rec8* p)
     return r;
 }
 
+// A neighbour block that starts with the grid position: v[0], v[1] the packed 21-bit cells (low,
+// high word), v[2..4] the FP32 offset inside the cell; v[5..7] belong to the pass.
+__device__ __forceinline__ void packGridBlock(float4* q, u64 cell, float4 loc, float f5, float f6, float f7)
+{
+    q[0] = make_float4(__uint_as_float(unsigned(cell)), __uint_as_float(unsigned(cell >> 32)), loc.x, loc.y);
+    q[1] = make_float4(loc.z, f5, f6, f7);
+}
+
+// W and dW/dv at the same v, pieces in shared memory
+__device__ __forceinline__ void lookupH32PairShared(const float4* tw, const float4* tdw, float v, float& w, float& dw)
+{
+    const float x = v * (0.5f * kHermIntervals);
+    const int k = int(x);
+    if (k >= kHermIntervals) {
+        w = dw = 0.f;
+        return;
+    }
+    const float t = x - float(k);
+    w = hermEval(tw[k], t);
+    dw = hermEval(tdw[k], t);
+}
+
 // W and dW/dv at the same v
 __device__ __forceinline__ void lookupH32Pair(const float4* __restrict__ tw, const float4* __restrict__ tdw, float v,
                                               float& w, float& dw)
@@ -425,6 +447,17 @@ struct CoordMixed {
         ry = fmaf(float(dy), u[1], t.yl - l.y);
         rz = fmaf(float(dz), u[2], t.zl - l.z);
         hjInv = l.w;
+    }
+    // the same difference from a neighbour block written by packGridBlock
+    __device__ __forceinline__ void diffBlock(const Target& t, const Rec8& b, float& rx, float& ry, float& rz) const
+    {
+        const u64 k = u64(__float_as_uint(b.v[0])) | (u64(__float_as_uint(b.v[1])) << 32);
+        int dx = wrap(t.ix - int(k & kGridMask), pbc[0]);
+        int dy = wrap(t.iy - int((k >> kGridBits) & kGridMask), pbc[1]);
+        int dz = wrap(t.iz - int(k >> (2 * kGridBits)), pbc[2]);
+        rx = fmaf(float(dx), u[0], t.xl - b.v[2]);
+        ry = fmaf(float(dy), u[1], t.yl - b.v[3]);
+        rz = fmaf(float(dz), u[2], t.zl - b.v[4]);
     }
 };
 
