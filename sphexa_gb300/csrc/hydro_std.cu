@@ -18,11 +18,24 @@ namespace sphgb {
 namespace {
 
 // ---------------------------------------------------------------- density / xmass
+// neighbour-side fields of the mixed density / xmass pass: grid position and m in one 32-byte block
+// per particle (one 256-bit load)
+__global__ void packXmassKernel(int64_t n, const void* m, const u64* __restrict__ cell, const float4* __restrict__ loc,
+                                float4* __restrict__ rec)
+{
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    packGridBlock(rec + 2 * j, cell[j], loc[j], ld<float>(m, j), 0.f, 0.f);
+}
+
 template<class P, bool StoreRho, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64 cf, CoordMixed cm, const void* h,
                                                           const void* m, const void* wh, const double2* w64,
-                                                          double K, void* out)
+                                                          double K, void* out, const Rec8* rec = nullptr)
 {
+    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
+    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
+    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -44,17 +57,17 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         double xm = mi / (rho0 * K * h3Inv);
         st<double>(out, i, StoreRho ? mi / xm : xm);
     } else {
-        const float4* tab = static_cast<const float4*>(wh);
         auto t = cm.target(i);
         float mi = ld<float>(m, i);
         KSum rho0;
         rho0.add(mi);
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
-            float rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
+            const Rec8 B = ldRec8(rec + j);  // cell xl yl zl m
+            float rx, ry, rz;
+            cm.diffBlock(t, B, rx, ry, rz);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            rho0.add(lookupH32(tab, dist * t.hInv) * ld<float>(m, j));
+            rho0.add(lookupH32Shared(hermTab, dist * t.hInv) * B.v[5]);
         }
         double hi = double(ld<float>(h, i));
         double rho = rho0.value64() * K / (hi * hi * hi);
@@ -394,14 +407,22 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
                                                                c->pairAcc.as<double>(), static_cast<double*>(out));
         return launched(c, "xmassOnceFinish");
     }
+    const Rec8* rec = nullptr;
+    if constexpr (std::is_same_v<P, MixedTag>) {
+        SPHGB_TRY(c->pack.ensure(sizeof(Rec8) * 3 * size_t(p->n)));  // the ME blocks' space, free here
+        packXmassKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->m, c->gridKey.as<u64>(),
+                                                                    c->gridLoc.as<float4>(), c->pack.as<float4>());
+        SPHGB_TRY(launched(c, "packXmassKernel"));
+        rec = c->pack.as<Rec8>();
+    }
     return withKernelForm(c, [&](auto smooth) {
         constexpr bool S = std::is_same_v<P, Fp64Tag> && decltype(smooth)::value;
         if (storeRho)
             xmassKernel<P, true, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c),
-                                                                           c->K, out);
+                                                                           c->K, out, rec);
         else
             xmassKernel<P, false, S><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, cm, p->h, p->m, wh, tabW64(c),
-                                                                            c->K, out);
+                                                                            c->K, out, rec);
         return launched(c, "xmassKernel");
     });
 }

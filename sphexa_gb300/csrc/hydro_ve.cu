@@ -76,12 +76,14 @@ int launchVeAux(sphgb_ctx* c, const sphgb_particles* p)
 }
 
 // ---------------------------------------------------------------- gradh (kx, gradh)
-// neighbour-side fields of the mixed gradh pass as one 8-byte record {xm m} per particle
-__global__ void packGradhKernel(int64_t n, const void* xm, const void* m, float2* __restrict__ rec)
+// neighbour-side fields of the mixed gradh pass: grid position, xm and m in one 32-byte block per
+// particle (one 256-bit load)
+__global__ void packGradhKernel(int64_t n, const void* xm, const void* m, const u64* __restrict__ cell,
+                                const float4* __restrict__ loc, float4* __restrict__ rec)
 {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (j >= n) return;
-    rec[j] = make_float2(ld<float>(xm, j), ld<float>(m, j));
+    packGridBlock(rec + 2 * j, cell[j], loc[j], ld<float>(xm, j), ld<float>(m, j), 0.f);
 }
 
 template<class P, bool Smooth = false>
@@ -91,8 +93,15 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
                                                           double K,
                                                           void* kxOut, void* gradhOut,
                                                           double* tapeWom = nullptr, double* tapeWr0 = nullptr,
-                                                          const float2* rec = nullptr)
+                                                          const Rec8* rec = nullptr)
 {
+    // mixed: the cubic pieces of W and dW/dv in shared memory, staged by the whole block
+    constexpr int kTabs = std::is_same_v<P, MixedTag> ? kHermIntervals : 1;
+    __shared__ float4 hermW[kTabs], hermDW[kTabs];
+    if constexpr (std::is_same_v<P, MixedTag>) {
+        stageHermTable(hermW, static_cast<const float4*>(wh));
+        stageHermTable(hermDW, static_cast<const float4*>(whd));
+    }
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -132,7 +141,6 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         st<double>(kxOut, i, kxi);
         st<double>(gradhOut, i, 1.0 - dhdrho * whomega);
     } else {
-        const float4 *tw = static_cast<const float4*>(wh), *tdw = static_cast<const float4*>(whd);
         auto t = cm.target(i);
         float mi = ld<float>(m, i), xmi = ld<float>(xm, i);
         KSum kx, whom, wr0;
@@ -141,17 +149,17 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         wr0.add(-3.f * mi);
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
-            float rx, ry, rz, hjInv;
-            cm.diff(t, j, rx, ry, rz, hjInv);
+            const Rec8 B = ldRec8(rec + j);  // cell xl yl zl xm m
+            float rx, ry, rz;
+            cm.diffBlock(t, B, rx, ry, rz);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             float v = dist * t.hInv;
             float w, dw;
-            lookupH32Pair(tw, tdw, v, w, dw);
+            lookupH32PairShared(hermW, hermDW, v, w, dw);
             float dterh = -(3.f * w + v * dw);
-            const float2 Q = rec[j];  // {xm m}
-            kx.add(w * Q.x);
-            whom.add(dterh * Q.x);
-            wr0.add(dterh * Q.y);
+            kx.add(w * B.v[5]);
+            whom.add(dterh * B.v[5]);
+            wr0.add(dterh * B.v[6]);
         }
         double hi = double(ld<float>(h, i)), hInv = 1.0 / hi, h3Inv = hInv * hInv * hInv;
         double kxi = kx.value64() * (K * h3Inv);
@@ -1281,9 +1289,10 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
         return launched(c, "gradhOnceFinish");
     }
     if (p->precision == SPHGB_MIXED) {
-        SPHGB_TRY(c->pack.ensure(sizeof(float4) * 4 * size_t(p->n)));  // the ME records' space, free here
-        float2* rec = reinterpret_cast<float2*>(c->pack.p);
-        packGradhKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->xm, p->m, rec);
+        SPHGB_TRY(c->pack.ensure(sizeof(Rec8) * 3 * size_t(p->n)));  // the ME blocks' space, free here
+        const Rec8* rec = c->pack.as<Rec8>();
+        packGradhKernel<<<gridFor(p->n, 256), 256, 0, c->stream>>>(p->n, p->xm, p->m, c->gridKey.as<u64>(),
+                                                                    c->gridLoc.as<float4>(), c->pack.as<float4>());
         SPHGB_TRY(launched(c, "packGradhKernel"));
         gradhKernel<MixedTag><<<blocks, kPairBlock, 0, c->stream>>>(lv, coordFp64(c, p), coordMixed(c), p->h, p->m,
                                                                     p->xm, c->whH32.p, c->whdH32.p, nullptr,
