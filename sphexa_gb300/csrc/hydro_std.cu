@@ -33,9 +33,6 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
                                                           const void* m, const void* wh, const double2* w64,
                                                           double K, void* out, const Rec8* rec = nullptr)
 {
-    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
-    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
-    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -67,7 +64,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
             float rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            rho0.add(lookupH32Shared(hermTab, dist * t.hInv) * B.v[5]);
+            rho0.add(lookupH32(static_cast<const float4*>(wh), dist * t.hInv) * B.v[5]);
         }
         double hi = double(ld<float>(h, i));
         double rho = rho0.value64() * K / (hi * hi * hi);

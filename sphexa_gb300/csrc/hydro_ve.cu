@@ -95,13 +95,6 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
                                                           double* tapeWom = nullptr, double* tapeWr0 = nullptr,
                                                           const Rec8* rec = nullptr)
 {
-    // mixed: the cubic pieces of W and dW/dv in shared memory, staged by the whole block
-    constexpr int kTabs = std::is_same_v<P, MixedTag> ? kHermIntervals : 1;
-    __shared__ float4 hermW[kTabs], hermDW[kTabs];
-    if constexpr (std::is_same_v<P, MixedTag>) {
-        stageHermTable(hermW, static_cast<const float4*>(wh));
-        stageHermTable(hermDW, static_cast<const float4*>(whd));
-    }
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -155,7 +148,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
             float v = dist * t.hInv;
             float w, dw;
-            lookupH32PairShared(hermW, hermDW, v, w, dw);
+            lookupH32Pair(static_cast<const float4*>(wh), static_cast<const float4*>(whd), v, w, dw);
             float dterh = -(3.f * w + v * dw);
             kx.add(w * B.v[5]);
             whom.add(dterh * B.v[5]);
@@ -290,9 +283,6 @@ template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
 iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
 {
-    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
-    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
-    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(a.wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -353,7 +343,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             T rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);
             T dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-            T w = lookupH32Shared(hermTab, dist * t.hInv);
+            T w = lookupH32(static_cast<const float4*>(a.wh), dist * t.hInv);
             T vw = Q.x * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             t11.add(rx * rxv);
@@ -466,9 +456,6 @@ template<class P, bool Smooth = false>
 __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf, CoordMixed cm, AvArgs a)
 {
     using T = typename P::T;
-    // mixed: the kernel function's cubic pieces in shared memory, staged by the whole block
-    __shared__ float4 hermTab[std::is_same_v<P, MixedTag> ? kHermIntervals : 1];
-    if constexpr (std::is_same_v<P, MixedTag>) stageHermTable(hermTab, static_cast<const float4*>(a.wh));
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
     const int64_t ii = i - lv.first;
@@ -525,7 +512,7 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             T vxij = vxi - B.v[5], vyij = vyi - B.v[6], vzij = vzi - B.v[7];
             T rv = rx * vxij + ry * vyij + rz * vzij;
             if (rv < 0.f) vsig_i = fmaxf(vsig_i, ci + Q.x - 3.f * rv * rinv);
-            T fw = Q.y * (divvi - Q.z) * lookupH32Shared(hermTab, dist * t.hInv);
+            T fw = Q.y * (divvi - Q.z) * lookupH32(static_cast<const float4*>(a.wh), dist * t.hInv);
             sx.add(fw * rx);
             sy.add(fw * ry);
             sz.add(fw * rz);
@@ -738,9 +725,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
         }
     } else {
         // neighbour fields from three 32-byte blocks per particle (meVePackKernel), one 256-bit
-        // load each; the kernel function's cubic pieces from shared memory
-        __shared__ float4 tabW[kHermIntervals];
-        stageHermTable(tabW, static_cast<const float4*>(a.wh));
+        // load each; the kernel function's 8 KB of cubic pieces stay in L1
+        const float4* tabW = static_cast<const float4*>(a.wh);
         auto t = cm.target(i);
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         T rhoiInv = __frcp_rn(rhoi);
@@ -763,8 +749,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T dist = r2 * rinv;
             T vxij = vxi - b0.v[6], vyij = vyi - b0.v[7], vzij = vzi - b1.v[0];
             T v1 = dist * hiInv, v2 = dist * hjInv;
-            T Wi = hiInv3 * lookupH32Shared(tabW, v1);
-            T Wj = (hjInv * hjInv * hjInv) * lookupH32Shared(tabW, v2);
+            T Wi = hiInv3 * lookupH32(tabW, v1);
+            T Wj = (hjInv * hjInv * hjInv) * lookupH32(tabW, v2);
             T gix = c11i * rx + c12i * ry + c13i * rz;
             T giy = c12i * rx + c22i * ry + c23i * rz;
             T giz = c13i * rx + c23i * ry + c33i * rz;

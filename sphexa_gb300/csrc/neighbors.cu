@@ -78,27 +78,15 @@ __device__ __forceinline__ void gridOffset(const NbrArgs& a, const int cj[3], fl
     for (int k = 0; k < 3; ++k) r[k] = fmaf(float(CoordMixed::wrap(cj[k] - co[k], a.box.pbc[k])), a.u[k], lv[k]);
 }
 
-// The 32 targets of a warp form kSub subgroups of 8 SFC-consecutive targets.  A staged candidate
-// joins the queue of every subgroup whose search box (its targets' 2h boxes) it meets, and each
-// target tests only its subgroup's queue: the subgroup boxes are smaller than the warp's, so a
-// target tests about a third fewer candidates (measured: 733 -> see DESIGN).
-constexpr int kSub = 4;
-constexpr int kSubLanes = kWarp / kSub;
-constexpr int kQueue = 2 * kWarp + 4;  // a queue row: 64 slots + 16 bytes, so that the four rows
-                                       // start in different banks (broadcast loads conflict-free)
-
 struct WarpSmem {
     int32_t stack[kStack];
-    // per subgroup: queue of staged candidates that lie in the subgroup's search box (negated
-    // offsets from the group origin, one array per axis so that one 16-byte broadcast load gives
-    // four candidates' coordinate for the packed FP32x2 arithmetic, and their particle indices,
-    // ascending)
-    alignas(16) float nx[kSub][kQueue];
-    alignas(16) float ny[kSub][kQueue];
-    alignas(16) float nz[kSub][kQueue];
-    alignas(16) uint32_t idx[kSub][kQueue];
-    // subgroup search boxes (x lo, x hi, y lo, y hi, z lo, z hi per subgroup) for the staging lanes
-    alignas(16) float sbox[kSub][8];
+    // queue of staged candidates that lie in the group's search box: negated offsets from the
+    // group origin, one array per axis so that one 16-byte broadcast load gives four candidates'
+    // coordinate for the packed FP32x2 arithmetic, and their particle indices (ascending)
+    alignas(16) float nx[2 * kWarp];
+    alignas(16) float ny[2 * kWarp];
+    alignas(16) float nz[2 * kWarp];
+    alignas(16) uint32_t idx[2 * kWarp];
 };
 
 __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
@@ -145,23 +133,15 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     const float dxi = reli[0], dyi = reli[1], dzi = reli[2];
     const float rf = valid ? __double2float_ru(twoH) : 0.f;
 
-    // subgroup and group search boxes relative to the origin
+    // group search box relative to the origin
     float gmin[3] = {valid ? dxi - rf : INFINITY, valid ? dyi - rf : INFINITY, valid ? dzi - rf : INFINITY};
     float gmax[3] = {valid ? dxi + rf : -INFINITY, valid ? dyi + rf : -INFINITY, valid ? dzi + rf : -INFINITY};
-    float smin[3], smax[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        for (int o = kSubLanes / 2; o > 0; o >>= 1) {
+    for (int k = 0; k < 3; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
             gmin[k] = fminf(gmin[k], __shfl_xor_sync(0xffffffffu, gmin[k], o));
             gmax[k] = fmaxf(gmax[k], __shfl_xor_sync(0xffffffffu, gmax[k], o));
         }
-        smin[k] = gmin[k];
-        smax[k] = gmax[k];
-        for (int o = kWarp / 2; o >= kSubLanes; o >>= 1) {
-            gmin[k] = fminf(gmin[k], __shfl_xor_sync(0xffffffffu, gmin[k], o));
-            gmax[k] = fmaxf(gmax[k], __shfl_xor_sync(0xffffffffu, gmax[k], o));
-        }
-    }
     // absolute position of the origin from its cell (FP32 suffices for pruning, see the pad)
     bool exactOnly = false;
     float gc[3], gs[3], Rg = 0.f;
@@ -212,40 +192,27 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         }
     };
 
-    // one chunk of m <= 32 contiguous candidates [ja, ja + m), staged by the warp: one candidate per
-    // lane (coalesced loads of cell and offset).  A candidate joins the queue of each subgroup whose
-    // search box it meets, up to the FP32 rounding of the offsets (cullPad); a dropped candidate is
-    // farther than 2h from every target of that subgroup along one axis, so the reference's FP64
-    // test rejects it too.  Appends keep ascending index order (ballot compaction).  When a queue
-    // holds 32 candidates, every target tests the first 32 slots of its subgroup's queue with a
-    // fixed trip count (a shorter queue is padded with far-away sentinels whose FP32 distance is
-    // +inf); the last, partial blocks are padded the same way.  Groups that need the exact test for
-    // every pair keep every candidate and test the filled slots.
+    // one chunk of m <= 32 contiguous candidates [ja, ja + m), staged by the warp.  Every target
+    // tests all 32 slots with a fixed trip count; slots >= m hold a far-away sentinel whose FP32
+    // distance is +inf.  Groups that need the exact test for every pair loop over the m slots.
+    // Candidates are staged 32 at a time (one per lane, coalesced loads of cell and offset); those
+    // outside the group's search box by more than the FP32 rounding of the offsets (cullPad) are
+    // dropped and the rest appended, in ascending index order, to the warp's queue by ballot
+    // compaction.  A dropped candidate is farther than 2h from every target along one axis, so the
+    // reference's FP64 test rejects it too.  Each full queue block of 32 is tested by every target
+    // with a fixed trip count; the last, partial block has far-away sentinels in its empty slots.
+    // Groups that need the exact test for every pair keep every candidate and test the filled slots.
     const float cullPad = 32.f * 0x1p-24f * (Rg + fmaxf(a.u[0], fmaxf(a.u[1], a.u[2])));
-    if ((lane & (kSubLanes - 1)) == 0) {
-        float* sbq = sm.sbox[lane / kSubLanes];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            sbq[2 * k] = smin[k] - cullPad;
-            sbq[2 * k + 1] = smax[k] + cullPad;
-        }
-    }
-    __syncwarp();
-    const int sub = lane / kSubLanes;
-    int qn[kSub] = {0, 0, 0, 0};  // candidates in each subgroup's queue (the same in every lane)
-    float* qx = sm.nx[sub];
-    float* qy = sm.ny[sub];
-    float* qz = sm.nz[sub];
-    const uint32_t* qi = sm.idx[sub];
-    auto testBlock = [&]() {
-        // this lane's queue length, by selects (an index into qn would put it in local memory)
-        const int mine = sub == 0 ? qn[0] : (sub == 1 ? qn[1] : (sub == 2 ? qn[2] : qn[3]));
-        const int filled = min(mine, kWarp);
+    const float bxl = gmin[0] - cullPad, bxh = gmax[0] + cullPad;
+    const float byl = gmin[1] - cullPad, byh = gmax[1] + cullPad;
+    const float bzl = gmin[2] - cullPad, bzh = gmax[2] + cullPad;
+    int qn = 0;  // candidates in the queue
+    auto testBlock = [&](int filled) {
         if (valid) tested += unsigned(filled);
         if (exactOnly) {
             if (valid)
                 for (int t = 0; t < filled; ++t) {
-                    const uint32_t j = qi[t];
+                    const uint32_t j = sm.idx[t];
                     if (exactIn(j)) take(j);
                 }
         } else {
@@ -255,9 +222,9 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
             const float2 dx2 = make_float2(dxi, dxi), dy2 = make_float2(dyi, dyi), dz2 = make_float2(dzi, dzi);
 #pragma unroll 2
             for (int t = 0; t < kWarp; t += 4) {
-                const float4 X = *reinterpret_cast<const float4*>(qx + t);
-                const float4 Y = *reinterpret_cast<const float4*>(qy + t);
-                const float4 Z = *reinterpret_cast<const float4*>(qz + t);
+                const float4 X = *reinterpret_cast<const float4*>(&sm.nx[t]);
+                const float4 Y = *reinterpret_cast<const float4*>(&sm.ny[t]);
+                const float4 Z = *reinterpret_cast<const float4*>(&sm.nz[t]);
                 const float2 ex0 = __fadd2_rn(dx2, make_float2(X.x, X.y));
                 const float2 ex1 = __fadd2_rn(dx2, make_float2(X.z, X.w));
                 const float2 ey0 = __fadd2_rn(dy2, make_float2(Y.x, Y.y));
@@ -267,7 +234,7 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
                 const float2 q0 = __ffma2_rn(ex0, ex0, __ffma2_rn(ey0, ey0, __fmul2_rn(ez0, ez0)));
                 const float2 q1 = __ffma2_rn(ex1, ex1, __ffma2_rn(ey1, ey1, __fmul2_rn(ez1, ez1)));
                 const float d2[4] = {q0.x, q0.y, q1.x, q1.y};
-                const uint4 J = *reinterpret_cast<const uint4*>(qi + t);
+                const uint4 J = *reinterpret_cast<const uint4*>(&sm.idx[t]);
                 const uint32_t js[4] = {J.x, J.y, J.z, J.w};
                 bool band = false;
 #pragma unroll
@@ -293,70 +260,50 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         }
         __syncwarp();
     };
-    // pads every queue shorter than a block with sentinels, tests one block, and moves each queue's
-    // remainder beyond the block to its front
-    auto testAndShift = [&]() {
-#pragma unroll
-        for (int q = 0; q < kSub; ++q)
-            if (lane >= qn[q]) {
-                sm.nx[q][lane] = -1e30f;
-                sm.ny[q][lane] = -1e30f;
-                sm.nz[q][lane] = -1e30f;
-            }
-        __syncwarp();
-        testBlock();
-#pragma unroll
-        for (int q = 0; q < kSub; ++q) {
-            const int rest = qn[q] > kWarp ? qn[q] - kWarp : 0;
-            if (lane < rest) {
-                sm.nx[q][lane] = sm.nx[q][kWarp + lane];
-                sm.ny[q][lane] = sm.ny[q][kWarp + lane];
-                sm.nz[q][lane] = sm.nz[q][kWarp + lane];
-                sm.idx[q][lane] = sm.idx[q][kWarp + lane];
-            }
-            qn[q] = rest;
-        }
-        __syncwarp();
-    };
     auto flush = [&](int64_t ja, int m) {
         float rj[3];
-        bool inRange = lane < m;
-        if (inRange) {
+        bool keep = false;
+        if (lane < m) {
             const int64_t j = ja + lane;
             int cj[3];
             unpackCell(a.cell[j], cj);
             gridOffset(a, cj, a.loc[j], co, lo, rj);
+            keep = exactOnly || (rj[0] >= bxl && rj[0] <= bxh && rj[1] >= byl && rj[1] <= byh && rj[2] >= bzl &&
+                                 rj[2] <= bzh);
         }
-        int most = 0;
-#pragma unroll
-        for (int q = 0; q < kSub; ++q) {
-            bool keep = false;
-            if (inRange) {
-                const float4 b0 = *reinterpret_cast<const float4*>(&sm.sbox[q][0]);
-                const float2 b1 = *reinterpret_cast<const float2*>(&sm.sbox[q][4]);
-                keep = exactOnly || (rj[0] >= b0.x && rj[0] <= b0.y && rj[1] >= b0.z && rj[1] <= b0.w &&
-                                     rj[2] >= b1.x && rj[2] <= b1.y);
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int q = qn + __popc(km & ((1u << lane) - 1u));
+            sm.nx[q] = -rj[0];
+            sm.ny[q] = -rj[1];
+            sm.nz[q] = -rj[2];
+            sm.idx[q] = uint32_t(ja + lane);
+        }
+        qn += __popc(km);
+        __syncwarp();
+        if (qn >= kWarp) {
+            testBlock(kWarp);
+            qn -= kWarp;
+            if (lane < qn) {  // move the queue's tail [32, 32 + qn) to the front
+                sm.nx[lane] = sm.nx[kWarp + lane];
+                sm.ny[lane] = sm.ny[kWarp + lane];
+                sm.nz[lane] = sm.nz[kWarp + lane];
+                sm.idx[lane] = sm.idx[kWarp + lane];
             }
-            const unsigned km = __ballot_sync(0xffffffffu, keep);
-            if (keep) {
-                const int slot = qn[q] + __popc(km & ((1u << lane) - 1u));
-                sm.nx[q][slot] = -rj[0];
-                sm.ny[q][slot] = -rj[1];
-                sm.nz[q][slot] = -rj[2];
-                sm.idx[q][slot] = uint32_t(ja + lane);
-            }
-            qn[q] += __popc(km);
-            most = max(most, qn[q]);
+            __syncwarp();
+        }
+    };
+    // the partial last block: sentinels (FP32 distance +inf) in the empty slots
+    auto drain = [&]() {
+        if (qn == 0) return;
+        if (lane >= qn) {
+            sm.nx[lane] = -1e30f;
+            sm.ny[lane] = -1e30f;
+            sm.nz[lane] = -1e30f;
         }
         __syncwarp();
-        if (most >= kWarp) testAndShift();
-    };
-    // the partial last blocks
-    auto drain = [&]() {
-        int most = 0;
-#pragma unroll
-        for (int q = 0; q < kSub; ++q) most = max(most, qn[q]);
-        if (most > 0) testAndShift();
+        testBlock(qn);
+        qn = 0;
     };
 
     int64_t pa = 0, pb = 0;  // pending contiguous candidate range

@@ -334,23 +334,6 @@ __device__ __forceinline__ float lookupH32(const float4* __restrict__ tab, float
     return hermEval(__ldg(tab + k), x - float(k));
 }
 
-// the same from a copy of the table in shared memory: a warp's 32 lookups land on random pieces,
-// which costs one L1 sector per lane from global memory but only a few shared-memory wavefronts
-__device__ __forceinline__ float lookupH32Shared(const float4* tab, float v)
-{
-    const float x = v * (0.5f * kHermIntervals);
-    const int k = int(x);
-    if (k >= kHermIntervals) return 0.f;  // v >= 2
-    return hermEval(tab[k], x - float(k));
-}
-
-// copies a kHermIntervals-piece table into shared memory (every thread of the block takes part)
-__device__ __forceinline__ void stageHermTable(float4* dst, const float4* __restrict__ src)
-{
-    for (int q = threadIdx.x; q < kHermIntervals; q += blockDim.x) dst[q] = __ldg(src + q);
-    __syncthreads();
-}
-
 // ---- 32-byte neighbour records, one 256-bit load each ----
 // A warp's gather of 16-byte records touches about one L1 sector per lane and record; packing a
 // neighbour's fields into 32-byte blocks halves the sector accesses per pair.
@@ -374,20 +357,6 @@ __device__ __forceinline__ void packGridBlock(float4* q, u64 cell, float4 loc, f
 {
     q[0] = make_float4(__uint_as_float(unsigned(cell)), __uint_as_float(unsigned(cell >> 32)), loc.x, loc.y);
     q[1] = make_float4(loc.z, f5, f6, f7);
-}
-
-// W and dW/dv at the same v, pieces in shared memory
-__device__ __forceinline__ void lookupH32PairShared(const float4* tw, const float4* tdw, float v, float& w, float& dw)
-{
-    const float x = v * (0.5f * kHermIntervals);
-    const int k = int(x);
-    if (k >= kHermIntervals) {
-        w = dw = 0.f;
-        return;
-    }
-    const float t = x - float(k);
-    w = hermEval(tw[k], t);
-    dw = hermEval(tdw[k], t);
 }
 
 // W and dW/dv at the same v
