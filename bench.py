@@ -435,6 +435,10 @@ def main() -> None:
         rec32["speedup_vs_fp64"] = rec32["value"] / rec64["value"]
         rec32["errors_vs_fp64"] = mixed_errors(ref64, r32)
         rec32["roofline"] = pair_roofline(st32, names, int(stats32["nc_sum"]), flops, fp32_peak, "fp32")
+        # every pair pass against the FP32 probe peak: counted flop/pair x pairs / stage time
+        rec32["pair_pass_fp32_frac"] = {
+            names[k]: round(int(stats32["nc_sum"]) * flops[names[k]] / (float(st32[k]) * 1e-3) / fp32_peak, 4)
+            for k in range(len(names)) if names[k] in flops and st32[k] > 0}
         rec32["neighbors_roofline"] = search_roofline(stats32, float(st32[1]), w.n, fp32_peak,
                                                       peaks.get("hbm_gbs"))
         rec32["dominant_stage"] = names[int(np.argmax(st32))]

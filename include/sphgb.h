@@ -34,8 +34,10 @@ typedef enum {
     SPHGB_ERR_NOCONV = 6,     /* h / neighbour-count iteration did not converge for some particles */
     SPHGB_ERR_NOTFOUND = 7,   /* no CUDA device / extension not usable */
     SPHGB_ERR_TOO_LARGE = 8,  /* request exceeds a fixed capacity */
-    SPHGB_ERR_INPUT = 9       /* a coordinate, h or box limit is not finite, or h <= 0; found by a check
+    SPHGB_ERR_INPUT = 9,      /* a coordinate, h or box limit is not finite, or h <= 0; found by a check
                                  pass before any key, tree or search kernel runs on the data */
+    SPHGB_ERR_TIMEOUT = 10    /* a bounded device-side wait gave up (the radix sort's look-back between
+                                 tiles); the results of that call are invalid, the context stays usable */
 } sphgb_status;
 
 typedef enum { SPHGB_FP64 = 0, SPHGB_MIXED = 1 } sphgb_precision;
@@ -189,6 +191,14 @@ int sphgb_get_order(sphgb_ctx* ctx, const uint32_t** order);
  * (domain/include/cstone/domain/domain.hpp:533-595); sphgb_domain_sync reorders the fields of
  * sphgb_particles, this call the rest (x_m1, du_m1, temp, ...) */
 int sphgb_apply_order(sphgb_ctx* ctx, void* field, int32_t elem_bytes);
+/* stable sort of n 64-bit keys by their bits [0, end_bit) with optional 32-bit values, device
+ * pointers, out of place (keys_in and vals_in are left as they are): the GPU sortByKeyGpu of the
+ * reference (domain/include/cstone/primitives/primitives_gpu.cu:323-340), the sort behind every
+ * sync.  vals_in and vals_out are both null or both set; 1 <= end_bit <= 64, n < 2^32.  The
+ * context keeps the scratch.  Synchronises the context's stream; SPHGB_ERR_TIMEOUT if a
+ * look-back wait between tiles gave up (the output is then invalid). */
+int sphgb_sort_by_key(sphgb_ctx* ctx, const uint64_t* keys_in, uint64_t* keys_out, const uint32_t* vals_in,
+                      uint32_t* vals_out, int64_t n, int32_t end_bit);
 
 /* ---- neighbours ---- */
 /* cstone::findNeighbors (domain/include/cstone/findneighbors.hpp:149-170): fixed h, no

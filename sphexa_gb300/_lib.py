@@ -13,9 +13,11 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libsphgb.so"
 
 SPHGB_OK = 0
+SPHGB_ERR_ARG = 1
 SPHGB_ERR_NOCONV = 6
 SPHGB_ERR_TOO_LARGE = 8
 SPHGB_ERR_INPUT = 9
+SPHGB_ERR_TIMEOUT = 10
 SPHGB_FP64, SPHGB_MIXED = 0, 1
 SPHGB_STD, SPHGB_VE = 0, 1
 SPHGB_KERNEL_TABLE, SPHGB_KERNEL_SMOOTH = 0, 1
@@ -106,6 +108,7 @@ SIGNATURES = {
     "sphgb_get_params": [_P, C.POINTER(SphgbParams)],
     "sphgb_target_groups": [_P, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)],
     "sphgb_apply_order": [_P, _P, C.c_int32],
+    "sphgb_sort_by_key": [_P, _P, _P, _P, _P, _I64, C.c_int32],
     "sphgb_find_neighbors": [_P, _P, _P, _P, _P, C.c_int32, _I64, _I64, C.c_uint32, _P, _P],
     "sphgb_find_neighbors_sph": [_P, C.POINTER(SphgbParticles), _I64, _I64],
     "sphgb_export_neighbors": [_P, _P],

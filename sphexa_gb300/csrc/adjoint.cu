@@ -981,6 +981,9 @@ int buildTranspose(sphgb_ctx* c)
     csrFromKeysKernel<<<gridFor(work, 256), 256, 0, c->stream>>>(c->adjKeys.as<u64>(), pairs, nWork,
                                                                 c->tOff.as<uint32_t>(), c->tIdx.as<uint32_t>());
     SPHGB_TRY(launched(c, "csrFromKeysKernel"));
+    SPHGB_TRY(sortStatusAsync(c));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    SPHGB_TRY(sortStatusAfterSync(c));
     c->transEpoch = c->nbrEpoch;
     c->transPairs = pairs;
     return SPHGB_OK;

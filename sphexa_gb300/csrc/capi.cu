@@ -83,6 +83,7 @@ const char* sphgb_status_string(int s)
     case SPHGB_ERR_NOTFOUND: return "no usable CUDA device";
     case SPHGB_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
     case SPHGB_ERR_INPUT: return "non-finite coordinate, smoothing length or box limit, or h <= 0";
+    case SPHGB_ERR_TIMEOUT: return "a bounded device wait gave up (radix sort look-back)";
     default: return "unknown status";
     }
 }
@@ -151,7 +152,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
                     &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pack,       &c->whx32,     &c->whH32, &c->whdH32,    &c->refMask,
                     &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape,
-                    &c->checkWord,  &c->whS64,      &c->whdS64};
+                    &c->checkWord,  &c->whS64,      &c->whdS64,     &c->sortLook,   &c->sortState};
     for (DBuf* b : bufs) b->release();
     if (c->dFlags) cudaFree(c->dFlags);
     for (auto& ev : c->ev)
@@ -310,6 +311,19 @@ int sphgb_apply_order(sphgb_ctx* c, void* field, int32_t elemBytes)
 {
     SPHGB_TRY(useDevice(c));
     return applyOrder(c, field, elemBytes);
+}
+
+int sphgb_sort_by_key(sphgb_ctx* c, const uint64_t* keysIn, uint64_t* keysOut, const uint32_t* valsIn,
+                      uint32_t* valsOut, int64_t n, int32_t endBit)
+{
+    SPHGB_TRY(useDevice(c));
+    if (n < 0 || (n > 0 && (!keysIn || !keysOut))) return SPHGB_ERR_ARG;
+    if (n > 0 && (keysIn == keysOut || (valsIn && valsIn == valsOut))) return SPHGB_ERR_ARG;
+    SPHGB_TRY(radixSort(c, reinterpret_cast<const u64*>(keysIn), reinterpret_cast<u64*>(keysOut), valsIn, valsOut, n,
+                        endBit));
+    SPHGB_TRY(sortStatusAsync(c));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    return sortStatusAfterSync(c);
 }
 
 int sphgb_find_neighbors(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h,

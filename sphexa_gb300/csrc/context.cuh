@@ -156,6 +156,11 @@ struct sphgb_ctx {
     sphgb::DBuf adjKeys, adjKeysAlt, tOff, tIdx, adjState;
     sphgb::DBuf scanTemp;  // tile sums of exclusiveScan
     bool sortSmemSet = false;
+    // radix sort: look-back words (256 per tile) and state (give-up flag, epochs, tickets, plan);
+    // the flag is read back by sortStatusAsync / sortStatusAfterSync around a stream sync
+    sphgb::DBuf sortLook, sortState;
+    uint32_t sortFlagHost = 0;
+    bool sortFlagPending = false;
     int64_t transEpoch = -1, transPairs = 0;
     // validity of the precomputes: the lists' epoch and the field pointers they were made from
     int64_t nbrEpoch = 0, prepEpoch = -1, prepEpoch64 = -1;
@@ -211,6 +216,10 @@ int buildTranspose(sphgb_ctx* c);
 // stable LSD radix sort of 64-bit keys (bits [0, endBit)) with optional 32-bit values, out of place
 int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* valsIn, uint32_t* valsOut, int64_t n,
               int endBit);
+// the radix sort's give-up flag: queue its copy to the host before a stream sync, test it after
+// (SPHGB_ERR_TIMEOUT when a look-back wait gave up; the flag is then cleared)
+int sortStatusAsync(sphgb_ctx* c);
+int sortStatusAfterSync(sphgb_ctx* c);
 // exclusive prefix sum of n 32-bit counts (out may not alias in)
 int exclusiveScan(sphgb_ctx* c, const uint32_t* in, uint32_t* out, int64_t n);
 int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_grads* g, int deterministic);

@@ -585,7 +585,9 @@ int buildTree(sphgb_ctx* c, bool rebalance)
     SPHGB_TRY(launched(c, "layoutKernel"));
     SPHGB_CUDA(cudaMemcpyAsync(c->levelRange, c->levelRangeDev.as<int32_t>() + (kMaxLevel + 2),
                                sizeof(int32_t) * (kMaxLevel + 2), cudaMemcpyDeviceToHost, st));
+    SPHGB_TRY(sortStatusAsync(c));  // the key and tree sorts of this sync
     SPHGB_CUDA(cudaStreamSynchronize(st));
+    SPHGB_TRY(sortStatusAfterSync(c));
     c->stats.num_leaves = L;
     c->stats.num_nodes = NN;
     c->stats.num_internal = S;

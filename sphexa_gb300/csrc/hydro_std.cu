@@ -58,9 +58,14 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         float mi = ld<float>(m, i);
         KSum rho0;
         rho0.add(mi);
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's block is loaded
+        Rec8 Bn = ldRec8(rec + jn);                         // while the current pair is evaluated
         for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            const Rec8 B = ldRec8(rec + j);  // cell xl yl zl m
+            const Rec8 B = Bn;  // cell xl yl zl m
+            if (k + 1 < nc) {
+                jn = lv.at(ii, k + 1);
+                Bn = ldRec8(rec + jn);
+            }
             float rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));

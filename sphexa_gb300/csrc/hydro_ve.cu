@@ -140,9 +140,14 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         kx.add(xmi);
         whom.add(-3.f * xmi);
         wr0.add(-3.f * mi);
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's block is loaded
+        Rec8 Bn = ldRec8(rec + jn);                         // while the current pair is evaluated
         for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            const Rec8 B = ldRec8(rec + j);  // cell xl yl zl xm m
+            const Rec8 B = Bn;  // cell xl yl zl xm m
+            if (k + 1 < nc) {
+                jn = lv.at(ii, k + 1);
+                Bn = ldRec8(rec + jn);
+            }
             float rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);
             float dist = sqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
@@ -500,10 +505,17 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
         auto t = cm.target(i);
         const float kh3 = float(a.K) * t.hInv * t.hInv * t.hInv;
         KSum sx, sy, sz;
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's fields are loaded
+        Rec8 Bn = ldRec8(a.rec + jn);                       // while the current pair is evaluated
+        float4 Qn = __ldg(a.rec2 + jn);
         for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            const Rec8 B = ldRec8(a.rec + j);  // cell xl yl zl vx vy vz
-            const float4 Q = __ldg(a.rec2 + j);  // c vol divv
+            const Rec8 B = Bn;     // cell xl yl zl vx vy vz
+            const float4 Q = Qn;  // c vol divv
+            if (k + 1 < nc) {
+                jn = lv.at(ii, k + 1);
+                Bn = ldRec8(a.rec + jn);
+                Qn = __ldg(a.rec2 + jn);
+            }
             T rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);
             T r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
@@ -731,11 +743,21 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         T rhoiInv = __frcp_rn(rhoi);
         KSum mx, my, mz, en, avE;
+        // the next neighbour's blocks are loaded while the current pair is evaluated
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);
+        Rec8 n0 = ldRec8(a.pack + 3 * int64_t(jn)), n1 = ldRec8(a.pack + 3 * int64_t(jn) + 1),
+             n2 = ldRec8(a.pack + 3 * int64_t(jn) + 2);
         for (unsigned k = 0; k < nc; ++k) {
-            uint32_t j = lv.at(ii, k);
-            const Rec8 b0 = ldRec8(a.pack + 3 * int64_t(j));      // cell xl yl zl 1/h vx vy
-            const Rec8 b1 = ldRec8(a.pack + 3 * int64_t(j) + 1);  // vz c c11 c12 c13 c22 c23 c33
-            const Rec8 b2 = ldRec8(a.pack + 3 * int64_t(j) + 2);  // m xm alpha rho m/rho m*prho
+            const uint32_t j = jn;
+            const Rec8 b0 = n0;  // cell xl yl zl 1/h vx vy
+            const Rec8 b1 = n1;  // vz c c11 c12 c13 c22 c23 c33
+            const Rec8 b2 = n2;  // m xm alpha rho m/rho m*prho
+            if (k + 1 < nc) {
+                jn = lv.at(ii, k + 1);
+                n0 = ldRec8(a.pack + 3 * int64_t(jn));
+                n1 = ldRec8(a.pack + 3 * int64_t(jn) + 1);
+                n2 = ldRec8(a.pack + 3 * int64_t(jn) + 2);
+            }
             const u64 cj = u64(__float_as_uint(b0.v[0])) | (u64(__float_as_uint(b0.v[1])) << 32);
             const int ddx = CoordMixed::wrap(t.ix - int(cj & kGridMask), cm.pbc[0]);
             const int ddy = CoordMixed::wrap(t.iy - int((cj >> kGridBits) & kGridMask), cm.pbc[1]);

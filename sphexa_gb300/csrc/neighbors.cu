@@ -87,9 +87,11 @@ struct WarpSmem {
     alignas(16) float ny[2 * kWarp];
     alignas(16) float nz[2 * kWarp];
     alignas(16) uint32_t idx[2 * kWarp];
+    // the second cull: box of the target positions (lo x y z, squared radius, hi x y z)
+    alignas(16) float cull[8];
 };
 
-__global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
+__global__ void __launch_bounds__(kNbrBlock, 7) nbrGroupKernel(NbrArgs a)
 {
     __shared__ WarpSmem smem[kWarpsPerBlock];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -206,6 +208,32 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
     const float bxl = gmin[0] - cullPad, bxh = gmax[0] + cullPad;
     const float byl = gmin[1] - cullPad, byh = gmax[1] + cullPad;
     const float bzl = gmin[2] - cullPad, bzh = gmax[2] + cullPad;
+    // second cull: the box of the target positions grown by the largest radius with rounded
+    // edges and corners (a candidate farther than max 2h from that box is farther than 2h_i from
+    // every target i); the pad covers the offsets' FP32 rounding, the factor the squared sum's
+    float tmn[3] = {valid ? dxi : INFINITY, valid ? dyi : INFINITY, valid ? dzi : INFINITY};
+    float tmx[3] = {valid ? dxi : -INFINITY, valid ? dyi : -INFINITY, valid ? dzi : -INFINITY};
+    float rfm = rf;
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            tmn[k] = fminf(tmn[k], __shfl_xor_sync(0xffffffffu, tmn[k], o));
+            tmx[k] = fmaxf(tmx[k], __shfl_xor_sync(0xffffffffu, tmx[k], o));
+        }
+        rfm = fmaxf(rfm, __shfl_xor_sync(0xffffffffu, rfm, o));
+    }
+    const float cullR = rfm + cullPad;
+    if (lane == 0) {
+        sm.cull[0] = tmn[0];
+        sm.cull[1] = tmn[1];
+        sm.cull[2] = tmn[2];
+        sm.cull[3] = cullR * cullR * (1.f + 0x1p-18f);
+        sm.cull[4] = tmx[0];
+        sm.cull[5] = tmx[1];
+        sm.cull[6] = tmx[2];
+        sm.cull[7] = 0.f;
+    }
+    __syncwarp();
     int qn = 0;  // candidates in the queue
     auto testBlock = [&](int filled) {
         if (valid) tested += unsigned(filled);
@@ -218,9 +246,12 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
         } else {
             // four slots per step on packed FP32x2 operations: e = d_i + (-r_j) rounds as
             // d_i - r_j, and d2 = fma(ex, ex, fma(ey, ey, ez * ez)) per slot as in scalar form.
-            // Every lane runs the loop (the band vote is warp-wide); invalid lanes take nothing.
+            // The block's decisions go into two 32-bit masks (d2 below the margin: neighbour; d2
+            // within it: exact FP64 test), then each lane appends its neighbours slot by slot in
+            // ascending order, one loop trip per neighbour instead of a predicated append per slot.
             const float2 dx2 = make_float2(dxi, dxi), dy2 = make_float2(dyi, dyi), dz2 = make_float2(dzi, dzi);
-#pragma unroll 2
+            uint32_t hit = 0, nearm = 0;
+#pragma unroll
             for (int t = 0; t < kWarp; t += 4) {
                 const float4 X = *reinterpret_cast<const float4*>(&sm.nx[t]);
                 const float4 Y = *reinterpret_cast<const float4*>(&sm.ny[t]);
@@ -234,28 +265,19 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
                 const float2 q0 = __ffma2_rn(ex0, ex0, __ffma2_rn(ey0, ey0, __fmul2_rn(ez0, ez0)));
                 const float2 q1 = __ffma2_rn(ex1, ex1, __ffma2_rn(ey1, ey1, __fmul2_rn(ez1, ez1)));
                 const float d2[4] = {q0.x, q0.y, q1.x, q1.y};
-                const uint4 J = *reinterpret_cast<const uint4*>(&sm.idx[t]);
-                const uint32_t js[4] = {J.x, J.y, J.z, J.w};
-                bool band = false;
 #pragma unroll
-                for (int s = 0; s < 4; ++s) band |= !(d2[s] < inBelow) && d2[s] <= outAbove;
-                if (__any_sync(0xffffffffu, valid && band)) {
-                    // a pair within the FP32 margin of the radius (rare): slot by slot, exact test
-                    if (valid) {
-#pragma unroll
-                        for (int s = 0; s < 4; ++s)
-                            if (d2[s] <= outAbove && (d2[s] < inBelow || exactIn(js[s]))) take(js[s]);
-                    }
-                } else {
-                    // the common case without divergence: predicated appends
-#pragma unroll
-                    for (int s = 0; s < 4; ++s) {
-                        const bool tk = valid && d2[s] < inBelow && js[s] != iu;
-                        if (tk && cnt < a.ngmax) *outp = js[s];
-                        outp += tk ? a.stride : 0;
-                        cnt += tk ? 1u : 0u;
-                    }
+                for (int s = 0; s < 4; ++s) {
+                    hit |= (d2[s] < inBelow ? 1u : 0u) << (t + s);
+                    nearm |= (d2[s] <= outAbove ? 1u : 0u) << (t + s);
                 }
+            }
+            if (valid) {
+                // a pair within the FP32 margin of the radius (rare): the exact test
+                for (uint32_t band = nearm & ~hit; band != 0; band &= band - 1u) {
+                    const int s = __ffs(band) - 1;
+                    if (exactIn(sm.idx[s])) hit |= 1u << s;
+                }
+                for (; hit != 0; hit &= hit - 1u) take(sm.idx[__ffs(hit) - 1]);
             }
         }
         __syncwarp();
@@ -268,8 +290,13 @@ __global__ void __launch_bounds__(kNbrBlock) nbrGroupKernel(NbrArgs a)
             int cj[3];
             unpackCell(a.cell[j], cj);
             gridOffset(a, cj, a.loc[j], co, lo, rj);
+            const float4 cl = *reinterpret_cast<const float4*>(&sm.cull[0]);
+            const float4 ch = *reinterpret_cast<const float4*>(&sm.cull[4]);
+            const float ex = fmaxf(fmaxf(cl.x - rj[0], rj[0] - ch.x), 0.f);
+            const float ey = fmaxf(fmaxf(cl.y - rj[1], rj[1] - ch.y), 0.f);
+            const float ez = fmaxf(fmaxf(cl.z - rj[2], rj[2] - ch.z), 0.f);
             keep = exactOnly || (rj[0] >= bxl && rj[0] <= bxh && rj[1] >= byl && rj[1] <= byh && rj[2] >= bzl &&
-                                 rj[2] <= bzh);
+                                 rj[2] <= bzh && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) <= cl.w);
         }
         const unsigned km = __ballot_sync(0xffffffffu, keep);
         if (keep) {

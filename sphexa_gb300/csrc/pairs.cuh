@@ -384,6 +384,7 @@ struct CoordMixed {
     const float4* loc;   // {xl, yl, zl, 1/h}
     float u[3];          // cell edge per axis (box length / 2^21)
     int pbc[3];
+    int sh[3];           // 32 - 21 on periodic axes, 0 on open ones (wrapShift)
     struct Target {
         int ix, iy, iz;
         float xl, yl, zl, hInv;
@@ -417,13 +418,17 @@ struct CoordMixed {
         rz = fmaf(float(dz), u[2], t.zl - l.z);
         hjInv = l.w;
     }
+    // minimum image of a cell difference d in (-2^21, 2^21) by sign extension from bit 20 (s =
+    // 11): d itself when |d| < 2^20, d -/+ 2^21 beyond; s = 0 leaves d unchanged.  The same
+    // image as wrap() except at exactly half the box, where both images are equally near.
+    __device__ __forceinline__ static int wrapShift(int d, int s) { return int(unsigned(d) << s) >> s; }
     // the same difference from a neighbour block written by packGridBlock
     __device__ __forceinline__ void diffBlock(const Target& t, const Rec8& b, float& rx, float& ry, float& rz) const
     {
         const u64 k = u64(__float_as_uint(b.v[0])) | (u64(__float_as_uint(b.v[1])) << 32);
-        int dx = wrap(t.ix - int(k & kGridMask), pbc[0]);
-        int dy = wrap(t.iy - int((k >> kGridBits) & kGridMask), pbc[1]);
-        int dz = wrap(t.iz - int(k >> (2 * kGridBits)), pbc[2]);
+        int dx = wrapShift(t.ix - int(k & kGridMask), sh[0]);
+        int dy = wrapShift(t.iy - int((k >> kGridBits) & kGridMask), sh[1]);
+        int dz = wrapShift(t.iz - int(k >> (2 * kGridBits)), sh[2]);
         rx = fmaf(float(dx), u[0], t.xl - b.v[2]);
         ry = fmaf(float(dy), u[1], t.yl - b.v[3]);
         rz = fmaf(float(dz), u[2], t.zl - b.v[4]);
@@ -438,6 +443,7 @@ inline CoordMixed coordMixed(const sphgb_ctx* c)
     for (int k = 0; k < 3; ++k) {
         r.u[k] = float(c->box.L[k] / double(1 << kGridBits));
         r.pbc[k] = c->box.pbc[k];
+        r.sh[k] = c->box.pbc[k] ? 32 - kGridBits : 0;
     }
     return r;
 }
