@@ -37,7 +37,7 @@ def sources() -> list[Path]:
 
 def _compile(src: Path, verbose: bool) -> tuple[Path, str]:
     obj = BUILD / (src.stem + ".o")
-    deps = [src] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "sphgb.h"]
+    deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.hpp")) + [ROOT / "include" / "sphgb.h"]
     if obj.exists() and all(obj.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return obj, ""
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]

@@ -93,7 +93,7 @@ struct sphgb_ctx {
     sphgb::DBuf levelRangeDev;
     bool haveTree = false;
 
-    // neighbour lists: nbr[k * stride + (i - first)], transposed for coalesced pair-loop reads
+    // neighbour lists in granules of four entries, transposed per granule (listSlot in pairs.cuh)
     int64_t nbrFirst = 0, nbrLast = 0, nbrStride = 0;
     uint32_t nbrNgmax = 0;
     sphgb::DBuf nbr, ncount, active, counters;

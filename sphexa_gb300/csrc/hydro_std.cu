@@ -58,12 +58,15 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         float mi = ld<float>(m, i);
         KSum rho0;
         rho0.add(mi);
-        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's block is loaded
-        Rec8 Bn = ldRec8(rec + jn);                         // while the current pair is evaluated
+        // the list entry two pairs ahead and the next neighbour's block are loaded while the
+        // current pair is evaluated
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i), jnn = nc > 1 ? lv.at(ii, 1) : uint32_t(i);
+        Rec8 Bn = ldRec8(rec + jn);
         for (unsigned k = 0; k < nc; ++k) {
             const Rec8 B = Bn;  // cell xl yl zl m
             if (k + 1 < nc) {
-                jn = lv.at(ii, k + 1);
+                jn = jnn;
+                if (k + 2 < nc) jnn = lv.at(ii, k + 2);
                 Bn = ldRec8(rec + jn);
             }
             float rx, ry, rz;

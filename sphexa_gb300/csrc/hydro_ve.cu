@@ -140,12 +140,15 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
         kx.add(xmi);
         whom.add(-3.f * xmi);
         wr0.add(-3.f * mi);
-        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's block is loaded
-        Rec8 Bn = ldRec8(rec + jn);                         // while the current pair is evaluated
+        // the list entry two pairs ahead and the next neighbour's block are loaded while the
+        // current pair is evaluated
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i), jnn = nc > 1 ? lv.at(ii, 1) : uint32_t(i);
+        Rec8 Bn = ldRec8(rec + jn);
         for (unsigned k = 0; k < nc; ++k) {
             const Rec8 B = Bn;  // cell xl yl zl xm m
             if (k + 1 < nc) {
-                jn = lv.at(ii, k + 1);
+                jn = jnn;
+                if (k + 2 < nc) jnn = lv.at(ii, k + 2);
                 Bn = ldRec8(rec + jn);
             }
             float rx, ry, rz;
@@ -505,14 +508,17 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
         auto t = cm.target(i);
         const float kh3 = float(a.K) * t.hInv * t.hInv * t.hInv;
         KSum sx, sy, sz;
-        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);  // the next neighbour's fields are loaded
-        Rec8 Bn = ldRec8(a.rec + jn);                       // while the current pair is evaluated
+        // the list entry two pairs ahead and the next neighbour's fields are loaded while the
+        // current pair is evaluated
+        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i), jnn = nc > 1 ? lv.at(ii, 1) : uint32_t(i);
+        Rec8 Bn = ldRec8(a.rec + jn);
         float4 Qn = __ldg(a.rec2 + jn);
         for (unsigned k = 0; k < nc; ++k) {
             const Rec8 B = Bn;     // cell xl yl zl vx vy vz
             const float4 Q = Qn;  // c vol divv
             if (k + 1 < nc) {
-                jn = lv.at(ii, k + 1);
+                jn = jnn;
+                if (k + 2 < nc) jnn = lv.at(ii, k + 2);
                 Bn = ldRec8(a.rec + jn);
                 Qn = __ldg(a.rec2 + jn);
             }
@@ -743,8 +749,10 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
         T hiInv = t.hInv, hiInv3 = hiInv * hiInv * hiInv;
         T rhoiInv = __frcp_rn(rhoi);
         KSum mx, my, mz, en, avE;
-        // the next neighbour's blocks are loaded while the current pair is evaluated
+        // the list entry two pairs ahead and the next neighbour's blocks are loaded while the
+        // current pair is evaluated
         uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i);
+        uint32_t jnn = nc > 1 ? lv.at(ii, 1) : uint32_t(i);
         Rec8 n0 = ldRec8(a.pack + 3 * int64_t(jn)), n1 = ldRec8(a.pack + 3 * int64_t(jn) + 1),
              n2 = ldRec8(a.pack + 3 * int64_t(jn) + 2);
         for (unsigned k = 0; k < nc; ++k) {
@@ -753,7 +761,8 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             const Rec8 b1 = n1;  // vz c c11 c12 c13 c22 c23 c33
             const Rec8 b2 = n2;  // m xm alpha rho m/rho m*prho
             if (k + 1 < nc) {
-                jn = lv.at(ii, k + 1);
+                jn = jnn;
+                if (k + 2 < nc) jnn = lv.at(ii, k + 2);
                 n0 = ldRec8(a.pack + 3 * int64_t(jn));
                 n1 = ldRec8(a.pack + 3 * int64_t(jn) + 1);
                 n2 = ldRec8(a.pack + 3 * int64_t(jn) + 2);
@@ -1153,7 +1162,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
            *accV = a.acc + 4 * a.n;
     long long* accS = reinterpret_cast<long long*>(a.acc + 5 * a.n);
     for (unsigned k = 0; k < nOwned; ++k) {
-        const uint32_t e = __ldg(a.owned + int64_t(k) * lv.stride + ii);
+        const uint32_t e = __ldg(a.owned + listSlot(ii, k, lv.stride));
         const uint32_t j = e & 0x7fffffffu;
         const bool mutual = (e >> 31) != 0;
         T rx, ry, rz;

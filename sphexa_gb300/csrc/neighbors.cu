@@ -13,8 +13,9 @@
 // offset inside the cell.  Offsets from the group origin are (cell difference, wrapped exactly
 // in integers) x cell edge + (offset difference), so neither staging nor the distance filter
 // runs an FP64 instruction.  Only pairs whose FP32 distance lies within a rounding margin of the
-// radius are re-tested in FP64 from the original coordinates.  Lists are stored transposed,
-// nbr[k * stride + (i - first)], so that the pair passes read them coalesced.
+// radius are re-tested in FP64 from the original coordinates.  Lists are stored in granules of four
+// entries transposed per granule (listSlot), written one 16-byte granule at a time, so that the pair
+// passes read them coalesced.
 #include <algorithm>
 
 
@@ -91,7 +92,7 @@ struct WarpSmem {
     alignas(16) float cull[8];
 };
 
-__global__ void __launch_bounds__(kNbrBlock, 7) nbrGroupKernel(NbrArgs a)
+__global__ void __launch_bounds__(kNbrBlock, 6) nbrGroupKernel(NbrArgs a)
 {
     __shared__ WarpSmem smem[kWarpsPerBlock];
     const int lane = threadIdx.x & (kWarp - 1);
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(kNbrBlock, 7) nbrGroupKernel(NbrArgs a)
     unsigned long long tested = 0, rechecked = 0;
     const int64_t ii = i - a.first;
     const uint32_t iu = uint32_t(i);
-    uint32_t* outp = a.nbr + ii;  // row cnt of this target's transposed list
+    GranuleWriter out(a.nbr, ii, a.stride, a.ngmax);
 
     // the reference's distanceSq decision in FP64 (findneighbors.hpp:33-60)
     auto exactIn = [&](uint32_t j) {
@@ -188,8 +189,7 @@ __global__ void __launch_bounds__(kNbrBlock, 7) nbrGroupKernel(NbrArgs a)
     };
     auto take = [&](uint32_t j) {
         if (j != iu) {
-            if (cnt < a.ngmax) *outp = j;
-            outp += a.stride;
+            out.put(cnt, j);
             ++cnt;
         }
     };
@@ -399,7 +399,10 @@ __global__ void __launch_bounds__(kNbrBlock, 7) nbrGroupKernel(NbrArgs a)
     }
     drain();
 
-    if (valid) a.count[ii] = cnt;
+    if (valid) {
+        out.finish(cnt);
+        a.count[ii] = cnt;
+    }
     // warp-aggregated statistics
     for (int o = 16; o > 0; o >>= 1) {
         tested += __shfl_xor_sync(0xffffffffu, tested, o);
@@ -489,7 +492,7 @@ __global__ void exportKernel(const uint32_t* __restrict__ nbr, const uint32_t* _
     int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (k >= nWork) return;
     uint32_t c = min(count[k], ngmax);
-    for (uint32_t q = 0; q < c; ++q) out[k * ngmax + q] = nbr[int64_t(q) * stride + k];
+    for (uint32_t q = 0; q < c; ++q) out[k * ngmax + q] = nbr[listSlot(k, q, stride)];
 }
 
 // ---- owned pair lists for the pair-once momentum-energy pass ----
@@ -502,7 +505,7 @@ __global__ void exportKernel(const uint32_t* __restrict__ nbr, const uint32_t* _
 // i owns every non-mutual entry and half of its mutual ones: the mutual pair {i, j} belongs to the
 // smaller index when i + j is odd and to the larger when it is even, so each particle owns about
 // half of its mutual pairs wherever it sits in the SFC order.  The owned entries are written
-// compacted, owned[k * stride + (i - first)] = j | mutual << 31, with their count per particle.
+// compacted in the granule layout of the lists, entry = j | mutual << 31, with their count per particle.
 struct MutualArgs {
     const double *x, *y, *z;
     const void* h;
@@ -572,7 +575,7 @@ __device__ bool mutualPair(const MutualArgs& a, int64_t i, int ci[3], float4 li,
 {
     if (j < a.first || j >= a.last) return false;
     const int64_t jj = j - a.first;
-    if (__ldg(a.count + jj) > a.ngmax && i > int64_t(__ldg(a.nbr + int64_t(a.ngmax - 1) * a.stride + jj)))
+    if (__ldg(a.count + jj) > a.ngmax && i > int64_t(__ldg(a.nbr + listSlot(jj, a.ngmax - 1, a.stride))))
         return false;
     int cj[3];
     unpackCell(__ldg(a.cell + j), cj);
@@ -616,12 +619,14 @@ __global__ void __launch_bounds__(128) ownedListKernel(MutualArgs a)
     unpackCell(__ldg(a.cell + i), ci);
     const float4 li = __ldg(a.loc + i);
     unsigned cnt = 0;
+    GranuleWriter out(a.owned, ii, a.stride, a.ngmax);
     for (unsigned k = 0; k < nc; ++k) {
-        const uint32_t j = __ldg(a.nbr + int64_t(k) * a.stride + ii);
+        const uint32_t j = __ldg(a.nbr + listSlot(ii, k, a.stride));
         const bool m = mutualPair(a, i, ci, li, j);
         const bool own = !m || ((((i ^ int64_t(j)) & 1) != 0) == (i < int64_t(j)));
-        if (own) a.owned[int64_t(cnt++) * a.stride + ii] = j | (m ? 0x80000000u : 0u);
+        if (own) out.put(cnt++, j | (m ? 0x80000000u : 0u));
     }
+    out.finish(cnt);
     a.ownedCount[ii] = cnt;
 }
 
@@ -691,7 +696,7 @@ int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, c
 int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, const void* h, int hIsFloat)
 {
     const int64_t nWork = c->nbrLast - c->nbrFirst;
-    SPHGB_TRY(c->owned.ensure(sizeof(uint32_t) * size_t(c->nbrNgmax) * size_t(c->nbrStride)));
+    SPHGB_TRY(c->owned.ensure(sizeof(uint32_t) * listCapacity(c->nbrNgmax) * size_t(c->nbrStride)));
     SPHGB_TRY(c->ownedCount.ensure(sizeof(uint32_t) * size_t(c->nbrStride)));
     SPHGB_TRY(c->ownedR2.ensure(sizeof(float) * size_t(c->n)));
     radius2Kernel<<<gridFor(c->n, 256), 256, 0, c->stream>>>(x, y, z, h, hIsFloat, c->n, c->box,
@@ -732,7 +737,7 @@ int prepareLists(sphgb_ctx* c, const double* x, const double* y, const double* z
     if (first < 0 || last > c->n || first >= last) return SPHGB_ERR_ARG;
     const int64_t nWork = last - first;
     c->nbrStride = (nWork + 31) / 32 * 32;
-    SPHGB_TRY(c->nbr.ensure(sizeof(uint32_t) * size_t(ngmax) * c->nbrStride));
+    SPHGB_TRY(c->nbr.ensure(sizeof(uint32_t) * listCapacity(ngmax) * c->nbrStride));
     SPHGB_TRY(c->ncount.ensure(sizeof(uint32_t) * c->nbrStride));
     SPHGB_TRY(c->active.ensure(sizeof(uint32_t) * c->nbrStride + c->nbrStride));
     SPHGB_TRY(c->counters.ensure(sizeof(unsigned long long) * 8));

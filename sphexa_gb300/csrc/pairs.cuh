@@ -1,8 +1,8 @@
 // Pair-loop building blocks shared by the std and VE passes.
 //
-// One thread per target particle i walks its own neighbour list nbr[k * stride + (i - first)];
-// a warp holds 32 SFC-consecutive targets, so each list row is one coalesced 128-byte read and
-// the neighbours of a warp overlap heavily in L1.
+// One thread per target particle i walks its own neighbour list; a warp holds 32 SFC-consecutive
+// targets, so entry k of the warp's 32 lists is one coalesced read (512 contiguous bytes shared by
+// four consecutive k) and the neighbours of a warp overlap heavily in L1.
 //
 // Two arithmetic forms:
 //   Fp64  : every operation in double, in the reference's order (the plain drop-in);
@@ -27,17 +27,56 @@ struct MixedTag {
 
 constexpr int kPairBlock = 128;
 
-// ---- neighbour list access ----
+// ---- neighbour list layout ----
+// Lists are stored in granules of kListGran entries, transposed per granule: entries 4g .. 4g+3 of
+// the list of target ii = i - first occupy the 16 contiguous bytes of granule (g * stride + ii).
+// The search writes a granule with one 16-byte store instead of four scattered 4-byte stores, and a
+// warp of 32 consecutive targets reads entry k of its lists from 512 contiguous bytes that also hold
+// entries k+1 .. of the same granule row.  The owned lists of the pair-once passes use the same layout.
+constexpr unsigned kListGran = 4;
+
+__host__ __device__ __forceinline__ int64_t listSlot(int64_t ii, unsigned k, int64_t stride)
+{
+    return (int64_t(k / kListGran) * stride + ii) * kListGran + (k % kListGran);
+}
+
+// entries per target that the buffers reserve for a capacity of ngmax (whole granules)
+inline size_t listCapacity(uint32_t ngmax) { return (size_t(ngmax) + kListGran - 1) / kListGran * kListGran; }
+
+// writes one target's list in order: entries collect in registers, every fourth one stores the
+// granule; finish() stores the last, partial granule.  Granules at or beyond the capacity are not
+// written (entries past ngmax of a capped list are dropped, as the reference drops them).
+struct GranuleWriter {
+    uint4* out;  // granule 0 of this target; granule g at out[g * stride]
+    int64_t stride;
+    unsigned capG;
+    uint32_t b0 = 0, b1 = 0, b2 = 0;
+    __device__ __forceinline__ GranuleWriter(uint32_t* base, int64_t ii, int64_t stride_, uint32_t ngmax)
+        : out(reinterpret_cast<uint4*>(base) + ii), stride(stride_), capG((ngmax + kListGran - 1) / kListGran)
+    {
+    }
+    __device__ __forceinline__ void put(unsigned cnt, uint32_t j)
+    {
+        const unsigned s = cnt % kListGran, g = cnt / kListGran;
+        b0 = s == 0 ? j : b0;
+        b1 = s == 1 ? j : b1;
+        b2 = s == 2 ? j : b2;
+        if (s == kListGran - 1 && g < capG) out[int64_t(g) * stride] = make_uint4(b0, b1, b2, j);
+    }
+    __device__ __forceinline__ void finish(unsigned cnt)
+    {
+        const unsigned g = cnt / kListGran;
+        if (cnt % kListGran != 0 && g < capG) out[int64_t(g) * stride] = make_uint4(b0, b1, b2, 0u);
+    }
+};
+
 struct ListView {
     const uint32_t* nbr;
     const uint32_t* count;
     int64_t stride, first, last;
     uint32_t ngmax;
     __device__ __forceinline__ unsigned capped(int64_t ii) const { return min(count[ii], ngmax); }
-    __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k) const
-    {
-        return __ldg(nbr + int64_t(k) * stride + ii);
-    }
+    __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k) const { return __ldg(nbr + listSlot(ii, k, stride)); }
 };
 
 inline ListView listView(const sphgb_ctx* c)
@@ -47,7 +86,7 @@ inline ListView listView(const sphgb_ctx* c)
 }
 
 // ---- owned lists: the pairs particle i evaluates in the pair-once FP64 passes ----
-// owned[k * stride + (i - first)] = j | mutual << 31, k < count[i - first]: every pair of i's list
+// entry k < count[i - first] of i's owned list (granule layout) = j | mutual << 31: every pair of i's list
 // that j does not list back, and half of the mutual pairs (the other half sits in the owned lists
 // of the other ends).  A mutual pair's evaluation also produces j's terms, added with FP64 atomics.
 struct OwnedView {
@@ -57,7 +96,7 @@ struct OwnedView {
     __device__ __forceinline__ unsigned size(int64_t ii) const { return __ldg(count + ii); }
     __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k, bool& mutual) const
     {
-        const uint32_t e = __ldg(owned + int64_t(k) * stride + ii);
+        const uint32_t e = __ldg(owned + listSlot(ii, k, stride));
         mutual = (e >> 31) != 0;
         return e & 0x7fffffffu;
     }
