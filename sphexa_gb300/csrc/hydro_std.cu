@@ -58,16 +58,20 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
         float mi = ld<float>(m, i);
         KSum rho0;
         rho0.add(mi);
-        // the list entry two pairs ahead and the next neighbour's block are loaded while the
-        // current pair is evaluated
-        uint32_t jn = nc > 0 ? lv.at(ii, 0) : uint32_t(i), jnn = nc > 1 ? lv.at(ii, 1) : uint32_t(i);
-        Rec8 Bn = ldRec8(rec + jn);
+        // the list is read a granule (four entries) per load, the next granule one ahead, and the
+        // next neighbour's block is loaded while the current pair is evaluated
+        uint4 G = nc > 0 ? lv.granule(ii, 0) : make_uint4(uint32_t(i), 0u, 0u, 0u);
+        uint4 Gn = nc > 4 ? lv.granule(ii, 1) : G;
+        Rec8 Bn = ldRec8(rec + G.x);
         for (unsigned k = 0; k < nc; ++k) {
             const Rec8 B = Bn;  // cell xl yl zl m
             if (k + 1 < nc) {
-                jn = jnn;
-                if (k + 2 < nc) jnn = lv.at(ii, k + 2);
-                Bn = ldRec8(rec + jn);
+                const unsigned s = (k + 1) & 3u;
+                if (s == 0) {
+                    G = Gn;
+                    if (k + 5 < nc) Gn = lv.granule(ii, (k + 5) >> 2);
+                }
+                Bn = ldRec8(rec + pick(G, s));
             }
             float rx, ry, rz;
             cm.diffBlock(t, B, rx, ry, rz);

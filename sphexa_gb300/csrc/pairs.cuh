@@ -77,7 +77,14 @@ struct ListView {
     uint32_t ngmax;
     __device__ __forceinline__ unsigned capped(int64_t ii) const { return min(count[ii], ngmax); }
     __device__ __forceinline__ uint32_t at(int64_t ii, unsigned k) const { return __ldg(nbr + listSlot(ii, k, stride)); }
+    // granule g of target ii: entries 4g .. 4g+3
+    __device__ __forceinline__ uint4 granule(int64_t ii, unsigned g) const
+    {
+        return __ldg(reinterpret_cast<const uint4*>(nbr) + (int64_t(g) * stride + ii));
+    }
 };
+// entry s of a granule
+__device__ __forceinline__ uint32_t pick(uint4 g, unsigned s) { return s == 0 ? g.x : s == 1 ? g.y : s == 2 ? g.z : g.w; }
 
 inline ListView listView(const sphgb_ctx* c)
 {
