@@ -292,7 +292,7 @@ __device__ __forceinline__ void iadEpilogue64(const IadDivvArgs& a, int64_t i, d
 }
 
 template<class P, bool Smooth = false>
-__global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 8 : 1)
+__global__ void __launch_bounds__(kPairBlock, std::is_same_v<P, MixedTag> ? 7 : 1)
 iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -347,7 +347,8 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         // one walk, as in the FP64 form: tau and M = sum xm_j W (v_j - v_i) r^T, c_i applied after
         KSum t11, t12, t13, t22, t23, t33;
         KSum M[9];
-        float Aabs = 0.f;  // sum over pairs of |xm_j W| |v_j - v_i|_1 |r|_1 >= sum |term| of every M entry
+        // A[a][c] = sum over pairs of |s_a| |r_c| >= sum |term| of M entry (a, c), s = xm_j W (v_j - v_i)
+        float A[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         for (unsigned k = 0; k < nc; ++k) {
             uint32_t j = lv.at(ii, k);
             const Rec8 B = ldRec8(a.rec + j);  // cell xl yl zl vx vy vz
@@ -367,7 +368,11 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             T xw = Q.y * w;
             const T dvx = B.v[5] - vxi, dvy = B.v[6] - vyi, dvz = B.v[7] - vzi;
             T sx = dvx * xw, sy = dvy * xw, sz = dvz * xw;
-            Aabs = fmaf(fabsf(xw) * (fabsf(dvx) + fabsf(dvy) + fabsf(dvz)), fabsf(rx) + fabsf(ry) + fabsf(rz), Aabs);
+            {
+                const float as[3] = {fabsf(sx), fabsf(sy), fabsf(sz)}, ar[3] = {fabsf(rx), fabsf(ry), fabsf(rz)};
+#pragma unroll
+                for (int q = 0; q < 9; ++q) A[q] = fmaf(as[q / 3], ar[q % 3], A[q]);
+            }
             M[0].add(sx * rx);
             M[1].add(sx * ry);
             M[2].add(sx * rz);
@@ -402,12 +407,14 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         double nk = a.K * (hInv * hInv * hInv) / double(ld<T>(a.kx, i));
         st<T>(a.divv, i, T(nk * (gx[0] + gy[1] + gz[2])));
         if (a.divvBound) {
-            // divv = -nk sum_ac C_ac M_ac with S = nk sum|C| sum|terms| >= every partial sum.  Its
-            // FP32 error is at most (eps_terms + eps_c + eps_xm + eps_kx) S with the measured input
-            // errors (1e-7, 7e-7, 4e-7, 2e-7 relative): about 1.4e-6 S; the flag bound is 4e-6 S
-            const double sC = fabs(double(cc[0])) + fabs(double(cc[3])) + fabs(double(cc[5])) +
-                              2.0 * (fabs(double(cc[1])) + fabs(double(cc[2])) + fabs(double(cc[4])));
-            a.divvBound[i] = float(4e-6 * fabs(nk) * sC * double(Aabs));
+            // divv = -nk sum_ac C_ac M_ac with S = nk sum_ac |C_ac| A_ac >= the sum of |C_ac term| over
+            // every entry and pair.  Its FP32 error is at most (eps_terms + eps_c + eps_xm + eps_kx) S
+            // with the measured input errors (1e-7, 7e-7, 4e-7, 2e-7 relative): about 1.4e-6 S; the
+            // flag bound is 4e-6 S
+            double sCA = 0.0;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) sCA += fabs(C[q / 3][q % 3]) * double(A[q]);
+            a.divvBound[i] = float(4e-6 * fabs(nk) * sCA);
         }
         if (a.curlv) {
             double cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
