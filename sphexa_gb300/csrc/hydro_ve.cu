@@ -392,41 +392,43 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
         st<T>(a.c22, i, cc[3]);
         st<T>(a.c23, i, cc[4]);
         st<T>(a.c33, i, cc[5]);
-        double m64[9];
+        // FP32 epilogue: the compensated sums collapse to FP32 (rounding 2^-24 of each entry), the
+        // gradient sums and the normalisation run in FP32
+        float m32[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) m64[q] = M[q].value64();
-        const double C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
-        double gx[3], gy[3], gz[3];
+        for (int q = 0; q < 9; ++q) m32[q] = M[q].value();
+        const float C[3][3] = {{cc[0], cc[1], cc[2]}, {cc[1], cc[3], cc[4]}, {cc[2], cc[4], cc[5]}};
+        float gx[3], gy[3], gz[3];
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-            gx[b] = -(C[b][0] * m64[0] + C[b][1] * m64[1] + C[b][2] * m64[2]);
-            gy[b] = -(C[b][0] * m64[3] + C[b][1] * m64[4] + C[b][2] * m64[5]);
-            gz[b] = -(C[b][0] * m64[6] + C[b][1] * m64[7] + C[b][2] * m64[8]);
+            gx[b] = -fmaf(C[b][0], m32[0], fmaf(C[b][1], m32[1], C[b][2] * m32[2]));
+            gy[b] = -fmaf(C[b][0], m32[3], fmaf(C[b][1], m32[4], C[b][2] * m32[5]));
+            gz[b] = -fmaf(C[b][0], m32[6], fmaf(C[b][1], m32[7], C[b][2] * m32[8]));
         }
-        double hInv = 1.0 / hi;
-        double nk = a.K * (hInv * hInv * hInv) / double(ld<T>(a.kx, i));
-        st<T>(a.divv, i, T(nk * (gx[0] + gy[1] + gz[2])));
+        const float hInvF = t.hInv;
+        const float nk = float(a.K) * (hInvF * hInvF * hInvF) / ld<T>(a.kx, i);
+        st<T>(a.divv, i, nk * (gx[0] + gy[1] + gz[2]));
         if (a.divvBound) {
             // divv = -nk sum_ac C_ac M_ac with S = nk sum_ac |C_ac| A_ac >= the sum of |C_ac term| over
             // every entry and pair.  Its FP32 error is at most (eps_terms + eps_c + eps_xm + eps_kx) S
-            // with the measured input errors (1e-7, 7e-7, 4e-7, 2e-7 relative): about 1.4e-6 S; the
-            // flag bound is 4e-6 S
-            double sCA = 0.0;
+            // with the measured input errors (1e-7, 7e-7, 4e-7, 2e-7 relative), about 1.4e-6 S, plus
+            // the epilogue's own rounding (a few 2^-24 S); the flag bound is 4e-6 S
+            float sCA = 0.f;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) sCA += fabs(C[q / 3][q % 3]) * double(A[q]);
-            a.divvBound[i] = float(4e-6 * fabs(nk) * sCA);
+            for (int q = 0; q < 9; ++q) sCA = fmaf(fabsf(C[q / 3][q % 3]), A[q], sCA);
+            a.divvBound[i] = 4e-6f * fabsf(nk) * sCA;
         }
         if (a.curlv) {
-            double cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
-            st<T>(a.curlv, i, T(nk * sqrt(cv0 * cv0 + cv1 * cv1 + cv2 * cv2)));
+            const float cv0 = gz[1] - gy[2], cv1 = gx[2] - gz[0], cv2 = gy[0] - gx[1];
+            st<T>(a.curlv, i, nk * sqrtf(fmaf(cv0, cv0, fmaf(cv1, cv1, cv2 * cv2))));
         }
         if (a.dV11) {
-            st<T>(a.dV11, i, T(nk * gx[0]));
-            st<T>(a.dV12, i, T(nk * (gx[1] + gy[0])));
-            st<T>(a.dV13, i, T(nk * (gx[2] + gz[0])));
-            st<T>(a.dV22, i, T(nk * gy[1]));
-            st<T>(a.dV23, i, T(nk * (gy[2] + gz[1])));
-            st<T>(a.dV33, i, T(nk * gz[2]));
+            st<T>(a.dV11, i, nk * gx[0]);
+            st<T>(a.dV12, i, nk * (gx[1] + gy[0]));
+            st<T>(a.dV13, i, nk * (gx[2] + gz[0]));
+            st<T>(a.dV22, i, nk * gy[1]);
+            st<T>(a.dV23, i, nk * (gy[2] + gz[1]));
+            st<T>(a.dV33, i, nk * gz[2]);
         }
     }
 }
