@@ -479,29 +479,8 @@ def main() -> None:
     if args.workload in ("fourier300", "sphere10M"):
         out["structure"] = structure_report(ctx, d64, stats, int(wl.params["ngmax"]))
 
-    # ---------------- mixed form on the same workload, errors against this run's FP64 results
-    if not args.no_mixed:
-        out["mixed"] = mixed_vs_fp64(wl, rec64, d64, args.steps, args.warmup)
-    d64 = None
-    torch.cuda.empty_cache()
-
-    # ---------------- the other configurations: Fourier 27M (the mixed form's own, v != 0) and the
-    # clustered 10M sphere, FP64 and mixed, with structure and per-field errors
-    if not args.no_configs and args.workload == "sedov200_jit":
-        out["configs"] = {}
-        for cname, (csteps, cwarm) in EXTRA_CONFIGS.items():
-            cw = make_workload(cname)
-            c64, cd, cstats, cst, _, _ = run_form(cw, "fp64", csteps, cwarm)
-            c64["roofline"] = pair_roofline(cst, names, int(cstats["nc_sum"]), flops, fp64_peak, "fp64")
-            blk = {"workload": WORKLOADS[cname][0], "n_particles": cw.n, "steps": csteps, "warmup": cwarm,
-                   "fp64": c64, "structure": structure_report(ctx, cd, cstats, int(cw.params["ngmax"]))}
-            blk["mixed"] = mixed_vs_fp64(cw, c64, cd, csteps, cwarm)
-            cd = None
-            out["configs"][cname] = blk
-            del cw
-            torch.cuda.empty_cache()
-
-    # ---------------- end to end through the C ABI with host buffers (pinned), FP64 form
+    # ---------------- end to end through the C ABI with host buffers (pinned), FP64 form, right after
+    # the device-timed sweeps so that both run under the same conditions
     if not args.no_e2e:
         d = sph.ParticlesData.from_workload(wl, "fp64", dev)
         host_in = {k: torch.from_numpy(np.ascontiguousarray(wl.fields[k], dtype=np.float64)).pin_memory()
@@ -533,6 +512,28 @@ def main() -> None:
                       "d2h_bytes_per_step": d2h, "steps": k_e2e,
                       "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
         del d
+
+    # ---------------- mixed form on the same workload, errors against this run's FP64 results
+    if not args.no_mixed:
+        out["mixed"] = mixed_vs_fp64(wl, rec64, d64, args.steps, args.warmup)
+    d64 = None
+    torch.cuda.empty_cache()
+
+    # ---------------- the other configurations: Fourier 27M (the mixed form's own, v != 0) and the
+    # clustered 10M sphere, FP64 and mixed, with structure and per-field errors
+    if not args.no_configs and args.workload == "sedov200_jit":
+        out["configs"] = {}
+        for cname, (csteps, cwarm) in EXTRA_CONFIGS.items():
+            cw = make_workload(cname)
+            c64, cd, cstats, cst, _, _ = run_form(cw, "fp64", csteps, cwarm)
+            c64["roofline"] = pair_roofline(cst, names, int(cstats["nc_sum"]), flops, fp64_peak, "fp64")
+            blk = {"workload": WORKLOADS[cname][0], "n_particles": cw.n, "steps": csteps, "warmup": cwarm,
+                   "fp64": c64, "structure": structure_report(ctx, cd, cstats, int(cw.params["ngmax"]))}
+            blk["mixed"] = mixed_vs_fp64(cw, c64, cd, csteps, cwarm)
+            cd = None
+            out["configs"][cname] = blk
+            del cw
+            torch.cuda.empty_cache()
 
     # ---------------- integration step on the same particles (FP64): time step, positions, h, sums
     if not args.no_integration:

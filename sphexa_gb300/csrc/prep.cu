@@ -40,6 +40,18 @@ __global__ void mixedCoordsKernel(const double* __restrict__ x, const double* __
     loc[i] = make_float4(l[0], l[1], l[2], float(1.0 / hi));
 }
 
+// 1/h into the w of the grid-form offsets, whose cells and offsets the neighbour search of this sweep
+// formed from the same positions.  For FP32 h, 1.0f / h (correctly rounded) equals float(1.0 / h) in
+// FP64: rounding to 53 bits first is innocuous for a quotient of 24-bit operands (53 >= 2 * 24 + 2).
+__global__ void gridHInvKernel(const void* __restrict__ h, int hIsFloat, int64_t n, float4* __restrict__ loc)
+{
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    float4 l = loc[i];
+    l.w = hIsFloat ? 1.0f / static_cast<const float*>(h)[i] : float(1.0 / static_cast<const double*>(h)[i]);
+    loc[i] = l;
+}
+
 // per particle 1/h, 1/h^3 and (1/h) / dx: the last turns a pair distance into table-interval units
 // with one multiply
 __global__ void recipKernel(const double* __restrict__ h, int64_t n, double* __restrict__ out)
@@ -117,6 +129,12 @@ int buildTables(sphgb_ctx* c)
 int prepareMixed(sphgb_ctx* c, sphgb_particles* p, int64_t, int64_t)
 {
     const int64_t n = p->n;
+    if (c->inSweep && c->xBuilt == p->x && c->gridKey.bytes >= sizeof(u64) * n && c->gridLoc.bytes >= sizeof(float4) * n) {
+        // the search of this sweep formed the grid form from these positions; only 1/h is missing
+        gridHInvKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(p->h, p->precision == SPHGB_MIXED, n,
+                                                              c->gridLoc.as<float4>());
+        return launched(c, "gridHInvKernel");
+    }
     SPHGB_TRY(c->gridKey.ensure(sizeof(u64) * n));
     SPHGB_TRY(c->gridLoc.ensure(sizeof(float4) * n));
     mixedCoordsKernel<<<gridFor(n, 256), 256, 0, c->stream>>>(p->x, p->y, p->z, p->h, p->precision == SPHGB_MIXED, n,
