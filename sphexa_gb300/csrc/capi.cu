@@ -145,7 +145,7 @@ int sphgb_destroy(sphgb_ctx* c)
     DBuf* bufs[] = {&c->keys,     &c->keysAlt,      &c->order,         &c->orderAlt,      &c->sortTemp,
                     &c->gatherScratch, &c->minmax,  &c->splitCount,    &c->splitOffset,   &c->leafKeysTmp,
                     &c->internalTmp,   &c->internalCodes, &c->leaves,  &c->layout,        &c->prefixes,
-                    &c->childOffsets,  &c->internalToLeaf, &c->nodeCenter, &c->nodeSize,  &c->nodeBoxF,
+                    &c->childOffsets,  &c->internalToLeaf, &c->nodeCenter, &c->nodeSize,  &c->nodeBoxF,     &c->nodeRange,
                     &c->levelRangeDev, &c->nbr,     &c->ncount,        &c->active,        &c->counters,
                     &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,

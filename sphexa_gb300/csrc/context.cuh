@@ -90,6 +90,7 @@ struct sphgb_ctx {
     sphgb::DBuf leaves, layout, prefixes, childOffsets, internalToLeaf;
     sphgb::DBuf nodeCenter, nodeSize;   // double3-packed, 3 doubles per node (reference nodeFpCenters)
     sphgb::DBuf nodeBoxF;               // float4 {cx, cy, cz, pad} + float4 {sx, sy, sz, -}: traversal
+    sphgb::DBuf nodeRange;              // uint2 per node: its particles [start, end) in SFC order
     sphgb::DBuf levelRangeDev;
     bool haveTree = false;
 

@@ -340,6 +340,20 @@ __global__ void octreeNodesKernel(const u64* __restrict__ internalCodes, const i
     boxF[2 * idx + 1] = make_float4(sf[0], sf[1], sf[2], 0.f);
 }
 
+// particles [start, end) of every node: from the first leaf (child-0 chain) to the last (child-7
+// chain) under it; a node's particles are contiguous in SFC order
+__global__ void nodeRangeKernel(int64_t numNodes, const int32_t* __restrict__ childOffsets,
+                                const int32_t* __restrict__ internalToLeaf, const uint32_t* __restrict__ layout,
+                                uint2* __restrict__ range)
+{
+    const int64_t n = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (n >= numNodes) return;
+    int32_t a = int32_t(n), b = int32_t(n), co;
+    for (int d = 0; d <= kMaxLevel && (co = childOffsets[a]) != 0; ++d) a = co;
+    for (int d = 0; d <= kMaxLevel && (co = childOffsets[b]) != 0; ++d) b = co + 7;
+    range[n] = make_uint2(layout[internalToLeaf[a]], layout[internalToLeaf[b] + 1]);
+}
+
 __global__ void layoutKernel(const u64* __restrict__ keys, int64_t n, const u64* __restrict__ leaves,
                              int64_t numLeaves, uint32_t* __restrict__ layout)
 {
@@ -583,6 +597,11 @@ int buildTree(sphgb_ctx* c, bool rebalance)
     layoutKernel<<<gridFor(L + 1, kBlock), kBlock, 0, st>>>(keys, n, c->leaves.as<u64>(), L,
                                                             c->layout.as<uint32_t>());
     SPHGB_TRY(launched(c, "layoutKernel"));
+    SPHGB_TRY(c->nodeRange.ensure(sizeof(uint2) * NN));
+    nodeRangeKernel<<<gridFor(NN, kBlock), kBlock, 0, st>>>(NN, c->childOffsets.as<int32_t>(),
+                                                            c->internalToLeaf.as<int32_t>(), c->layout.as<uint32_t>(),
+                                                            c->nodeRange.as<uint2>());
+    SPHGB_TRY(launched(c, "nodeRangeKernel"));
     SPHGB_CUDA(cudaMemcpyAsync(c->levelRange, c->levelRangeDev.as<int32_t>() + (kMaxLevel + 2),
                                sizeof(int32_t) * (kMaxLevel + 2), cudaMemcpyDeviceToHost, st));
     SPHGB_TRY(sortStatusAsync(c));  // the key and tree sorts of this sync

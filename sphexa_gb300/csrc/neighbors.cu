@@ -7,8 +7,10 @@
 // distanceSq (minimum image by rint when the 2h box of i leaves a periodic box).
 //
 // Per warp: one depth-first walk of the octree in SFC order against the group's search box, so
-// candidate leaves arrive in ascending particle order and every list comes out sorted.
-// Contiguous leaf ranges are merged and staged 32 candidates at a time in shared memory.
+// candidate ranges arrive in ascending particle order and every list comes out sorted.  Leaves,
+// internal nodes whose box lies inside the search box and internal nodes of few particles each
+// give one contiguous particle range (per-node ranges precomputed with the tree); contiguous
+// ranges are merged and staged 32 candidates at a time in shared memory.
 // Positions are read in the grid form of the mixed passes: a 21-bit cell per axis plus an FP32
 // offset inside the cell.  Offsets from the group origin are (cell difference, wrapped exactly
 // in integers) x cell edge + (offset difference), so neither staging nor the distance filter
@@ -28,6 +30,9 @@ namespace {
 constexpr int kNbrBlock = 128;
 constexpr int kWarpsPerBlock = kNbrBlock / kWarp;
 constexpr int kStack = 192;  // 8 children x (21 levels + 3)
+// internal nodes of at most this many particles are taken whole (about eight leaves of 13-16:
+// the octree's last level when a cell of 64 + particles splits into small leaves)
+constexpr uint32_t kCoarseNode = 128;
 
 struct NbrArgs {
     const double *x, *y, *z;
@@ -42,6 +47,7 @@ struct NbrArgs {
     const int32_t* internalToLeaf;
     const uint32_t* layout;
     const float4* nodeBox;
+    const uint2* nodeRange;  // particles [start, end) per node
     int64_t numNodes;
     DevBox box;
     uint32_t ngmax;
@@ -334,8 +340,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6) nbrGroupKernel(NbrArgs a)
     };
 
     int64_t pa = 0, pb = 0;  // pending contiguous candidate range
-    auto addLeaf = [&](int32_t leaf) {
-        const int64_t la = a.layout[leaf], lb = a.layout[leaf + 1];
+    auto addRange = [&](int64_t la, int64_t lb) {
         if (la == lb) return;
         if (la != pb) {
             while (pb > pa) {
@@ -358,23 +363,31 @@ __global__ void __launch_bounds__(kNbrBlock, 6) nbrGroupKernel(NbrArgs a)
     __syncwarp();
     bool overflow = false;
     while (sp > 0) {
-        const int32_t node = sm.stack[--sp];
+        // stack entries: node index, sign bit set when the node's box lies inside the search box
+        const int32_t e = sm.stack[--sp];
+        const int32_t node = e & 0x7fffffff;
+        // a leaf, an internal node inside the search box (all its children would be walked) or one
+        // of at most kCoarseNode particles: one contiguous range of particles instead of a walk over
+        // its leaves.  Extra candidates only cost staging: the culls and the pair test decide.
         const int32_t co8 = a.childOffsets[node];
-        if (co8 == 0) {
-            addLeaf(a.internalToLeaf[node]);
+        const uint2 nr = a.nodeRange[node];
+        if (co8 == 0 || e < 0 || nr.y - nr.x <= kCoarseNode) {
+            addRange(nr.x, nr.y);
             continue;
         }
-        bool ov = false;
+        bool ov = false, inside = false;
         const int32_t child = co8 + (lane & 7);
         if (lane < 8) {
             const float4 c4 = a.nodeBox[2 * child], s4 = a.nodeBox[2 * child + 1];
             const float cc[3] = {c4.x, c4.y, c4.z}, ss[3] = {s4.x, s4.y, s4.z};
             ov = true;
+            inside = true;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 float dd = fabsf(cc[k] - gc[k]);
                 if (b.pbc[k]) dd = fminf(dd, b.Lf[k] - dd);
                 ov = ov && (dd <= ss[k] + gs[k]);
+                inside = inside && (dd + ss[k] <= gs[k]);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, ov);
@@ -384,7 +397,7 @@ __global__ void __launch_bounds__(kNbrBlock, 6) nbrGroupKernel(NbrArgs a)
             break;
         }
         __syncwarp();
-        if (ov) sm.stack[sp + __popc(m >> (lane + 1))] = child;
+        if (ov) sm.stack[sp + __popc(m >> (lane + 1))] = inside ? int32_t(uint32_t(child) | 0x80000000u) : child;
         sp += k;
         __syncwarp();
     }
@@ -679,6 +692,7 @@ int runSearch(sphgb_ctx* c, const double* x, const double* y, const double* z, c
     a.internalToLeaf = c->internalToLeaf.as<int32_t>();
     a.layout = c->layout.as<uint32_t>();
     a.nodeBox = c->nodeBoxF.as<float4>();
+    a.nodeRange = c->nodeRange.as<uint2>();
     a.numNodes = c->numNodes;
     a.box = c->box;
     a.ngmax = ngmax;
