@@ -1222,27 +1222,28 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         }
         T si = vxij * gix + vyij * giy + vzij * giz;
         T sj = vxij * gjx + vyij * gjy + vzij * gjz;
+        // the reference's terms, factored: with hv = visc / 2, A = m_j hv / rho_i and B = hv m_j /
+        // rho_j, the momentum term momi a_i + momj a_j + (av a_i + bv a_j) / 2 is W_i (momi + A) G_i +
+        // W_j (momj + B) G_j, the energy term m_j am W_i s_i and the viscous work A W_i s_i + B W_j s_j
+        const T hv = T(0.5) * visc;
+        const T wsi = Wi * si, wsj = Wj * sj;
         {  // i's terms
-            T av = mj * rhoiInv * visc, bv = __ldg(auxMoR + j) * visc;
-            T momi = mj * prhoi * am, momj = __ldg(auxMprho + j) * bm;
-            T avWi = av * Wi, bvWj = bv * Wj;
-            T ki = momi * Wi + T(0.5) * avWi, kj = momj * Wj + T(0.5) * bvWj;
-            mx -= ki * gix + kj * gjx;
-            my -= ki * giy + kj * gjy;
-            mz -= ki * giz + kj * gjz;
-            en -= mj * am * Wi * si;
-            avE -= T(0.5) * (avWi * si + bvWj * sj);
+            const T A = mj * rhoiInv * hv, B = __ldg(auxMoR + j) * hv;
+            const T ki = Wi * (mj * prhoi * am + A), kj = Wj * (__ldg(auxMprho + j) * bm + B);
+            mx = fma(-ki, gix, fma(-kj, gjx, mx));
+            my = fma(-ki, giy, fma(-kj, gjy, my));
+            mz = fma(-ki, giz, fma(-kj, gjz, mz));
+            en = fma(-(mj * am), wsi, en);
+            avE = fma(-A, wsi, fma(-B, wsj, avE));
         }
-        if (mutual) {  // j's terms of the same pair
-            T av = mi * __ldg(auxRhoInv + j) * visc, bv = moRi * visc;
-            T momi = mi * prhoA[j] * bm, momj = mprhoi * am;
-            T avWj = av * Wj, bvWi = bv * Wi;
-            T kj = momi * Wj + T(0.5) * avWj, ki = momj * Wi + T(0.5) * bvWi;
-            atomicAdd(accX + j, kj * gjx + ki * gix);
-            atomicAdd(accY + j, kj * gjy + ki * giy);
-            atomicAdd(accZ + j, kj * gjz + ki * giz);
-            atomicAdd(accE + j, -(mi * bm * Wj * sj));
-            atomicAdd(accV + j, -T(0.5) * (avWj * sj + bvWi * si));
+        if (mutual) {  // j's terms of the same pair (i and j trade places, G and v_ij change sign)
+            const T A = mi * __ldg(auxRhoInv + j) * hv, B = moRi * hv;
+            const T kj = Wj * (mi * prhoA[j] * bm + A), ki = Wi * (mprhoi * am + B);
+            atomicAdd(accX + j, fma(kj, gjx, ki * gix));
+            atomicAdd(accY + j, fma(kj, gjy, ki * giy));
+            atomicAdd(accZ + j, fma(kj, gjz, ki * giz));
+            atomicAdd(accE + j, -(mi * bm) * wsj);
+            atomicAdd(accV + j, -fma(A, wsj, B * wsi));
             atomicMax(accS + j, __double_as_longlong(vsig));
         }
     }
