@@ -491,16 +491,25 @@ def main() -> None:
         d2h = sum(t.numel() * t.element_size() for t in host_out.values())
         boxe = sph.Box(wl.box.copy(), wl.bc.copy())
 
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        phases = []  # per step: H2D, sweep, D2H milliseconds (CUDA events on the launching stream)
+
         def e2e_step():
+            evs[0].record()
             for k, t in host_in.items():
                 d.f[k].copy_(t, non_blocking=True)
+            evs[1].record()
             sph.sweep(ctx, d, boxe, args.variant, False)
+            evs[2].record()
             for k in outs:
                 host_out[k].copy_(d.f[k], non_blocking=True)
+            evs[3].record()
             torch.cuda.synchronize()
+            phases.append([evs[q].elapsed_time(evs[q + 1]) for q in range(3)])
 
         for _ in range(max(1, args.warmup)):
             e2e_step()
+        phases.clear()
         barrier()
         t0 = time.perf_counter()
         k_e2e = max(3, args.steps // 2)
@@ -508,8 +517,11 @@ def main() -> None:
             e2e_step()
         barrier()
         wall_ms = R.max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+        med = np.median(np.array(phases), axis=0) if phases else [None] * 3
         out["e2e"] = {"value": R.job_throughput(n, k_e2e, world, wall_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
                       "d2h_bytes_per_step": d2h, "steps": k_e2e,
+                      "ms_per_step": wall_ms / k_e2e,
+                      "phases_ms_median": {"h2d": float(med[0]), "sweep": float(med[1]), "d2h": float(med[2])},
                       "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
         del d
 

@@ -721,6 +721,83 @@ __global__ void __launch_bounds__(kAdjBlock) densityAdjScatterT(StdScatterArgs<T
     atomicAdd(a.bh + k, bh);
 }
 
+// seeds of particle k in the pair type: K times the acceleration seeds and -K/2 times the du seed;
+// false when they are all zero
+template<class T>
+__device__ __forceinline__ bool seedsOfT(const StdScatterArgs<T>& a, int64_t k, T gA[3], T& gE)
+{
+    gA[0] = a.sAx ? T(a.K * double(a.sAx[k])) : T(0);
+    gA[1] = a.sAy ? T(a.K * double(a.sAy[k])) : T(0);
+    gA[2] = a.sAz ? T(a.K * double(a.sAz[k])) : T(0);
+    gE = a.sDu ? T(-0.5 * a.K * a.sDu[k]) : T(0);
+    return gA[0] != T(0) || gA[1] != T(0) || gA[2] != T(0) || gE != T(0);
+}
+
+// the momentum-energy adjoint of the mixed form over owned lists: one evaluation per owned entry,
+// a mutual pair's entry giving both directed terms (the neighbour's through its own seeds), as the
+// FP64 meAdjOnceKernel; the grid-form geometry is antisymmetric (r_ji = -r_ij exactly), so the one
+// evaluation equals the two of the scatter form.  Half the pair evaluations and atomics of
+// meAdjScatterT.
+template<class T, bool Smooth>
+__global__ void __launch_bounds__(kAdjBlock) meAdjOnceT(StdScatterArgs<T> a, OwnedView ov)
+{
+    const auto tab = kernelTab<Smooth>(a.wh);
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= a.n) return;
+    T gA[3], gE;
+    const bool anyK = seedsOfT(a, k, gA, gE);
+    T bx[3] = {0, 0, 0}, bv[3] = {0, 0, 0}, bh = 0, brho = 0, bp = 0, bc = 0, bC[6] = {0, 0, 0, 0, 0, 0};
+    const stdad::MeSide<T> S = stdSideT(a, k);
+    const T zero[3] = {T(0), T(0), T(0)};
+    const unsigned cnt = ov.size(k);
+    for (unsigned q = 0; q < cnt; ++q) {
+        bool mutual;
+        const uint32_t j = ov.at(k, q, mutual);
+        T gAj[3] = {T(0), T(0), T(0)}, gEj = T(0);
+        const bool anyJ = mutual && seedsOfT(a, j, gAj, gEj);
+        if (!anyK && !anyJ) continue;
+        const stdad::MeSide<T> J = stdSideT(a, j);
+        T r[3], d, rinv;
+        geomT(a, k, j, r, d, rinv);
+        const T v[3] = {a.vx[k] - a.vx[j], a.vy[k] - a.vy[j], a.vz[k] - a.vz[j]};
+        T dwi, dwj;
+        const T wi = lookupSlopeT(tab, d * S.hInv, dwi), wj = lookupSlopeT(tab, d * J.hInv, dwj);
+        stdad::MeGrad<T> o;
+        stdad::meStdAdjPair<T>(r, d, rinv, v, S, J, wi, dwi, wj, dwj, anyK ? gA : zero, anyK ? gE : T(0), gAj, gEj, o);
+        for (int t = 0; t < 3; ++t) {
+            bx[t] += o.r[t];
+            bv[t] += o.v[t];
+        }
+        bh += o.hI;
+        brho += o.rhoI;
+        bp += o.pI;
+        bc += o.c;
+        for (int t = 0; t < 6; ++t) bC[t] += o.CI[t];
+        atomicAdd(a.bx + j, -o.r[0]);
+        atomicAdd(a.by + j, -o.r[1]);
+        atomicAdd(a.bz + j, -o.r[2]);
+        atomicAdd(a.bvx + j, -o.v[0]);
+        atomicAdd(a.bvy + j, -o.v[1]);
+        atomicAdd(a.bvz + j, -o.v[2]);
+        atomicAdd(a.bh + j, o.hJ);
+        atomicAdd(a.bRho + j, o.rhoJ);
+        atomicAdd(a.bP + j, o.pJ);
+        atomicAdd(a.bC + j, o.c);
+        for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + j, o.CJ[t]);
+    }
+    atomicAdd(a.bx + k, bx[0]);
+    atomicAdd(a.by + k, bx[1]);
+    atomicAdd(a.bz + k, bx[2]);
+    atomicAdd(a.bvx + k, bv[0]);
+    atomicAdd(a.bvy + k, bv[1]);
+    atomicAdd(a.bvz + k, bv[2]);
+    atomicAdd(a.bh + k, bh);
+    atomicAdd(a.bRho + k, brho + (a.sRho ? a.sRho[k] : T(0)));
+    atomicAdd(a.bP + k, bp);
+    atomicAdd(a.bC + k, bc);
+    for (int t = 0; t < 6; ++t) atomicAdd(a.bCij + t * a.n + k, bC[t]);
+}
+
 // ---- one evaluation per owned entry of the owned lists (mutual pairs give both directed terms) ----
 __device__ __forceinline__ stdad::MeSide<> stdSide(const AdjArgs& a, int64_t i)
 {
@@ -1065,13 +1142,20 @@ static int adjointStdScatter(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds
             SPHGB_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * n, c->stream));
     }
     SPHGB_CUDA(cudaMemsetAsync(st, 0, sizeof(T) * 9 * n, c->stream));
+    if (fp32 && !c->deterministic && (c->ownedEpoch != c->nbrEpoch || !c->ownedFromLists))
+        SPHGB_TRY(buildOwnedFromLists(c));
     const unsigned blocks = gridFor(n, kAdjBlock), eb = gridFor(n, 256);
     SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
         constexpr bool S = !fp32 && decltype(smooth)::value;  // the FP32 form has one (linear) table
         stdQuotKernel<T><<<eb, 256, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "stdQuotKernel"));
-        meAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
-        SPHGB_TRY(launched(c, "meAdjScatterT"));
+        if (fp32 && !c->deterministic) {  // owned lists of the frozen lists: one evaluation per mutual pair
+            meAdjOnceT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a, ownedView(c));
+            SPHGB_TRY(launched(c, "meAdjOnceT"));
+        } else {
+            meAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
+            SPHGB_TRY(launched(c, "meAdjScatterT"));
+        }
         iadPrepT<T><<<eb, 256, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "iadPrepT"));
         iadAdjScatterT<T, S><<<blocks, kAdjBlock, 0, c->stream>>>(a);
@@ -1103,7 +1187,7 @@ int adjointStd(sphgb_ctx* c, sphgb_particles* p, const sphgb_seeds* s, sphgb_gra
         return adjointStdScatter<float>(c, p, s, g);
     }
     // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
-    const bool once = !deterministic && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
+    const bool once = !deterministic && !c->deterministic && c->ownedEpoch == c->nbrEpoch && !c->ownedFromLists;
     if (!deterministic && !once) return adjointStdScatter<double>(c, p, s, g);
     const int64_t n = p->n;
     if (deterministic) SPHGB_TRY(buildTranspose(c));

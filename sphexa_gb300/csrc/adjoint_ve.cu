@@ -1328,7 +1328,7 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
                                    {{meVeAdjKernel<true, false, false, S>, meVeAdjKernel<true, false, true, S>},
                                     {meVeAdjKernel<true, true, false, S>, meVeAdjKernel<true, true, true, S>}}};
             // one evaluation per mutual pair: owned lists of the current lists, order-free sums allowed
-            if (!two && !c->deterministic && !a.avClean && c->ownedEpoch == c->nbrEpoch) {
+            if (!two && !c->deterministic && !a.avClean && c->ownedEpoch == c->nbrEpoch && !c->ownedFromLists) {
                 if (withDu) meVeAdjOnceKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
                 else meVeAdjOnceKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
             } else
@@ -1337,7 +1337,7 @@ int adjointVe(sphgb_ctx* c, sphgb_particles* p, const double* alphaPrev, int avC
         }
         veAvSeedKernel<<<eb, 256, 0, c->stream>>>(a);
         SPHGB_TRY(launched(c, "veAvSeedKernel"));
-        const bool once = !two && !c->deterministic && c->ownedEpoch == c->nbrEpoch;
+        const bool once = !two && !c->deterministic && c->ownedEpoch == c->nbrEpoch && !c->ownedFromLists;
         if (two) veAvAdjKernel<true, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);
         else if (once) veAvAdjOnceKernel<S><<<pb, kVeAdjBlock, 0, c->stream>>>(a, ownedView(c));
         else veAvAdjKernel<false, S><<<pb, kVeAdjBlock, 0, c->stream>>>(a);

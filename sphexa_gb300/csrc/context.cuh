@@ -103,6 +103,7 @@ struct sphgb_ctx {
     // j | mutual << 31 for the pairs i evaluates, ownedCount per particle; valid for epoch ownedEpoch
     sphgb::DBuf owned, ownedCount, ownedR2;
     int64_t ownedEpoch = -1;
+    bool ownedFromLists = false;  // owned lists decided from list membership (mixed adjoint); the FP64 passes skip them
     // summation mode of the FP64 passes (order-fixed, or one evaluation per mutual pair) and the
     // per-particle accumulators of the pair-once passes (up to 6 x n doubles)
     bool deterministic = false;
@@ -214,6 +215,8 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
                          double* minDt);
 
 int buildTranspose(sphgb_ctx* c);
+// owned lists of the current lists from list membership (mixed adjoint)
+int buildOwnedFromLists(sphgb_ctx* c);
 // stable LSD radix sort of 64-bit keys (bits [0, endBit)) with optional 32-bit values, out of place
 int radixSort(sphgb_ctx* c, const u64* keysIn, u64* keysOut, const uint32_t* valsIn, uint32_t* valsOut, int64_t n,
               int endBit);

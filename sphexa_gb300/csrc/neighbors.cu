@@ -643,6 +643,41 @@ __global__ void __launch_bounds__(128) ownedListKernel(MutualArgs a)
     a.ownedCount[ii] = cnt;
 }
 
+// owned lists from list membership alone: (i, j) is mutual when i is in j's (capped, ascending)
+// list, found by binary search, so the decision holds whatever the positions are now (frozen lists
+// after moved particles).  Ownership of a mutual pair as in ownedListKernel (index parity).
+__global__ void __launch_bounds__(128) ownedByListKernel(const uint32_t* __restrict__ nbr,
+                                                         const uint32_t* __restrict__ count, int64_t first, int64_t last,
+                                                         int64_t stride, uint32_t ngmax, uint32_t* __restrict__ owned,
+                                                         uint32_t* __restrict__ ownedCount)
+{
+    const int64_t i = first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= last) return;
+    const int64_t ii = i - first;
+    const unsigned nc = min(__ldg(count + ii), ngmax);
+    unsigned cnt = 0;
+    GranuleWriter out(owned, ii, stride, ngmax);
+    for (unsigned k = 0; k < nc; ++k) {
+        const uint32_t j = __ldg(nbr + listSlot(ii, k, stride));
+        bool m = false;
+        if (int64_t(j) >= first && int64_t(j) < last) {
+            const int64_t jj = int64_t(j) - first;
+            unsigned lo = 0, hi = min(__ldg(count + jj), ngmax);  // search [lo, hi) of j's sorted list
+            while (lo < hi) {
+                const unsigned mid = (lo + hi) >> 1;
+                const uint32_t e = __ldg(nbr + listSlot(jj, mid, stride));
+                if (int64_t(e) < i) lo = mid + 1;
+                else hi = mid;
+            }
+            m = lo < min(__ldg(count + jj), ngmax) && int64_t(__ldg(nbr + listSlot(jj, lo, stride))) == i;
+        }
+        const bool own = !m || ((((i ^ int64_t(j)) & 1) != 0) == (i < int64_t(j)));
+        if (own) out.put(cnt++, j | (m ? 0x80000000u : 0u));
+    }
+    out.finish(cnt);
+    ownedCount[ii] = cnt;
+}
+
 __global__ void fillOnes(uint32_t* p, int64_t n)
 {
     int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -741,6 +776,7 @@ int buildOwned(sphgb_ctx* c, const double* x, const double* y, const double* z, 
     ownedListKernel<<<gridFor(nWork, 128), 128, 0, c->stream>>>(a);
     SPHGB_TRY(launched(c, "ownedListKernel"));
     c->ownedEpoch = c->nbrEpoch;
+    c->ownedFromLists = false;
     return SPHGB_OK;
 }
 
@@ -788,6 +824,20 @@ int finishStats(sphgb_ctx* c, int64_t hIters)
 }
 
 }  // namespace
+
+int buildOwnedFromLists(sphgb_ctx* c)
+{
+    const int64_t nWork = c->nbrLast - c->nbrFirst;
+    SPHGB_TRY(c->owned.ensure(sizeof(uint32_t) * listCapacity(c->nbrNgmax) * size_t(c->nbrStride)));
+    SPHGB_TRY(c->ownedCount.ensure(sizeof(uint32_t) * size_t(c->nbrStride)));
+    ownedByListKernel<<<gridFor(nWork, 128), 128, 0, c->stream>>>(c->nbr.as<uint32_t>(), c->ncount.as<uint32_t>(),
+                                                                 c->nbrFirst, c->nbrLast, c->nbrStride, c->nbrNgmax,
+                                                                 c->owned.as<uint32_t>(), c->ownedCount.as<uint32_t>());
+    SPHGB_TRY(launched(c, "ownedByListKernel"));
+    c->ownedEpoch = c->nbrEpoch;
+    c->ownedFromLists = true;
+    return SPHGB_OK;
+}
 
 int findNeighborsSph(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
 {

@@ -118,7 +118,8 @@ inline OwnedView ownedView(const sphgb_ctx* c)
 // owned lists of the current neighbour lists, and lists covering every particle
 inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first, int64_t last)
 {
-    return !c->deterministic && p->precision == SPHGB_FP64 && c->ownedEpoch == c->nbrEpoch && first == 0 &&
+    return !c->deterministic && p->precision == SPHGB_FP64 && c->ownedEpoch == c->nbrEpoch && !c->ownedFromLists &&
+           first == 0 &&
            last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
 }
 
