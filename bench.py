@@ -43,7 +43,7 @@ STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
 # dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count.
 # "me" and "av" are the pair-once kernels of the default (non-deterministic) FP64 mode.
-NCU_DRAM_BYTES_PER_PARTICLE = {"me": 584.7, "iad_divv": 564.3, "av": 381.7}
+NCU_DRAM_BYTES_PER_PARTICLE = {"me": 582.6, "iad_divv": 564.3, "av": 381.7}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
 STAGES_STD = ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
 # FP32 distance test of one search candidate against the target's radius: 3 coordinate differences,
