@@ -1,5 +1,5 @@
 // Adjoint (reverse mode) of the standard SPH chain  density -> EOS -> IAD -> momentum-energy
-// over the frozen neighbour lists of the last search, in FP64.
+// over the frozen neighbour lists of the last search, FP64 and mixed (FP32 pair arithmetic).
 //
 // Forward functions differentiated (reference j-loops):
 //   rho_i = K h_i^-3 (m_i + sum_j m_j w(r_ij / h_i))                 hydro_std/density.hpp:41-60
@@ -11,10 +11,15 @@
 // slope of the interval, so forward and adjoint describe the same piecewise function.  The
 // Courant time step is not differentiated.
 //
-// Scatter without atomics: every pair (i owns the list, j is the neighbour) is evaluated twice,
-// once by thread i over its list for the partials of i's quantities and once by thread j over the
-// transposed list for the partials of j's quantities.  Each thread writes only its own particle,
-// so the sums are deterministic.  No per-pair value is stored.
+// Three walks of the pairs, no per-pair value stored:
+//   deterministic (FP64): every pair (i owns the list, j is the neighbour) is evaluated twice, once
+//     by thread i over its list for the partials of i's quantities and once by thread j over the
+//     transposed list for the partials of j's quantities; each thread writes only its own particle,
+//     so the sums are bit-reproducible;
+//   once (FP64, and the mixed momentum-energy term): one evaluation per owned entry of the owned
+//     lists, a mutual pair giving both directed terms, the neighbour's partials by atomics;
+//   scatter (the mixed IAD and density terms, FP64 with a deterministic context): every list entry
+//     evaluated by its owner, the neighbour's partials by atomics.
 #include "adjoint_std.cuh"
 #include "pairs.cuh"
 

@@ -99,7 +99,7 @@ struct sphgb_ctx {
     uint32_t nbrNgmax = 0;
     sphgb::DBuf nbr, ncount, active, counters;
     bool haveNbr = false;
-    // owned pair lists of the pair-once momentum-energy pass: owned[k * stride + (i - first)] =
+    // owned pair lists of the pair-once passes, in the granule layout of the lists (listSlot): entry
     // j | mutual << 31 for the pairs i evaluates, ownedCount per particle; valid for epoch ownedEpoch
     sphgb::DBuf owned, ownedCount, ownedR2;
     int64_t ownedEpoch = -1;
