@@ -46,15 +46,16 @@ VEAD_HD void symv(const double C[6], const double r[3], double o[3])
     o[2] = C[2] * r[0] + C[4] * r[1] + C[5] * r[2];
 }
 
-// Cb += s * d(a . C r) / dC
+// Cb += s * d(a . C r) / dC, with s folded into a first (3 products and 9 FMAs)
 VEAD_HD void symvAdj(const double a[3], const double r[3], double s, double Cb[6])
 {
-    Cb[0] += s * (a[0] * r[0]);
-    Cb[1] += s * (a[0] * r[1] + a[1] * r[0]);
-    Cb[2] += s * (a[0] * r[2] + a[2] * r[0]);
-    Cb[3] += s * (a[1] * r[1]);
-    Cb[4] += s * (a[1] * r[2] + a[2] * r[1]);
-    Cb[5] += s * (a[2] * r[2]);
+    const double sa0 = s * a[0], sa1 = s * a[1], sa2 = s * a[2];
+    Cb[0] = fma(sa0, r[0], Cb[0]);
+    Cb[1] = fma(sa0, r[1], fma(sa1, r[0], Cb[1]));
+    Cb[2] = fma(sa0, r[2], fma(sa2, r[0], Cb[2]));
+    Cb[3] = fma(sa1, r[1], Cb[3]);
+    Cb[4] = fma(sa1, r[2], fma(sa2, r[1], Cb[4]));
+    Cb[5] = fma(sa2, r[2], Cb[5]);
 }
 
 // r^T g r with the stored components (avRvCorrection's quadratic form, momentum_energy_kern.hpp:43-50)
@@ -79,12 +80,6 @@ VEAD_HD void quadAdjG(const double r[3], double s, double gb[6])
     gb[3] += s * r[1] * r[1];
     gb[4] += s * r[1] * r[2];
     gb[5] += s * r[2] * r[2];
-}
-
-// d(h^-3 w(d/h))/dh with v = d/h
-VEAD_HD double dWdh(double hInv, double w, double dw, double v)
-{
-    return -hInv * hInv * hInv * hInv * (3.0 * w + v * dw);
 }
 
 // ------------------------------------------------------------------ momentum-energy
@@ -253,11 +248,18 @@ VEAD_HD void meTail(const double r[3], double rinv, const double v[3], const MeS
     symv(I.C, b.Aib, CAi);
     symv(J.C, b.Ajb, CAj);
     for (int k = 0; k < 3; ++k) o.r[k] += -f.Wi * CAi[k] - f.Wj * CAj[k];
-    // W_i = h_i^-3 w(d / h_i)
-    o.hI = Wib * dWdh(I.hInv, wi, dwi, f.v1) - v1b * f.v1 * I.hInv;
-    o.hJ = Wjb * dWdh(J.hInv, wj, dwj, f.v2) - v2b * f.v2 * J.hInv;
-    db += Wib * f.hi3 * dwi * I.hInv + Wjb * f.hj3 * dwj * J.hInv + v1b * I.hInv + v2b * J.hInv;
-    for (int k = 0; k < 3; ++k) o.r[k] += db * r[k] * rinv;
+    // W_i = h_i^-3 w(d / h_i): dW_i/dh_i = -h_i^-4 (3 w + v1 dw), dW_i/dd = h_i^-4 dw
+    const double bi4 = Wib * (f.hi3 * I.hInv), bj4 = Wjb * (f.hj3 * J.hInv);
+    o.hI = -bi4 * fma(f.v1, dwi, 3.0 * wi);
+    o.hJ = -bj4 * fma(f.v2, dwj, 3.0 * wj);
+    db = fma(bi4, dwi, fma(bj4, dwj, db));
+    if constexpr (AvClean) {
+        o.hI -= v1b * f.v1 * I.hInv;
+        o.hJ -= v2b * f.v2 * J.hInv;
+        db += v1b * I.hInv + v2b * J.hInv;
+    }
+    const double dr = db * rinv;  // d|r|/dr = r / |r|
+    for (int k = 0; k < 3; ++k) o.r[k] = fma(dr, r[k], o.r[k]);
 }
 
 VEAD_HD void meGradZero(MeGrad& o)
@@ -317,6 +319,30 @@ VEAD_HD void meAdjMutual(const double r[3], double d, double rinv, const double 
     MeFwd f;
     meFwd(r, d, rinv, v, I, J, wi, wj, false, 0.0, f);
     meGradZero(o);
+    if constexpr (!WithDu) {
+        // no du seed: u_i = prho_i s, u_j = prho_j s and t = s, so every projection follows from
+        // s . A_i and s . A_j, and Abar_i = (am prho_i + hv_i) s, Abar_j = (bm prho_j + hv_j) s
+        double s3[3];
+        for (int k = 0; k < 3; ++k) s3[k] = J.m * mbI[k] - I.m * mbJ[k];
+        const double sAi = s3[0] * f.Ai[0] + s3[1] * f.Ai[1] + s3[2] * f.Ai[2];
+        const double sAj = s3[0] * f.Aj[0] + s3[1] * f.Aj[1] + s3[2] * f.Aj[2];
+        const double hvi = 0.5 * f.visc * I.rhoInv, hvj = 0.5 * f.visc * J.rhoInv;
+        const double ci = fma(f.am, I.prho, hvi), cj = fma(f.bm, J.prho, hvj);
+        MeBar b;
+        for (int k = 0; k < 3; ++k) {
+            b.Aib[k] = ci * s3[k];
+            b.Ajb[k] = cj * s3[k];
+        }
+        b.amb = I.prho * sAi;
+        b.bmb = J.prho * sAj;
+        b.viscb = 0.5 * (sAi * I.rhoInv + sAj * J.rhoInv);
+        o.prhoI = f.am * sAi;
+        o.prhoJ = f.bm * sAj;
+        o.rhoI = -hvi * sAi * I.rhoInv;
+        o.rhoJ = -hvj * sAj * J.rhoInv;
+        meTail<false>(r, rinv, v, I, J, wi, dwi, wj, dwj, f, b, o);
+        return;
+    }
     double sv[3], ui[3], uj[3], t[3];
     const double sigma = WithDu ? J.m * avEbI + I.m * avEbJ : 0.0;
     for (int k = 0; k < 3; ++k) {
@@ -427,9 +453,11 @@ VEAD_HD void avAdj(const double r[3], double d, double rinv, const double v[3], 
     o.divvJ = -facb * volj;
     o.xmJ = volb * kxInvj;
     o.kxJ = -volb * volj * kxInvj;
+    // W = K h^-3 w(d / h): dW/dh = -K h^-4 (3 w + v1 dw), dW/dd = K h^-4 dw
     const double v1 = d * hiInv;
-    o.hI = Wkb * K * dWdh(hiInv, wi, dwi, v1);
-    double db = Wkb * K * hi3 * dwi * hiInv;
+    const double b4 = Wkb * K * (hi3 * hiInv);
+    o.hI = -b4 * fma(v1, dwi, 3.0 * wi);
+    double db = b4 * dwi;
     const double fw = fac * Wk;
     for (int k = 0; k < 3; ++k) {
         o.r[k] = -fw * CGb[k];
@@ -448,7 +476,8 @@ VEAD_HD void avAdj(const double r[3], double d, double rinv, const double v[3], 
             o.v[k] += rvb * r[k];
         }
     }
-    for (int k = 0; k < 3; ++k) o.r[k] += db * r[k] * rinv;
+    const double dr = db * rinv;  // d|r|/dr = r / |r|
+    for (int k = 0; k < 3; ++k) o.r[k] = fma(dr, r[k], o.r[k]);
 }
 
 // i's C partials from the AV pair sum: Cb += -sym(Gb R^T), R = sum_j fac_j W_j r_j
@@ -555,7 +584,8 @@ VEAD_HD void iadDivvAdj(const double r[3], double d, double rinv, const double v
     const double v1b = wb * dwi;
     o.hI = -v1b * v1 * hiInv;
     const double db = v1b * hiInv;
-    for (int k = 0; k < 3; ++k) o.r[k] += db * r[k] * rinv;
+    const double dr = db * rinv;  // d|r|/dr = r / |r|
+    for (int k = 0; k < 3; ++k) o.r[k] = fma(dr, r[k], o.r[k]);
 }
 
 // ------------------------------------------------------------------ EOS
@@ -625,7 +655,8 @@ VEAD_HD void gradhAdj(const double r[3], double d, double rinv, double hiInv, do
     const double v1b = -dterhb * wdi + wb * dwi + wdb * dwdi;
     o.hI = -v1b * v1 * hiInv;
     const double db = v1b * hiInv;
-    for (int k = 0; k < 3; ++k) o.r[k] = db * r[k] * rinv;
+    const double dr = db * rinv;
+    for (int k = 0; k < 3; ++k) o.r[k] = dr * r[k];
 }
 
 // ------------------------------------------------------------------ xmass
@@ -644,7 +675,8 @@ VEAD_HD void xmassAdj(const double r[3], double d, double rinv, double hiInv, do
     const double v1b = R0b * mj * dwi;
     hIb = -v1b * v1 * hiInv;
     const double db = v1b * hiInv;
-    for (int k = 0; k < 3; ++k) rb[k] = db * r[k] * rinv;
+    const double dr = db * rinv;
+    for (int k = 0; k < 3; ++k) rb[k] = dr * r[k];
 }
 
 }  // namespace vead

@@ -1157,8 +1157,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
     const unsigned nOwned = __ldg(a.ownedCount + ii);
     const KTab<Smooth> tabX{a.w64};
     const T* aux = static_cast<const T*>(a.aux);
-    const T *auxRho = aux, *auxMoR = aux + a.n, *auxMprho = aux + 3 * a.n, *auxLnXm = aux + 4 * a.n,
-            *auxRhoInv = aux + 5 * a.n;
+    const T *auxRho = aux, *auxLnXm = aux + 4 * a.n, *auxRhoInv = aux + 5 * a.n;
     const double* hInv3 = a.hInv64 + a.n;
     const double* hInvDx = a.hInv64 + 2 * a.n;
     const T *vxA = static_cast<const T*>(a.vx), *vyA = static_cast<const T*>(a.vy),
@@ -1167,7 +1166,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
 
     const T hi = ld<T>(a.h, i), mi = ld<T>(a.m, i), ci = ld<T>(a.c, i), ai = ld<T>(a.alpha, i);
     const T xmi = ld<T>(a.xm, i), prhoi = prhoA[i];
-    const T rhoi = auxRho[i], lnxmi = auxLnXm[i], rhoiInv = auxRhoInv[i], moRi = auxMoR[i], mprhoi = auxMprho[i];
+    const T rhoi = auxRho[i], lnxmi = auxLnXm[i], rhoiInv = auxRhoInv[i];
     const T vxi = vxA[i], vyi = vyA[i], vzi = vzA[i];
     const T c11i = ld<T>(a.c11, i), c12i = ld<T>(a.c12, i), c13i = ld<T>(a.c13, i);
     const T c22i = ld<T>(a.c22, i), c23i = ld<T>(a.c23, i), c33i = ld<T>(a.c33, i);
@@ -1223,28 +1222,29 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         }
         T si = vxij * gix + vyij * giy + vzij * giz;
         T sj = vxij * gjx + vyij * gjy + vzij * gjz;
-        // the reference's terms, factored: with hv = visc / 2, A = m_j hv / rho_i and B = hv m_j /
-        // rho_j, the momentum term momi a_i + momj a_j + (av a_i + bv a_j) / 2 is W_i (momi + A) G_i +
-        // W_j (momj + B) G_j, the energy term m_j am W_i s_i and the viscous work A W_i s_i + B W_j s_j
+        // the reference's terms, factored: with hv = visc / 2, t_i = hv / rho_i and t_j = hv / rho_j,
+        // P_i = W_i (prho_i am + t_i) and P_j = W_j (prho_j bm + t_j), i's momentum term momi a_i +
+        // momj a_j + (av a_i + bv a_j) / 2 is m_j V with V = P_i G_i + P_j G_j and its viscous work
+        // m_j Q with Q = t_i W_i s_i + t_j W_j s_j; j's terms of the same pair are m_i V and m_i Q
+        // (i and j trade places, G and v_ij change sign); the energy terms m_j am W_i s_i and
+        // m_i bm W_j s_j stay apart
         const T hv = T(0.5) * visc;
         const T wsi = Wi * si, wsj = Wj * sj;
-        {  // i's terms
-            const T A = mj * rhoiInv * hv, B = __ldg(auxMoR + j) * hv;
-            const T ki = Wi * (mj * prhoi * am + A), kj = Wj * (__ldg(auxMprho + j) * bm + B);
-            mx = fma(-ki, gix, fma(-kj, gjx, mx));
-            my = fma(-ki, giy, fma(-kj, gjy, my));
-            mz = fma(-ki, giz, fma(-kj, gjz, mz));
-            en = fma(-(mj * am), wsi, en);
-            avE = fma(-A, wsi, fma(-B, wsj, avE));
-        }
-        if (mutual) {  // j's terms of the same pair (i and j trade places, G and v_ij change sign)
-            const T A = mi * __ldg(auxRhoInv + j) * hv, B = moRi * hv;
-            const T kj = Wj * (mi * prhoA[j] * bm + A), ki = Wi * (mprhoi * am + B);
-            atomicAdd(accX + j, fma(kj, gjx, ki * gix));
-            atomicAdd(accY + j, fma(kj, gjy, ki * giy));
-            atomicAdd(accZ + j, fma(kj, gjz, ki * giz));
+        const T ti = rhoiInv * hv, tj = __ldg(auxRhoInv + j) * hv;
+        const T Pi = Wi * fma(prhoi, am, ti), Pj = Wj * fma(prhoA[j], bm, tj);
+        const T Vx = fma(Pi, gix, Pj * gjx), Vy = fma(Pi, giy, Pj * gjy), Vz = fma(Pi, giz, Pj * gjz);
+        const T Q = fma(ti, wsi, tj * wsj);
+        mx = fma(-mj, Vx, mx);
+        my = fma(-mj, Vy, my);
+        mz = fma(-mj, Vz, mz);
+        en = fma(-(mj * am), wsi, en);
+        avE = fma(-mj, Q, avE);
+        if (mutual) {
+            atomicAdd(accX + j, mi * Vx);
+            atomicAdd(accY + j, mi * Vy);
+            atomicAdd(accZ + j, mi * Vz);
             atomicAdd(accE + j, -(mi * bm) * wsj);
-            atomicAdd(accV + j, -fma(A, wsj, B * wsi));
+            atomicAdd(accV + j, -mi * Q);
             atomicMax(accS + j, __double_as_longlong(vsig));
         }
     }
