@@ -351,12 +351,12 @@ int sphgb_conserved_quantities(sphgb_ctx* ctx, const sphgb_particles* p, int64_t
  * pointers; `box` is a host struct, updated in place.  Needs no context and allocates nothing: its
  * reduction scratch is a fixed 3 MiB device array inside the library (held by every GPU that loads
  * it until the process exits), which caps n at 268,435,456; larger n returns SPHGB_ERR_TOO_LARGE.
- * The first call on a device looks up that array's device address with cudaGetSymbolAddress (a
- * runtime call that must not run while a stream is being captured), so make the first call on each
- * device before any stream capture begins; the address is kept for the life of the process, so do
- * not call this entry point on a device after cudaDeviceReset of that device.  Every call shares the
- * array: calls that overlap on the GPU, on one device, race.  Runs on `stream` (0 = legacy default)
- * and returns after synchronising it. */
+ * The first call on a device looks up that array's device address with cudaGetSymbolAddress; the
+ * address is kept for the life of the process, so do not call this entry point on a device after
+ * cudaDeviceReset of that device.  Every call shares the array: calls that overlap on the GPU, on
+ * one device, race.  Runs on `stream` (0 = legacy default) and returns after synchronising it (the
+ * open-box path also reads the extrema back to the host), so a call cannot be part of a stream
+ * capture (CUDA graph). */
 int sphgb_sfc_keys_noalloc(const double* x, const double* y, const double* z, int64_t n, sphgb_box* box,
                            uint64_t* keys, void* stream);
 
