@@ -108,6 +108,10 @@ struct sphgb_ctx {
     // per-particle accumulators of the pair-once passes (up to 6 x n doubles)
     bool deterministic = false;
     sphgb::DBuf pairAcc;
+    // within one sweep: |r| and 1/|r| of every owned entry (double2 at k * nbrStride + i - nbrFirst),
+    // stored by the pair-once xmass pass and read by the later pair-once passes of the same sweep
+    sphgb::DBuf pairGeo;
+    bool geoValid = false;
     // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
     bool inSweep = false, sweepPrepared = false;
     // within one sweep: the EOS ran in the gradh epilogue / the per-particle quotients are formed

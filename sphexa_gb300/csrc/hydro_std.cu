@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
 template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, KTab<Smooth> tab,
-                                                               const double* hInvDx, double* acc)
+                                                               const double* hInvDx, double* acc, PairGeo geo)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -105,7 +105,9 @@ __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, Owned
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
         const double r2 = rx * rx + ry * ry + rz * rz;
-        const double dist = r2 * invDist(r2);
+        const double rinv = invDist(r2);
+        const double dist = r2 * rinv;
+        if (geo.g) geo.g[geo.at(ii, k)] = make_double2(dist, rinv);
         rho0 += lookupX(tab, dist * hiInvDx) * __ldg(m + j);
         if (mutual) atomicAdd(acc + j, lookupX(tab, dist * __ldg(hInvDx + j)) * mi);
     }
@@ -402,7 +404,7 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
             constexpr bool S = decltype(smooth)::value;
             xmassOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>());
+                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>(), pairGeo(c, true));
             return launched(c, "xmassOnceKernel");
         }));
         const unsigned eb = gridFor(last - first, 256);

@@ -872,7 +872,8 @@ template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, const double* xm,
                                                                KTab<Smooth> tw, KTab<Smooth> tdw,
-                                                               const double* hInv64, int64_t n, double* acc)
+                                                               const double* hInv64, int64_t n, double* acc,
+                                                               PairGeo geo)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -887,10 +888,14 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
         const uint32_t j = ov.at(ii, k, mutual);
-        double rx, ry, rz;
-        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        const double r2 = rx * rx + ry * ry + rz * rz;
-        const double dist = r2 * invDist(r2);
+        double dist;
+        if (geo.g) dist = __ldg(geo.g + geo.at(ii, k)).x;
+        else {
+            double rx, ry, rz;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            const double r2 = rx * rx + ry * ry + rz * rz;
+            dist = r2 * invDist(r2);
+        }
         {
             const double v = dist * hiInv;
             const TabSlot sl = tabSlot(dist * hiInvDx);
@@ -973,7 +978,7 @@ __global__ void gradhEosFinish(int64_t n, const double* h, const double* m, cons
 // FP64 atomics.  The inversion and divv/curlv follow per particle in iadOnceFinish.
 template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, IadDivvArgs a,
-                                                             const double* hInv64, int64_t n, double* acc)
+                                                             const double* hInv64, int64_t n, double* acc, PairGeo geo)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -994,8 +999,12 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
         const uint32_t j = ov.at(ii, k, mutual);
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        const double r2 = rx * rx + ry * ry + rz * rz;
-        const double dist = r2 * invDist(r2);
+        double dist;
+        if (geo.g) dist = __ldg(geo.g + geo.at(ii, k)).x;
+        else {
+            const double r2 = rx * rx + ry * ry + rz * rz;
+            dist = r2 * invDist(r2);
+        }
         const double dvx = vx[j] - vxi, dvy = vy[j] - vyi, dvz = vz[j] - vzi;
         {
             const double w = lookupX(tab, dist * hiInvDx);
@@ -1064,7 +1073,7 @@ __global__ void iadOnceFinish(int64_t first, int64_t last, int64_t n, IadDivvArg
 // the signal-velocity candidate c_i + c_j - 3 (r.v) / |r| of approaching pairs is symmetric.
 template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf, AvArgs a,
-                                                            const double* hInv64, int64_t n, double* acc)
+                                                            const double* hInv64, int64_t n, double* acc, PairGeo geo)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -1087,9 +1096,16 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
         const uint32_t j = ov.at(ii, k, mutual);
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        const double r2 = rx * rx + ry * ry + rz * rz;
-        const double rinv = invDist(r2);
-        const double dist = r2 * rinv;
+        double rinv, dist;
+        if (geo.g) {
+            const double2 gd = __ldg(geo.g + geo.at(ii, k));
+            dist = gd.x;
+            rinv = gd.y;
+        } else {
+            const double r2 = rx * rx + ry * ry + rz * rz;
+            rinv = invDist(r2);
+            dist = r2 * rinv;
+        }
         const double rv = rx * (vxi - vx[j]) + ry * (vyi - vy[j]) + rz * (vzi - vz[j]);
         const bool approaching = negative(rv);
         double vs = 0.0;
@@ -1148,7 +1164,7 @@ __global__ void avOnceFinish(int64_t first, int64_t last, int64_t n, AvArgs a, c
 // stay in registers; j's go to its accumulators with FP64 atomics (the signal-velocity maximum as an
 // integer maximum of non-negative bit patterns).
 template<bool Smooth>
-__global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordFp64 cf, MeVeArgs a)
+__global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordFp64 cf, MeVeArgs a, PairGeo geo)
 {
     using T = double;
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -1185,9 +1201,16 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         const bool mutual = (e >> 31) != 0;
         T rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        T r2 = rx * rx + ry * ry + rz * rz;
-        T rinv = invDist(r2);
-        T dist = r2 * rinv;
+        T rinv, dist;
+        if (geo.g) {
+            const double2 gd = __ldg(geo.g + geo.at(ii, k));
+            dist = gd.x;
+            rinv = gd.y;
+        } else {
+            const T r2 = rx * rx + ry * ry + rz * rz;
+            rinv = invDist(r2);
+            dist = r2 * rinv;
+        }
         T vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
         T Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
         T Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
@@ -1307,7 +1330,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
             gradhOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
                 static_cast<const double*>(p->xm), KTab<S>{tabW64(c)}, KTab<S>{tabDW64(c)}, c->hInv64.as<double>(),
-                n, c->pairAcc.as<double>());
+                n, c->pairAcc.as<double>(), pairGeo(c, false));
             return launched(c, "gradhOnceKernel");
         }));
         if (c->inSweep && p->u && p->prho && p->c) {  // EOS and quotients fused into the epilogue
@@ -1446,7 +1469,8 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
             SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 15 * size_t(n), c->stream));
             SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
                 iadOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
-                    lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+                    lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>(),
+                    pairGeo(c, false));
                 return launched(c, "iadOnceKernel");
             }));
             iadOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
@@ -1499,7 +1523,8 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * 4 * size_t(n), c->stream));
         SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
             avOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
-                lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>());
+                lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>(),
+                pairGeo(c, false));
             return launched(c, "avOnceKernel");
         }));
         avOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
@@ -1593,7 +1618,8 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
             a.ownedCount = c->ownedCount.as<uint32_t>();
             a.acc = c->pairAcc.as<double>();
             SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
-                meVeOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a);
+                meVeOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a,
+                                                                                              pairGeo(c, false));
                 return launched(c, "meVeOnceKernel");
             }));
             meVeOnceFinish<<<blocks, kPairBlock, 0, c->stream>>>(lv, a);

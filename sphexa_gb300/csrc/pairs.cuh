@@ -123,6 +123,41 @@ inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first
            last == p->n && c->nbrFirst == 0 && c->nbrLast == p->n;
 }
 
+// ---- pair geometry shared by the pair-once passes of one sweep ----
+// Inside one sweep positions and h stay put, so |r| and 1/|r| of an owned entry (the FP64 difference,
+// its square, the reciprocal square root: about a dozen FP64-pipe instructions) are formed once by
+// the xmass pass and loaded by gradh (which then needs no geometry at all), IAD, AV and
+// momentum-energy (which still form the difference vector).  Entry k of target ii at k * stride + ii:
+// a warp's 32 targets read 512 contiguous bytes per entry.
+struct PairGeo {
+    double2* g;  // null: the pass forms the geometry itself
+    int64_t stride;
+    __device__ __forceinline__ int64_t at(int64_t ii, unsigned k) const { return int64_t(k) * stride + ii; }
+};
+
+// store: the space for the xmass pass to fill (null when it cannot be had within half of the free
+// device memory, or outside a sweep); otherwise the geometry this sweep's xmass pass stored, or null
+inline PairGeo pairGeo(sphgb_ctx* c, bool store)
+{
+    PairGeo g{nullptr, c->nbrStride};
+    if (!c->inSweep) return g;
+    if (store) {
+        c->geoValid = false;
+        const size_t need = sizeof(double2) * size_t(c->nbrNgmax) * size_t(c->nbrStride);
+        if (c->pairGeo.bytes < need) {
+            size_t freeB = 0, totalB = 0;
+            if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || need > (freeB + c->pairGeo.bytes) / 2) return g;
+            if (c->pairGeo.ensure(need) != SPHGB_OK) {
+                (void)cudaGetLastError();
+                return g;
+            }
+        }
+        c->geoValid = true;
+    }
+    if (c->geoValid) g.g = c->pairGeo.as<double2>();
+    return g;
+}
+
 // ---- forward tape of the VE adjoint: sections of n doubles in c->veTape ----
 constexpr int kTapeG = 0;      // G_i = -K h_i^-3 C_i S_i of the AV switch (3 sections)
 constexpr int kTapeP = 3;      // P_i = sum xm_j W_ij (v_j - v_i) r_ij^T of divv/curlv, row-major (9)

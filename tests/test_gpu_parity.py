@@ -245,6 +245,34 @@ def test_pair_once_passes_match_ordered_sums(gpu_ctx, case):
         assert ctx.stats()["capped"] > 0
 
 
+@pytest.mark.parametrize("case", ["fourier", "sphere"])
+def test_sweep_pair_geometry_matches_passes(gpu_ctx, case):
+    """Inside one sweep the pair-once xmass pass stores |r| and 1/|r| of every owned entry and the
+    later pair-once passes load them; the entry points called one by one form the geometry in every
+    pass.  Both give the same outputs to rounding (the atomics' order differs between runs)."""
+    from sphexa_gb300 import sph, workloads as W
+    wl = {"fourier": lambda: W.fourier(16, seed=61, rho_seed=62, v_seed=63),
+          "sphere": lambda: W.sphere(20000, seed=64)}[case]()
+    gpu_ctx.set_deterministic(False)
+    whole = run_gpu(gpu_ctx, wl, "ve", False, "fp64")
+    ctx = gpu_ctx
+    d = sph.ParticlesData.from_workload(wl, "fp64", "cuda:0")
+    box = sph.Box(wl.box.copy(), wl.bc.copy())
+    sph.Domain(ctx, box).sync(d)
+    sph.find_neighbors_sfc(ctx, 0, wl.n, d)
+    sph.compute_xmass(ctx, d)
+    sph.compute_ve_def_gradh(ctx, d)
+    sph.compute_eos(ctx, d)
+    sph.compute_iad_divv_curlv(ctx, d)
+    sph.compute_av_switches(ctx, d)
+    sph.compute_momentum_energy(ctx, d, False)
+    for f in ("xm", "kx", "gradh", "prho", "c11", "c12", "c23", "divv", "curlv", "alpha", "ax", "ay", "az", "du"):
+        err = np.max(np.abs(getattr(d, f).cpu().numpy() - whole[f])) / field_scale(whole, f)
+        tol = fp64_tol(whole, f, "ve")
+        assert err <= tol, f"{case} {f}: {err:.3e} (bar {tol:.1e})"
+    assert d.minDtCourant == whole["minDt"]
+
+
 def test_individual_passes_equal_sweep(gpu_ctx):
     """The reference-named entry points called one by one give the sweep's results (bit for bit,
     with the order-fixed summation)."""
