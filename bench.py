@@ -42,8 +42,9 @@ VE_FLOPS_PER_PAIR = {"xmass": 20.2, "gradh": 34.4, "iad_divv": 37.6 + 59.3, "av"
 STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
 # dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count.
-# "me" and "av" are the pair-once kernels of the default (non-deterministic) FP64 mode.
-NCU_DRAM_BYTES_PER_PARTICLE = {"me": 559.7, "iad_divv": 564.3, "av": 381.7}
+# The pair-once kernels of the default FP64 mode inside a sweep: most of it is the stream of the
+# sweep's pair-geometry cache (32 bytes per owned entry), read instead of recomputed.
+NCU_DRAM_BYTES_PER_PARTICLE = {"me": 2288.7, "iad_divv": 2309.6, "av": 2082.9}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
 STAGES_STD = ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
 # FP32 distance test of one search candidate against the target's radius: 3 coordinate differences,
@@ -481,12 +482,11 @@ def main() -> None:
 
     # ---------------- end to end through the C ABI with host buffers (pinned), FP64 form, right after
     # the device-timed sweeps so that both run under the same conditions.  Every step copies its
-    # inputs host -> device, sweeps, and copies ax ay az du device -> host.  Headline: pipelined over
-    # two device particle sets, the next step's input copy (copy stream) overlapping this step's
-    # sweep and this step's result copy overlapping the next sweep; "serial": the same three
-    # phases back to back on one stream.
+    # inputs host -> device, sweeps, and copies ax ay az du device -> host, on one stream.  (Copies of
+    # neighbouring steps on a second stream do not overlap the sweep: its own host read-backs and
+    # field moves use the same copy engines, measured equal to the serial form.)
     if not args.no_e2e:
-        sets = [sph.ParticlesData.from_workload(wl, "fp64", dev) for _ in range(2)]
+        d = sph.ParticlesData.from_workload(wl, "fp64", dev)
         host_in = {k: torch.from_numpy(np.ascontiguousarray(wl.fields[k], dtype=np.float64)).pin_memory()
                    for k in sph.INPUTS}
         outs = ("ax", "ay", "az", "du")
@@ -494,86 +494,42 @@ def main() -> None:
         h2d = sum(t.numel() * t.element_size() for t in host_in.values())
         d2h = sum(t.numel() * t.element_size() for t in host_out.values())
         boxe = sph.Box(wl.box.copy(), wl.bc.copy())
-        ev = lambda: torch.cuda.Event(enable_timing=True)
+
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        phases = []  # per step: H2D, sweep, D2H milliseconds (CUDA events on the launching stream)
+
+        def e2e_step():
+            evs[0].record()
+            for k, t in host_in.items():
+                d.f[k].copy_(t, non_blocking=True)
+            evs[1].record()
+            sph.sweep(ctx, d, boxe, args.variant, False)
+            evs[2].record()
+            for k in outs:
+                host_out[k].copy_(d.f[k], non_blocking=True)
+            evs[3].record()
+            torch.cuda.synchronize()
+            phases.append([evs[q].elapsed_time(evs[q + 1]) for q in range(3)])
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        phases.clear()
+        barrier()
+        t0 = time.perf_counter()
         k_e2e = max(3, args.steps // 2)
-
-        def serial_run(k):
-            """k steps on the default stream; per step the H2D, sweep and D2H times."""
-            d = sets[0]
-            ph = []
-            for _ in range(k):
-                e = [ev() for _ in range(4)]
-                e[0].record()
-                for f, t in host_in.items():
-                    d.f[f].copy_(t, non_blocking=True)
-                e[1].record()
-                sph.sweep(ctx, d, boxe, args.variant, False)
-                e[2].record()
-                for f in outs:
-                    host_out[f].copy_(d.f[f], non_blocking=True)
-                e[3].record()
-                torch.cuda.synchronize()
-                ph.append([e[q].elapsed_time(e[q + 1]) for q in range(3)])
-            return ph
-
-        sweep_stream, copy_stream = torch.cuda.Stream(), torch.cuda.Stream()
-
-        def pipelined_run(k):
-            """k steps over the two sets: step s sweeps set s % 2 on the sweep stream; the copy stream
-            loads step s + 1's inputs into the other set (after the sweep that last used it) before
-            this sweep is issued, then copies step s's results out once its sweep has finished."""
-            ctx.set_stream(sweep_stream)
-            loaded = [ev(), ev()]
-            swept = [ev(), ev()]
-            used = [False, False]
-            with torch.cuda.stream(copy_stream):
-                for f, t in host_in.items():
-                    sets[0].f[f].copy_(t, non_blocking=True)
-                loaded[0].record(copy_stream)
-            for s in range(k):
-                b, nb = s % 2, 1 - s % 2
-                if s + 1 < k:
-                    with torch.cuda.stream(copy_stream):
-                        if used[nb]:
-                            copy_stream.wait_event(swept[nb])
-                        for f, t in host_in.items():
-                            sets[nb].f[f].copy_(t, non_blocking=True)
-                        loaded[nb].record(copy_stream)
-                sweep_stream.wait_event(loaded[b])
-                sph.sweep(ctx, sets[b], boxe, args.variant, False)
-                swept[b].record(sweep_stream)
-                used[b] = True
-                with torch.cuda.stream(copy_stream):
-                    copy_stream.wait_event(swept[b])
-                    for f in outs:
-                        host_out[f].copy_(sets[b].f[f], non_blocking=True)
-            torch.cuda.synchronize()
-            ctx.set_stream(torch.cuda.default_stream())
-
-        def timed_wall(fn, k):
-            barrier()
-            t0 = time.perf_counter()
-            r = fn(k)
-            torch.cuda.synchronize()
-            barrier()
-            return R.max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev), r
-
-        serial_run(max(1, args.warmup))
-        wall_s, phases = timed_wall(serial_run, k_e2e)
+        for _ in range(k_e2e):
+            e2e_step()
+        barrier()
+        wall_ms = R.max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
         med = np.median(np.array(phases), axis=0)
-        pipelined_run(max(2, args.warmup))
-        wall_p, _ = timed_wall(pipelined_run, k_e2e)
         finite = all(bool(torch.isfinite(host_out[f]).all()) for f in outs)  # the host reads the result
-        out["e2e"] = {"value": R.job_throughput(n, k_e2e, world, wall_p), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                      "d2h_bytes_per_step": d2h, "steps": k_e2e, "ms_per_step": wall_p / k_e2e,
-                      "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du, pipelined over "
-                              "two device particle sets (copies on a second stream overlap the sweeps)",
+        out["e2e"] = {"value": R.job_throughput(n, k_e2e, world, wall_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "steps": k_e2e, "ms_per_step": wall_ms / k_e2e,
+                      "phases_ms_median": {"h2d": float(med[0]), "sweep": float(med[1]), "d2h": float(med[2])},
+                      "h2d_gbs": h2d / (float(med[0]) * 1e6), "d2h_gbs": d2h / (float(med[2]) * 1e6),
                       "outputs_finite": finite,
-                      "serial": {"value": R.job_throughput(n, k_e2e, world, wall_s), "ms_per_step": wall_s / k_e2e,
-                                 "phases_ms_median": {"h2d": float(med[0]), "sweep": float(med[1]),
-                                                      "d2h": float(med[2])},
-                                 "h2d_gbs": h2d / (float(med[0]) * 1e6), "d2h_gbs": d2h / (float(med[2]) * 1e6)}}
-        del sets
+                      "path": "pinned host inputs -> sphgb_sweep (C ABI) -> pinned host ax ay az du"}
+        del d
 
     # ---------------- mixed form on the same workload, errors against this run's FP64 results
     if not args.no_mixed:

@@ -150,7 +150,7 @@ int sphgb_destroy(sphgb_ctx* c)
                     &c->gridKey,
                     &c->gridLoc,  &c->hInv64,       &c->reduceScratch, &c->aux,         &c->adjKeys,
                     &c->adjKeysAlt, &c->tOff,       &c->tIdx,          &c->adjState,      &c->whx64,
-                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pairGeo,    &c->pack,       &c->whx32,     &c->whH32, &c->whdH32,    &c->refMask,
+                    &c->whdx64,     &c->owned,      &c->ownedCount, &c->ownedR2,    &c->pairAcc,    &c->pairGeo,    &c->geoRows,    &c->pack,       &c->whx32,     &c->whH32, &c->whdH32,    &c->refMask,
                     &c->refFp64,    &c->divvBound,  &c->intScratch, &c->scanTemp, &c->veTape,
                     &c->checkWord,  &c->whS64,      &c->whdS64,     &c->sortLook,   &c->sortState};
     for (DBuf* b : bufs) b->release();

@@ -108,9 +108,11 @@ struct sphgb_ctx {
     // per-particle accumulators of the pair-once passes (up to 6 x n doubles)
     bool deterministic = false;
     sphgb::DBuf pairAcc;
-    // within one sweep: |r| and 1/|r| of every owned entry (double2 at k * nbrStride + i - nbrFirst),
-    // stored by the pair-once xmass pass and read by the later pair-once passes of the same sweep
-    sphgb::DBuf pairGeo;
+    // within one sweep: |r|, 1/|r| and the kernel function at both ends of every owned entry, stored
+    // by the pair-once xmass pass and read by the later pair-once passes of the same sweep (PairGeo in
+    // pairs.cuh); geoRows: per warp of 32 targets its longest owned list, then its first row
+    sphgb::DBuf pairGeo, geoRows;
+    size_t geoRowCount = 0;
     bool geoValid = false;
     // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
     bool inSweep = false, sweepPrepared = false;

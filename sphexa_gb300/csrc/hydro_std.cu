@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, Owned
     auto t = cf.target(i);
     const double hi = h[i], mi = m[i], twoH = 2.0 * hi, hiInvDx = hInvDx[i];
     const bool wrap = cf.needsWrap(t, twoH);
+    const int64_t gb = geo.base(ii);
     double rho0 = 0.0;
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
@@ -107,9 +108,17 @@ __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, Owned
         const double r2 = rx * rx + ry * ry + rz * rz;
         const double rinv = invDist(r2);
         const double dist = r2 * rinv;
-        if (geo.g) geo.g[geo.at(ii, k)] = make_double2(dist, rinv);
-        rho0 += lookupX(tab, dist * hiInvDx) * __ldg(m + j);
-        if (mutual) atomicAdd(acc + j, lookupX(tab, dist * __ldg(hInvDx + j)) * mi);
+        const double wi = lookupX(tab, dist * hiInvDx);
+        rho0 += wi * __ldg(m + j);
+        if (geo.g) {  // the sweep's later pair-once passes load the geometry and both kernel values
+            const double wj = lookupX(tab, dist * __ldg(hInvDx + j));
+            const int64_t e = gb + 32 * int64_t(k);
+            geo.g[e] = make_double2(dist, rinv);
+            geo.w[e] = make_double2(wi, wj);
+            if (mutual) atomicAdd(acc + j, wj * mi);
+        } else if (mutual) {
+            atomicAdd(acc + j, lookupX(tab, dist * __ldg(hInvDx + j)) * mi);
+        }
     }
     atomicAdd(acc + i, rho0);
 }
@@ -400,11 +409,13 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
         const int64_t n = p->n;
         SPHGB_TRY(c->pairAcc.ensure(sizeof(double) * size_t(n)));
         SPHGB_CUDA(cudaMemsetAsync(c->pairAcc.p, 0, sizeof(double) * size_t(n), c->stream));
+        PairGeo geo;
+        SPHGB_TRY(pairGeoStore(c, &geo));
         SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
             constexpr bool S = decltype(smooth)::value;
             xmassOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>(), pairGeo(c, true));
+                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>(), geo);
             return launched(c, "xmassOnceKernel");
         }));
         const unsigned eb = gridFor(last - first, 256);

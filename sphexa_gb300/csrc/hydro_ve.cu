@@ -884,13 +884,18 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
     auto t = cf.target(i);
     const double hi = h[i], mi = m[i], xmi = xm[i], twoH = 2.0 * hi, hiInv = hInv[i], hiInvDx = hInvDx[i];
     const bool wrap = cf.needsWrap(t, twoH);
+    const int64_t gb = geo.base(ii);
     double kx = 0.0, whom = 0.0, wr0 = 0.0;
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
         const uint32_t j = ov.at(ii, k, mutual);
         double dist;
-        if (geo.g) dist = __ldg(geo.g + geo.at(ii, k)).x;
-        else {
+        double2 wv = make_double2(0.0, 0.0);
+        if (geo.g) {
+            const int64_t e = gb + 32 * int64_t(k);
+            dist = __ldg(geo.g + e).x;
+            wv = __ldg(geo.w + e);
+        } else {
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
             const double r2 = rx * rx + ry * ry + rz * rz;
@@ -899,7 +904,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
         {
             const double v = dist * hiInv;
             const TabSlot sl = tabSlot(dist * hiInvDx);
-            const double w = lookupX(tw, sl), dw = lookupX(tdw, sl);
+            const double w = geo.g ? wv.x : lookupX(tw, sl), dw = lookupX(tdw, sl);
             const double dterh = -(3.0 * w + v * dw);
             const double xmj = __ldg(xm + j);
             kx += w * xmj;
@@ -909,7 +914,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
         if (mutual) {
             const double v = dist * __ldg(hInv + j);
             const TabSlot sl = tabSlot(dist * __ldg(hInvDx + j));
-            const double w = lookupX(tw, sl), dw = lookupX(tdw, sl);
+            const double w = geo.g ? wv.y : lookupX(tw, sl), dw = lookupX(tdw, sl);
             const double dterh = -(3.0 * w + v * dw);
             atomicAdd(acc + j, w * xmi);
             atomicAdd(acc + n + j, dterh * xmi);
@@ -993,6 +998,7 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
     const double hi = ld<double>(a.h, i), twoH = 2.0 * hi, hiInvDx = hInvDx[i];
     const bool wrap = cf.needsWrap(t, twoH);
     const double vxi = vx[i], vyi = vy[i], vzi = vz[i], voli = vol[i], xmi = xm[i];
+    const int64_t gb = geo.base(ii);
     double tau[6] = {0, 0, 0, 0, 0, 0}, M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
@@ -1000,14 +1006,18 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
         double dist;
-        if (geo.g) dist = __ldg(geo.g + geo.at(ii, k)).x;
-        else {
+        double2 wv = make_double2(0.0, 0.0);
+        if (geo.g) {
+            const int64_t e = gb + 32 * int64_t(k);
+            dist = __ldg(geo.g + e).x;
+            wv = __ldg(geo.w + e);
+        } else {
             const double r2 = rx * rx + ry * ry + rz * rz;
             dist = r2 * invDist(r2);
         }
         const double dvx = vx[j] - vxi, dvy = vy[j] - vyi, dvz = vz[j] - vzi;
         {
-            const double w = lookupX(tab, dist * hiInvDx);
+            const double w = geo.g ? wv.x : lookupX(tab, dist * hiInvDx);
             const double vw = vol[j] * w, xw = xm[j] * w;
             const double rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             tau[0] += rx * rxv;
@@ -1028,7 +1038,7 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
             M[8] += sz * rz;
         }
         if (mutual) {
-            const double w = lookupX(tab, dist * __ldg(hInvDx + j));
+            const double w = geo.g ? wv.y : lookupX(tab, dist * __ldg(hInvDx + j));
             const double vw = voli * w, xw = xmi * w;
             const double rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
             atomicAdd(acc + j, rx * rxv);
@@ -1088,6 +1098,7 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
     const double hi = ld<double>(a.h, i), ci = c[i], divvi = divv[i], voli = vol[i];
     const double vxi = vx[i], vyi = vy[i], vzi = vz[i], twoH = 2.0 * hi, hiInvDx = hInvDx[i];
     const bool wrap = cf.needsWrap(t, twoH);
+    const int64_t gb = geo.base(ii);
     double Sx = 0, Sy = 0, Sz = 0;
     long long vsigBits = 0;
     long long* accV = reinterpret_cast<long long*>(acc + 3 * n);
@@ -1097,10 +1108,13 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
         double rinv, dist;
+        double2 wv = make_double2(0.0, 0.0);
         if (geo.g) {
-            const double2 gd = __ldg(geo.g + geo.at(ii, k));
+            const int64_t e = gb + 32 * int64_t(k);
+            const double2 gd = __ldg(geo.g + e);
             dist = gd.x;
             rinv = gd.y;
+            wv = __ldg(geo.w + e);
         } else {
             const double r2 = rx * rx + ry * ry + rz * rz;
             rinv = invDist(r2);
@@ -1114,12 +1128,12 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
             vsigBits = maxBitsNonNeg(vsigBits, vs);
         }
         const double dd = divvi - divv[j];
-        const double fw = vol[j] * dd * lookupX(tabX, dist * hiInvDx);
+        const double fw = vol[j] * dd * (geo.g ? wv.x : lookupX(tabX, dist * hiInvDx));
         Sx += fw * rx;
         Sy += fw * ry;
         Sz += fw * rz;
         if (mutual) {
-            const double fwj = voli * dd * lookupX(tabX, dist * __ldg(hInvDx + j));
+            const double fwj = voli * dd * (geo.g ? wv.y : lookupX(tabX, dist * __ldg(hInvDx + j)));
             atomicAdd(acc + j, fwj * rx);
             atomicAdd(acc + n + j, fwj * ry);
             atomicAdd(acc + 2 * n + j, fwj * rz);
@@ -1190,6 +1204,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
     auto t = cf.target(i);
     const T hiInv3 = hInv3[i], hiInvDx = hInvDx[i], twoH = 2.0 * hi;
     const bool wrap = cf.needsWrap(t, twoH);
+    const int64_t gb = geo.base(ii);
     T mx = 0, my = 0, mz = 0, en = 0, avE = 0;
     long long maxvBits = 0;
     double *accX = a.acc, *accY = a.acc + a.n, *accZ = a.acc + 2 * a.n, *accE = a.acc + 3 * a.n,
@@ -1201,19 +1216,22 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         const bool mutual = (e >> 31) != 0;
         T rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        T rinv, dist;
+        T rinv, dist, Wi, Wj;
         if (geo.g) {
-            const double2 gd = __ldg(geo.g + geo.at(ii, k));
+            const int64_t e = gb + 32 * int64_t(k);
+            const double2 gd = __ldg(geo.g + e), wv = __ldg(geo.w + e);
             dist = gd.x;
             rinv = gd.y;
+            Wi = hiInv3 * wv.x;
+            Wj = __ldg(hInv3 + j) * wv.y;
         } else {
             const T r2 = rx * rx + ry * ry + rz * rz;
             rinv = invDist(r2);
             dist = r2 * rinv;
+            Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
+            Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
         }
         T vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
-        T Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
-        T Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
         T gix = c11i * rx + c12i * ry + c13i * rz;
         T giy = c12i * rx + c22i * ry + c23i * rz;
         T giz = c13i * rx + c23i * ry + c33i * rz;
@@ -1330,7 +1348,7 @@ int passGradh(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last)
             gradhOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), coordFp64(c, p), static_cast<const double*>(p->h), static_cast<const double*>(p->m),
                 static_cast<const double*>(p->xm), KTab<S>{tabW64(c)}, KTab<S>{tabDW64(c)}, c->hInv64.as<double>(),
-                n, c->pairAcc.as<double>(), pairGeo(c, false));
+                n, c->pairAcc.as<double>(), pairGeoRead(c));
             return launched(c, "gradhOnceKernel");
         }));
         if (c->inSweep && p->u && p->prho && p->c) {  // EOS and quotients fused into the epilogue
@@ -1470,7 +1488,7 @@ int passIadDivvCurlv(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t la
             SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
                 iadOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
                     lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>(),
-                    pairGeo(c, false));
+                    pairGeoRead(c));
                 return launched(c, "iadOnceKernel");
             }));
             iadOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
@@ -1524,7 +1542,7 @@ int passAVswitches(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last
         SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
             avOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), coordFp64(c, p), a, c->hInv64.as<double>(), n, c->pairAcc.as<double>(),
-                pairGeo(c, false));
+                pairGeoRead(c));
             return launched(c, "avOnceKernel");
         }));
         avOnceFinish<<<gridFor(last - first, 256), 256, 0, c->stream>>>(first, last, n, a, c->pairAcc.as<double>());
@@ -1619,7 +1637,7 @@ int passMomentumEnergyVe(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_
             a.acc = c->pairAcc.as<double>();
             SPHGB_TRY(withKernelForm(c, [&](auto smooth) {
                 meVeOnceKernel<decltype(smooth)::value><<<blocks, kPairBlock, 0, c->stream>>>(lv, cf, a,
-                                                                                              pairGeo(c, false));
+                                                                                              pairGeoRead(c));
                 return launched(c, "meVeOnceKernel");
             }));
             meVeOnceFinish<<<blocks, kPairBlock, 0, c->stream>>>(lv, a);

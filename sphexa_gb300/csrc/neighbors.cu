@@ -678,6 +678,14 @@ __global__ void __launch_bounds__(128) ownedByListKernel(const uint32_t* __restr
     ownedCount[ii] = cnt;
 }
 
+// longest owned list of each warp of 32 targets
+__global__ void warpMaxKernel(const uint32_t* __restrict__ count, int64_t n, uint32_t* __restrict__ wmax)
+{
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const uint32_t m = __reduce_max_sync(0xffffffffu, i < n ? __ldg(count + i) : 0u);
+    if ((threadIdx.x & 31) == 0 && i < n) wmax[i >> 5] = m;
+}
+
 __global__ void fillOnes(uint32_t* p, int64_t n)
 {
     int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -824,6 +832,39 @@ int finishStats(sphgb_ctx* c, int64_t hIters)
 }
 
 }  // namespace
+
+int pairGeoStore(sphgb_ctx* c, PairGeo* out)
+{
+    *out = PairGeo{nullptr, nullptr, nullptr};
+    c->geoValid = false;
+    if (!c->inSweep || c->ownedEpoch != c->nbrEpoch || c->ownedFromLists) return SPHGB_OK;
+    const int64_t nWork = c->nbrLast - c->nbrFirst, nWarps = (nWork + 31) / 32;
+    if (nWork <= 0) return SPHGB_OK;
+    SPHGB_TRY(c->geoRows.ensure(sizeof(uint32_t) * 2 * size_t(nWarps)));
+    uint32_t* wmax = c->geoRows.as<uint32_t>();
+    uint32_t* rowOff = wmax + nWarps;
+    warpMaxKernel<<<gridFor(nWarps * 32, 256), 256, 0, c->stream>>>(c->ownedCount.as<uint32_t>(), nWork, wmax);
+    SPHGB_TRY(launched(c, "warpMaxKernel"));
+    SPHGB_TRY(exclusiveScan(c, wmax, rowOff, nWarps));
+    uint32_t lastOff = 0, lastMax = 0;
+    SPHGB_CUDA(cudaMemcpyAsync(&lastOff, rowOff + nWarps - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaMemcpyAsync(&lastMax, wmax + nWarps - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    SPHGB_CUDA(cudaStreamSynchronize(c->stream));
+    const size_t rows = size_t(lastOff) + lastMax;
+    const size_t need = 2 * 32 * sizeof(double2) * rows;  // {|r|, 1/|r|} and the two kernel values
+    if (c->pairGeo.bytes < need) {
+        size_t freeB = 0, totalB = 0;
+        if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || need > (freeB + c->pairGeo.bytes) / 2) return SPHGB_OK;
+        if (c->pairGeo.ensure(need) != SPHGB_OK) {
+            (void)cudaGetLastError();
+            return SPHGB_OK;
+        }
+    }
+    c->geoRowCount = rows;
+    c->geoValid = true;
+    *out = pairGeoRead(c);
+    return SPHGB_OK;
+}
 
 int buildOwnedFromLists(sphgb_ctx* c)
 {

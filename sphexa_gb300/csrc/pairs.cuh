@@ -124,38 +124,34 @@ inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first
 }
 
 // ---- pair geometry shared by the pair-once passes of one sweep ----
-// Inside one sweep positions and h stay put, so |r| and 1/|r| of an owned entry (the FP64 difference,
-// its square, the reciprocal square root: about a dozen FP64-pipe instructions) are formed once by
-// the xmass pass and loaded by gradh (which then needs no geometry at all), IAD, AV and
-// momentum-energy (which still form the difference vector).  Entry k of target ii at k * stride + ii:
-// a warp's 32 targets read 512 contiguous bytes per entry.
+// Inside one sweep positions and h stay put, so an owned entry's |r| and 1/|r| (the FP64 difference,
+// its square and the reciprocal square root: about a dozen FP64-pipe instructions) and the kernel
+// function at both ends, w(|r| / h_i) and w(|r| / h_j), are formed once by the xmass pass and loaded
+// by gradh (which then needs no difference vector), IAD, AV and momentum-energy.  Layout: the 32
+// targets of a warp own rows rowOff[w] .. rowOff[w] + (their longest owned list) - 1, a row holding
+// entry k of all 32 side by side, so a warp reads 512 contiguous bytes per entry and array.
 struct PairGeo {
-    double2* g;  // null: the pass forms the geometry itself
-    int64_t stride;
-    __device__ __forceinline__ int64_t at(int64_t ii, unsigned k) const { return int64_t(k) * stride + ii; }
+    const uint32_t* rowOff;  // first row of each warp of 32 targets
+    double2* g;              // {|r|, 1/|r|}; null: the pass forms the geometry itself
+    double2* w;              // {w(|r| / h_i), w(|r| / h_j)}
+    // entry k of target ii is at base(ii) + 32 k
+    __device__ __forceinline__ int64_t base(int64_t ii) const
+    {
+        return g ? int64_t(__ldg(rowOff + (ii >> 5))) * 32 + (ii & 31) : 0;
+    }
 };
 
-// store: the space for the xmass pass to fill (null when it cannot be had within half of the free
-// device memory, or outside a sweep); otherwise the geometry this sweep's xmass pass stored, or null
-inline PairGeo pairGeo(sphgb_ctx* c, bool store)
+// the space for the xmass pass of this sweep to fill (rows from the owned counts; null outside a
+// sweep or when it cannot be had within half of the free device memory)
+int pairGeoStore(sphgb_ctx* c, PairGeo* out);
+
+// what this sweep's xmass pass stored, or null
+inline PairGeo pairGeoRead(const sphgb_ctx* c)
 {
-    PairGeo g{nullptr, c->nbrStride};
-    if (!c->inSweep) return g;
-    if (store) {
-        c->geoValid = false;
-        const size_t need = sizeof(double2) * size_t(c->nbrNgmax) * size_t(c->nbrStride);
-        if (c->pairGeo.bytes < need) {
-            size_t freeB = 0, totalB = 0;
-            if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || need > (freeB + c->pairGeo.bytes) / 2) return g;
-            if (c->pairGeo.ensure(need) != SPHGB_OK) {
-                (void)cudaGetLastError();
-                return g;
-            }
-        }
-        c->geoValid = true;
-    }
-    if (c->geoValid) g.g = c->pairGeo.as<double2>();
-    return g;
+    if (!c->inSweep || !c->geoValid) return PairGeo{nullptr, nullptr, nullptr};
+    double2* g = c->pairGeo.as<double2>();
+    const int64_t nWarps = (c->nbrLast - c->nbrFirst + 31) / 32;
+    return PairGeo{c->geoRows.as<uint32_t>() + nWarps, g, g + 32 * c->geoRowCount};
 }
 
 // ---- forward tape of the VE adjoint: sections of n doubles in c->veTape ----
