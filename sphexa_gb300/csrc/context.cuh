@@ -113,6 +113,7 @@ struct sphgb_ctx {
     // pairs.cuh); geoRows: per warp of 32 targets its longest owned list, then its first row
     sphgb::DBuf pairGeo, geoRows;
     size_t geoRowCount = 0;
+    int geoArrays = 0;  // 5: with the difference and velocity-difference vectors, 2: without
     bool geoValid = false;
     // inside sphgb_sweep_passes the per-particle precomputes are built by the first pass only
     bool inSweep = false, sweepPrepared = false;

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            double r2 = rx * rx + ry * ry + rz * rz;
+            double r2 = dist2(rx, ry, rz);
             rho0 += lookupX(tab, r2 * invDist(r2) * hInvDx) * ld<double>(m, j);
         }
         double xm = mi / (rho0 * K * h3Inv);
@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
 template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, KTab<Smooth> tab,
-                                                               const double* hInvDx, double* acc, PairGeo geo)
+                                                               const double* hInvDx, double* acc, PairGeo geo,
+                                                               const double* vx, const double* vy, const double* vz)
 {
     const int64_t i = lv.first + blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= lv.last) return;
@@ -99,13 +100,14 @@ __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, Owned
     const double hi = h[i], mi = m[i], twoH = 2.0 * hi, hiInvDx = hInvDx[i];
     const bool wrap = cf.needsWrap(t, twoH);
     const int64_t gb = geo.base(ii);
+    const double vxi = geo.x ? vx[i] : 0.0, vyi = geo.x ? vy[i] : 0.0, vzi = geo.x ? vz[i] : 0.0;
     double rho0 = 0.0;
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
         const uint32_t j = ov.at(ii, k, mutual);
         double rx, ry, rz;
         cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double r2 = dist2(rx, ry, rz);
         const double rinv = invDist(r2);
         const double dist = r2 * rinv;
         const double wi = lookupX(tab, dist * hiInvDx);
@@ -115,6 +117,12 @@ __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, Owned
             const int64_t e = gb + 32 * int64_t(k);
             geo.g[e] = make_double2(dist, rinv);
             geo.w[e] = make_double2(wi, wj);
+            if (geo.x) {
+                const double dvx = __ldg(vx + j) - vxi, dvy = __ldg(vy + j) - vyi, dvz = __ldg(vz + j) - vzi;
+                geo.x[e] = make_double2(rx, ry);
+                geo.x[geo.plane + e] = make_double2(rz, dvx);
+                geo.x[2 * geo.plane + e] = make_double2(dvy, dvz);
+            }
             if (mutual) atomicAdd(acc + j, wj * mi);
         } else if (mutual) {
             atomicAdd(acc + j, lookupX(tab, dist * __ldg(hInvDx + j)) * mi);
@@ -201,7 +209,7 @@ __global__ void __launch_bounds__(kPairBlock) iadKernel(ListView lv, CoordFp64 c
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            double r2 = rx * rx + ry * ry + rz * rz;
+            double r2 = dist2(rx, ry, rz);
             double w = lookupX(tab, r2 * invDist(r2) * hInvDx);
             double vw = ld<double>(vol, j) * w;
             t11 += rx * rx * vw;
@@ -298,7 +306,7 @@ __global__ void __launch_bounds__(kPairBlock) meStdKernel(ListView lv, CoordFp64
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            T r2 = rx * rx + ry * ry + rz * rz;
+            T r2 = dist2(rx, ry, rz);
             T rinv = invDist(r2);
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
@@ -415,7 +423,9 @@ int launchXmass(sphgb_ctx* c, sphgb_particles* p, int64_t first, int64_t last, v
             constexpr bool S = decltype(smooth)::value;
             xmassOnceKernel<S><<<blocks, kPairBlock, 0, c->stream>>>(
                 lv, ownedView(c), cf, static_cast<const double*>(p->h), static_cast<const double*>(p->m),
-                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>(), geo);
+                KTab<S>{tabW64(c)}, c->hInv64.as<double>() + 2 * n, c->pairAcc.as<double>(), geo,
+                static_cast<const double*>(p->vx), static_cast<const double*>(p->vy),
+                static_cast<const double*>(p->vz));
             return launched(c, "xmassOnceKernel");
         }));
         const unsigned eb = gridFor(last - first, 256);

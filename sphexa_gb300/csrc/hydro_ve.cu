@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhKernel(ListView lv, CoordFp64
             uint32_t j = lv.at(ii, k);
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            double r2 = rx * rx + ry * ry + rz * rz;
+            double r2 = dist2(rx, ry, rz);
             double dist = r2 * invDist(r2);
             double v = dist * hInv;
             const TabSlot sl = tabSlot(dist * hInvDx);
@@ -316,7 +316,7 @@ iadDivvKernel(ListView lv, CoordFp64 cf, CoordMixed cm, IadDivvArgs a)
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            T r2 = rx * rx + ry * ry + rz * rz;
+            T r2 = dist2(rx, ry, rz);
             T w = lookupX(tab, r2 * invDist(r2) * hInvDx);
             T vw = ld<T>(a.vol, j) * w;
             T rxv = rx * vw, ryv = ry * vw, rzv = rz * vw;
@@ -502,12 +502,12 @@ __global__ void __launch_bounds__(kPairBlock) avKernel(ListView lv, CoordFp64 cf
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            T r2 = rx * rx + ry * ry + rz * rz;
+            T r2 = dist2(rx, ry, rz);
             T rinv = invDist(r2);
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
-            T rv = rx * vxij + ry * vyij + rz * vzij;
-            if (negative(rv)) vsigBits = maxBitsNonNeg(vsigBits, ci + ld<T>(a.c, j) - 3.0 * rv * rinv);
+            T rv = fma(rz, vzij, fma(ry, vyij, rx * vxij));  // one order in every FP64 form
+            if (negative(rv)) vsigBits = maxBitsNonNeg(vsigBits, fma(-3.0 * rv, rinv, ci + ld<T>(a.c, j)));
             T fw = ld<T>(a.vol, j) * (divvi - ld<T>(a.divv, j)) * lookupX(tabX, dist * hInvDx);
             Sx += fw * rx;
             Sy += fw * ry;
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             uint32_t j = lv.at(ii, k);
             T rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            T r2 = rx * rx + ry * ry + rz * rz;
+            T r2 = dist2(rx, ry, rz);
             T rinv = invDist(r2);
             T dist = r2 * rinv;
             T vxij = vxi - ld<T>(a.vx, j), vyij = vyi - ld<T>(a.vy, j), vzij = vzi - ld<T>(a.vz, j);
@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             T gjz = c13j * rx + c23j * ry + c33j * rz;
             T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
             T rhoj = __ldg(auxRho + j);
-            T rv = rx * vxij + ry * vyij + rz * vzij;
+            T rv = fma(rz, vzij, fma(ry, vyij, rx * vxij));
             if constexpr (AvClean) {
                 T gj[6] = {ld<T>(a.dV11, j), ld<T>(a.dV12, j), ld<T>(a.dV13, j),
                            ld<T>(a.dV22, j), ld<T>(a.dV23, j), ld<T>(a.dV33, j)};
@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(kPairBlock) meVeKernel(ListView lv, CoordFp64 
             }
             T wij = rv * rinv;
             T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
-            maxvBits = maxBitsNonNeg(maxvBits, T(0.5) * (ci + cj) - T(2) * wij);
+            maxvBits = maxBitsNonNeg(maxvBits, fma(T(-2), wij, T(0.5) * (ci + cj)));
             // Atwood number |rhoi - rhoj| / (rhoi + rhoj) against Atmin / Atmax, without dividing
             // and with the comparisons on bit patterns (all operands >= 0)
             T dr = fabs(rhoi - rhoj), sr = rhoi + rhoj;
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(kPairBlock) gradhOnceKernel(ListView lv, Owned
         } else {
             double rx, ry, rz;
             cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-            const double r2 = rx * rx + ry * ry + rz * rz;
+            const double r2 = dist2(rx, ry, rz);
             dist = r2 * invDist(r2);
         }
         {
@@ -1003,19 +1003,27 @@ __global__ void __launch_bounds__(kPairBlock) iadOnceKernel(ListView lv, OwnedVi
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
         const uint32_t j = ov.at(ii, k, mutual);
-        double rx, ry, rz;
-        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        double dist;
+        double rx, ry, rz, dvx, dvy, dvz, dist;
         double2 wv = make_double2(0.0, 0.0);
-        if (geo.g) {
+        if (geo.x) {
             const int64_t e = gb + 32 * int64_t(k);
+            const double2 a0 = __ldg(geo.x + e), a1 = __ldg(geo.x + geo.plane + e),
+                          a2 = __ldg(geo.x + 2 * geo.plane + e);
+            rx = a0.x, ry = a0.y, rz = a1.x, dvx = a1.y, dvy = a2.x, dvz = a2.y;
             dist = __ldg(geo.g + e).x;
             wv = __ldg(geo.w + e);
         } else {
-            const double r2 = rx * rx + ry * ry + rz * rz;
-            dist = r2 * invDist(r2);
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            if (geo.g) {
+                const int64_t e = gb + 32 * int64_t(k);
+                dist = __ldg(geo.g + e).x;
+                wv = __ldg(geo.w + e);
+            } else {
+                const double r2 = dist2(rx, ry, rz);
+                dist = r2 * invDist(r2);
+            }
+            dvx = vx[j] - vxi, dvy = vy[j] - vyi, dvz = vz[j] - vzi;
         }
-        const double dvx = vx[j] - vxi, dvy = vy[j] - vyi, dvz = vz[j] - vzi;
         {
             const double w = geo.g ? wv.x : lookupX(tab, dist * hiInvDx);
             const double vw = vol[j] * w, xw = xm[j] * w;
@@ -1105,9 +1113,7 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
     for (unsigned k = 0; k < no; ++k) {
         bool mutual;
         const uint32_t j = ov.at(ii, k, mutual);
-        double rx, ry, rz;
-        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        double rinv, dist;
+        double rx, ry, rz, rinv, dist, rv;
         double2 wv = make_double2(0.0, 0.0);
         if (geo.g) {
             const int64_t e = gb + 32 * int64_t(k);
@@ -1115,16 +1121,26 @@ __global__ void __launch_bounds__(kPairBlock) avOnceKernel(ListView lv, OwnedVie
             dist = gd.x;
             rinv = gd.y;
             wv = __ldg(geo.w + e);
+            if (geo.x) {  // v_i - v_j = -dv exactly
+                const double2 a0 = __ldg(geo.x + e), a1 = __ldg(geo.x + geo.plane + e),
+                              a2 = __ldg(geo.x + 2 * geo.plane + e);
+                rx = a0.x, ry = a0.y, rz = a1.x;
+                rv = fma(rz, -a2.y, fma(ry, -a2.x, rx * -a1.y));
+            } else {
+                cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+                rv = fma(rz, vzi - vz[j], fma(ry, vyi - vy[j], rx * (vxi - vx[j])));
+            }
         } else {
-            const double r2 = rx * rx + ry * ry + rz * rz;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            const double r2 = dist2(rx, ry, rz);
             rinv = invDist(r2);
             dist = r2 * rinv;
+            rv = fma(rz, vzi - vz[j], fma(ry, vyi - vy[j], rx * (vxi - vx[j])));
         }
-        const double rv = rx * (vxi - vx[j]) + ry * (vyi - vy[j]) + rz * (vzi - vz[j]);
         const bool approaching = negative(rv);
         double vs = 0.0;
         if (approaching) {
-            vs = ci + c[j] - 3.0 * rv * rinv;
+            vs = fma(-3.0 * rv, rinv, ci + c[j]);
             vsigBits = maxBitsNonNeg(vsigBits, vs);
         }
         const double dd = divvi - divv[j];
@@ -1214,24 +1230,31 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         const uint32_t e = __ldg(a.owned + listSlot(ii, k, lv.stride));
         const uint32_t j = e & 0x7fffffffu;
         const bool mutual = (e >> 31) != 0;
-        T rx, ry, rz;
-        cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-        T rinv, dist, Wi, Wj;
+        T rx, ry, rz, rinv, Wi, Wj, vxij, vyij, vzij;
         if (geo.g) {
             const int64_t e = gb + 32 * int64_t(k);
             const double2 gd = __ldg(geo.g + e), wv = __ldg(geo.w + e);
-            dist = gd.x;
             rinv = gd.y;
             Wi = hiInv3 * wv.x;
             Wj = __ldg(hInv3 + j) * wv.y;
+            if (geo.x) {  // v_ij = v_i - v_j = -dv exactly
+                const double2 a0 = __ldg(geo.x + e), a1 = __ldg(geo.x + geo.plane + e),
+                              a2 = __ldg(geo.x + 2 * geo.plane + e);
+                rx = a0.x, ry = a0.y, rz = a1.x;
+                vxij = -a1.y, vyij = -a2.x, vzij = -a2.y;
+            } else {
+                cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+                vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
+            }
         } else {
-            const T r2 = rx * rx + ry * ry + rz * rz;
+            cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
+            const T r2 = dist2(rx, ry, rz);
             rinv = invDist(r2);
-            dist = r2 * rinv;
+            const T dist = r2 * rinv;
             Wi = hiInv3 * lookupX(tabX, dist * hiInvDx);
             Wj = __ldg(hInv3 + j) * lookupX(tabX, dist * __ldg(hInvDx + j));
+            vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
         }
-        T vxij = vxi - vxA[j], vyij = vyi - vyA[j], vzij = vzi - vzA[j];
         T gix = c11i * rx + c12i * ry + c13i * rz;
         T giy = c12i * rx + c22i * ry + c23i * rz;
         T giz = c13i * rx + c23i * ry + c33i * rz;
@@ -1242,10 +1265,10 @@ __global__ void __launch_bounds__(kPairBlock) meVeOnceKernel(ListView lv, CoordF
         T gjz = c13j * rx + c23j * ry + c33j * rz;
         T mj = ld<T>(a.m, j), cj = ld<T>(a.c, j), xmj = ld<T>(a.xm, j);
         T rhoj = __ldg(auxRho + j);
-        T rv = rx * vxij + ry * vyij + rz * vzij;
+        T rv = fma(rz, vzij, fma(ry, vyij, rx * vxij));
         T wij = rv * rinv;
         T visc = artificialViscosity<T>(ai, ld<T>(a.alpha, j), ci, cj, wij);
-        const T vsig = T(0.5) * (ci + cj) - T(2) * wij;
+        const T vsig = fma(T(-2), wij, T(0.5) * (ci + cj));
         maxvBits = maxBitsNonNeg(maxvBits, vsig);
         T dr = fabs(rhoi - rhoj), sr = rhoi + rhoj;
         T am, bm;

@@ -835,7 +835,7 @@ int finishStats(sphgb_ctx* c, int64_t hIters)
 
 int pairGeoStore(sphgb_ctx* c, PairGeo* out)
 {
-    *out = PairGeo{nullptr, nullptr, nullptr};
+    *out = PairGeo{nullptr, nullptr, nullptr, nullptr, 0};
     c->geoValid = false;
     if (!c->inSweep || c->ownedEpoch != c->nbrEpoch || c->ownedFromLists) return SPHGB_OK;
     const int64_t nWork = c->nbrLast - c->nbrFirst, nWarps = (nWork + 31) / 32;
@@ -851,16 +851,27 @@ int pairGeoStore(sphgb_ctx* c, PairGeo* out)
     SPHGB_CUDA(cudaMemcpyAsync(&lastMax, wmax + nWarps - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
     SPHGB_CUDA(cudaStreamSynchronize(c->stream));
     const size_t rows = size_t(lastOff) + lastMax;
-    const size_t need = 2 * 32 * sizeof(double2) * rows;  // {|r|, 1/|r|} and the two kernel values
-    if (c->pairGeo.bytes < need) {
+    // five arrays (|r| and 1/|r|, the two kernel values, r and dv) or the first two, whichever fits
+    // in the buffer already held or in half of the free device memory
+    int arrays = 0;
+    for (int a : {5, 2}) {
+        const size_t need = size_t(a) * 32 * sizeof(double2) * rows;
+        if (c->pairGeo.bytes >= need) {
+            arrays = a;
+            break;
+        }
         size_t freeB = 0, totalB = 0;
-        if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || need > (freeB + c->pairGeo.bytes) / 2) return SPHGB_OK;
+        if (cudaMemGetInfo(&freeB, &totalB) != cudaSuccess || need > (freeB + c->pairGeo.bytes) / 2) continue;
         if (c->pairGeo.ensure(need) != SPHGB_OK) {
             (void)cudaGetLastError();
-            return SPHGB_OK;
+            continue;
         }
+        arrays = a;
+        break;
     }
+    if (arrays == 0) return SPHGB_OK;
     c->geoRowCount = rows;
+    c->geoArrays = arrays;
     c->geoValid = true;
     *out = pairGeoRead(c);
     return SPHGB_OK;

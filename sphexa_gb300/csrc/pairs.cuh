@@ -124,16 +124,19 @@ inline bool pairOnce(const sphgb_ctx* c, const sphgb_particles* p, int64_t first
 }
 
 // ---- pair geometry shared by the pair-once passes of one sweep ----
-// Inside one sweep positions and h stay put, so an owned entry's |r| and 1/|r| (the FP64 difference,
-// its square and the reciprocal square root: about a dozen FP64-pipe instructions) and the kernel
-// function at both ends, w(|r| / h_i) and w(|r| / h_j), are formed once by the xmass pass and loaded
-// by gradh (which then needs no difference vector), IAD, AV and momentum-energy.  Layout: the 32
-// targets of a warp own rows rowOff[w] .. rowOff[w] + (their longest owned list) - 1, a row holding
-// entry k of all 32 side by side, so a warp reads 512 contiguous bytes per entry and array.
+// Inside one sweep positions, velocities and h stay put, so an owned entry's |r| and 1/|r| (the FP64
+// difference, its square and the reciprocal square root: about a dozen FP64-pipe instructions), the
+// kernel function at both ends, w(|r| / h_i) and w(|r| / h_j), and, where the memory is there, the
+// difference vector r = x_i - x_j and the velocity difference dv = v_j - v_i are formed once by the
+// xmass pass and loaded by gradh, IAD, AV and momentum-energy.  Layout: the 32 targets of a warp own
+// rows rowOff[w] .. rowOff[w] + (their longest owned list) - 1, a row holding entry k of all 32 side
+// by side, so a warp reads 512 contiguous bytes per entry and array.
 struct PairGeo {
     const uint32_t* rowOff;  // first row of each warp of 32 targets
     double2* g;              // {|r|, 1/|r|}; null: the pass forms the geometry itself
     double2* w;              // {w(|r| / h_i), w(|r| / h_j)}
+    double2* x;              // {rx, ry}, {rz, dvx}, {dvy, dvz} at x, x + plane, x + 2 plane; or null
+    int64_t plane;           // entries per array
     // entry k of target ii is at base(ii) + 32 k
     __device__ __forceinline__ int64_t base(int64_t ii) const
     {
@@ -148,10 +151,10 @@ int pairGeoStore(sphgb_ctx* c, PairGeo* out);
 // what this sweep's xmass pass stored, or null
 inline PairGeo pairGeoRead(const sphgb_ctx* c)
 {
-    if (!c->inSweep || !c->geoValid) return PairGeo{nullptr, nullptr, nullptr};
+    if (!c->inSweep || !c->geoValid) return PairGeo{nullptr, nullptr, nullptr, nullptr, 0};
     double2* g = c->pairGeo.as<double2>();
-    const int64_t nWarps = (c->nbrLast - c->nbrFirst + 31) / 32;
-    return PairGeo{c->geoRows.as<uint32_t>() + nWarps, g, g + 32 * c->geoRowCount};
+    const int64_t nWarps = (c->nbrLast - c->nbrFirst + 31) / 32, plane = 32 * int64_t(c->geoRowCount);
+    return PairGeo{c->geoRows.as<uint32_t>() + nWarps, g, g + plane, c->geoArrays == 5 ? g + 2 * plane : nullptr, plane};
 }
 
 // ---- forward tape of the VE adjoint: sections of n doubles in c->veTape ----
@@ -252,6 +255,14 @@ inline CoordFp64 coordFp64(const sphgb_ctx* c, const sphgb_particles* p)
 // 1/sqrt(r2) and sqrt(r2) in FP64 through the reciprocal square root: one special-function
 // seed plus FMA refinement instead of an IEEE sqrt and an IEEE divide
 __device__ __forceinline__ double invDist(double r2) { return rsqrt(r2); }
+
+// |r|^2 in one fixed order of FMAs: every FP64 pass, the order-fixed and the pair-once forms and the
+// per-sweep geometry cache form the same bits for a pair, so their Courant time steps agree exactly
+template<class T>
+__device__ __forceinline__ T dist2(T x, T y, T z)
+{
+    return fma(z, z, fma(y, y, x * x));
+}
 
 // ---- FP64 pair-loop arithmetic kept off the FP64 pipe ----
 // On GB300 the SM's FP64 pipe retires 2 lanes per cycle: one warp-wide FP64 instruction holds it

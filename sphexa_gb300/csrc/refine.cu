@@ -44,7 +44,7 @@ __device__ __forceinline__ double pairDist(const RefArgs& a, const CoordFp64::Ta
 {
     double rx, ry, rz;
     a.cf.diffFast(t, j, twoH, wrap, rx, ry, rz);
-    const double r2 = rx * rx + ry * ry + rz * rz;
+    const double r2 = dist2(rx, ry, rz);
     return r2 * invDist(r2);
 }
 
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kRefBlock) refDivvKernel(RefArgs a, int64_t cn
         const uint32_t j = a.lv.at(ii, k);
         double rx, ry, rz;
         a.cf.diffFast(tg, j, twoH, wrap, rx, ry, rz);
-        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double r2 = dist2(rx, ry, rz);
         const double w = lookupX(a.tw, r2 * invDist(r2) * hInv * kTabInvDx);
         const double vw = a.vol64[j] * w;
         t11 += rx * rx * vw;
