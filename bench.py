@@ -43,8 +43,8 @@ STD_FLOPS_PER_PAIR = {"density": 20.2, "iad": 37.6, "me": 117.3}
 # DRAM bytes per particle of one launch, from ncu captures at 1 M particles (dram__bytes_read.sum +
 # dram__bytes_write.sum, profiles/*_sedov100_jit_1M.md); traffic grows with the particle count.
 # The pair-once kernels of the default FP64 mode inside a sweep: most of it is the stream of the
-# sweep's pair-geometry cache (32 bytes per owned entry), read instead of recomputed.
-NCU_DRAM_BYTES_PER_PARTICLE = {"me": 2288.7, "iad_divv": 2309.6, "av": 2082.9}
+# sweep's pair-geometry cache (80 bytes per owned entry), read instead of recomputed.
+NCU_DRAM_BYTES_PER_PARTICLE = {"me": 4808.1, "iad_divv": 4823.9, "av": 4581.1}
 STAGES_VE = ["sync", "neighbors", "xmass", "gradh", "eos", "iad_divv", "av", "me"]
 STAGES_STD = ["sync", "neighbors", "density", "eos", "iad", "me", "-", "-"]
 # FP32 distance test of one search candidate against the target's radius: 3 coordinate differences,
