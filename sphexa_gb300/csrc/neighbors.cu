@@ -795,6 +795,9 @@ int prepareLists(sphgb_ctx* c, const double* x, const double* y, const double* z
     if (first < 0 || last > c->n || first >= last) return SPHGB_ERR_ARG;
     const int64_t nWork = last - first;
     c->nbrStride = (nWork + 31) / 32 * 32;
+    // lists larger than the buffers hold: the pair-geometry cache of an earlier sweep gives its
+    // memory back first (the next FP64 sweep sizes it again within half of the free memory)
+    if (c->nbr.bytes < sizeof(uint32_t) * listCapacity(ngmax) * c->nbrStride) c->pairGeo.release();
     SPHGB_TRY(c->nbr.ensure(sizeof(uint32_t) * listCapacity(ngmax) * c->nbrStride));
     SPHGB_TRY(c->ncount.ensure(sizeof(uint32_t) * c->nbrStride));
     SPHGB_TRY(c->active.ensure(sizeof(uint32_t) * c->nbrStride + c->nbrStride));
