@@ -85,7 +85,8 @@ __global__ void __launch_bounds__(kPairBlock) xmassKernel(ListView lv, CoordFp64
 }
 
 // FP64 xmass / density with one evaluation per mutual pair over the owned lists: i adds
-// W(d / h_i) m_j, and for a mutual pair j receives W(d / h_j) m_i by an FP64 atomic
+// W(d / h_i) m_j, and for a mutual pair j receives W(d / h_j) m_i by an FP64 atomic.  Inside a
+// sweep it also fills the pair-geometry cache (geo) the later pair-once passes read.
 template<bool Smooth>
 __global__ void __launch_bounds__(kPairBlock) xmassOnceKernel(ListView lv, OwnedView ov, CoordFp64 cf,
                                                                const double* h, const double* m, KTab<Smooth> tab,

@@ -13,9 +13,10 @@
 // xm_j/kx_j, m_j*prho_j) are formed once per particle; 1/|r| comes from rsqrt and serves both
 // |r| and rv/|r|; the Atwood-number branches are decided by comparison, and the ramp's four
 // pow() calls become one exp() of the precomputed ln xm difference; the periodic wrap tests run
-// only for targets whose 2h box touches a periodic face.  Results agree with the reference to
-// rounding (<= 1e-12 relative).  The mixed form runs the same loops in FP32 on grid-local
-// offsets with Kahan sums.
+// only for targets whose 2h box touches a periodic face; inside a sweep the pair-once passes read
+// r, v_j - v_i, |r|, 1/|r| and both kernel values from the cache the xmass pass fills (PairGeo).
+// Results agree with the reference to rounding (<= 1e-12 relative).  The mixed form runs the same
+// loops in FP32 on grid-local offsets with Kahan sums.
 #include "pairs.cuh"
 
 namespace sphgb {
