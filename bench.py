@@ -162,6 +162,10 @@ WORKLOADS = {
     "sphere10M": ("sphere10M: 10000000 particles in the unit sphere, open boundaries, r = sqrt(U) (seed 4), "
                   "u = 0.05, v = 0, h from the local number density",
                   lambda W: W.sphere(10_000_000)),
+    # the same Sedov set at 30^3 = 27,000 particles: a case both arms finish in seconds on any host
+    "sedov30_jit": ("sedov30_jit: 27000 particles, periodic [-0.5,0.5]^3, jitter +-0.25 spacing (seed 2), "
+                    "Sedov u, v = 0, frozen h",
+                    lambda W: W.sedov(30, jitter=0.25, seed=2)),
 }
 
 
