@@ -245,7 +245,13 @@ int sphgb_compute_momentum_energy(sphgb_ctx* ctx, sphgb_particles* p, int64_t fi
                                   int32_t av_clean, float* group_dt, double* minDtCourant);
 
 /* ---- whole sweep: sync + neighbours + the pair passes of one propagator step
- *      (main/src/propagator/std_hydro.hpp:124-168, ve_hydro.hpp:130-204) ---- */
+ *      (main/src/propagator/std_hydro.hpp:124-168, ve_hydro.hpp:130-204) ----
+ * Positions, velocities and h cannot change between the passes of one call, so the FP64 VE sweep
+ * (default mode) forms each owned pair's geometry and kernel values once, in the xmass pass, and
+ * the later passes read them: a context-owned buffer of up to 80 bytes per owned pair (8M
+ * particles: 35 GB), taken only when it fits in half of the free device memory, kept between
+ * calls, given back when larger neighbour lists need the space.  The pass entry points above form
+ * the geometry in every call. */
 int sphgb_sweep(sphgb_ctx* ctx, sphgb_particles* p, sphgb_box* box, int32_t variant, int32_t av_clean,
                 double* minDtCourant);
 /* same chain without the domain sync (keys, sort, tree reused): the frozen-tree sweep */
