@@ -462,7 +462,8 @@ def main() -> None:
     roofline = pair_roofline(st64, names, pairs, flops, fp64_peak, "fp64")
     traffic = NCU_DRAM_BYTES_PER_PARTICLE.get(roofline["kernel"])
     roofline["traffic"] = traffic * n if traffic else None
-    roofline["traffic_source"] = "ncu dram bytes of the same kernel at 1M particles, scaled by particles"
+    roofline["traffic_source"] = ("ncu dram bytes of the same kernel at 1M particles, scaled by particles; most of it "
+                                  "is the sweep's pair-geometry cache (80 B per owned pair), read instead of recomputed")
     roofline["hbm_peak_gbs"] = peaks.get("hbm_gbs")
     if traffic and peaks.get("hbm_gbs"):  # the same kernel against HBM: DRAM bytes over its time
         gbs = float(traffic * n / (roofline["ms"] * 1e-3) / 1e9)
